@@ -1,0 +1,321 @@
+/*
+ * mitrace_gpu.h - C ABI of the GB300 (sm_103a) path tracer that stands in for
+ * MiTrace's Tracer::Tracer render entry point.
+ *
+ * Everything crossing this boundary is plain C: POD structs, raw pointers and
+ * sizes.  No exception, C++ type or torch type crosses it.  Every function
+ * returns an mt_status (MT_OK on success); mt_last_error() gives a
+ * human-readable message for the last failure on the calling thread.
+ *
+ * Reference interface that each group replaces (paths inside the MiTrace
+ * project):
+ *   mt_create / mt_destroy   Tracer::Tracer(shared_ptr<RenderBuffer>, const Scene&)
+ *                            src/Tracer/Tracer.hpp:121, Tracer.cpp:633-640, plus the
+ *                            Scene::Scene data it reads (src/Scene/Scene.hpp:30)
+ *   mt_start                 Tracer::StartRender()     Tracer.hpp:124, Tracer.cpp:718-779
+ *   mt_wait                  Tracer::WaitForRender()   Tracer.hpp:125, Tracer.cpp:781-799
+ *   mt_kill                  Tracer::KillRender()      Tracer.hpp:126, Tracer.cpp:801-804
+ *   mt_get_stats             Tracer::GetStats()        Tracer.hpp:127, Tracer.cpp:806-821
+ *   mt_is_done               Tracer::IsDone()          Tracer.hpp:128, Tracer.cpp:823-828
+ *   mt_trace_rays*           Tracer::IntersectScene()  src/Tracer/Intersect.hpp:10,
+ *                            Intersect.cpp:201-219 (closest hit) and the shadow-ray
+ *                            use of it at Tracer.cpp:317-322 (any hit)
+ *   mt_brdf_batch            Tracer::BRDF::EvaluateBRDF/DiffusePdf/SpecularPdf
+ *                            src/Tracer/BRDF.hpp:52-97
+ *   mt_bvh_build             Scene::BVH::BVH(const Mesh&, ...) src/Scene/BVH.hpp:135,
+ *                            BVH.cpp:274-282 (host builder, same topology)
+ */
+#ifndef MITRACE_GPU_H
+#define MITRACE_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MT_ABI_VERSION 1
+
+typedef enum mt_status {
+    MT_OK = 0,
+    MT_ERR_CUDA = 1,     /* a CUDA runtime call failed */
+    MT_ERR_OOM = 2,      /* device or host allocation failed */
+    MT_ERR_INVALID = 3,  /* bad argument or malformed scene */
+    MT_ERR_TIMEOUT = 4,  /* a bounded wait ran out */
+    MT_ERR_KILLED = 5,   /* the render was cancelled with mt_kill */
+    MT_ERR_STATE = 6     /* call not valid in the handle's current state */
+} mt_status;
+
+/* ------------------------------------------------------------------------ */
+/* Scene description (host memory, borrowed for the duration of mt_create).  */
+/* ------------------------------------------------------------------------ */
+
+/* One flattened BVH node, 32 bytes, same meaning as Scene::BVHNode
+ * (src/Scene/BVH.hpp:74-119): an AABB and either two child node indices
+ * (inner node) or {first index | 0x80000000, count} into the index array. */
+typedef struct mt_bvh_node {
+    float lo[3];
+    float hi[3];
+    uint32_t a; /* child A, or leaf: first index | MT_BVH_LEAF_BIT */
+    uint32_t b; /* child B, or leaf: triangle count                */
+} mt_bvh_node;
+
+#define MT_BVH_LEAF_BIT 0x80000000u
+
+/* A de-indexed triangle mesh as Scene::Mesh holds it (src/Scene/Mesh.hpp:13-42,
+ * Mesh.cpp:24-41): 3 vertices per triangle, in triangle order. */
+typedef struct mt_mesh_desc {
+    uint32_t num_triangles;
+    const float* positions; /* 9 * num_triangles floats (required)          */
+    const float* normals;   /* 9 * num_triangles floats (required)          */
+    const float* uv0;       /* 6 * num_triangles floats, or NULL            */
+    /* Optional prebuilt BVH in the reference layout.  When NULL the library
+     * builds one on the host with mt_bvh_build semantics, if the mesh has more
+     * than bvh_max_triangles triangles and BVHs are enabled (Mesh.cpp:37-40). */
+    const mt_bvh_node* bvh_nodes;
+    uint32_t num_bvh_nodes;
+    const uint32_t* bvh_indices;
+    uint32_t num_bvh_indices;
+} mt_mesh_desc;
+
+/* Texture: Scene::Texture + Scene::Image (src/Scene/Texture.hpp, Image.hpp).
+ * Texels are RGB8 (alpha dropped, Image.cpp:93) or, for the float
+ * environment-map extension, RGB32F.  Exactly one of rgb8 / rgb32f is set. */
+typedef struct mt_texture_desc {
+    uint32_t width;
+    uint32_t height;
+    const uint8_t* rgb8;
+    const float* rgb32f;
+    int32_t filter;    /* 0 nearest, 1 linear (Image::FilterMode)     */
+    float offset[2];   /* KHR_texture_transform offset (Texture.cpp:12-15) */
+    float scale[2];    /* KHR_texture_transform scale                 */
+} mt_texture_desc;
+
+#define MT_FILTER_NEAREST 0
+#define MT_FILTER_LINEAR 1
+
+/* Scene::Material (src/Scene/Material.hpp:11-136).  Texture slots are indices
+ * into mt_scene_desc.textures or -1. */
+typedef struct mt_material_desc {
+    float base_color_factor[4];
+    float emissive_factor[3];
+    float normal_scale;
+    float metallic_factor;
+    float roughness_factor;
+    float occlusion_strength;
+    int32_t base_color_tex;
+    int32_t metallic_roughness_tex;
+    int32_t normal_tex;
+    int32_t occlusion_tex;
+    int32_t emissive_tex;
+} mt_material_desc;
+
+/* Scene::MeshInstance (src/Scene/Mesh.hpp:44-72): mesh, material and a
+ * column-major model-to-world matrix (glm::mat4 layout). */
+typedef struct mt_instance_desc {
+    uint32_t mesh;
+    uint32_t material;
+    float transform[16];
+} mt_instance_desc;
+
+/* Scene::Light (src/Scene/Light.hpp:14-66) after its constructor ran:
+ * color already multiplied by intensity, cone angles as cosines, direction
+ * = rotation applied to (0,0,-1). */
+typedef struct mt_light_desc {
+    int32_t type; /* MT_LIGHT_* */
+    float position[3];
+    float color[3];
+    float point_size;
+    float spot_inner_cos;
+    float spot_outer_cos;
+    float direction[3];
+} mt_light_desc;
+
+#define MT_LIGHT_POINT 0
+#define MT_LIGHT_DIRECTIONAL 1
+#define MT_LIGHT_SPOT 2
+#define MT_LIGHT_AREA 3
+
+/* Scene::Camera (src/Scene/Camera.hpp:10-36). */
+typedef struct mt_camera_desc {
+    int32_t type; /* 0 perspective, 1 orthographic */
+    float camera_to_world[16];
+    float yfov;        /* radians */
+    float aspect;      /* camera aspect ratio */
+    float ortho_size[2];
+} mt_camera_desc;
+
+typedef struct mt_scene_desc {
+    uint32_t num_meshes;
+    const mt_mesh_desc* meshes;
+    uint32_t num_instances;
+    const mt_instance_desc* instances;
+    uint32_t num_materials;
+    const mt_material_desc* materials;
+    uint32_t num_textures;
+    const mt_texture_desc* textures;
+    uint32_t num_lights;
+    const mt_light_desc* lights;
+    mt_camera_desc camera;
+    int32_t env_texture; /* index into textures, or -1 (Scene::SampleSkybox) */
+} mt_scene_desc;
+
+/* The hot-path subset of Config::ConfigOptions (src/CLI/Config.hpp:43-80),
+ * passed explicitly instead of through the global singleton. */
+typedef struct mt_config {
+    uint32_t width;
+    uint32_t height;
+    uint32_t samples;
+    uint32_t bounces;
+    float ev_exposure;
+    float hdri_primary_intensity;
+    float hdri_secondary_intensity;
+    float emission_base_intensity;
+    int32_t bvh_disable;
+    uint32_t bvh_max_triangles;
+    uint32_t bvh_max_depth;
+    int32_t firefly_enable;
+    float firefly_threshold;
+    float terminate_energy;
+    int32_t debug_mode; /* only 0 (DebugNone) is supported */
+    uint32_t reserved0;
+    uint64_t seed;      /* seeds the counter-based RNG */
+    uint32_t reserved[8];
+} mt_config;
+
+/* Fills *cfg with the reference defaults (Config.hpp:50-70). */
+void mt_config_defaults(mt_config* cfg);
+
+/* ------------------------------------------------------------------------ */
+/* Handle lifecycle and the Tracer-equivalent render API.                   */
+/* ------------------------------------------------------------------------ */
+
+typedef struct mt_handle mt_handle;
+
+typedef struct mt_stats {
+    float progress;                 /* 0..1                              */
+    float time_elapsed;             /* seconds since mt_start            */
+    float estimated_time_remaining; /* seconds                           */
+    float reserved;
+    uint64_t rays;                  /* path + shadow rays (Tracer.cpp:146,319) */
+    uint64_t samples;               /* camera samples (Tracer.cpp:342)   */
+} mt_stats;
+
+/* Uploads the scene to the current CUDA device, builds missing BVHs on the
+ * host, and allocates the render state.  *out is NULL on failure. */
+mt_status mt_create(const mt_scene_desc* scene, const mt_config* cfg, mt_handle** out);
+void mt_destroy(mt_handle* h);
+
+/* Starts an asynchronous render on the handle's own stream and returns.
+ * Calling it while a render is running returns MT_ERR_STATE. */
+mt_status mt_start(mt_handle* h);
+/* Blocks until the render ends; copies the W*H*3 float RGB image (row-major,
+ * y*W+x, tonemapped, as RenderBuffer holds it) into rgb_out when it is not
+ * NULL.  Returns MT_ERR_KILLED if mt_kill stopped the render. */
+mt_status mt_wait(mt_handle* h, float* rgb_out);
+/* Cooperative cancel, callable from any thread (Tracer.cpp:801-804). */
+mt_status mt_kill(mt_handle* h);
+/* Thread-safe progress/counters, callable while a render runs. */
+mt_status mt_get_stats(const mt_handle* h, mt_stats* out);
+/* 1 when a render was started and has finished, else 0. */
+int mt_is_done(const mt_handle* h);
+
+/* Synchronous render into a caller-owned DEVICE buffer (W*H*3 floats) on the
+ * given CUDA stream (0 = the handle's stream).  Returns when the work is
+ * enqueued; rays/samples are added to the handle's counters. */
+mt_status mt_render_device(mt_handle* h, float* d_rgb_out, void* cuda_stream);
+
+/* ------------------------------------------------------------------------ */
+/* Ray queries (test and microbench entry points).                          */
+/* ------------------------------------------------------------------------ */
+
+/* 32-byte ray.  tmax is only read by any-hit queries: the ray counts as
+ * occluded when the closest-hit semantics of IntersectScene would report a
+ * hit at world distance <= tmax (Tracer.cpp:322). */
+typedef struct mt_ray {
+    float origin[3];
+    float tmax;
+    float direction[3];
+    float pad;
+} mt_ray;
+
+/* 32-byte hit record of the closest hit (RayHit, src/Tracer/Ray.hpp:24-43).
+ * instance == MT_NO_HIT on a miss.  bvh_tests / tri_tests are the counters of
+ * the winning instance only, as RayHit carries them (Intersect.cpp:186-187);
+ * they are filled only by the counting query variant. */
+typedef struct mt_hit {
+    float distance; /* world-space distance (Intersect.cpp:182)          */
+    float u;        /* barycentric weight of vertex 1                     */
+    float v;        /* barycentric weight of vertex 2                     */
+    uint32_t instance;
+    uint32_t triangle;
+    uint32_t bv_index;
+    uint32_t bvh_tests;
+    uint32_t tri_tests;
+} mt_hit;
+
+#define MT_NO_HIT 0xFFFFFFFFu
+
+#define MT_QUERY_CLOSEST 0
+#define MT_QUERY_ANY 1          /* writes occluded (1) / visible (0) into hit.instance */
+#define MT_QUERY_CLOSEST_COUNT 2 /* closest hit plus bvh/triangle test counters */
+
+/* Host buffers: copies rays in, runs the query, copies hits out (blocking). */
+mt_status mt_trace_rays(mt_handle* h, const mt_ray* rays, uint64_t n, mt_hit* hits, int query);
+/* Device buffers on a caller stream (0 = handle stream); does not block. */
+mt_status mt_trace_rays_device(mt_handle* h, const mt_ray* d_rays, uint64_t n, mt_hit* d_hits,
+                               int query, void* cuda_stream);
+
+/* ------------------------------------------------------------------------ */
+/* BRDF batch (test entry point).                                           */
+/* ------------------------------------------------------------------------ */
+
+/* One BRDF query: L, V, N unit-ish vectors plus material scalars. */
+typedef struct mt_brdf_query {
+    float L[3];
+    float V[3];
+    float N[3];
+    float base_color[3];
+    float roughness;
+    float metallic;
+} mt_brdf_query;
+
+/* Output per query: EvaluateBRDF rgb, DiffusePdf, SpecularPdf. */
+typedef struct mt_brdf_result {
+    float f[3];
+    float diffuse_pdf;
+    float specular_pdf;
+} mt_brdf_result;
+
+/* Host buffers; needs no scene (h may be NULL). */
+mt_status mt_brdf_batch(const mt_brdf_query* q, uint64_t n, mt_brdf_result* out);
+
+/* ------------------------------------------------------------------------ */
+/* Host BVH builder.                                                        */
+/* ------------------------------------------------------------------------ */
+
+/* Builds the BVH of one de-indexed mesh with the reference's split rule
+ * (centroid mean, straddlers duplicated, child box = clipped parent) and its
+ * flattening order.  max_depth is Config::bvhMaxDepth (the builder applies the
+ * two "-1" steps of Mesh.cpp:40 and BVH.cpp:211 itself).  The arrays are
+ * allocated by the library; free them with mt_bvh_free. */
+mt_status mt_bvh_build(const float* positions, uint32_t num_triangles, uint32_t max_triangles,
+                       uint32_t max_depth, mt_bvh_node** nodes, uint32_t* num_nodes,
+                       uint32_t** indices, uint32_t* num_indices);
+void mt_bvh_free(mt_bvh_node* nodes, uint32_t* indices);
+
+/* ------------------------------------------------------------------------ */
+/* Diagnostics.                                                             */
+/* ------------------------------------------------------------------------ */
+
+const char* mt_last_error(void);
+int mt_abi_version(void);
+/* Number of kernel launches this handle issued since creation. */
+uint64_t mt_kernel_launches(const mt_handle* h);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MITRACE_GPU_H */

@@ -1,0 +1,838 @@
+// mt_api.cu - the C ABI (include/mitrace_gpu.h): scene upload, render
+// orchestration and ray queries.  Host code here is compiled with
+// -ffp-contract=off so the instance bounds and inverses it precomputes carry
+// the same float values as a plain IEEE evaluation.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <limits>
+#include <mutex>
+#include <new>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/mitrace_gpu.h"
+#include "mt_device.cuh"
+#include "mt_kernels.h"
+
+using namespace mt;
+
+namespace {
+
+thread_local std::string g_err;
+
+mt_status set_err(mt_status code, const std::string& msg)
+{
+    g_err = msg;
+    return code;
+}
+
+#define MT_CUDA(call)                                                                             \
+    do {                                                                                          \
+        cudaError_t e_ = (call);                                                                  \
+        if (e_ != cudaSuccess) {                                                                  \
+            return set_err(e_ == cudaErrorMemoryAllocation ? MT_ERR_OOM : MT_ERR_CUDA,            \
+                           std::string(#call) + ": " + cudaGetErrorString(e_));                   \
+        }                                                                                         \
+    } while (0)
+
+inline float hmin(float x, float y) { return (y < x) ? y : x; }
+inline float hmax(float x, float y) { return (x < y) ? y : x; }
+
+// Column-major 4x4 times (x,y,z,w) with GLM's pairing (c0*x + c1*y) + (c2*z + c3*w).
+void mat_vec(const float* m, const float v[4], float r[4])
+{
+    for (int k = 0; k < 4; ++k)
+        r[k] = (m[k] * v[0] + m[4 + k] * v[1]) + (m[8 + k] * v[2] + m[12 + k] * v[3]);
+}
+
+// 4x4 inverse by cofactor expansion, evaluated once per instance (the
+// reference evaluates glm::inverse per ray per instance, Intersect.cpp:151-152;
+// the value is ray-independent).
+void inverse4(const float* a, float* out)
+{
+    float inv[16];
+    inv[0] = a[5] * a[10] * a[15] - a[5] * a[11] * a[14] - a[9] * a[6] * a[15] +
+             a[9] * a[7] * a[14] + a[13] * a[6] * a[11] - a[13] * a[7] * a[10];
+    inv[4] = -a[4] * a[10] * a[15] + a[4] * a[11] * a[14] + a[8] * a[6] * a[15] -
+             a[8] * a[7] * a[14] - a[12] * a[6] * a[11] + a[12] * a[7] * a[10];
+    inv[8] = a[4] * a[9] * a[15] - a[4] * a[11] * a[13] - a[8] * a[5] * a[15] +
+             a[8] * a[7] * a[13] + a[12] * a[5] * a[11] - a[12] * a[7] * a[9];
+    inv[12] = -a[4] * a[9] * a[14] + a[4] * a[10] * a[13] + a[8] * a[5] * a[14] -
+              a[8] * a[6] * a[13] - a[12] * a[5] * a[10] + a[12] * a[6] * a[9];
+    inv[1] = -a[1] * a[10] * a[15] + a[1] * a[11] * a[14] + a[9] * a[2] * a[15] -
+             a[9] * a[3] * a[14] - a[13] * a[2] * a[11] + a[13] * a[3] * a[10];
+    inv[5] = a[0] * a[10] * a[15] - a[0] * a[11] * a[14] - a[8] * a[2] * a[15] +
+             a[8] * a[3] * a[14] + a[12] * a[2] * a[11] - a[12] * a[3] * a[10];
+    inv[9] = -a[0] * a[9] * a[15] + a[0] * a[11] * a[13] + a[8] * a[1] * a[15] -
+             a[8] * a[3] * a[13] - a[12] * a[1] * a[11] + a[12] * a[3] * a[9];
+    inv[13] = a[0] * a[9] * a[14] - a[0] * a[10] * a[13] - a[8] * a[1] * a[14] +
+              a[8] * a[2] * a[13] + a[12] * a[1] * a[10] - a[12] * a[2] * a[9];
+    inv[2] = a[1] * a[6] * a[15] - a[1] * a[7] * a[14] - a[5] * a[2] * a[15] +
+             a[5] * a[3] * a[14] + a[13] * a[2] * a[7] - a[13] * a[3] * a[6];
+    inv[6] = -a[0] * a[6] * a[15] + a[0] * a[7] * a[14] + a[4] * a[2] * a[15] -
+             a[4] * a[3] * a[14] - a[12] * a[2] * a[7] + a[12] * a[3] * a[6];
+    inv[10] = a[0] * a[5] * a[15] - a[0] * a[7] * a[13] - a[4] * a[1] * a[15] +
+              a[4] * a[3] * a[13] + a[12] * a[1] * a[7] - a[12] * a[3] * a[5];
+    inv[14] = -a[0] * a[5] * a[14] + a[0] * a[6] * a[13] + a[4] * a[1] * a[14] -
+              a[4] * a[2] * a[13] - a[12] * a[1] * a[6] + a[12] * a[2] * a[5];
+    inv[3] = -a[1] * a[6] * a[11] + a[1] * a[7] * a[10] + a[5] * a[2] * a[11] -
+             a[5] * a[3] * a[10] - a[9] * a[2] * a[7] + a[9] * a[3] * a[6];
+    inv[7] = a[0] * a[6] * a[11] - a[0] * a[7] * a[10] - a[4] * a[2] * a[11] +
+             a[4] * a[3] * a[10] + a[8] * a[2] * a[7] - a[8] * a[3] * a[6];
+    inv[11] = -a[0] * a[5] * a[11] + a[0] * a[7] * a[9] + a[4] * a[1] * a[11] -
+              a[4] * a[3] * a[9] - a[8] * a[1] * a[7] + a[8] * a[3] * a[5];
+    inv[15] = a[0] * a[5] * a[10] - a[0] * a[6] * a[9] - a[4] * a[1] * a[10] +
+              a[4] * a[2] * a[9] + a[8] * a[1] * a[6] - a[8] * a[2] * a[5];
+    const float det = a[0] * inv[0] + a[1] * inv[4] + a[2] * inv[8] + a[3] * inv[12];
+    const float s = 1.0f / det;
+    for (int i = 0; i < 16; ++i) out[i] = inv[i] * s;
+}
+
+template <class T>
+struct DevArray {
+    T* p = nullptr;
+    size_t n = 0;
+    ~DevArray() { reset(); }
+    void reset()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    cudaError_t alloc(size_t count)
+    {
+        reset();
+        n = count;
+        if (count == 0) return cudaSuccess;
+        return cudaMalloc(reinterpret_cast<void**>(&p), count * sizeof(T));
+    }
+    cudaError_t upload(const T* src, size_t count, cudaStream_t st)
+    {
+        cudaError_t e = alloc(count);
+        if (e != cudaSuccess || count == 0) return e;
+        return cudaMemcpyAsync(p, src, count * sizeof(T), cudaMemcpyHostToDevice, st);
+    }
+};
+
+// Maximum BVH depth (edges from the root to the deepest leaf) of a flattened BVH.
+bool bvh_depth(const std::vector<mt_bvh_node>& nodes, const std::vector<uint32_t>& idx,
+               uint32_t num_tris, uint32_t& depth, std::string& why)
+{
+    depth = 0;
+    if (nodes.empty()) {
+        why = "empty BVH";
+        return false;
+    }
+    std::vector<std::pair<uint32_t, uint32_t>> st{{0u, 0u}};
+    size_t visited = 0;
+    while (!st.empty()) {
+        const auto [ni, d] = st.back();
+        st.pop_back();
+        if (ni >= nodes.size() || ++visited > nodes.size()) {
+            why = "BVH node index out of range or cyclic";
+            return false;
+        }
+        depth = std::max(depth, d);
+        const mt_bvh_node& n = nodes[ni];
+        if (n.a & MT_BVH_LEAF_BIT) {
+            const uint64_t first = n.a & ~MT_BVH_LEAF_BIT, count = n.b & ~MT_BVH_LEAF_BIT;
+            if (first + count > idx.size()) {
+                why = "BVH leaf range outside the index array";
+                return false;
+            }
+            for (uint64_t i = first; i < first + count; ++i)
+                if (idx[i] >= num_tris) {
+                    why = "BVH index names a missing triangle";
+                    return false;
+                }
+        } else {
+            if (n.b != n.a + 1) {
+                why = "BVH siblings are not adjacent";
+                return false;
+            }
+            st.push_back({n.a, d + 1});
+            st.push_back({n.b, d + 1});
+        }
+    }
+    return true;
+}
+
+}  // namespace
+
+struct mt_handle {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    mt_config cfg{};
+    DevScene S{};
+    // scene storage
+    DevArray<float4> nodes, slots;
+    DevArray<float> normals, uvs;
+    DevArray<DevMesh> meshes;
+    DevArray<DevInstance> instances;
+    DevArray<DevMaterial> materials;
+    DevArray<DevTexture> textures;
+    DevArray<DevLight> lights;
+    std::vector<DevArray<uint8_t>> tex8;
+    std::vector<DevArray<float>> texf;
+    DevArray<int> error_flag;
+    uint64_t scene_bytes = 0;
+    // wavefront storage (allocated on first render)
+    uint32_t batch = 0;
+    uint64_t band_capacity = 0;  // samples the band planes hold
+    DevArray<float4> pstate;     // 10 float4 planes
+    DevArray<uint4> phit;
+    DevArray<float4> sq;         // 3 float4 planes
+    DevArray<uint32_t> queues;   // 2 planes
+    DevArray<uint32_t> counts;
+    DevArray<unsigned long long> rays;
+    DevArray<float> samples;     // 3 planes
+    DevArray<float> image;
+    unsigned long long* rays_host = nullptr;  // pinned
+    // query scratch
+    DevArray<mt_ray> qrays;
+    DevArray<mt_hit> qhits;
+    // async render
+    std::mutex mu;
+    std::thread worker;
+    std::atomic<int> running{0};
+    std::atomic<int> started{0};
+    std::atomic<int> done{0};
+    std::atomic<int> kill{0};
+    std::atomic<int> result{MT_OK};
+    std::string worker_err;
+    std::atomic<uint64_t> stat_rays{0}, stat_samples{0};
+    std::atomic<uint64_t> work_total{1}, work_done{0};
+    std::chrono::steady_clock::time_point t0;
+    std::atomic<uint64_t> launches{0};
+
+    ~mt_handle()
+    {
+        if (worker.joinable()) worker.join();
+        if (rays_host) cudaFreeHost(rays_host);
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+namespace {
+
+mt_status upload_scene(mt_handle* h, const mt_scene_desc* d)
+{
+    const mt_config& cfg = h->cfg;
+    cudaStream_t st = h->stream;
+    std::vector<float4> nodes, slots;
+    std::vector<float> normals, uvs;
+    std::vector<DevMesh> meshes(d->num_meshes);
+    std::vector<std::pair<std::vector<float>, std::vector<float>>> bounds(d->num_meshes);
+    std::vector<float> mesh_lo(3 * d->num_meshes), mesh_hi(3 * d->num_meshes);
+    uint32_t attr = 0;
+    for (uint32_t mi = 0; mi < d->num_meshes; ++mi) {
+        const mt_mesh_desc& md = d->meshes[mi];
+        if (!md.positions || !md.normals || md.num_triangles == 0)
+            return set_err(MT_ERR_INVALID, "mesh " + std::to_string(mi) +
+                                               ": positions and normals are required (GLTF.cpp:328-329)");
+        const uint32_t T = md.num_triangles;
+        const float* P = md.positions;
+        // Mesh::CalculateAABB (Mesh.cpp:43-54)
+        float lo[3] = {std::numeric_limits<float>::max(), std::numeric_limits<float>::max(),
+                       std::numeric_limits<float>::max()};
+        float hi[3] = {std::numeric_limits<float>::lowest(), std::numeric_limits<float>::lowest(),
+                       std::numeric_limits<float>::lowest()};
+        for (uint64_t v = 0; v < 3ull * T; ++v)
+            for (int k = 0; k < 3; ++k) {
+                lo[k] = hmin(lo[k], P[3 * v + k]);
+                hi[k] = hmax(hi[k], P[3 * v + k]);
+            }
+        std::memcpy(&mesh_lo[3 * mi], lo, 12);
+        std::memcpy(&mesh_hi[3 * mi], hi, 12);
+
+        DevMesh m{};
+        m.node_off = static_cast<uint32_t>(nodes.size() / 2);
+        m.slot_off = static_cast<uint32_t>(slots.size() / 3);
+        m.attr_off = attr;
+        m.num_tris = T;
+        m.has_uv = md.uv0 != nullptr;
+        const bool want_bvh = !cfg.bvh_disable && T > cfg.bvh_max_triangles;  // Mesh.cpp:37-40
+        std::vector<mt_bvh_node> bn;
+        std::vector<uint32_t> bi;
+        if (want_bvh) {
+            if (md.bvh_nodes && md.bvh_indices) {
+                bn.assign(md.bvh_nodes, md.bvh_nodes + md.num_bvh_nodes);
+                bi.assign(md.bvh_indices, md.bvh_indices + md.num_bvh_indices);
+            } else {
+                std::string err;
+                const int rc = build_bvh(P, T, cfg.bvh_max_triangles, cfg.bvh_max_depth, bn, bi, err);
+                if (rc != MT_OK) return set_err(static_cast<mt_status>(rc), "mesh " + std::to_string(mi) + ": " + err);
+            }
+            uint32_t depth = 0;
+            std::string why;
+            if (!bvh_depth(bn, bi, T, depth, why))
+                return set_err(MT_ERR_INVALID, "mesh " + std::to_string(mi) + ": " + why);
+            if (depth + 2 > MT_STACK_SIZE)
+                return set_err(MT_ERR_INVALID, "mesh " + std::to_string(mi) + ": BVH depth " +
+                                                   std::to_string(depth) + " exceeds the traversal stack (" +
+                                                   std::to_string(MT_STACK_SIZE - 2) + ")");
+            m.has_bvh = 1;
+            for (const mt_bvh_node& n : bn) {
+                float4 a, b;
+                a.x = n.lo[0]; a.y = n.lo[1]; a.z = n.lo[2];
+                b.x = n.hi[0]; b.y = n.hi[1]; b.z = n.hi[2];
+                std::memcpy(&a.w, &n.a, 4);
+                std::memcpy(&b.w, &n.b, 4);
+                nodes.push_back(a);
+                nodes.push_back(b);
+            }
+        } else {
+            bi.resize(T);
+            for (uint32_t t = 0; t < T; ++t) bi[t] = t;
+        }
+        m.num_slots = static_cast<uint32_t>(bi.size());
+        for (uint32_t t : bi) {
+            const float* v0 = P + 9ull * t;
+            const float* v1 = v0 + 3;
+            const float* v2 = v0 + 6;
+            float4 A, B, C;
+            A.x = v0[0]; A.y = v0[1]; A.z = v0[2];
+            std::memcpy(&A.w, &t, 4);
+            B.x = v1[0] - v0[0]; B.y = v1[1] - v0[1]; B.z = v1[2] - v0[2]; B.w = 0.0f;
+            C.x = v2[0] - v0[0]; C.y = v2[1] - v0[1]; C.z = v2[2] - v0[2]; C.w = 0.0f;
+            slots.push_back(A);
+            slots.push_back(B);
+            slots.push_back(C);
+        }
+        normals.insert(normals.end(), md.normals, md.normals + 9ull * T);
+        if (md.uv0)
+            uvs.insert(uvs.end(), md.uv0, md.uv0 + 6ull * T);
+        else
+            uvs.insert(uvs.end(), 6ull * T, 0.0f);
+        attr += T;
+        meshes[mi] = m;
+    }
+
+    std::vector<DevTexture> texs(d->num_textures);
+    h->tex8.resize(d->num_textures);
+    h->texf.resize(d->num_textures);
+    for (uint32_t ti = 0; ti < d->num_textures; ++ti) {
+        const mt_texture_desc& t = d->textures[ti];
+        const size_t n = static_cast<size_t>(t.width) * t.height * 3;
+        if (n == 0 || (!t.rgb8 && !t.rgb32f))
+            return set_err(MT_ERR_INVALID, "texture " + std::to_string(ti) + " has no texels");
+        DevTexture x{};
+        x.w = t.width;
+        x.h = t.height;
+        x.filter = t.filter;
+        x.offx = t.offset[0];
+        x.offy = t.offset[1];
+        x.sclx = t.scale[0];
+        x.scly = t.scale[1];
+        if (t.rgb32f) {
+            MT_CUDA(h->texf[ti].upload(t.rgb32f, n, st));
+            x.rgbf = h->texf[ti].p;
+            h->scene_bytes += n * 4;
+        } else {
+            MT_CUDA(h->tex8[ti].upload(t.rgb8, n, st));
+            x.rgb8 = h->tex8[ti].p;
+            h->scene_bytes += n;
+        }
+        texs[ti] = x;
+    }
+
+    std::vector<DevMaterial> mats(d->num_materials);
+    for (uint32_t i = 0; i < d->num_materials; ++i) {
+        const mt_material_desc& m = d->materials[i];
+        DevMaterial x{};
+        std::memcpy(x.base, m.base_color_factor, 16);
+        std::memcpy(x.emissive, m.emissive_factor, 12);
+        x.normal_scale = m.normal_scale;
+        x.metallic = m.metallic_factor;
+        x.roughness = m.roughness_factor;
+        x.base_tex = m.base_color_tex;
+        x.mr_tex = m.metallic_roughness_tex;
+        x.nrm_tex = m.normal_tex;
+        x.em_tex = m.emissive_tex;
+        for (int ti : {x.base_tex, x.mr_tex, x.nrm_tex, x.em_tex})
+            if (ti >= static_cast<int>(d->num_textures))
+                return set_err(MT_ERR_INVALID, "material " + std::to_string(i) + " names a missing texture");
+        mats[i] = x;
+    }
+
+    std::vector<DevInstance> insts(d->num_instances);
+    for (uint32_t i = 0; i < d->num_instances; ++i) {
+        const mt_instance_desc& id = d->instances[i];
+        if (id.mesh >= d->num_meshes || id.material >= d->num_materials)
+            return set_err(MT_ERR_INVALID, "instance " + std::to_string(i) + " names a missing mesh or material");
+        DevInstance x{};
+        std::memcpy(x.model, id.transform, 64);
+        inverse4(id.transform, x.inv);
+        x.mesh = id.mesh;
+        x.material = id.material;
+        // MeshInstance::CalculateWorldAABB (Mesh.cpp:56-80)
+        const float* a = &mesh_lo[3 * id.mesh];
+        const float* b = &mesh_hi[3 * id.mesh];
+        const float corners[8][3] = {{a[0], a[1], a[2]}, {a[0], a[1], b[2]}, {a[0], b[1], a[2]},
+                                     {a[0], b[1], b[2]}, {b[0], a[1], a[2]}, {b[0], a[1], b[2]},
+                                     {b[0], b[1], a[2]}, {b[0], b[1], b[2]}};
+        for (int k = 0; k < 3; ++k) {
+            x.wlo[k] = std::numeric_limits<float>::max();
+            x.whi[k] = std::numeric_limits<float>::lowest();
+        }
+        for (const auto& c : corners) {
+            const float v[4] = {c[0], c[1], c[2], 1.0f};
+            float w[4];
+            mat_vec(id.transform, v, w);
+            for (int k = 0; k < 3; ++k) {
+                x.wlo[k] = hmin(x.wlo[k], w[k]);
+                x.whi[k] = hmax(x.whi[k], w[k]);
+            }
+        }
+        insts[i] = x;
+    }
+
+    std::vector<DevLight> lights(d->num_lights);
+    for (uint32_t i = 0; i < d->num_lights; ++i) {
+        const mt_light_desc& l = d->lights[i];
+        DevLight x{};
+        x.type = l.type;
+        std::memcpy(x.pos, l.position, 12);
+        std::memcpy(x.color, l.color, 12);
+        std::memcpy(x.dir, l.direction, 12);
+        x.point_size = l.point_size;
+        x.inner_cos = l.spot_inner_cos;
+        x.outer_cos = l.spot_outer_cos;
+        x.simple = (l.color[0] + l.color[1] + l.color[2]) / 3.0f;  // PrepareLights, Tracer.cpp:123-132
+        lights[i] = x;
+    }
+    if (d->env_texture >= static_cast<int>(d->num_textures))
+        return set_err(MT_ERR_INVALID, "env texture index out of range");
+
+    MT_CUDA(h->nodes.upload(nodes.data(), nodes.size(), st));
+    MT_CUDA(h->slots.upload(slots.data(), slots.size(), st));
+    MT_CUDA(h->normals.upload(normals.data(), normals.size(), st));
+    MT_CUDA(h->uvs.upload(uvs.data(), uvs.size(), st));
+    MT_CUDA(h->meshes.upload(meshes.data(), meshes.size(), st));
+    MT_CUDA(h->instances.upload(insts.data(), insts.size(), st));
+    MT_CUDA(h->materials.upload(mats.data(), mats.size(), st));
+    MT_CUDA(h->textures.upload(texs.data(), texs.size(), st));
+    MT_CUDA(h->lights.upload(lights.data(), lights.size(), st));
+    MT_CUDA(h->error_flag.alloc(1));
+    MT_CUDA(cudaMemsetAsync(h->error_flag.p, 0, sizeof(int), st));
+    h->scene_bytes += nodes.size() * 16 + slots.size() * 16 + normals.size() * 4 + uvs.size() * 4 +
+                      insts.size() * sizeof(DevInstance);
+    MT_CUDA(cudaStreamSynchronize(st));
+
+    DevScene& S = h->S;
+    S.nodes = h->nodes.p;
+    S.slots = h->slots.p;
+    S.normals = h->normals.p;
+    S.uvs = h->uvs.p;
+    S.meshes = h->meshes.p;
+    S.instances = h->instances.p;
+    S.materials = h->materials.p;
+    S.textures = h->textures.p;
+    S.lights = h->lights.p;
+    S.num_instances = d->num_instances;
+    S.num_lights = d->num_lights;
+    S.env = d->env_texture;
+    S.hdri_prim = cfg.hdri_primary_intensity;
+    S.hdri_sec = cfg.hdri_secondary_intensity;
+    S.emission_base = cfg.emission_base_intensity;
+    S.cam_type = d->camera.type;
+    std::memcpy(S.c2w, d->camera.camera_to_world, 64);
+    S.fov_scale = tanf(d->camera.yfov * 0.5f);
+    S.cam_aspect = d->camera.aspect;
+    S.ortho_x = d->camera.ortho_size[0];
+    S.ortho_y = d->camera.ortho_size[1];
+    S.width = cfg.width;
+    S.height = cfg.height;
+    S.bounces = cfg.bounces;
+    S.spp = cfg.samples;
+    S.terminate_energy = cfg.terminate_energy;
+    S.exposure = powf(2.0f, -cfg.ev_exposure);
+    S.px_w = 1.0f / static_cast<float>(cfg.width);
+    S.px_h = 1.0f / static_cast<float>(cfg.height);
+    S.render_aspect = static_cast<float>(cfg.width) / static_cast<float>(cfg.height);
+    S.key0 = static_cast<uint32_t>(cfg.seed);
+    S.key1 = static_cast<uint32_t>(cfg.seed >> 32);
+    S.firefly_enable = cfg.firefly_enable;
+    S.firefly_k = cfg.firefly_threshold;
+    S.error_flag = h->error_flag.p;
+    return MT_OK;
+}
+
+uint64_t env_u64(const char* name, uint64_t dflt)
+{
+    const char* v = std::getenv(name);
+    if (!v || !*v) return dflt;
+    return std::strtoull(v, nullptr, 10);
+}
+
+// Sizes the wavefront: a batch of paths and the per-sample planes of one band
+// of image rows (the firefly clamp needs every sample of a pixel at once).
+mt_status ensure_wave(mt_handle* h)
+{
+    if (h->batch) return MT_OK;
+    const mt_config& c = h->cfg;
+    const uint64_t npix = static_cast<uint64_t>(c.width) * c.height;
+    const uint64_t total = npix * c.samples;
+    uint64_t batch = env_u64("MT_BATCH_PATHS", 1ull << 22);
+    batch = std::max<uint64_t>(1024, std::min<uint64_t>(batch, total));
+    const uint64_t budget = env_u64("MT_SAMPLE_BUDGET_MB", 12288) << 20;
+    uint64_t rows = budget / (static_cast<uint64_t>(c.width) * c.samples * 12ull);
+    rows = std::max<uint64_t>(1, std::min<uint64_t>(rows, c.height));
+    h->band_capacity = rows * c.width * c.samples;
+    h->batch = static_cast<uint32_t>(batch);
+    MT_CUDA(h->pstate.alloc(10ull * batch));
+    MT_CUDA(h->phit.alloc(batch));
+    MT_CUDA(h->sq.alloc(3ull * batch));
+    MT_CUDA(h->queues.alloc(2ull * batch));
+    MT_CUDA(h->counts.alloc(4));
+    MT_CUDA(h->rays.alloc(1));
+    MT_CUDA(h->samples.alloc(3ull * h->band_capacity));
+    MT_CUDA(h->image.alloc(npix * 3));
+    MT_CUDA(cudaMallocHost(reinterpret_cast<void**>(&h->rays_host), sizeof(unsigned long long)));
+    return MT_OK;
+}
+
+struct WaveViews {
+    PathState P;
+    ShadowQueue SQ;
+    WaveBuffers W;
+};
+
+WaveViews views(mt_handle* h)
+{
+    WaveViews v{};
+    const uint64_t B = h->batch;
+    float4* s = h->pstate.p;
+    v.P.ro = s + 0 * B;
+    v.P.rd = s + 1 * B;
+    v.P.cur = s + 2 * B;
+    v.P.tot = s + 3 * B;
+    v.P.prev = s + 4 * B;
+    v.P.emit = s + 5 * B;
+    v.P.direct = s + 6 * B;
+    v.P.indirect = s + 7 * B;
+    v.P.sky = s + 8 * B;
+    v.P.hitA = s + 9 * B;
+    v.P.hitB = h->phit.p;
+    v.SQ.o = h->sq.p;
+    v.SQ.d = h->sq.p + B;
+    v.SQ.c = h->sq.p + 2 * B;
+    v.W.q[0] = h->queues.p;
+    v.W.q[1] = h->queues.p + B;
+    v.W.counts = h->counts.p;
+    v.W.rays = h->rays.p;
+    v.W.sr = h->samples.p;
+    v.W.sg = h->samples.p + h->band_capacity;
+    v.W.sb = h->samples.p + 2 * h->band_capacity;
+    return v;
+}
+
+// Enqueues a whole render into `out` on `st`.  With sync_each_batch the host
+// waits for every batch (progress/kill granularity for the async API).
+mt_status render_into(mt_handle* h, float* out, cudaStream_t st, bool sync_each_batch)
+{
+    mt_status rc = ensure_wave(h);
+    if (rc != MT_OK) return rc;
+    const mt_config& c = h->cfg;
+    const WaveViews v = views(h);
+    MT_CUDA(cudaMemsetAsync(h->rays.p, 0, sizeof(unsigned long long), st));
+    const uint64_t rows_per_band = h->band_capacity / (static_cast<uint64_t>(c.width) * c.samples);
+    uint64_t total_batches = 0;
+    for (uint64_t r0 = 0; r0 < c.height; r0 += rows_per_band) {
+        const uint64_t rows = std::min<uint64_t>(rows_per_band, c.height - r0);
+        total_batches += (rows * c.width * c.samples + h->batch - 1) / h->batch;
+    }
+    h->work_total = std::max<uint64_t>(1, total_batches);
+    h->work_done = 0;
+    uint64_t launches = 0;
+    for (uint64_t r0 = 0; r0 < c.height; r0 += rows_per_band) {
+        const uint64_t rows = std::min<uint64_t>(rows_per_band, c.height - r0);
+        const uint32_t band_pix = static_cast<uint32_t>(rows * c.width);
+        const uint32_t pix_base = static_cast<uint32_t>(r0 * c.width);
+        const uint64_t paths = static_cast<uint64_t>(band_pix) * c.samples;
+        for (uint64_t g0 = 0; g0 < paths; g0 += h->batch) {
+            if (h->kill.load()) {
+                h->launches += launches;
+                return set_err(MT_ERR_KILLED, "render killed");
+            }
+            const uint32_t n = static_cast<uint32_t>(std::min<uint64_t>(h->batch, paths - g0));
+            MT_CUDA(launch_batch(h->S, v.P, v.SQ, v.W, g0, n, band_pix, pix_base, st, &launches));
+            if (sync_each_batch) {
+                MT_CUDA(cudaMemcpyAsync(h->rays_host, h->rays.p, sizeof(unsigned long long),
+                                        cudaMemcpyDeviceToHost, st));
+                MT_CUDA(cudaStreamSynchronize(st));
+                h->stat_rays = *h->rays_host;
+                h->stat_samples += n;
+            }
+            h->work_done += 1;
+        }
+        MT_CUDA(launch_resolve(h->S, v.W, band_pix, pix_base, out, st));
+        ++launches;
+    }
+    h->launches += launches;
+    return MT_OK;
+}
+
+void worker_main(mt_handle* h)
+{
+    cudaSetDevice(h->device);
+    mt_status rc = render_into(h, h->image.p ? h->image.p : nullptr, h->stream, true);
+    if (rc == MT_OK) {
+        cudaError_t e = cudaStreamSynchronize(h->stream);
+        if (e != cudaSuccess) rc = set_err(MT_ERR_CUDA, cudaGetErrorString(e));
+    }
+    if (rc == MT_OK) {
+        int flag = 0;
+        if (cudaMemcpy(&flag, h->error_flag.p, sizeof(int), cudaMemcpyDeviceToHost) == cudaSuccess && flag)
+            rc = set_err(MT_ERR_INVALID, "device error flag set (traversal stack overflow)");
+        if (cudaMemcpy(h->rays_host, h->rays.p, 8, cudaMemcpyDeviceToHost) == cudaSuccess)
+            h->stat_rays = *h->rays_host;
+    }
+    if (rc != MT_OK) h->worker_err = g_err;
+    h->result = rc;
+    h->done = 1;
+    h->running = 0;
+}
+
+mt_status check_handle(const mt_handle* h)
+{
+    if (!h) return set_err(MT_ERR_INVALID, "null handle");
+    return MT_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* mt_last_error(void) { return g_err.c_str(); }
+int mt_abi_version(void) { return MT_ABI_VERSION; }
+
+void mt_config_defaults(mt_config* c)
+{
+    if (!c) return;
+    std::memset(c, 0, sizeof(*c));
+    c->width = 1280;
+    c->height = 720;
+    c->samples = 64;
+    c->bounces = 5;
+    c->ev_exposure = 8.0f;
+    c->hdri_primary_intensity = 350.0f;
+    c->hdri_secondary_intensity = 350.0f;
+    c->emission_base_intensity = 1.0f;
+    c->bvh_disable = 0;
+    c->bvh_max_triangles = 32;
+    c->bvh_max_depth = 32;
+    c->firefly_enable = 1;
+    c->firefly_threshold = 6.0f;
+    c->terminate_energy = 0.01f;
+    c->debug_mode = 0;
+    c->seed = 0;
+}
+
+mt_status mt_create(const mt_scene_desc* scene, const mt_config* cfg, mt_handle** out)
+{
+    if (!out) return set_err(MT_ERR_INVALID, "out is null");
+    *out = nullptr;
+    if (!scene || !cfg) return set_err(MT_ERR_INVALID, "scene and config are required");
+    if (cfg->width == 0 || cfg->height == 0 || cfg->samples == 0)
+        return set_err(MT_ERR_INVALID, "width, height and samples must be positive");
+    if (static_cast<uint64_t>(cfg->width) * cfg->height > 0xFFFFFFFFull / 2)
+        return set_err(MT_ERR_INVALID, "image too large");
+    if (cfg->debug_mode != 0) return set_err(MT_ERR_INVALID, "debug modes are not supported");
+    if (scene->num_meshes && !scene->meshes) return set_err(MT_ERR_INVALID, "meshes is null");
+    if (scene->num_instances && !scene->instances) return set_err(MT_ERR_INVALID, "instances is null");
+    if (scene->num_materials && !scene->materials) return set_err(MT_ERR_INVALID, "materials is null");
+    if (scene->num_textures && !scene->textures) return set_err(MT_ERR_INVALID, "textures is null");
+    if (scene->num_lights && !scene->lights) return set_err(MT_ERR_INVALID, "lights is null");
+    mt_handle* h = new (std::nothrow) mt_handle();
+    if (!h) return set_err(MT_ERR_OOM, "host allocation failed");
+    h->cfg = *cfg;
+    cudaError_t e = cudaGetDevice(&h->device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete h;
+        return set_err(MT_ERR_CUDA, std::string("CUDA unavailable: ") + cudaGetErrorString(e));
+    }
+    const mt_status rc = upload_scene(h, scene);
+    if (rc != MT_OK) {
+        delete h;
+        return rc;
+    }
+    *out = h;
+    return MT_OK;
+}
+
+void mt_destroy(mt_handle* h)
+{
+    if (!h) return;
+    h->kill = 1;
+    if (h->worker.joinable()) h->worker.join();
+    cudaStreamSynchronize(h->stream);
+    delete h;
+}
+
+mt_status mt_start(mt_handle* h)
+{
+    if (check_handle(h) != MT_OK) return MT_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(h->mu);
+    if (h->running) return set_err(MT_ERR_STATE, "a render is already running");
+    if (h->worker.joinable()) h->worker.join();
+    mt_status rc = ensure_wave(h);
+    if (rc != MT_OK) return rc;
+    h->kill = 0;
+    h->done = 0;
+    h->result = MT_OK;
+    h->stat_rays = 0;
+    h->stat_samples = 0;
+    h->work_done = 0;
+    h->t0 = std::chrono::steady_clock::now();
+    h->running = 1;
+    h->started = 1;
+    h->worker = std::thread(worker_main, h);
+    return MT_OK;
+}
+
+mt_status mt_wait(mt_handle* h, float* rgb_out)
+{
+    if (check_handle(h) != MT_OK) return MT_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(h->mu);
+    if (!h->started) return set_err(MT_ERR_STATE, "no render was started");
+    if (h->worker.joinable()) h->worker.join();
+    const mt_status rc = static_cast<mt_status>(h->result.load());
+    if (rc != MT_OK) return set_err(rc, h->worker_err);
+    if (rgb_out) {
+        const size_t bytes = static_cast<size_t>(h->cfg.width) * h->cfg.height * 3 * sizeof(float);
+        MT_CUDA(cudaMemcpy(rgb_out, h->image.p, bytes, cudaMemcpyDeviceToHost));
+    }
+    return MT_OK;
+}
+
+mt_status mt_kill(mt_handle* h)
+{
+    if (check_handle(h) != MT_OK) return MT_ERR_INVALID;
+    h->kill = 1;
+    return MT_OK;
+}
+
+mt_status mt_get_stats(const mt_handle* h, mt_stats* out)
+{
+    if (check_handle(h) != MT_OK || !out) return set_err(MT_ERR_INVALID, "null argument");
+    mt_stats s{};
+    const double el = h->started ? std::chrono::duration<double>(std::chrono::steady_clock::now() - h->t0).count() : 0.0;
+    s.progress = static_cast<float>(static_cast<double>(h->work_done.load()) / static_cast<double>(h->work_total.load()));
+    if (s.progress > 1.0f) s.progress = 1.0f;
+    s.time_elapsed = static_cast<float>(el);
+    s.estimated_time_remaining = s.progress > 0.0f ? s.time_elapsed / s.progress * (1.0f - s.progress) : 0.0f;
+    s.rays = h->stat_rays.load();
+    s.samples = h->stat_samples.load();
+    *out = s;
+    return MT_OK;
+}
+
+int mt_is_done(const mt_handle* h) { return h && h->started && h->done ? 1 : 0; }
+
+uint64_t mt_kernel_launches(const mt_handle* h) { return h ? h->launches.load() : 0; }
+
+mt_status mt_render_device(mt_handle* h, float* d_rgb_out, void* cuda_stream)
+{
+    if (check_handle(h) != MT_OK || !d_rgb_out) return set_err(MT_ERR_INVALID, "null argument");
+    if (h->running) return set_err(MT_ERR_STATE, "an asynchronous render is running");
+    cudaStream_t st = cuda_stream ? static_cast<cudaStream_t>(cuda_stream) : h->stream;
+    h->kill = 0;
+    const mt_status rc = render_into(h, d_rgb_out, st, false);
+    if (rc == MT_OK) h->stat_samples += static_cast<uint64_t>(h->cfg.width) * h->cfg.height * h->cfg.samples;
+    return rc;
+}
+
+mt_status mt_trace_rays_device(mt_handle* h, const mt_ray* d_rays, uint64_t n, mt_hit* d_hits, int query,
+                               void* cuda_stream)
+{
+    if (check_handle(h) != MT_OK) return MT_ERR_INVALID;
+    if (n && (!d_rays || !d_hits)) return set_err(MT_ERR_INVALID, "null ray or hit buffer");
+    if (query != MT_QUERY_CLOSEST && query != MT_QUERY_ANY && query != MT_QUERY_CLOSEST_COUNT)
+        return set_err(MT_ERR_INVALID, "unknown query");
+    if ((reinterpret_cast<uintptr_t>(d_rays) | reinterpret_cast<uintptr_t>(d_hits)) & 15)
+        return set_err(MT_ERR_INVALID, "ray and hit buffers must be 16-byte aligned");
+    cudaStream_t st = cuda_stream ? static_cast<cudaStream_t>(cuda_stream) : h->stream;
+    MT_CUDA(launch_trace(h->S, d_rays, n, d_hits, query, st));
+    h->launches += n ? 1 : 0;
+    return MT_OK;
+}
+
+mt_status mt_trace_rays(mt_handle* h, const mt_ray* rays, uint64_t n, mt_hit* hits, int query)
+{
+    if (check_handle(h) != MT_OK) return MT_ERR_INVALID;
+    if (n == 0) return MT_OK;
+    if (!rays || !hits) return set_err(MT_ERR_INVALID, "null ray or hit buffer");
+    if (h->qrays.n < n) {
+        MT_CUDA(h->qrays.alloc(n));
+        MT_CUDA(h->qhits.alloc(n));
+    }
+    MT_CUDA(cudaMemcpyAsync(h->qrays.p, rays, n * sizeof(mt_ray), cudaMemcpyHostToDevice, h->stream));
+    const mt_status rc = mt_trace_rays_device(h, h->qrays.p, n, h->qhits.p, query, h->stream);
+    if (rc != MT_OK) return rc;
+    MT_CUDA(cudaMemcpyAsync(hits, h->qhits.p, n * sizeof(mt_hit), cudaMemcpyDeviceToHost, h->stream));
+    MT_CUDA(cudaStreamSynchronize(h->stream));
+    int flag = 0;
+    MT_CUDA(cudaMemcpy(&flag, h->error_flag.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (flag) return set_err(MT_ERR_INVALID, "device error flag set (traversal stack overflow)");
+    return MT_OK;
+}
+
+mt_status mt_brdf_batch(const mt_brdf_query* q, uint64_t n, mt_brdf_result* out)
+{
+    if (n == 0) return MT_OK;
+    if (!q || !out) return set_err(MT_ERR_INVALID, "null argument");
+    mt_brdf_query* dq = nullptr;
+    mt_brdf_result* dr = nullptr;
+    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(&dq), n * sizeof(mt_brdf_query));
+    if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&dr), n * sizeof(mt_brdf_result));
+    if (e == cudaSuccess) e = cudaMemcpy(dq, q, n * sizeof(mt_brdf_query), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = launch_brdf(dq, n, dr, 0);
+    if (e == cudaSuccess) e = cudaMemcpy(out, dr, n * sizeof(mt_brdf_result), cudaMemcpyDeviceToHost);
+    if (dq) cudaFree(dq);
+    if (dr) cudaFree(dr);
+    if (e != cudaSuccess) return set_err(MT_ERR_CUDA, cudaGetErrorString(e));
+    return MT_OK;
+}
+
+mt_status mt_bvh_build(const float* positions, uint32_t num_triangles, uint32_t max_triangles,
+                       uint32_t max_depth, mt_bvh_node** nodes, uint32_t* num_nodes, uint32_t** indices,
+                       uint32_t* num_indices)
+{
+    if (!positions || !nodes || !num_nodes || !indices || !num_indices)
+        return set_err(MT_ERR_INVALID, "null argument");
+    std::vector<mt_bvh_node> bn;
+    std::vector<uint32_t> bi;
+    std::string err;
+    const int rc = build_bvh(positions, num_triangles, max_triangles, max_depth, bn, bi, err);
+    if (rc != MT_OK) return set_err(static_cast<mt_status>(rc), err);
+    *nodes = static_cast<mt_bvh_node*>(std::malloc(bn.size() * sizeof(mt_bvh_node)));
+    *indices = static_cast<uint32_t*>(std::malloc(std::max<size_t>(1, bi.size()) * sizeof(uint32_t)));
+    if (!*nodes || !*indices) {
+        std::free(*nodes);
+        std::free(*indices);
+        return set_err(MT_ERR_OOM, "host allocation failed");
+    }
+    std::memcpy(*nodes, bn.data(), bn.size() * sizeof(mt_bvh_node));
+    std::memcpy(*indices, bi.data(), bi.size() * sizeof(uint32_t));
+    *num_nodes = static_cast<uint32_t>(bn.size());
+    *num_indices = static_cast<uint32_t>(bi.size());
+    return MT_OK;
+}
+
+void mt_bvh_free(mt_bvh_node* nodes, uint32_t* indices)
+{
+    std::free(nodes);
+    std::free(indices);
+}
+
+}  // extern "C"

@@ -1,0 +1,705 @@
+// mt_device.cuh - device-side data layout and functions of the GB300 path tracer.
+//
+// Arithmetic that decides WHICH triangle a ray hits (slab test, Moller-Trumbore,
+// ray-to-local transform, world distance) and the camera-ray construction use
+// explicit round-to-nearest intrinsics (__fadd_rn/__fmul_rn/__fdiv_rn/
+// __fsqrt_rn) so the compiler cannot contract them into FMAs; with the same
+// association order as the reference's GLM calls this gives bit-identical
+// results to the reference traversal run with IEEE single precision
+// (src/Tracer/Intersect.cpp:9-219).  Shading uses the same exact operations;
+// only the transcendental calls (sinf, cosf, acosf, atan2f, powf) can differ by
+// an ulp from the host C library.
+#pragma once
+
+#include <cfloat>
+#include <cstdint>
+
+#include "../../include/mitrace_gpu.h"
+
+namespace mt {
+
+// ---------------------------------------------------------------------------
+// Exact-rounding vector math (GLM association order, see header comment).
+// ---------------------------------------------------------------------------
+struct f3 {
+    float x, y, z;
+};
+
+__device__ __forceinline__ f3 mk(float x, float y, float z) { return f3{x, y, z}; }
+__device__ __forceinline__ f3 splat(float s) { return f3{s, s, s}; }
+__device__ __forceinline__ f3 operator+(f3 a, f3 b)
+{
+    return {__fadd_rn(a.x, b.x), __fadd_rn(a.y, b.y), __fadd_rn(a.z, b.z)};
+}
+__device__ __forceinline__ f3 operator-(f3 a, f3 b)
+{
+    return {__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y), __fsub_rn(a.z, b.z)};
+}
+__device__ __forceinline__ f3 operator-(f3 a) { return {-a.x, -a.y, -a.z}; }
+__device__ __forceinline__ f3 operator*(f3 a, f3 b)
+{
+    return {__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y), __fmul_rn(a.z, b.z)};
+}
+__device__ __forceinline__ f3 operator*(f3 a, float s)
+{
+    return {__fmul_rn(a.x, s), __fmul_rn(a.y, s), __fmul_rn(a.z, s)};
+}
+__device__ __forceinline__ f3 operator*(float s, f3 a) { return a * s; }
+__device__ __forceinline__ f3 operator/(f3 a, float s)
+{
+    return {__fdiv_rn(a.x, s), __fdiv_rn(a.y, s), __fdiv_rn(a.z, s)};
+}
+__device__ __forceinline__ f3 operator/(f3 a, f3 b)
+{
+    return {__fdiv_rn(a.x, b.x), __fdiv_rn(a.y, b.y), __fdiv_rn(a.z, b.z)};
+}
+__device__ __forceinline__ f3 operator+(f3 a, float s)
+{
+    return {__fadd_rn(a.x, s), __fadd_rn(a.y, s), __fadd_rn(a.z, s)};
+}
+__device__ __forceinline__ float gmin(float x, float y) { return (y < x) ? y : x; }
+__device__ __forceinline__ float gmax(float x, float y) { return (x < y) ? y : x; }
+__device__ __forceinline__ float gclamp(float x, float lo, float hi)
+{
+    return gmin(gmax(x, lo), hi);
+}
+__device__ __forceinline__ f3 vmin(f3 a, f3 b) { return {gmin(a.x, b.x), gmin(a.y, b.y), gmin(a.z, b.z)}; }
+__device__ __forceinline__ f3 vmax(f3 a, f3 b) { return {gmax(a.x, b.x), gmax(a.y, b.y), gmax(a.z, b.z)}; }
+__device__ __forceinline__ float dot(f3 a, f3 b)
+{
+    return __fadd_rn(__fadd_rn(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y)), __fmul_rn(a.z, b.z));
+}
+__device__ __forceinline__ f3 cross(f3 a, f3 b)
+{
+    return {__fsub_rn(__fmul_rn(a.y, b.z), __fmul_rn(b.y, a.z)),
+            __fsub_rn(__fmul_rn(a.z, b.x), __fmul_rn(b.z, a.x)),
+            __fsub_rn(__fmul_rn(a.x, b.y), __fmul_rn(b.x, a.y))};
+}
+__device__ __forceinline__ float length(f3 v) { return __fsqrt_rn(dot(v, v)); }
+__device__ __forceinline__ f3 normalize(f3 v) { return v * __fdiv_rn(1.0f, __fsqrt_rn(dot(v, v))); }
+__device__ __forceinline__ f3 reflect(f3 i, f3 n) { return i - n * dot(n, i) * 2.0f; }
+__device__ __forceinline__ f3 ld3(const float* p) { return {p[0], p[1], p[2]}; }
+__device__ __forceinline__ f3 xyz(float4 v) { return {v.x, v.y, v.z}; }
+
+// Column-major 4x4 times (x, y, z, w): (c0*x + c1*y) + (c2*z + c3*w).
+__device__ __forceinline__ float mrow(const float* m, int r, float x, float y, float z, float w)
+{
+    return __fadd_rn(__fadd_rn(__fmul_rn(m[r], x), __fmul_rn(m[4 + r], y)),
+                     __fadd_rn(__fmul_rn(m[8 + r], z), __fmul_rn(m[12 + r], w)));
+}
+__device__ __forceinline__ f3 xform_point(const float* m, f3 p)
+{
+    return {mrow(m, 0, p.x, p.y, p.z, 1.0f), mrow(m, 1, p.x, p.y, p.z, 1.0f),
+            mrow(m, 2, p.x, p.y, p.z, 1.0f)};
+}
+__device__ __forceinline__ f3 xform_dir(const float* m, f3 d)
+{
+    return {mrow(m, 0, d.x, d.y, d.z, 0.0f), mrow(m, 1, d.x, d.y, d.z, 0.0f),
+            mrow(m, 2, d.x, d.y, d.z, 0.0f)};
+}
+
+constexpr float kPi = 3.14159265358979323846f;
+
+// ---------------------------------------------------------------------------
+// Device scene layout.
+// ---------------------------------------------------------------------------
+// BVH node: two float4, (lo.xyz, a) and (hi.xyz, b) with a/b as raw bits, the
+// reference's 32-byte node (src/Scene/BVH.hpp:74-119).  Node indices are the
+// reference's, so the siblings of a pair sit at (a, a+1).
+// Triangle slot: three float4 (v0.xyz | original triangle id, e1.xyz, e2.xyz);
+// for BVH meshes the slots follow the BVH index array, so a leaf's triangles
+// are contiguous; e1 = v1 - v0 and e2 = v2 - v0 are the same IEEE differences
+// the Moller-Trumbore test forms.
+struct DevMesh {
+    uint32_t node_off;   // first node in DevScene::nodes (in nodes, not float4s)
+    uint32_t slot_off;   // first triangle slot
+    uint32_t num_slots;  // slots of this mesh (triangles, or BVH indices)
+    uint32_t has_bvh;
+    uint32_t attr_off;   // first triangle of this mesh in normals/uvs arrays
+    uint32_t has_uv;
+    uint32_t num_tris;
+    uint32_t pad;
+};
+
+struct DevInstance {
+    float model[16];
+    float inv[16];
+    float wlo[3];
+    uint32_t mesh;
+    float whi[3];
+    uint32_t material;
+};
+
+struct DevMaterial {
+    float base[4];
+    float emissive[3];
+    float normal_scale;
+    float metallic;
+    float roughness;
+    int32_t base_tex, mr_tex, nrm_tex, em_tex;
+};
+
+struct DevTexture {
+    const uint8_t* rgb8;
+    const float* rgbf;
+    uint32_t w, h;
+    int32_t filter;
+    float offx, offy, sclx, scly;
+    uint32_t pad;
+};
+
+struct DevLight {
+    int32_t type;
+    float pos[3];
+    float color[3];
+    float dir[3];
+    float point_size, inner_cos, outer_cos, simple;
+};
+
+struct DevScene {
+    const float4* nodes;
+    const float4* slots;
+    const float* normals;  // 9 floats per triangle
+    const float* uvs;      // 6 floats per triangle
+    const DevMesh* meshes;
+    const DevInstance* instances;
+    const DevMaterial* materials;
+    const DevTexture* textures;
+    const DevLight* lights;
+    uint32_t num_instances;
+    uint32_t num_lights;
+    int32_t env;
+    float hdri_prim, hdri_sec, emission_base;
+    // camera
+    int32_t cam_type;
+    float c2w[16];
+    float fov_scale, cam_aspect, ortho_x, ortho_y;
+    // render settings
+    uint32_t width, height, bounces, spp;
+    float terminate_energy, exposure, px_w, px_h, render_aspect;
+    uint32_t key0, key1;
+    int32_t firefly_enable;
+    float firefly_k;
+    int* error_flag;
+};
+
+#define MT_STACK_SIZE 64
+#define MT_ERRBIT_STACK 1
+
+// ---------------------------------------------------------------------------
+// Intersection (restates src/Tracer/Intersect.cpp)
+// ---------------------------------------------------------------------------
+// IntersectRayAABB, Intersect.cpp:9-18, with 1/d hoisted (same values).
+__device__ __forceinline__ float slab(f3 o, f3 inv, f3 lo, f3 hi)
+{
+    const f3 t1 = (lo - o) * inv;
+    const f3 t2 = (hi - o) * inv;
+    const f3 tmin = vmin(t1, t2);
+    const f3 tmax = vmax(t1, t2);
+    const float enter = gmax(gmax(tmin.x, tmin.y), tmin.z);
+    const float exit = gmin(gmin(tmax.x, tmax.y), tmax.z);
+    return enter <= exit ? exit : -1.0f;
+}
+
+// Moller-Trumbore (1997), two-sided with |det| > FLT_EPSILON, edge-inclusive.
+// The det<0 branch is folded onto the det>0 one by negating u, v and det, which
+// is exact, so the accept/reject decisions equal the two-branch form.
+// On accept returns the raw numerators; t = dot(e2,q)/det, (u,v)/det.
+__device__ __forceinline__ bool tri_test(f3 o, f3 d, f3 v0, f3 e1, f3 e2, float& t, float& u,
+                                         float& v, float& det)
+{
+    const f3 p = cross(d, e2);
+    det = dot(e1, p);
+    if (!(fabsf(det) > FLT_EPSILON)) return false;
+    const float sg = det > 0.0f ? 1.0f : -1.0f;
+    const float adet = fabsf(det);
+    const f3 s = o - v0;
+    u = dot(s, p);
+    const float us = u * sg;
+    if (us < 0.0f || us > adet) return false;
+    const f3 q = cross(s, e1);
+    v = dot(d, q);
+    const float vs = v * sg;
+    if (vs < 0.0f || __fadd_rn(us, vs) > adet) return false;
+    const float inv = __fdiv_rn(1.0f, det);
+    t = __fmul_rn(dot(e2, q), inv);
+    return true;
+}
+
+struct LocalHit {
+    float t, u, v;
+    uint32_t slot;     // winning slot (triangle id is in its v0.w)
+    uint32_t bv;       // leaf node index (reference node numbering)
+    uint32_t bvh_tests, tri_tests;
+};
+
+__device__ __forceinline__ uint32_t f2u(float f) { return __float_as_uint(f); }
+
+// IntersectTrianglesBVH (Intersect.cpp:47-141): explicit stack of
+// {node, exit distance}; pops skip boxes with exit < 0 or exit > best + 0.1;
+// the nearer child (by exit distance) is pushed last.  Returns true when a
+// hit at t < FLT_MAX was found.  ANY_TMAX >= 0 stops at the first accepted hit
+// for which stop(t) says so (any-hit shadow query).
+template <bool COUNT, class StopFn>
+__device__ __forceinline__ void traverse_bvh(const DevScene& S, const DevMesh& m, f3 o, f3 d,
+                                             LocalHit& h, StopFn stop, bool& stopped)
+{
+    const float4* __restrict__ nodes = S.nodes + 2ull * m.node_off;
+    const float4* __restrict__ slots = S.slots + 3ull * m.slot_off;
+    const f3 inv = {__fdiv_rn(1.0f, d.x), __fdiv_rn(1.0f, d.y), __fdiv_rn(1.0f, d.z)};
+    uint32_t stk_node[MT_STACK_SIZE];
+    float stk_dist[MT_STACK_SIZE];
+    int sp = 0;
+    {
+        const float4 a = __ldg(nodes + 0), b = __ldg(nodes + 1);
+        stk_node[0] = 0;
+        stk_dist[0] = slab(o, inv, xyz(a), xyz(b));
+        sp = 1;
+    }
+    const float minDelta = 0.1f;
+    while (sp > 0) {
+        --sp;
+        const uint32_t ni = stk_node[sp];
+        const float nd = stk_dist[sp];
+        if (COUNT) ++h.bvh_tests;
+        if (nd < 0.0f) continue;
+        if (nd > __fadd_rn(h.t, minDelta)) continue;
+        const uint32_t na = f2u(__ldg(&nodes[2 * ni].w));
+        const uint32_t nb = f2u(__ldg(&nodes[2 * ni + 1].w));
+        if (na & MT_BVH_LEAF_BIT) {
+            const uint32_t first = na & ~MT_BVH_LEAF_BIT;
+            const uint32_t count = nb & ~MT_BVH_LEAF_BIT;
+            for (uint32_t i = first; i < first + count; ++i) {
+                const float4 A = __ldg(slots + 3 * i);
+                const float4 B = __ldg(slots + 3 * i + 1);
+                const float4 C = __ldg(slots + 3 * i + 2);
+                float t, u, v, det;
+                if (COUNT) ++h.tri_tests;
+                if (tri_test(o, d, xyz(A), xyz(B), xyz(C), t, u, v, det)) {
+                    if (t > 0.0f && t < h.t) {
+                        const float id = __fdiv_rn(1.0f, det);
+                        h.t = t;
+                        h.u = __fmul_rn(u, id);
+                        h.v = __fmul_rn(v, id);
+                        h.slot = i;
+                        h.bv = ni;
+                        if (stop(t)) {
+                            stopped = true;
+                            return;
+                        }
+                    }
+                }
+            }
+        } else {
+            const float4 a0 = __ldg(nodes + 2 * na), a1 = __ldg(nodes + 2 * na + 1);
+            const float4 b0 = __ldg(nodes + 2 * nb), b1 = __ldg(nodes + 2 * nb + 1);
+            const float da = slab(o, inv, xyz(a0), xyz(a1));
+            const float db = slab(o, inv, xyz(b0), xyz(b1));
+            const float lim = __fadd_rn(h.t, minDelta);
+            const bool pa = da >= 0.0f && da <= lim;
+            const bool pb = db >= 0.0f && db <= lim;
+            if (sp + 2 > MT_STACK_SIZE) {
+                atomicOr(S.error_flag, MT_ERRBIT_STACK);
+                return;
+            }
+            if (pa && pb) {
+                if (da < db) {
+                    stk_node[sp] = nb; stk_dist[sp] = db; ++sp;
+                    stk_node[sp] = na; stk_dist[sp] = da; ++sp;
+                } else {
+                    stk_node[sp] = na; stk_dist[sp] = da; ++sp;
+                    stk_node[sp] = nb; stk_dist[sp] = db; ++sp;
+                }
+            } else if (pa) {
+                stk_node[sp] = na; stk_dist[sp] = da; ++sp;
+            } else if (pb) {
+                stk_node[sp] = nb; stk_dist[sp] = db; ++sp;
+            }
+        }
+    }
+}
+
+// IntersectTrianglesLinear (Intersect.cpp:20-45).
+template <bool COUNT, class StopFn>
+__device__ __forceinline__ void traverse_linear(const DevScene& S, const DevMesh& m, f3 o, f3 d,
+                                                LocalHit& h, StopFn stop, bool& stopped)
+{
+    const float4* __restrict__ slots = S.slots + 3ull * m.slot_off;
+    for (uint32_t i = 0; i < m.num_slots; ++i) {
+        const float4 A = __ldg(slots + 3 * i);
+        const float4 B = __ldg(slots + 3 * i + 1);
+        const float4 C = __ldg(slots + 3 * i + 2);
+        float t, u, v, det;
+        if (COUNT) ++h.tri_tests;
+        if (tri_test(o, d, xyz(A), xyz(B), xyz(C), t, u, v, det)) {
+            if (t > 0.0f && t < h.t) {
+                const float id = __fdiv_rn(1.0f, det);
+                h.t = t;
+                h.u = __fmul_rn(u, id);
+                h.v = __fmul_rn(v, id);
+                h.slot = i;
+                if (stop(t)) {
+                    stopped = true;
+                    return;
+                }
+            }
+        }
+    }
+}
+
+struct SceneHit {
+    bool hit;
+    uint32_t inst, tri, bv, bvh_tests, tri_tests;
+    float u, v, dist;
+    f3 world_pos;
+};
+
+// IntersectScene + IntersectMeshInstance (Intersect.cpp:143-219).
+// ANY: stops at the first accepted hit whose world distance is <= tmax and
+// reports it; the visit order up to that point is the closest-hit order, so the
+// verdict equals "closest hit distance <= tmax" (Tracer.cpp:322) whenever the
+// world distance is monotone in local t (rigid/affine instance transforms).
+template <bool COUNT, bool ANY>
+__device__ __forceinline__ SceneHit intersect_scene(const DevScene& S, f3 o, f3 d, float tmax)
+{
+    SceneHit best;
+    best.hit = false;
+    best.dist = FLT_MAX;
+    best.bvh_tests = best.tri_tests = 0;
+    best.inst = best.tri = best.bv = 0;
+    best.u = best.v = 0.0f;
+    best.world_pos = splat(0.0f);
+    const f3 winv = {__fdiv_rn(1.0f, d.x), __fdiv_rn(1.0f, d.y), __fdiv_rn(1.0f, d.z)};
+    for (uint32_t ii = 0; ii < S.num_instances; ++ii) {
+        const DevInstance& I = S.instances[ii];
+        const f3 wlo = {__ldg(&I.wlo[0]), __ldg(&I.wlo[1]), __ldg(&I.wlo[2])};
+        const f3 whi = {__ldg(&I.whi[0]), __ldg(&I.whi[1]), __ldg(&I.whi[2])};
+        if (slab(o, winv, wlo, whi) < 0.0f) continue;
+        float inv[16], model[16];
+#pragma unroll
+        for (int k = 0; k < 16; ++k) inv[k] = __ldg(&I.inv[k]);
+        const f3 lo = xform_point(inv, o);
+        const f3 ld = normalize(xform_dir(inv, d));
+        const DevMesh m = S.meshes[__ldg(&I.mesh)];
+        LocalHit h;
+        h.t = FLT_MAX;
+        h.u = h.v = 0.0f;
+        h.slot = 0;
+        h.bv = 0;
+        h.bvh_tests = h.tri_tests = 0;
+        bool stopped = false;
+        auto stop = [&](float t) -> bool {
+            if (!ANY) return false;
+#pragma unroll
+            for (int k = 0; k < 16; ++k) model[k] = __ldg(&I.model[k]);
+            const f3 wp = xform_point(model, lo + t * ld);
+            return !(length(wp - o) > tmax);
+        };
+        if (m.has_bvh)
+            traverse_bvh<COUNT>(S, m, lo, ld, h, stop, stopped);
+        else
+            traverse_linear<COUNT>(S, m, lo, ld, h, stop, stopped);
+        if (ANY && stopped) {
+            best.hit = true;
+            best.inst = ii;
+            return best;
+        }
+        if (!(h.t < FLT_MAX)) continue;
+#pragma unroll
+        for (int k = 0; k < 16; ++k) model[k] = __ldg(&I.model[k]);
+        const f3 wp = xform_point(model, lo + h.t * ld);
+        const float wd = length(wp - o);
+        if (!ANY && wd < best.dist) {
+            best.hit = true;
+            best.dist = wd;
+            best.world_pos = wp;
+            best.inst = ii;
+            best.tri = f2u(__ldg(&S.slots[3ull * (m.slot_off + h.slot)].w));
+            best.bv = h.bv;
+            best.u = h.u;
+            best.v = h.v;
+            best.bvh_tests = h.bvh_tests;
+            best.tri_tests = h.tri_tests;
+        }
+    }
+    return best;
+}
+
+// ---------------------------------------------------------------------------
+// Philox4x32-10 (Salmon et al., SC'11) and the draw slots shared with the
+// CPU oracle's counter mode.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint4 philox(uint4 c, uint32_t k0, uint32_t k1)
+{
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        if (r) {
+            k0 += 0x9E3779B9u;
+            k1 += 0xBB67AE85u;
+        }
+        const uint32_t lo0 = 0xD2511F53u * c.x, hi0 = __umulhi(0xD2511F53u, c.x);
+        const uint32_t lo1 = 0xCD9E8D57u * c.z, hi1 = __umulhi(0xCD9E8D57u, c.z);
+        c = make_uint4(hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0);
+    }
+    return c;
+}
+
+__device__ __forceinline__ float u01(uint32_t x)
+{
+    return __fmul_rn(static_cast<float>(x >> 8), 1.0f / 16777216.0f);
+}
+// a + (b - a) * u, in the libstdc++ uniform_real_distribution order u*(b-a)+a.
+__device__ __forceinline__ float urange(uint32_t x, float a, float b)
+{
+    return __fadd_rn(__fmul_rn(u01(x), __fsub_rn(b, a)), a);
+}
+
+enum : uint32_t { SLOT_JITTER = 0, SLOT_LOBE = 1, SLOT_FALLBACK = 2, SLOT_LIGHT_JITTER = 3, SLOT_LIGHT_PICK = 4 };
+
+__device__ __forceinline__ uint4 draw(const DevScene& S, uint32_t pixel, uint32_t sample,
+                                      uint32_t bounce, uint32_t slot)
+{
+    return philox(make_uint4(pixel, sample, (bounce << 8) | slot, 0u), S.key0, S.key1);
+}
+
+// ---------------------------------------------------------------------------
+// Camera (src/Tracer/Camera.cpp:17-50)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void camera_ray(const DevScene& S, float u, float v, f3& o, f3& d)
+{
+    if (S.cam_type == 0) {
+        const float px = __fmul_rn(__fmul_rn(__fsub_rn(__fmul_rn(2.0f, u), 1.0f), S.fov_scale),
+                                   S.render_aspect);
+        const float py = __fmul_rn(__fsub_rn(__fmul_rn(2.0f, v), 1.0f), S.fov_scale);
+        // normalize(vec4(px, -py, -1, 0)): vec4 dot pairs (x+y) + (z+w)
+        const float l2 = __fadd_rn(__fadd_rn(__fmul_rn(px, px), __fmul_rn(-py, -py)),
+                                   __fadd_rn(1.0f, 0.0f));
+        const float s = __fdiv_rn(1.0f, __fsqrt_rn(l2));
+        const float cx = __fmul_rn(px, s), cy = __fmul_rn(-py, s), cz = __fmul_rn(-1.0f, s),
+                    cw = __fmul_rn(0.0f, s);
+        o = {mrow(S.c2w, 0, 0, 0, 0, 1), mrow(S.c2w, 1, 0, 0, 0, 1), mrow(S.c2w, 2, 0, 0, 0, 1)};
+        d = normalize(f3{mrow(S.c2w, 0, cx, cy, cz, cw), mrow(S.c2w, 1, cx, cy, cz, cw),
+                         mrow(S.c2w, 2, cx, cy, cz, cw)});
+    } else {
+        const float px = __fdiv_rn(
+            __fmul_rn(__fmul_rn(__fsub_rn(__fmul_rn(2.0f, u), 1.0f), S.ortho_x), S.render_aspect),
+            S.cam_aspect);
+        const float py = __fmul_rn(__fsub_rn(__fmul_rn(2.0f, v), 1.0f), S.ortho_y);
+        o = {mrow(S.c2w, 0, px, -py, 0, 1), mrow(S.c2w, 1, px, -py, 0, 1),
+             mrow(S.c2w, 2, px, -py, 0, 1)};
+        d = normalize(f3{mrow(S.c2w, 0, 0, 0, -1, 0), mrow(S.c2w, 1, 0, 0, -1, 0),
+                         mrow(S.c2w, 2, 0, 0, -1, 0)});
+    }
+}
+
+// ---------------------------------------------------------------------------
+// BRDF (src/Tracer/BRDF.hpp:9-97)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ f3 fresnel_schlick(float c, f3 f0)
+{
+    c = gclamp(c, 0.0f, 1.0f);
+    const float p = powf(__fsub_rn(1.0f, c), 5.0f);
+    return f0 + (splat(1.0f) - f0) * splat(p);
+}
+__device__ __forceinline__ f3 base_reflectivity(f3 base, float metallic)
+{
+    metallic = gclamp(metallic, 0.0f, 1.0f);
+    return splat(0.04f) * __fsub_rn(1.0f, metallic) + base * metallic;
+}
+__device__ __forceinline__ float distribution_ggx(float nh, float r)
+{
+    nh = gclamp(nh, 0.0f, 1.0f);
+    const float a = __fmul_rn(r, r);
+    const float a2 = __fmul_rn(a, a);
+    const float nh2 = __fmul_rn(nh, nh);
+    float den = __fadd_rn(__fmul_rn(nh2, __fsub_rn(a2, 1.0f)), 1.0f);
+    den = __fmul_rn(__fmul_rn(kPi, den), den);
+    return __fdiv_rn(a2, den);
+}
+__device__ __forceinline__ float geometry_schlick_ggx(float nv, float r)
+{
+    nv = gclamp(nv, 0.0f, 1.0f);
+    const float rr = __fadd_rn(r, 1.0f);
+    const float k = __fdiv_rn(__fmul_rn(rr, rr), 8.0f);
+    const float den = __fadd_rn(__fmul_rn(nv, __fsub_rn(1.0f, k)), k);
+    return __fdiv_rn(nv, den);
+}
+__device__ __forceinline__ f3 eval_brdf(f3 L, f3 V, f3 N, f3 base, float roughness, float metallic)
+{
+    roughness = gmax(roughness, 0.05f);
+    const float nl = gmax(dot(N, L), 0.0f);
+    const float nv = gmax(dot(N, V), 0.0f);
+    if (nl <= 0.0f || nv <= 0.0f) return splat(0.0f);
+    const f3 h = normalize(V + L);
+    const float nh = gmax(dot(N, h), 0.0f);
+    const float hv = gmax(dot(h, V), 0.0f);
+    const f3 f0 = base_reflectivity(base, metallic);
+    const f3 f = fresnel_schlick(hv, f0);
+    const float dd = distribution_ggx(nh, roughness);
+    const float g = __fmul_rn(geometry_schlick_ggx(nv, roughness), geometry_schlick_ggx(nl, roughness));
+    const f3 kd = (splat(1.0f) - f) * __fsub_rn(1.0f, metallic);
+    const f3 diffuse = (kd * base) / kPi;
+    const f3 spec = (f * __fmul_rn(dd, g)) /
+                    gmax(__fmul_rn(__fmul_rn(4.0f, nv), nl), 0.001f);
+    return vmax(diffuse + spec, splat(0.0f));
+}
+__device__ __forceinline__ float diffuse_pdf(f3 L, f3 N) { return __fdiv_rn(gmax(dot(N, L), 0.0f), kPi); }
+__device__ __forceinline__ float specular_pdf(f3 L, f3 V, f3 N, float roughness)
+{
+    const float nl = gmax(dot(N, L), 0.0f);
+    const float nv = gmax(dot(N, V), 0.0f);
+    if (nl <= 0.0f || nv <= 0.0f) return 0.0f;
+    const f3 h = normalize(V + L);
+    const float nh = gmax(dot(N, h), 0.0f);
+    const float vh = gmax(dot(V, h), 0.0f);
+    if (vh <= 0.0f) return 0.0f;
+    return __fdiv_rn(__fmul_rn(distribution_ggx(nh, gmax(roughness, 0.05f)), nh), __fmul_rn(4.0f, vh));
+}
+
+// ---------------------------------------------------------------------------
+// Sampling helpers (src/Tracer/Tracer.cpp:26-121)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void build_tbn(f3 n, f3& t, f3& b)
+{
+    const f3 up = (fabsf(n.z) < 0.999f) ? f3{0, 0, 1} : f3{1, 0, 0};
+    t = normalize(cross(up, n));
+    b = cross(n, t);
+}
+__device__ __forceinline__ f3 cosine_hemisphere(float u1, float u2, f3 n)
+{
+    const float r = __fsqrt_rn(u1);
+    const float phi = __fmul_rn(__fmul_rn(2.0f, kPi), u2);
+    f3 t, b;
+    build_tbn(n, t, b);
+    const float lx = __fmul_rn(r, cosf(phi)), ly = __fmul_rn(r, sinf(phi));
+    const float lz = __fsqrt_rn(gmax(0.0f, __fsub_rn(1.0f, u1)));
+    return normalize(t * lx + b * ly + n * lz);
+}
+__device__ __forceinline__ float specular_probability(f3 view, f3 n, f3 base, float metallic)
+{
+    const f3 f0 = base_reflectivity(base, metallic);
+    const f3 f = fresnel_schlick(gmax(dot(n, view), 0.0f), f0);
+    const float p = __fdiv_rn(__fadd_rn(__fadd_rn(f.x, f.y), f.z), 3.0f);
+    return gclamp(p, 0.05f, 0.95f);
+}
+__device__ __forceinline__ f3 compute_normal(f3 surf, f3 tex)
+{
+    const f3 n = normalize(surf);
+    const f3 up = (fabsf(n.y) < 0.9f) ? f3{0, 1, 0} : f3{1, 0, 0};
+    const f3 t = normalize(cross(n, up));
+    const f3 b = normalize(cross(t, n));
+    const f3 r = {__fadd_rn(__fadd_rn(__fmul_rn(t.x, tex.x), __fmul_rn(b.x, tex.y)), __fmul_rn(n.x, tex.z)),
+                  __fadd_rn(__fadd_rn(__fmul_rn(t.y, tex.x), __fmul_rn(b.y, tex.y)), __fmul_rn(n.y, tex.z)),
+                  __fadd_rn(__fadd_rn(__fmul_rn(t.z, tex.x), __fmul_rn(b.z, tex.y)), __fmul_rn(n.z, tex.z))};
+    return normalize(r);
+}
+__device__ __forceinline__ f3 aces(f3 c, float expo)
+{
+    const f3 col = c * expo;
+    return (col * (col * 2.51f + 0.03f)) / (col * (col * 2.43f + 0.59f) + 0.14f);
+}
+
+// ---------------------------------------------------------------------------
+// Textures and materials (Image.cpp:11-75, Texture.cpp:12-61, Material.hpp:82-135)
+// ---------------------------------------------------------------------------
+struct f4 {
+    float x, y, z, w;
+};
+__device__ __forceinline__ f4 texel(const DevTexture& t, int x, int y)
+{
+    long long idx = (static_cast<long long>(y) * t.w + x) * 3;
+    const long long maxIdx = static_cast<long long>(t.w) * t.h * 3 - 3;
+    idx = idx < 0 ? 0 : (idx > maxIdx ? maxIdx : idx);
+    if (t.rgbf) return {__ldg(t.rgbf + idx), __ldg(t.rgbf + idx + 1), __ldg(t.rgbf + idx + 2), 1.0f};
+    return {__fdiv_rn(static_cast<float>(__ldg(t.rgb8 + idx)), 255.0f),
+            __fdiv_rn(static_cast<float>(__ldg(t.rgb8 + idx + 1)), 255.0f),
+            __fdiv_rn(static_cast<float>(__ldg(t.rgb8 + idx + 2)), 255.0f), 1.0f};
+}
+__device__ __forceinline__ f4 mix4(f4 a, f4 b, float s)
+{
+    const float r = __fsub_rn(1.0f, s);
+    return {__fadd_rn(__fmul_rn(a.x, r), __fmul_rn(b.x, s)), __fadd_rn(__fmul_rn(a.y, r), __fmul_rn(b.y, s)),
+            __fadd_rn(__fmul_rn(a.z, r), __fmul_rn(b.z, s)), __fadd_rn(__fmul_rn(a.w, r), __fmul_rn(b.w, s))};
+}
+__device__ __forceinline__ f4 image_sample(const DevTexture& t, float uvx, float uvy)
+{
+    const float u = __fsub_rn(uvx, floorf(uvx));
+    const float v = __fsub_rn(uvy, floorf(uvy));
+    const int W = static_cast<int>(t.w), H = static_cast<int>(t.h);
+    if (t.filter == MT_FILTER_LINEAR) {
+        const int x0 = static_cast<int>(floorf(__fmul_rn(u, static_cast<float>(W))));
+        const int x1 = min(x0 + 1, W - 1);
+        const int y0 = static_cast<int>(floorf(__fmul_rn(v, static_cast<float>(H))));
+        const int y1 = min(y0 + 1, H - 1);
+        const float sx = __fsub_rn(u, __fdiv_rn(static_cast<float>(x0), static_cast<float>(W)));
+        const float sy = __fsub_rn(v, __fdiv_rn(static_cast<float>(y0), static_cast<float>(H)));
+        return mix4(mix4(texel(t, x0, y0), texel(t, x1, y0), sx),
+                    mix4(texel(t, x0, y1), texel(t, x1, y1), sx), sy);
+    }
+    int ix = static_cast<int>(__fmul_rn(u, static_cast<float>(W))) % W;
+    int iy = static_cast<int>(__fmul_rn(v, static_cast<float>(H))) % H;
+    if (ix < 0) ix += W;
+    if (iy < 0) iy += H;
+    return texel(t, ix, iy);
+}
+__device__ __forceinline__ f4 tex_sample(const DevScene& S, int ti, float u, float v)
+{
+    const DevTexture t = S.textures[ti];
+    return image_sample(t, __fadd_rn(__fmul_rn(u, t.sclx), t.offx), __fadd_rn(__fmul_rn(v, t.scly), t.offy));
+}
+
+struct MatPoint {
+    f4 base;
+    float metallic, roughness;
+    f3 normal, emission;
+};
+
+__device__ __forceinline__ MatPoint sample_material(const DevScene& S, uint32_t mi, float u, float v)
+{
+    const DevMaterial M = S.materials[mi];
+    MatPoint p;
+    if (M.base_tex >= 0) {
+        const f4 t = tex_sample(S, M.base_tex, u, v);
+        p.base = {__fmul_rn(t.x, M.base[0]), __fmul_rn(t.y, M.base[1]), __fmul_rn(t.z, M.base[2]),
+                  __fmul_rn(t.w, M.base[3])};
+    } else {
+        p.base = {M.base[0], M.base[1], M.base[2], M.base[3]};
+    }
+    if (M.mr_tex >= 0) {
+        const f4 t = tex_sample(S, M.mr_tex, u, v);
+        p.metallic = __fmul_rn(t.z, M.metallic);
+        p.roughness = __fmul_rn(t.y, M.roughness);
+    } else {
+        p.metallic = M.metallic;
+        p.roughness = M.roughness;
+    }
+    if (M.nrm_tex >= 0) {
+        const f4 t = tex_sample(S, M.nrm_tex, u, v);
+        p.normal = normalize((f3{t.x, t.y, t.z} * M.normal_scale * 2.0f) + (-1.0f));
+    } else {
+        p.normal = f3{0.0f, 0.0f, 1.0f};
+    }
+    if (M.em_tex >= 0) {
+        const f4 t = tex_sample(S, M.em_tex, u, v);
+        p.emission = f3{t.x, t.y, t.z} * f3{M.emissive[0], M.emissive[1], M.emissive[2]};
+    } else {
+        p.emission = f3{M.emissive[0], M.emissive[1], M.emissive[2]};
+    }
+    return p;
+}
+
+// Scene::SampleSkybox (Scene.cpp:61-73), Image::SampleEquirectangular (Image.cpp:63-75)
+__device__ __forceinline__ f3 sample_sky(const DevScene& S, f3 d, bool primary)
+{
+    if (S.env < 0) return splat(0.0f);
+    const float mult = primary ? S.hdri_prim : S.hdri_sec;
+    const float theta = atan2f(d.z, d.x);
+    const float phi = acosf(__fdiv_rn(d.y, length(d)));
+    const float u = __fdiv_rn(__fadd_rn(theta, kPi), __fmul_rn(2.0f, kPi));
+    const float v = __fdiv_rn(phi, kPi);
+    const DevTexture t = S.textures[S.env];
+    const f4 c = image_sample(t, u, v);
+    return f3{__fmul_rn(c.x, mult), __fmul_rn(c.y, mult), __fmul_rn(c.z, mult)};
+}
+
+}  // namespace mt

@@ -1,0 +1,486 @@
+// mt_kernels.cu - sm_103a kernels of the wavefront path tracer.
+//
+// The reference walks one path at a time per CPU thread (Tracer::RenderBlock ->
+// ProcessRayForward -> GeneratePath, src/Tracer/Tracer.cpp:134-348, 550-616).
+// Here a batch of paths (pixels x samples of one image band) moves through
+// bounce-synchronous stages; between stages the live paths are compacted into
+// queues with warp-aggregated atomics:
+//   raygen   camera rays + jitter              (Tracer.cpp:578-586, Camera.cpp:17-50)
+//   extend   closest hit of live paths         (Tracer.cpp:145, Intersect.cpp:201-219)
+//   shade    miss/sky, emission, light pick, shadow-ray setup, lobe sampling,
+//            energy cut-off                    (Tracer.cpp:147-208, 243-339)
+//   shadow   occlusion of the NEE rays          (Tracer.cpp:317-336)
+//   finalize per-sample total + ACES            (Tracer.cpp:344-346, 212-222)
+//   resolve  per-pixel firefly clamp + mean     (Tracer.cpp:490-548, 593-601)
+#include <cuda_runtime.h>
+
+#include "mt_device.cuh"
+#include "mt_kernels.h"
+
+namespace mt {
+
+__device__ __forceinline__ uint32_t warp_append(uint32_t* counter)
+{
+    const unsigned mask = __activemask();
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(mask) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(counter, static_cast<uint32_t>(__popc(mask)));
+    base = __shfl_sync(mask, base, leader);
+    return base + __popc(mask & ((1u << lane) - 1u));
+}
+
+// ---------------------------------------------------------------------------
+// Ray queries
+// ---------------------------------------------------------------------------
+template <int QUERY>
+__global__ void __launch_bounds__(128) k_trace(DevScene S, const mt_ray* __restrict__ rays,
+                                               uint64_t n, mt_hit* __restrict__ hits)
+{
+    for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+        const float4 a = __ldg(reinterpret_cast<const float4*>(rays + i));
+        const float4 b = __ldg(reinterpret_cast<const float4*>(rays + i) + 1);
+        mt_hit h;
+        if (QUERY == MT_QUERY_ANY) {
+            const SceneHit sh = intersect_scene<false, true>(S, xyz(a), xyz(b), a.w);
+            h.distance = 0.0f;
+            h.u = h.v = 0.0f;
+            h.instance = sh.hit ? 1u : 0u;
+            h.triangle = h.bv_index = h.bvh_tests = h.tri_tests = 0;
+        } else {
+            const SceneHit sh =
+                intersect_scene<QUERY == MT_QUERY_CLOSEST_COUNT, false>(S, xyz(a), xyz(b), 0.0f);
+            if (sh.hit) {
+                h.distance = sh.dist;
+                h.u = sh.u;
+                h.v = sh.v;
+                h.instance = sh.inst;
+                h.triangle = sh.tri;
+                h.bv_index = sh.bv;
+                h.bvh_tests = sh.bvh_tests;
+                h.tri_tests = sh.tri_tests;
+            } else {
+                h.distance = h.u = h.v = 0.0f;
+                h.instance = MT_NO_HIT;
+                h.triangle = h.bv_index = h.bvh_tests = h.tri_tests = 0;
+            }
+        }
+        float4* dst = reinterpret_cast<float4*>(hits + i);
+        dst[0] = make_float4(h.distance, h.u, h.v, __uint_as_float(h.instance));
+        dst[1] = make_float4(__uint_as_float(h.triangle), __uint_as_float(h.bv_index),
+                             __uint_as_float(h.bvh_tests), __uint_as_float(h.tri_tests));
+    }
+}
+
+__global__ void k_brdf(const mt_brdf_query* __restrict__ q, uint64_t n, mt_brdf_result* __restrict__ out)
+{
+    for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+        const mt_brdf_query x = q[i];
+        const f3 L = ld3(x.L), V = ld3(x.V), N = ld3(x.N), B = ld3(x.base_color);
+        const f3 f = eval_brdf(L, V, N, B, x.roughness, x.metallic);
+        mt_brdf_result r;
+        r.f[0] = f.x;
+        r.f[1] = f.y;
+        r.f[2] = f.z;
+        r.diffuse_pdf = diffuse_pdf(L, N);
+        r.specular_pdf = specular_pdf(L, V, N, x.roughness);
+        out[i] = r;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Wavefront render stages
+// ---------------------------------------------------------------------------
+struct BatchInfo {
+    uint64_t g0;        // first path (sample-major index inside the band)
+    uint32_t n;         // paths in this batch
+    uint32_t band_pix;  // pixels in the band
+    uint32_t pix_base;  // first pixel (y*W+x) of the band
+};
+
+__device__ __forceinline__ void path_coords(const DevScene& S, const BatchInfo& B, uint32_t p,
+                                            uint32_t& pixel, uint32_t& sample)
+{
+    const uint64_t g = B.g0 + p;
+    sample = static_cast<uint32_t>(g / B.band_pix);
+    pixel = B.pix_base + static_cast<uint32_t>(g - static_cast<uint64_t>(sample) * B.band_pix);
+}
+
+__global__ void __launch_bounds__(256) k_raygen(DevScene S, PathState P, BatchInfo B,
+                                                uint32_t* __restrict__ q0, uint32_t* counts)
+{
+    if (blockIdx.x == 0 && threadIdx.x == 0) counts[0] = B.n;
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < B.n; p += gridDim.x * blockDim.x) {
+        uint32_t pixel, sample;
+        path_coords(S, B, p, pixel, sample);
+        const uint32_t x = pixel % S.width, y = pixel / S.width;
+        const uint4 r = draw(S, pixel, sample, 0, SLOT_JITTER);
+        const float u = __fadd_rn(__fmul_rn(static_cast<float>(x), S.px_w), urange(r.x, 0.0f, S.px_w));
+        const float v = __fadd_rn(__fmul_rn(static_cast<float>(y), S.px_h), urange(r.y, 0.0f, S.px_h));
+        f3 o, d;
+        camera_ray(S, u, v, o, d);
+        P.ro[p] = make_float4(o.x, o.y, o.z, 0.0f);
+        P.rd[p] = make_float4(d.x, d.y, d.z, 0.0f);
+        const float4 one = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+        const float4 zero = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        P.cur[p] = one;
+        P.tot[p] = one;
+        P.prev[p] = zero;
+        P.emit[p] = zero;
+        P.direct[p] = zero;
+        P.indirect[p] = zero;
+        P.sky[p] = zero;
+        q0[p] = p;
+    }
+}
+
+__global__ void __launch_bounds__(128) k_extend(DevScene S, PathState P,
+                                                const uint32_t* __restrict__ q,
+                                                uint32_t* counts, int cur,
+                                                unsigned long long* rays)
+{
+    const uint32_t n = counts[cur];
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        counts[cur ^ 1] = 0;
+        counts[2] = 0;
+        atomicAdd(rays, static_cast<unsigned long long>(n));
+    }
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t p = q[i];
+        const float4 o = P.ro[p], d = P.rd[p];
+        const SceneHit h = intersect_scene<false, false>(S, xyz(o), xyz(d), 0.0f);
+        if (h.hit) {
+            P.hitA[p] = make_float4(h.world_pos.x, h.world_pos.y, h.world_pos.z, h.dist);
+            P.hitB[p] = make_uint4(h.inst, h.tri, __float_as_uint(h.u), __float_as_uint(h.v));
+        } else {
+            P.hitB[p] = make_uint4(MT_NO_HIT, 0u, 0u, 0u);
+        }
+    }
+}
+
+__device__ __forceinline__ f3 ld4(const float4* p, uint32_t i)
+{
+    const float4 v = p[i];
+    return {v.x, v.y, v.z};
+}
+__device__ __forceinline__ void st4(float4* p, uint32_t i, f3 v, float w = 0.0f)
+{
+    p[i] = make_float4(v.x, v.y, v.z, w);
+}
+
+__global__ void __launch_bounds__(128) k_shade(DevScene S, PathState P, ShadowQueue SQ,
+                                               BatchInfo B, uint32_t bounce,
+                                               const uint32_t* __restrict__ q,
+                                               uint32_t* __restrict__ nq, uint32_t* counts,
+                                               int cur)
+{
+    const uint32_t n = counts[cur];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t p = q[i];
+        const uint4 hb = P.hitB[p];
+        const f3 rd = ld4(P.rd, p);
+        const f3 cur_e = ld4(P.cur, p);
+        if (hb.x == MT_NO_HIT) {
+            // Tracer.cpp:244-252: previous vertex's base colour times energy times sky.
+            const f3 color = bounce > 0 ? ld4(P.prev, p) : splat(1.0f);
+            st4(P.sky, p, ld4(P.sky, p) + (color * cur_e) * sample_sky(S, rd, bounce == 0));
+            continue;
+        }
+        uint32_t pixel, sample;
+        path_coords(S, B, p, pixel, sample);
+        const float4 ha = P.hitA[p];
+        const f3 hit_pos = xyz(ha);
+        const float hit_dist = ha.w;
+        const float bu = __uint_as_float(hb.z), bv = __uint_as_float(hb.w);
+        const DevInstance& I = S.instances[hb.x];
+        const DevMesh m = S.meshes[__ldg(&I.mesh)];
+        // RayHitGeometryInfo (Ray.cpp:7-48)
+        const uint32_t tri = m.attr_off + hb.y;
+        const float w = __fsub_rn(__fsub_rn(1.0f, bu), bv);
+        const float* nr = S.normals + 9ull * tri;
+        f3 ni = {__fadd_rn(__fadd_rn(__fmul_rn(w, __ldg(nr + 0)), __fmul_rn(bu, __ldg(nr + 3))), __fmul_rn(bv, __ldg(nr + 6))),
+                 __fadd_rn(__fadd_rn(__fmul_rn(w, __ldg(nr + 1)), __fmul_rn(bu, __ldg(nr + 4))), __fmul_rn(bv, __ldg(nr + 7))),
+                 __fadd_rn(__fadd_rn(__fmul_rn(w, __ldg(nr + 2)), __fmul_rn(bu, __ldg(nr + 5))), __fmul_rn(bv, __ldg(nr + 8)))};
+        ni = normalize(ni);
+        float model[16];
+#pragma unroll
+        for (int k = 0; k < 16; ++k) model[k] = __ldg(&I.model[k]);
+        // normalize(model * vec4(n, 0)) with the vec4 pairwise dot
+        const float nx = mrow(model, 0, ni.x, ni.y, ni.z, 0.0f);
+        const float ny = mrow(model, 1, ni.x, ni.y, ni.z, 0.0f);
+        const float nz = mrow(model, 2, ni.x, ni.y, ni.z, 0.0f);
+        const float nw = mrow(model, 3, ni.x, ni.y, ni.z, 0.0f);
+        const float ns = __fdiv_rn(1.0f, __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(nx, nx), __fmul_rn(ny, ny)),
+                                                              __fadd_rn(__fmul_rn(nz, nz), __fmul_rn(nw, nw)))));
+        const f3 geom_n = {__fmul_rn(nx, ns), __fmul_rn(ny, ns), __fmul_rn(nz, ns)};
+        float tu = 0.0f, tv = 0.0f;
+        if (m.has_uv) {
+            const float* uv = S.uvs + 6ull * tri;
+            tu = __fadd_rn(__fadd_rn(__fmul_rn(w, __ldg(uv + 0)), __fmul_rn(bu, __ldg(uv + 2))), __fmul_rn(bv, __ldg(uv + 4)));
+            tv = __fadd_rn(__fadd_rn(__fmul_rn(w, __ldg(uv + 1)), __fmul_rn(bu, __ldg(uv + 3))), __fmul_rn(bv, __ldg(uv + 5)));
+        }
+        const MatPoint mp = sample_material(S, __ldg(&I.material), tu, tv);
+        const f3 base = {__fadd_rn(__fmul_rn(mp.base.x, 0.96f), 0.04f),
+                         __fadd_rn(__fmul_rn(mp.base.y, 0.96f), 0.04f),
+                         __fadd_rn(__fmul_rn(mp.base.z, 0.96f), 0.04f)};
+        const f3 N = compute_normal(geom_n, mp.normal);
+        const f3 view = -rd;
+
+        // Emission (Tracer.cpp:255)
+        st4(P.emit, p, ld4(P.emit, p) + (cur_e * S.emission_base) * mp.emission);
+
+        // Weighted reservoir light pick (Tracer.cpp:257-279)
+        int chosen = -1;
+        float pick = 0.0f, total = 0.0f;
+        uint4 rp = make_uint4(0, 0, 0, 0);
+        for (uint32_t li = 0; li < S.num_lights; ++li) {
+            if ((li & 3) == 0) rp = draw(S, pixel, sample, bounce, SLOT_LIGHT_PICK + (li >> 2));
+            const DevLight& L = S.lights[li];
+            const f3 lp = f3{__ldg(&L.pos[0]), __ldg(&L.pos[1]), __ldg(&L.pos[2])} - hit_pos;
+            const float score = __fdiv_rn(__ldg(&L.simple), __fadd_rn(dot(lp, lp), 1.0f));
+            total = __fadd_rn(total, score);
+            const uint32_t word = (li & 3) == 0 ? rp.x : ((li & 3) == 1 ? rp.y : ((li & 3) == 2 ? rp.z : rp.w));
+            if (__fmul_rn(urange(word, 0.0f, 1.0f), total) < score) {
+                chosen = static_cast<int>(li);
+                pick = score;
+            }
+        }
+        pick = __fdiv_rn(pick, total);
+        if (chosen >= 0) {
+            const DevLight& L = S.lights[chosen];
+            const int type = __ldg(&L.type);
+            const f3 lpos0 = {__ldg(&L.pos[0]), __ldg(&L.pos[1]), __ldg(&L.pos[2])};
+            f3 lpos = lpos0;
+            if (type == MT_LIGHT_POINT || type == MT_LIGHT_SPOT) {
+                const uint4 rj = draw(S, pixel, sample, bounce, SLOT_LIGHT_JITTER);
+                const float a = urange(rj.x, 0.0f, __fmul_rn(2.0f, kPi));
+                const float b = urange(rj.y, -kPi / 2.0f, kPi / 2.0f);
+                const f3 dir = normalize(f3{__fmul_rn(cosf(a), cosf(b)), sinf(b), __fmul_rn(sinf(a), cosf(b))});
+                lpos = lpos0 + dir * __ldg(&L.point_size);
+            }
+            const f3 lvec = lpos - hit_pos;
+            const f3 ldir = normalize(lvec);
+            f3 lcol = {__ldg(&L.color[0]), __ldg(&L.color[1]), __ldg(&L.color[2])};
+            if (type == MT_LIGHT_SPOT) {
+                const f3 sd = {__ldg(&L.dir[0]), __ldg(&L.dir[1]), __ldg(&L.dir[2])};
+                const float dd = dot(-ldir, sd);
+                const float inten = __fdiv_rn(__fsub_rn(dd, __ldg(&L.outer_cos)),
+                                              __fsub_rn(__ldg(&L.inner_cos), __ldg(&L.outer_cos)));
+                lcol = lcol * gclamp(inten, 0.0f, 1.0f);
+            }
+            const float llen = length(lvec);
+            const f3 brdf = eval_brdf(ldir, view, N, base, mp.roughness, mp.metallic);
+            const float nl = gmax(dot(N, ldir), 0.0f);
+            const float fall = __fdiv_rn(1.0f, __fadd_rn(__fmul_rn(llen, llen), 1.0f));
+            const f3 le = brdf * nl * fall;
+            const f3 contrib = ((cur_e * le) * lcol) / pick;
+            const uint32_t slot = warp_append(&counts[2]);
+            const f3 so = hit_pos + lvec * 0.0001f;
+            SQ.o[slot] = make_float4(so.x, so.y, so.z, llen);
+            SQ.d[slot] = make_float4(ldir.x, ldir.y, ldir.z, __uint_as_float(p));
+            SQ.c[slot] = make_float4(contrib.x, contrib.y, contrib.z, bounce == 0 ? 1.0f : 0.0f);
+        }
+
+        // Bounce sampling (Tracer.cpp:177-208); the last vertex never extends.
+        if (bounce + 1 >= S.bounces) continue;
+        const float ps = specular_probability(view, N, base, mp.metallic);
+        const uint4 rl = draw(S, pixel, sample, bounce, SLOT_LOBE);
+        f3 nd;
+        if (urange(rl.x, 0.0f, 1.0f) < ps) {
+            // SampleGGXDirection (Tracer.cpp:49-72)
+            const float u1 = urange(rl.y, 0.0f, 1.0f), u2 = urange(rl.z, 0.0f, 1.0f);
+            const float alpha = gmax(__fmul_rn(mp.roughness, mp.roughness), 0.0025f);
+            const float alpha2 = __fmul_rn(alpha, alpha);
+            const float phi = __fmul_rn(__fmul_rn(2.0f, kPi), u2);
+            const float tan2 = __fdiv_rn(__fmul_rn(alpha2, u1), gmax(__fsub_rn(1.0f, u1), 0.0001f));
+            const float cosT = __fdiv_rn(1.0f, __fsqrt_rn(__fadd_rn(1.0f, tan2)));
+            const float sinT = __fsqrt_rn(gmax(0.0f, __fsub_rn(1.0f, __fmul_rn(cosT, cosT))));
+            f3 t, b;
+            build_tbn(N, t, b);
+            f3 h = normalize(t * __fmul_rn(sinT, cosf(phi)) + b * __fmul_rn(sinT, sinf(phi)) + N * cosT);
+            if (dot(h, -rd) < 0.0f) h = -h;
+            const f3 r = reflect(rd, h);
+            if (dot(r, N) > 0.0f) {
+                nd = normalize(r);
+            } else {
+                const uint4 rf = draw(S, pixel, sample, bounce, SLOT_FALLBACK);
+                nd = cosine_hemisphere(urange(rf.x, 0.0f, 1.0f), urange(rf.y, 0.0f, 1.0f), N);
+            }
+        } else {
+            nd = cosine_hemisphere(urange(rl.y, 0.0f, 1.0f), urange(rl.z, 0.0f, 1.0f), N);
+        }
+        const float dp = diffuse_pdf(nd, N);
+        const float sp = specular_pdf(nd, view, N, mp.roughness);
+        const float pdf = __fadd_rn(__fmul_rn(__fsub_rn(1.0f, ps), dp), __fmul_rn(ps, sp));
+        const f3 brdf = eval_brdf(nd, view, N, base, mp.roughness, mp.metallic);
+        const float nl = gmax(dot(N, nd), 0.0f);
+        const f3 energy = pdf > 0.0f ? brdf * __fdiv_rn(nl, pdf) : splat(0.0f);
+        if (chosen >= 0) st4(P.cur, p, cur_e * energy);  // Tracer.cpp:339
+        const f3 tot = ld4(P.tot, p) * energy;
+        st4(P.tot, p, tot);
+        if (length(tot) < S.terminate_energy) continue;  // Tracer.cpp:207-208
+        const f3 ro = xyz(P.ro[p]);
+        const f3 no = (ro + rd * hit_dist) + N * 0.0001f;
+        st4(P.ro, p, no);
+        st4(P.rd, p, nd);
+        st4(P.prev, p, base);
+        nq[warp_append(&counts[cur ^ 1])] = p;
+    }
+}
+
+__global__ void __launch_bounds__(128) k_shadow(DevScene S, PathState P, ShadowQueue SQ,
+                                                const uint32_t* counts,
+                                                unsigned long long* rays)
+{
+    const uint32_t n = counts[2];
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(rays, static_cast<unsigned long long>(n));
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float4 o = SQ.o[i], d = SQ.d[i];
+        const SceneHit h = intersect_scene<false, true>(S, xyz(o), xyz(d), o.w);
+        if (h.hit) continue;
+        const float4 c = SQ.c[i];
+        const uint32_t p = __float_as_uint(d.w);
+        float4* acc = c.w != 0.0f ? P.direct : P.indirect;
+        const float4 a = acc[p];
+        acc[p] = make_float4(__fadd_rn(a.x, c.x), __fadd_rn(a.y, c.y), __fadd_rn(a.z, c.z), 0.0f);
+    }
+}
+
+__global__ void __launch_bounds__(256) k_finalize(DevScene S, PathState P, BatchInfo B,
+                                                  float* __restrict__ sr, float* __restrict__ sg,
+                                                  float* __restrict__ sb)
+{
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < B.n; p += gridDim.x * blockDim.x) {
+        const f3 total = ((ld4(P.emit, p) + ld4(P.direct, p)) + ld4(P.indirect, p)) + ld4(P.sky, p);
+        const f3 c = aces(total, S.exposure);
+        const uint64_t g = B.g0 + p;
+        sr[g] = c.x;
+        sg[g] = c.y;
+        sb[g] = c.z;
+    }
+}
+
+// CleanupFireflies + average: population mean/variance of the sample
+// intensities in sample order, reject |I - mean| > k*sigma, mean of the rest.
+__global__ void __launch_bounds__(256) k_resolve(const float* __restrict__ sr, const float* __restrict__ sg,
+                                                 const float* __restrict__ sb, uint32_t band_pix,
+                                                 uint32_t spp, uint32_t pix_base, int enable, float k,
+                                                 float* __restrict__ out)
+{
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < band_pix; j += gridDim.x * blockDim.x) {
+        f3 acc = splat(0.0f);
+        uint32_t kept = spp;
+        if (enable) {
+            float sum = 0.0f;
+            for (uint32_t s = 0; s < spp; ++s) {
+                const uint64_t g = static_cast<uint64_t>(s) * band_pix + j;
+                sum = __fadd_rn(sum, __fdiv_rn(__fadd_rn(__fadd_rn(sr[g], sg[g]), sb[g]), 3.0f));
+            }
+            const float mean = __fdiv_rn(sum, static_cast<float>(spp));
+            float var = 0.0f;
+            for (uint32_t s = 0; s < spp; ++s) {
+                const uint64_t g = static_cast<uint64_t>(s) * band_pix + j;
+                const float df = __fsub_rn(__fdiv_rn(__fadd_rn(__fadd_rn(sr[g], sg[g]), sb[g]), 3.0f), mean);
+                var = __fadd_rn(var, __fmul_rn(df, df));
+            }
+            var = __fdiv_rn(var, static_cast<float>(spp));
+            const float thr = __fmul_rn(k, __fsqrt_rn(var));
+            for (uint32_t s = 0; s < spp; ++s) {
+                const uint64_t g = static_cast<uint64_t>(s) * band_pix + j;
+                const f3 c = {sr[g], sg[g], sb[g]};
+                const float in = __fdiv_rn(__fadd_rn(__fadd_rn(c.x, c.y), c.z), 3.0f);
+                if (fabsf(__fsub_rn(in, mean)) > thr)
+                    --kept;
+                else
+                    acc = acc + c;
+            }
+            if (kept == 0) kept = 1;
+        } else {
+            for (uint32_t s = 0; s < spp; ++s) {
+                const uint64_t g = static_cast<uint64_t>(s) * band_pix + j;
+                acc = acc + f3{sr[g], sg[g], sb[g]};
+            }
+        }
+        const f3 r = acc / static_cast<float>(kept);
+        float* o = out + 3ull * (pix_base + j);
+        o[0] = r.x;
+        o[1] = r.y;
+        o[2] = r.z;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Host-side launchers
+// ---------------------------------------------------------------------------
+static int g_sms = 0;
+static int sm_count()
+{
+    if (g_sms == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
+        if (g_sms <= 0) g_sms = 1;
+    }
+    return g_sms;
+}
+
+static unsigned grid_for(uint64_t n, unsigned block, unsigned per_sm)
+{
+    const uint64_t need = (n + block - 1) / block;
+    const uint64_t cap = static_cast<uint64_t>(sm_count()) * per_sm;
+    return static_cast<unsigned>(need < cap ? (need ? need : 1) : cap);
+}
+
+cudaError_t launch_trace(const DevScene& S, const mt_ray* rays, uint64_t n, mt_hit* hits, int query,
+                         cudaStream_t st)
+{
+    if (n == 0) return cudaSuccess;
+    const unsigned g = grid_for(n, 128, 64);
+    switch (query) {
+        case MT_QUERY_ANY: k_trace<MT_QUERY_ANY><<<g, 128, 0, st>>>(S, rays, n, hits); break;
+        case MT_QUERY_CLOSEST_COUNT: k_trace<MT_QUERY_CLOSEST_COUNT><<<g, 128, 0, st>>>(S, rays, n, hits); break;
+        default: k_trace<MT_QUERY_CLOSEST><<<g, 128, 0, st>>>(S, rays, n, hits); break;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_brdf(const mt_brdf_query* q, uint64_t n, mt_brdf_result* out, cudaStream_t st)
+{
+    if (n == 0) return cudaSuccess;
+    k_brdf<<<grid_for(n, 128, 32), 128, 0, st>>>(q, n, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch(const DevScene& S, const PathState& P, const ShadowQueue& SQ,
+                         const WaveBuffers& W, uint64_t g0, uint32_t n, uint32_t band_pix,
+                         uint32_t pix_base, cudaStream_t st, uint64_t* launches)
+{
+    BatchInfo B{g0, n, band_pix, pix_base};
+    const unsigned gw = grid_for(n, 128, 16);
+    k_raygen<<<grid_for(n, 256, 8), 256, 0, st>>>(S, P, B, W.q[0], W.counts);
+    uint64_t l = 1;
+    int cur = 0;
+    for (uint32_t b = 0; b < S.bounces; ++b) {
+        k_extend<<<gw, 128, 0, st>>>(S, P, W.q[cur], W.counts, cur, W.rays);
+        k_shade<<<gw, 128, 0, st>>>(S, P, SQ, B, b, W.q[cur], W.q[cur ^ 1], W.counts, cur);
+        k_shadow<<<gw, 128, 0, st>>>(S, P, SQ, W.counts, W.rays);
+        l += 3;
+        cur ^= 1;
+    }
+    k_finalize<<<grid_for(n, 256, 8), 256, 0, st>>>(S, P, B, W.sr, W.sg, W.sb);
+    ++l;
+    if (launches) *launches += l;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_resolve(const DevScene& S, const WaveBuffers& W, uint32_t band_pix, uint32_t pix_base,
+                           float* out, cudaStream_t st)
+{
+    k_resolve<<<grid_for(band_pix, 256, 8), 256, 0, st>>>(W.sr, W.sg, W.sb, band_pix, S.spp, pix_base,
+                                                          S.firefly_enable, S.firefly_k, out);
+    return cudaGetLastError();
+}
+
+}  // namespace mt

@@ -1,0 +1,62 @@
+// mt_kernels.h - buffers shared by the host orchestration and the kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/mitrace_gpu.h"
+
+namespace mt {
+
+struct DevScene;
+
+// Per-path state of one wavefront batch, structure-of-arrays, indexed by the
+// path's position in the batch.
+struct PathState {
+    float4* ro;        // ray origin
+    float4* rd;        // ray direction
+    float4* cur;       // currentEnergy of the shading walk (Tracer.cpp:236)
+    float4* tot;       // totalEnergy of the path generation (Tracer.cpp:138)
+    float4* prev;      // base colour of the previous vertex (Tracer.cpp:247)
+    float4* emit;      // LightOutput::emittedLight
+    float4* direct;    // LightOutput::directLight
+    float4* indirect;  // LightOutput::indirectLight
+    float4* sky;       // LightOutput::skyLight
+    float4* hitA;      // world position xyz, world distance
+    uint4* hitB;       // instance (MT_NO_HIT on miss), triangle, u bits, v bits
+};
+
+// Shadow rays queued by the shade stage.
+struct ShadowQueue {
+    float4* o;  // origin xyz, max distance |lightVec|
+    float4* d;  // direction xyz, owning path index (bits)
+    float4* c;  // contribution xyz, 1 = direct (first vertex) / 0 = indirect
+};
+
+struct WaveBuffers {
+    uint32_t* q[2];                // ping-pong queues of live path indices
+    uint32_t* counts;              // [0],[1] queue sizes, [2] shadow-queue size
+    unsigned long long* rays;      // rays traced (extension + shadow)
+    float* sr;                     // per-sample tonemapped R, sample-major in a band
+    float* sg;
+    float* sb;
+};
+
+cudaError_t launch_trace(const DevScene& S, const mt_ray* rays, uint64_t n, mt_hit* hits, int query,
+                         cudaStream_t st);
+cudaError_t launch_brdf(const mt_brdf_query* q, uint64_t n, mt_brdf_result* out, cudaStream_t st);
+cudaError_t launch_batch(const DevScene& S, const PathState& P, const ShadowQueue& SQ,
+                         const WaveBuffers& W, uint64_t g0, uint32_t n, uint32_t band_pix,
+                         uint32_t pix_base, cudaStream_t st, uint64_t* launches);
+cudaError_t launch_resolve(const DevScene& S, const WaveBuffers& W, uint32_t band_pix,
+                           uint32_t pix_base, float* out, cudaStream_t st);
+
+// Host BVH builder (mt_bvh.cpp).
+int build_bvh(const float* positions, uint32_t num_triangles, uint32_t max_triangles,
+              uint32_t cfg_max_depth, std::vector<mt_bvh_node>& nodes,
+              std::vector<uint32_t>& indices, std::string& err);
+
+}  // namespace mt

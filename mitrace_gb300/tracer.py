@@ -1,0 +1,122 @@
+"""Python view of the C ABI, shaped like MiTrace's ``Tracer::Tracer``
+(src/Tracer/Tracer.hpp:121-128): construct with a scene, ``StartRender`` (non
+blocking), ``WaitForRender``, ``KillRender``, ``GetStats``, ``IsDone``.  The
+image lands in a ``RenderBuffer``-like float32 array (H, W, 3) of tonemapped
+means (src/Tracer/RenderBuffer.hpp:11-35).
+
+Also exposes the ray-query and BRDF test entry points.  Every call goes to
+``libmitrace_gb300.so``; there is no other implementation.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _abi as A
+from .scenes import PackedScene, SceneData
+
+
+@dataclass
+class Stats:
+    progress: float
+    timeElapsed: float
+    estimatedTimeRemaining: float
+    rays: int
+    samples: int
+
+
+class Tracer:
+    def __init__(self, scene: SceneData, config: A.mt_config):
+        self.scene = scene
+        self.config = config
+        self._packed = PackedScene(scene)
+        h = C.c_void_p()
+        A.check(A.lib.mt_create(self._packed.ptr(), C.byref(config), C.byref(h)), "mt_create")
+        self.handle = h
+        self.width, self.height = config.width, config.height
+        self.image = np.zeros((self.height, self.width, 3), dtype=np.float32)
+
+    # --- reference-shaped API ------------------------------------------------
+    def StartRender(self):
+        A.check(A.lib.mt_start(self.handle), "mt_start")
+
+    def WaitForRender(self) -> np.ndarray:
+        A.check(A.lib.mt_wait(self.handle, self.image.ctypes.data_as(C.c_void_p)), "mt_wait")
+        return self.image
+
+    def KillRender(self):
+        A.check(A.lib.mt_kill(self.handle), "mt_kill")
+
+    def GetStats(self) -> Stats:
+        s = A.mt_stats()
+        A.check(A.lib.mt_get_stats(self.handle, C.byref(s)), "mt_get_stats")
+        return Stats(s.progress, s.time_elapsed, s.estimated_time_remaining, s.rays, s.samples)
+
+    def IsDone(self) -> bool:
+        return bool(A.lib.mt_is_done(self.handle))
+
+    # --- device-resident entry points ------------------------------------------
+    def render_device(self, out_ptr: int, stream_ptr: int = 0):
+        A.check(A.lib.mt_render_device(self.handle, C.c_void_p(out_ptr), C.c_void_p(stream_ptr)), "mt_render_device")
+
+    def trace_device(self, rays_ptr: int, n: int, hits_ptr: int, query: int = A.MT_QUERY_CLOSEST, stream_ptr: int = 0):
+        A.check(A.lib.mt_trace_rays_device(self.handle, C.c_void_p(rays_ptr), n, C.c_void_p(hits_ptr), query,
+                                           C.c_void_p(stream_ptr)), "mt_trace_rays_device")
+
+    def trace(self, rays: np.ndarray, query: int = A.MT_QUERY_CLOSEST) -> np.ndarray:
+        """rays: (n, 8) float32 in mt_ray layout.  Returns an (n, 8) uint32 view
+        of mt_hit records (distance/u/v are float bits)."""
+        rays = np.ascontiguousarray(rays, dtype=np.float32)
+        assert rays.ndim == 2 and rays.shape[1] == 8
+        hits = np.zeros((rays.shape[0], 8), dtype=np.uint32)
+        A.check(A.lib.mt_trace_rays(self.handle, rays.ctypes.data_as(C.c_void_p), rays.shape[0],
+                                    hits.ctypes.data_as(C.c_void_p), query), "mt_trace_rays")
+        return hits
+
+    def kernel_launches(self) -> int:
+        return int(A.lib.mt_kernel_launches(self.handle))
+
+    def close(self):
+        if getattr(self, "handle", None):
+            A.lib.mt_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+def brdf_batch(q: np.ndarray) -> np.ndarray:
+    """q: (n, 14) float32 in mt_brdf_query layout -> (n, 5) float32 results."""
+    q = np.ascontiguousarray(q, dtype=np.float32)
+    assert q.ndim == 2 and q.shape[1] == 14
+    out = np.zeros((q.shape[0], 5), dtype=np.float32)
+    A.check(A.lib.mt_brdf_batch(q.ctypes.data_as(C.c_void_p), q.shape[0], out.ctypes.data_as(C.c_void_p)),
+            "mt_brdf_batch")
+    return out
+
+
+def bvh_build(positions: np.ndarray, max_triangles=32, max_depth=32):
+    """Host BVH build of one mesh (T, 3, 3) -> ((N, 8) uint32 nodes, (M,) uint32 indices)."""
+    pos = np.ascontiguousarray(positions, dtype=np.float32)
+    nodes = C.POINTER(A.mt_bvh_node)()
+    idx = C.POINTER(C.c_uint32)()
+    nn, ni = C.c_uint32(), C.c_uint32()
+    A.check(A.lib.mt_bvh_build(pos.ctypes.data_as(C.c_void_p), pos.shape[0], max_triangles, max_depth,
+                               C.byref(nodes), C.byref(nn), C.byref(idx), C.byref(ni)), "mt_bvh_build")
+    try:
+        n = np.ctypeslib.as_array(C.cast(nodes, C.POINTER(C.c_uint32)), shape=(nn.value * 8,)).reshape(-1, 8).copy()
+        i = np.ctypeslib.as_array(idx, shape=(max(ni.value, 1),))[: ni.value].copy()
+    finally:
+        A.lib.mt_bvh_free(C.cast(nodes, C.c_void_p), C.cast(idx, C.c_void_p))
+    return n, i
