@@ -1,0 +1,378 @@
+#!/usr/bin/env python3
+"""Benchmark of the path-tracing hot path on one GB300.
+
+A step is one full render of the material-grid scene (7x7 spheres of 4096
+triangles on a ground plane, float sky with a sun disk, 2 point lights) at
+1920x1080 and 256 samples per pixel, through the C ABI.  The metric is the
+reference's own throughput figure, Mrays/s, with rays counted the way
+Tracer::GeneratePath / ProcessRayForward count them (one per extension ray,
+one per shadow ray; src/Tracer/Tracer.cpp:146,319).
+
+  value      device-resident: mt_render_device into a device image, CUDA-event
+             time of each step on the launching stream, L2 flushed between steps
+  e2e        host API: mt_create from host arrays (scene upload, BVH build),
+             mt_start, mt_wait into a host image, mt_destroy; wall clock
+  roofline   the traversal ("extend") kernel: algorithmic bytes per launch
+             (64 B per inner-node expansion, 40 B per triangle test, 48 B per
+             ray, counted by an untimed counting pass of the same render) over
+             its CUDA-event launch time recorded inside the timed steps
+  cpu_baseline  the CPU oracle (restatement of the reference, -Ofast, all host
+             cores, reference tile queue) on a bounded band of rows
+
+--impl reference times that CPU implementation alone (the reference itself
+cannot be built here).  Under torchrun with N > 1 every rank renders its own
+copy of the image ("replicas only": a render does not shard across GPUs in this
+build) and rank 0 reports the aggregate.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+PEAKS_FILE = ROOT / "MEASURED_PEAKS.json"
+TRAFFIC_FILE = ROOT / "profiles" / "extend_traffic.json"
+FALLBACK_HBM_GBS = 6800.0
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=3)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--width", type=int, default=1920)
+    p.add_argument("--height", type=int, default=1080)
+    p.add_argument("--spp", type=int, default=256)
+    p.add_argument("--e2e-steps", type=int, default=None)
+    p.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU baseline sample")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def workload_name(a):
+    return f"material_grid_{a.width}x{a.height}_{a.spp}spp"
+
+
+# --------------------------------------------------------------------------- clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        sm, smax, reasons, power = [], [], set(), []
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+                power.append(float(f[3]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm), "power_w_max": max(power) if power else None}
+
+
+# --------------------------------------------------------------------------- CPU baseline
+def cpu_baseline(scene, cfg, target_seconds, fast=True):
+    """The oracle (restated reference, reference tile queue and threads) on a
+    band of rows around the image centre, sized to about target_seconds."""
+    from oracle import oracle_py as orc
+    import mitrace_gb300 as mt
+
+    threads = os.cpu_count() or 1
+    o = orc.OracleScene(mt.PackedScene(scene), cfg, fast=fast)
+    H = cfg.height
+    rows = 4
+    r0 = H // 2 - rows // 2
+    t = time.perf_counter()
+    _, rays, samples = o.render(orc.RNG_MT19937, threads, r0, r0 + rows)
+    dt = time.perf_counter() - t
+    rows = max(4, min(H, int(rows * target_seconds / max(dt, 1e-3))))
+    r0 = max(0, H // 2 - rows // 2)
+    t = time.perf_counter()
+    _, rays, samples = o.render(orc.RNG_MT19937, threads, r0, r0 + rows)
+    dt = time.perf_counter() - t
+    return {
+        "value": rays / dt / 1e6,
+        "unit": "Mrays/s",
+        "cores": threads,
+        "kind": "port",
+        "sample": f"rows {r0}-{r0 + rows} of {cfg.width}x{H} at {cfg.samples} spp "
+                  f"({samples} samples, {rays} rays, {dt:.1f} s, mt19937 per 32x32 tile)",
+        "seconds": dt,
+        "msamples_s": samples / dt / 1e6,
+        "cpu": cpu_model(),
+    }
+
+
+def cpu_model():
+    try:
+        for ln in open("/proc/cpuinfo"):
+            if ln.lower().startswith(("model name", "cpu model")):
+                return ln.split(":", 1)[1].strip()
+        out = subprocess.run(["lscpu"], capture_output=True, text=True).stdout
+        for ln in out.splitlines():
+            if "Model name" in ln:
+                return ln.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    return os.uname().machine
+
+
+def run_reference(a):
+    import mitrace_gb300.scenes as S
+
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    scene, cfg = S.material_grid(width=a.width, height=a.height, samples=a.spp)
+    vals = []
+    base = None
+    for i in range(a.warmup + a.steps):
+        r = cpu_baseline(scene, cfg, a.cpu_seconds / 2 if i < a.warmup else a.cpu_seconds)
+        if i >= a.warmup:
+            vals.append(r["value"])
+            base = r
+    v = statistics.median(vals)
+    line = {
+        "impl": "reference", "metric": "Mrays/s", "value": v, "unit": "Mrays/s", "n_gpus": a.gpus,
+        "steps": a.steps, "warmup": a.warmup, "ms_per_step": base["seconds"] * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": workload_name(a), "width": a.width, "height": a.height, "spp": a.spp,
+                   "note": "reference's CPU path restated (cannot be built here); bounded band per step"},
+        "cpu_baseline": {k: base[k] for k in ("value", "unit", "cores", "kind", "sample")} | {"value": v},
+        "e2e": {"value": v, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# --------------------------------------------------------------------------- GPU arm
+def run_ours(a):
+    import ctypes as C
+
+    import numpy as np
+    import torch
+
+    import mitrace_gb300 as mt
+    from mitrace_gb300 import _abi as A
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    scene, cfg = mt.material_grid(width=a.width, height=a.height, samples=a.spp)
+    tr = mt.Tracer(scene, cfg)
+    stream = torch.cuda.current_stream(dev)
+    sptr = stream.cuda_stream
+    out = torch.empty((a.height, a.width, 3), dtype=torch.float32, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)  # 256 MiB > 129 MB L2
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    # untimed counting pass: traversal work per render (deterministic: fixed seed)
+    A.check(A.lib.mt_profile_enable(tr.handle, 0, 1), "profile")
+    tr.render_device(out.data_ptr(), sptr)
+    prof = A.mt_profile()
+    A.check(A.lib.mt_profile_read(tr.handle, C.byref(prof)), "profile_read")
+    ext = prof.stage[A.MT_STAGE_EXTEND]
+    shd = prof.stage[A.MT_STAGE_SHADOW]
+    rays_per_render = int(ext.rays + shd.rays)
+    counts = {"extend_rays": int(ext.rays), "shadow_rays": int(shd.rays), "extend_node_pops": int(ext.node_pops),
+              "extend_inner_pops": int(ext.inner_pops), "extend_tri_tests": int(ext.tri_tests),
+              "shadow_node_pops": int(shd.node_pops), "shadow_inner_pops": int(shd.inner_pops),
+              "shadow_tri_tests": int(shd.tri_tests)}
+    A.check(A.lib.mt_profile_enable(tr.handle, 0, 0), "profile")
+    A.check(A.lib.mt_profile_reset(tr.handle), "profile_reset")
+
+    for _ in range(a.warmup):
+        tr.render_device(out.data_ptr(), sptr)
+    torch.cuda.synchronize()
+    # the warm-up renders must count the same rays as the counting pass
+    st = tr.GetStats()
+    assert st.rays == rays_per_render, (st.rays, rays_per_render)
+
+    A.check(A.lib.mt_profile_enable(tr.handle, 1, 0), "profile")
+    A.check(A.lib.mt_profile_reset(tr.handle), "profile_reset")
+    clocks = ClockSampler(local)
+    launches0 = tr.kernel_launches()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(a.steps)]
+    barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    for i in range(a.steps):
+        flush.fill_(i & 0xFF)  # evict the scene from L2 between steps (not timed)
+        ev[i][0].record(stream)
+        tr.render_device(out.data_ptr(), sptr)
+        ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    clk = clocks.stop()
+    launches = tr.kernel_launches() - launches0
+    ms = sum(s.elapsed_time(e) for s, e in ev)
+    A.check(A.lib.mt_profile_read(tr.handle, C.byref(prof)), "profile_read")
+    st = tr.GetStats()
+    assert st.rays == rays_per_render
+    ms_t = torch.tensor([ms], dtype=torch.float64, device=dev)
+    if world > 1:
+        torch.distributed.all_reduce(ms_t, op=torch.distributed.ReduceOp.MAX)
+    ms_max = float(ms_t.item())
+    total_rays = rays_per_render * a.steps * world
+    value = total_rays / (ms_max / 1e3) / 1e6
+
+    # roofline of the extend (closest-hit traversal) kernel
+    ext_t = prof.stage[1]
+    per_launch_ms = ext_t.milliseconds / max(1, ext_t.launches)
+    alg_bytes_render = 64 * counts["extend_inner_pops"] + 40 * counts["extend_tri_tests"] + 48 * counts["extend_rays"]
+    launches_per_render = ext_t.launches / a.steps
+    bytes_per_launch = alg_bytes_render / launches_per_render
+    achieved = bytes_per_launch / (per_launch_ms / 1e3) / 1e9
+    peak, peak_src = FALLBACK_HBM_GBS, "fallback"
+    if PEAKS_FILE.exists():
+        try:
+            peak, peak_src = float(json.loads(PEAKS_FILE.read_text())["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    traffic = None
+    if TRAFFIC_FILE.exists():
+        try:
+            t = json.loads(TRAFFIC_FILE.read_text())
+            if t.get("workload") == workload_name(a):
+                traffic = t.get("dram_bytes_per_launch")
+        except Exception:
+            pass
+    stage_ms = {n: round(prof.stage[i].milliseconds / a.steps, 3) for i, n in
+                enumerate(["raygen", "extend", "shade", "shadow", "finalize", "resolve"])}
+
+    # e2e through the host API
+    e2e_steps = a.e2e_steps if a.e2e_steps is not None else max(1, min(a.steps, 3))
+    tr.close()
+    del out
+    torch.cuda.empty_cache()
+    img = np.empty((a.height, a.width, 3), dtype=np.float32)
+    t_e2e = []
+    for i in range(e2e_steps + 1):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        with mt.Tracer(scene, cfg) as t2:
+            t2.StartRender()
+            img[...] = t2.WaitForRender()
+        torch.cuda.synchronize()
+        if i > 0:  # the first one is a warm-up
+            t_e2e.append(time.perf_counter() - t0)
+    e2e_s = sum(t_e2e)
+    e2e_value = rays_per_render * len(t_e2e) / e2e_s / 1e6
+
+    if rank != 0:
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return
+    line = {
+        "metric": "Mrays/s",
+        "value": value,
+        "unit": "Mrays/s",
+        "n_gpus": world,
+        "steps": a.steps,
+        "warmup": a.warmup,
+        "ms_per_step": ms_max / a.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic",
+        "config": {
+            "workload": workload_name(a), "width": a.width, "height": a.height, "spp": a.spp, "bounces": cfg.bounces,
+            "triangles": scene.num_triangles, "instances": len(scene.instances), "lights": len(scene.lights),
+            "rays_per_step": rays_per_render, "samples_per_step": a.width * a.height * a.spp,
+            "l2": "256 MiB buffer written between timed steps (not timed)",
+            "parallelism": "replicas" if world > 1 else "single GPU",
+        },
+        "msamples_per_s": a.width * a.height * a.spp * a.steps * world / (ms_max / 1e3) / 1e6,
+        "e2e": {"value": e2e_value, "unit": "Mrays/s", "h2d_bytes_per_step": int(scene.nbytes()),
+                "d2h_bytes_per_step": int(img.nbytes), "seconds_per_step": e2e_s / len(t_e2e)},
+        "gpu_launches": int(launches),
+        "roofline": {"bound": "hbm", "kernel": "k_extend", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic, "peak_source": peak_src,
+                     "alg_bytes_per_launch": bytes_per_launch, "launch_ms": per_launch_ms,
+                     "launches": int(ext_t.launches)},
+        "traversal_counts_per_step": counts,
+        "stage_ms_per_step": stage_ms,
+        "clocks": clk,
+    }
+    if not a.no_cpu_baseline:
+        cb = cpu_baseline(scene, cfg, a.cpu_seconds)
+        line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        line["cpu_baseline"]["cpu"] = cb["cpu"]
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    a = parse()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_ours(a)
+
+
+if __name__ == "__main__":
+    main()

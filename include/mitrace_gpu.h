@@ -260,6 +260,10 @@ typedef struct mt_hit {
 #define MT_QUERY_CLOSEST 0
 #define MT_QUERY_ANY 1          /* writes occluded (1) / visible (0) into hit.instance */
 #define MT_QUERY_CLOSEST_COUNT 2 /* closest hit plus bvh/triangle test counters */
+/* Closest hit; bv_index / bvh_tests / tri_tests then hold the inner-node
+ * expansions, BVH pops and triangle tests summed over ALL instances the ray
+ * visited (the work the traversal did, not only the winner's counters). */
+#define MT_QUERY_CLOSEST_TOTALS 3
 
 /* Host buffers: copies rays in, runs the query, copies hits out (blocking). */
 mt_status mt_trace_rays(mt_handle* h, const mt_ray* rays, uint64_t n, mt_hit* hits, int query);
@@ -308,6 +312,36 @@ void mt_bvh_free(mt_bvh_node* nodes, uint32_t* indices);
 /* ------------------------------------------------------------------------ */
 /* Diagnostics.                                                             */
 /* ------------------------------------------------------------------------ */
+
+/* Per-stage profile of the wavefront render.  Stages are MT_STAGE_*. */
+typedef struct mt_stage_profile {
+    uint64_t launches;
+    double milliseconds; /* summed CUDA-event time of the stage's launches   */
+    uint64_t rays;       /* rays the stage traced (extend / shadow)          */
+    uint64_t node_pops;  /* BVH stack pops, all instances (bvhTests)         */
+    uint64_t inner_pops; /* pops that expanded an inner node (2 child boxes) */
+    uint64_t tri_tests;  /* triangle tests, all instances (triangleTests)    */
+} mt_stage_profile;
+
+#define MT_STAGE_RAYGEN 0
+#define MT_STAGE_EXTEND 1
+#define MT_STAGE_SHADE 2
+#define MT_STAGE_SHADOW 3
+#define MT_STAGE_FINALIZE 4
+#define MT_STAGE_RESOLVE 5
+#define MT_NUM_STAGES 6
+
+typedef struct mt_profile {
+    mt_stage_profile stage[MT_NUM_STAGES];
+} mt_profile;
+
+/* timing: record CUDA events around every stage launch of later renders.
+ * counting: later renders use traversal kernels that also tally node pops,
+ * inner pops and triangle tests (slower; meant for an untimed pass). */
+mt_status mt_profile_enable(mt_handle* h, int timing, int counting);
+/* Synchronizes the handle's render and returns the accumulated profile. */
+mt_status mt_profile_read(mt_handle* h, mt_profile* out);
+mt_status mt_profile_reset(mt_handle* h);
 
 const char* mt_last_error(void);
 int mt_abi_version(void);

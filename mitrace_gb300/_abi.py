@@ -168,6 +168,26 @@ class mt_hit(C.Structure):
     ]
 
 
+class mt_stage_profile(C.Structure):
+    _fields_ = [
+        ("launches", C.c_uint64),
+        ("milliseconds", C.c_double),
+        ("rays", C.c_uint64),
+        ("node_pops", C.c_uint64),
+        ("inner_pops", C.c_uint64),
+        ("tri_tests", C.c_uint64),
+    ]
+
+
+MT_STAGE_RAYGEN, MT_STAGE_EXTEND, MT_STAGE_SHADE, MT_STAGE_SHADOW, MT_STAGE_FINALIZE, MT_STAGE_RESOLVE = range(6)
+MT_NUM_STAGES = 6
+MT_QUERY_CLOSEST_TOTALS = 3
+
+
+class mt_profile(C.Structure):
+    _fields_ = [("stage", mt_stage_profile * MT_NUM_STAGES)]
+
+
 class mt_brdf_query(C.Structure):
     _fields_ = [
         ("L", C.c_float * 3),
@@ -204,6 +224,9 @@ PROTOTYPES = [
     ("mt_last_error", C.c_char_p, []),
     ("mt_abi_version", C.c_int, []),
     ("mt_kernel_launches", C.c_uint64, [_VP]),
+    ("mt_profile_enable", C.c_int, [_VP, C.c_int, C.c_int]),
+    ("mt_profile_read", C.c_int, [_VP, C.POINTER(mt_profile)]),
+    ("mt_profile_reset", C.c_int, [_VP]),
 ]
 
 

@@ -100,6 +100,10 @@ template <class T>
 struct DevArray {
     T* p = nullptr;
     size_t n = 0;
+    DevArray() = default;
+    DevArray(const DevArray&) = delete;
+    DevArray& operator=(const DevArray&) = delete;
+    DevArray(DevArray&& o) noexcept : p(o.p), n(o.n) { o.p = nullptr; o.n = 0; }
     ~DevArray() { reset(); }
     void reset()
     {
@@ -192,10 +196,18 @@ struct mt_handle {
     DevArray<float4> sq;         // 3 float4 planes
     DevArray<uint32_t> queues;   // 2 planes
     DevArray<uint32_t> counts;
-    DevArray<unsigned long long> rays;
+    DevArray<unsigned long long> rays;  // [0] extension, [1] shadow
     DevArray<float> samples;     // 3 planes
     DevArray<float> image;
-    unsigned long long* rays_host = nullptr;  // pinned
+    unsigned long long* rays_host = nullptr;  // pinned, 2 words
+    cudaEvent_t render_done = nullptr;        // end of the last synchronous render
+    bool render_pending = false;
+    // profiling
+    Profiler prof;
+    DevArray<unsigned long long> prof_counts;  // 6 words
+    double prof_ms[MT_NUM_STAGES] = {};
+    uint64_t prof_launches[MT_NUM_STAGES] = {};
+    uint64_t prof_rays[2] = {};
     // query scratch
     DevArray<mt_ray> qrays;
     DevArray<mt_hit> qhits;
@@ -217,6 +229,7 @@ struct mt_handle {
     {
         if (worker.joinable()) worker.join();
         if (rays_host) cudaFreeHost(rays_host);
+        if (render_done) cudaEventDestroy(render_done);
         if (stream) cudaStreamDestroy(stream);
     }
 };
@@ -493,10 +506,12 @@ mt_status ensure_wave(mt_handle* h)
     MT_CUDA(h->sq.alloc(3ull * batch));
     MT_CUDA(h->queues.alloc(2ull * batch));
     MT_CUDA(h->counts.alloc(4));
-    MT_CUDA(h->rays.alloc(1));
+    MT_CUDA(h->rays.alloc(2));
     MT_CUDA(h->samples.alloc(3ull * h->band_capacity));
     MT_CUDA(h->image.alloc(npix * 3));
-    MT_CUDA(cudaMallocHost(reinterpret_cast<void**>(&h->rays_host), sizeof(unsigned long long)));
+    MT_CUDA(cudaMallocHost(reinterpret_cast<void**>(&h->rays_host), 2 * sizeof(unsigned long long)));
+    h->rays_host[0] = h->rays_host[1] = 0;
+    MT_CUDA(cudaEventCreateWithFlags(&h->render_done, cudaEventDisableTiming));
     return MT_OK;
 }
 
@@ -543,7 +558,8 @@ mt_status render_into(mt_handle* h, float* out, cudaStream_t st, bool sync_each_
     if (rc != MT_OK) return rc;
     const mt_config& c = h->cfg;
     const WaveViews v = views(h);
-    MT_CUDA(cudaMemsetAsync(h->rays.p, 0, sizeof(unsigned long long), st));
+    MT_CUDA(cudaMemsetAsync(h->rays.p, 0, 2 * sizeof(unsigned long long), st));
+    Profiler* prof = (h->prof.timing || h->prof.counting) ? &h->prof : nullptr;
     const uint64_t rows_per_band = h->band_capacity / (static_cast<uint64_t>(c.width) * c.samples);
     uint64_t total_batches = 0;
     for (uint64_t r0 = 0; r0 < c.height; r0 += rows_per_band) {
@@ -564,20 +580,36 @@ mt_status render_into(mt_handle* h, float* out, cudaStream_t st, bool sync_each_
                 return set_err(MT_ERR_KILLED, "render killed");
             }
             const uint32_t n = static_cast<uint32_t>(std::min<uint64_t>(h->batch, paths - g0));
-            MT_CUDA(launch_batch(h->S, v.P, v.SQ, v.W, g0, n, band_pix, pix_base, st, &launches));
+            MT_CUDA(launch_batch(h->S, v.P, v.SQ, v.W, g0, n, band_pix, pix_base, st, &launches, prof));
             if (sync_each_batch) {
-                MT_CUDA(cudaMemcpyAsync(h->rays_host, h->rays.p, sizeof(unsigned long long),
+                MT_CUDA(cudaMemcpyAsync(h->rays_host, h->rays.p, 2 * sizeof(unsigned long long),
                                         cudaMemcpyDeviceToHost, st));
                 MT_CUDA(cudaStreamSynchronize(st));
-                h->stat_rays = *h->rays_host;
+                h->stat_rays = h->rays_host[0] + h->rays_host[1];
                 h->stat_samples += n;
             }
             h->work_done += 1;
         }
-        MT_CUDA(launch_resolve(h->S, v.W, band_pix, pix_base, out, st));
+        MT_CUDA(launch_resolve(h->S, v.W, band_pix, pix_base, out, st, prof));
         ++launches;
     }
+    MT_CUDA(cudaMemcpyAsync(h->rays_host, h->rays.p, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+    MT_CUDA(cudaEventRecord(h->render_done, st));
+    h->render_pending = true;
     h->launches += launches;
+    return MT_OK;
+}
+
+// Folds the finished render's ray counters (and profile) into the handle.
+mt_status settle_render(mt_handle* h)
+{
+    if (!h->render_pending) return MT_OK;
+    MT_CUDA(cudaEventSynchronize(h->render_done));
+    h->render_pending = false;
+    h->stat_rays = h->rays_host[0] + h->rays_host[1];
+    h->prof_rays[0] += h->rays_host[0];
+    h->prof_rays[1] += h->rays_host[1];
+    if (h->prof.timing) MT_CUDA(h->prof.collect(h->prof_ms, h->prof_launches));
     return MT_OK;
 }
 
@@ -589,12 +621,11 @@ void worker_main(mt_handle* h)
         cudaError_t e = cudaStreamSynchronize(h->stream);
         if (e != cudaSuccess) rc = set_err(MT_ERR_CUDA, cudaGetErrorString(e));
     }
+    if (rc == MT_OK) rc = settle_render(h);
     if (rc == MT_OK) {
         int flag = 0;
         if (cudaMemcpy(&flag, h->error_flag.p, sizeof(int), cudaMemcpyDeviceToHost) == cudaSuccess && flag)
             rc = set_err(MT_ERR_INVALID, "device error flag set (traversal stack overflow)");
-        if (cudaMemcpy(h->rays_host, h->rays.p, 8, cudaMemcpyDeviceToHost) == cudaSuccess)
-            h->stat_rays = *h->rays_host;
     }
     if (rc != MT_OK) h->worker_err = g_err;
     h->result = rc;
@@ -725,6 +756,8 @@ mt_status mt_kill(mt_handle* h)
 mt_status mt_get_stats(const mt_handle* h, mt_stats* out)
 {
     if (check_handle(h) != MT_OK || !out) return set_err(MT_ERR_INVALID, "null argument");
+    if (!h->running && h->render_pending && cudaEventQuery(h->render_done) == cudaSuccess)
+        settle_render(const_cast<mt_handle*>(h));
     mt_stats s{};
     const double el = h->started ? std::chrono::duration<double>(std::chrono::steady_clock::now() - h->t0).count() : 0.0;
     s.progress = static_cast<float>(static_cast<double>(h->work_done.load()) / static_cast<double>(h->work_total.load()));
@@ -740,6 +773,61 @@ mt_status mt_get_stats(const mt_handle* h, mt_stats* out)
 int mt_is_done(const mt_handle* h) { return h && h->started && h->done ? 1 : 0; }
 
 uint64_t mt_kernel_launches(const mt_handle* h) { return h ? h->launches.load() : 0; }
+
+mt_status mt_profile_enable(mt_handle* h, int timing, int counting)
+{
+    if (check_handle(h) != MT_OK) return MT_ERR_INVALID;
+    if (h->running) return set_err(MT_ERR_STATE, "a render is running");
+    if (counting && !h->prof_counts.p) {
+        MT_CUDA(h->prof_counts.alloc(6));
+        MT_CUDA(cudaMemset(h->prof_counts.p, 0, 6 * sizeof(unsigned long long)));
+    }
+    h->prof.timing = timing != 0;
+    h->prof.counting = counting != 0;
+    h->prof.d_counts = h->prof_counts.p;
+    return MT_OK;
+}
+
+mt_status mt_profile_reset(mt_handle* h)
+{
+    if (check_handle(h) != MT_OK) return MT_ERR_INVALID;
+    if (h->running) return set_err(MT_ERR_STATE, "a render is running");
+    mt_status rc = settle_render(h);
+    if (rc != MT_OK) return rc;
+    for (int i = 0; i < MT_NUM_STAGES; ++i) {
+        h->prof_ms[i] = 0.0;
+        h->prof_launches[i] = 0;
+    }
+    h->prof_rays[0] = h->prof_rays[1] = 0;
+    if (h->prof_counts.p) MT_CUDA(cudaMemset(h->prof_counts.p, 0, 6 * sizeof(unsigned long long)));
+    return MT_OK;
+}
+
+mt_status mt_profile_read(mt_handle* h, mt_profile* out)
+{
+    if (check_handle(h) != MT_OK || !out) return set_err(MT_ERR_INVALID, "null argument");
+    if (h->running) return set_err(MT_ERR_STATE, "a render is running");
+    mt_status rc = settle_render(h);
+    if (rc != MT_OK) return rc;
+    std::memset(out, 0, sizeof(*out));
+    for (int i = 0; i < MT_NUM_STAGES; ++i) {
+        out->stage[i].launches = h->prof_launches[i];
+        out->stage[i].milliseconds = h->prof_ms[i];
+    }
+    out->stage[MT_STAGE_EXTEND].rays = h->prof_rays[0];
+    out->stage[MT_STAGE_SHADOW].rays = h->prof_rays[1];
+    if (h->prof_counts.p) {
+        unsigned long long c[6];
+        MT_CUDA(cudaMemcpy(c, h->prof_counts.p, sizeof(c), cudaMemcpyDeviceToHost));
+        out->stage[MT_STAGE_EXTEND].node_pops = c[0];
+        out->stage[MT_STAGE_EXTEND].inner_pops = c[1];
+        out->stage[MT_STAGE_EXTEND].tri_tests = c[2];
+        out->stage[MT_STAGE_SHADOW].node_pops = c[3];
+        out->stage[MT_STAGE_SHADOW].inner_pops = c[4];
+        out->stage[MT_STAGE_SHADOW].tri_tests = c[5];
+    }
+    return MT_OK;
+}
 
 mt_status mt_render_device(mt_handle* h, float* d_rgb_out, void* cuda_stream)
 {
@@ -757,7 +845,7 @@ mt_status mt_trace_rays_device(mt_handle* h, const mt_ray* d_rays, uint64_t n, m
 {
     if (check_handle(h) != MT_OK) return MT_ERR_INVALID;
     if (n && (!d_rays || !d_hits)) return set_err(MT_ERR_INVALID, "null ray or hit buffer");
-    if (query != MT_QUERY_CLOSEST && query != MT_QUERY_ANY && query != MT_QUERY_CLOSEST_COUNT)
+    if (query < MT_QUERY_CLOSEST || query > MT_QUERY_CLOSEST_TOTALS)
         return set_err(MT_ERR_INVALID, "unknown query");
     if ((reinterpret_cast<uintptr_t>(d_rays) | reinterpret_cast<uintptr_t>(d_hits)) & 15)
         return set_err(MT_ERR_INVALID, "ray and hit buffers must be 16-byte aligned");

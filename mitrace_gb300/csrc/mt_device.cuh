@@ -230,7 +230,7 @@ struct LocalHit {
     float t, u, v;
     uint32_t slot;     // winning slot (triangle id is in its v0.w)
     uint32_t bv;       // leaf node index (reference node numbering)
-    uint32_t bvh_tests, tri_tests;
+    uint32_t bvh_tests, tri_tests, inner;
 };
 
 __device__ __forceinline__ uint32_t f2u(float f) { return __float_as_uint(f); }
@@ -291,6 +291,7 @@ __device__ __forceinline__ void traverse_bvh(const DevScene& S, const DevMesh& m
                 }
             }
         } else {
+            if (COUNT) ++h.inner;
             const float4 a0 = __ldg(nodes + 2 * na), a1 = __ldg(nodes + 2 * na + 1);
             const float4 b0 = __ldg(nodes + 2 * nb), b1 = __ldg(nodes + 2 * nb + 1);
             const float da = slab(o, inv, xyz(a0), xyz(a1));
@@ -350,6 +351,7 @@ __device__ __forceinline__ void traverse_linear(const DevScene& S, const DevMesh
 struct SceneHit {
     bool hit;
     uint32_t inst, tri, bv, bvh_tests, tri_tests;
+    uint32_t tot_pops, tot_inner, tot_tris;  // summed over all visited instances (COUNT only)
     float u, v, dist;
     f3 world_pos;
 };
@@ -366,6 +368,7 @@ __device__ __forceinline__ SceneHit intersect_scene(const DevScene& S, f3 o, f3 
     best.hit = false;
     best.dist = FLT_MAX;
     best.bvh_tests = best.tri_tests = 0;
+    best.tot_pops = best.tot_inner = best.tot_tris = 0;
     best.inst = best.tri = best.bv = 0;
     best.u = best.v = 0.0f;
     best.world_pos = splat(0.0f);
@@ -386,7 +389,7 @@ __device__ __forceinline__ SceneHit intersect_scene(const DevScene& S, f3 o, f3 
         h.u = h.v = 0.0f;
         h.slot = 0;
         h.bv = 0;
-        h.bvh_tests = h.tri_tests = 0;
+        h.bvh_tests = h.tri_tests = h.inner = 0;
         bool stopped = false;
         auto stop = [&](float t) -> bool {
             if (!ANY) return false;
@@ -399,17 +402,22 @@ __device__ __forceinline__ SceneHit intersect_scene(const DevScene& S, f3 o, f3 
             traverse_bvh<COUNT>(S, m, lo, ld, h, stop, stopped);
         else
             traverse_linear<COUNT>(S, m, lo, ld, h, stop, stopped);
+        if (COUNT) {
+            best.tot_pops += h.bvh_tests;
+            best.tot_inner += h.inner;
+            best.tot_tris += h.tri_tests;
+        }
         if (ANY && stopped) {
             best.hit = true;
             best.inst = ii;
             return best;
         }
-        if (!(h.t < FLT_MAX)) continue;
+        if (ANY || !(h.t < FLT_MAX)) continue;
 #pragma unroll
         for (int k = 0; k < 16; ++k) model[k] = __ldg(&I.model[k]);
         const f3 wp = xform_point(model, lo + h.t * ld);
         const float wd = length(wp - o);
-        if (!ANY && wd < best.dist) {
+        if (wd < best.dist) {
             best.hit = true;
             best.dist = wd;
             best.world_pos = wp;

@@ -49,8 +49,8 @@ __global__ void __launch_bounds__(128) k_trace(DevScene S, const mt_ray* __restr
             h.instance = sh.hit ? 1u : 0u;
             h.triangle = h.bv_index = h.bvh_tests = h.tri_tests = 0;
         } else {
-            const SceneHit sh =
-                intersect_scene<QUERY == MT_QUERY_CLOSEST_COUNT, false>(S, xyz(a), xyz(b), 0.0f);
+            constexpr bool kCount = QUERY == MT_QUERY_CLOSEST_COUNT || QUERY == MT_QUERY_CLOSEST_TOTALS;
+            const SceneHit sh = intersect_scene<kCount, false>(S, xyz(a), xyz(b), 0.0f);
             if (sh.hit) {
                 h.distance = sh.dist;
                 h.u = sh.u;
@@ -64,6 +64,11 @@ __global__ void __launch_bounds__(128) k_trace(DevScene S, const mt_ray* __restr
                 h.distance = h.u = h.v = 0.0f;
                 h.instance = MT_NO_HIT;
                 h.triangle = h.bv_index = h.bvh_tests = h.tri_tests = 0;
+            }
+            if (QUERY == MT_QUERY_CLOSEST_TOTALS) {
+                h.bv_index = sh.tot_inner;
+                h.bvh_tests = sh.tot_pops;
+                h.tri_tests = sh.tot_tris;
             }
         }
         float4* dst = reinterpret_cast<float4*>(hits + i);
@@ -136,10 +141,31 @@ __global__ void __launch_bounds__(256) k_raygen(DevScene S, PathState P, BatchIn
     }
 }
 
+// Adds this thread's traversal totals to cnt[0..2] (pops, inner pops, tri tests)
+// with one atomic per warp.
+__device__ __forceinline__ void flush_counts(unsigned long long* cnt, uint32_t pops, uint32_t inner,
+                                             uint32_t tris)
+{
+    unsigned long long a = pops, b = inner, c = tris;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_down_sync(0xffffffffu, a, o);
+        b += __shfl_down_sync(0xffffffffu, b, o);
+        c += __shfl_down_sync(0xffffffffu, c, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(cnt + 0, a);
+        atomicAdd(cnt + 1, b);
+        atomicAdd(cnt + 2, c);
+    }
+}
+
+template <bool COUNT>
 __global__ void __launch_bounds__(128) k_extend(DevScene S, PathState P,
                                                 const uint32_t* __restrict__ q,
                                                 uint32_t* counts, int cur,
-                                                unsigned long long* rays)
+                                                unsigned long long* rays,
+                                                unsigned long long* cnt)
 {
     const uint32_t n = counts[cur];
     if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -147,10 +173,16 @@ __global__ void __launch_bounds__(128) k_extend(DevScene S, PathState P,
         counts[2] = 0;
         atomicAdd(rays, static_cast<unsigned long long>(n));
     }
+    uint32_t pops = 0, inner = 0, tris = 0;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const uint32_t p = q[i];
         const float4 o = P.ro[p], d = P.rd[p];
-        const SceneHit h = intersect_scene<false, false>(S, xyz(o), xyz(d), 0.0f);
+        const SceneHit h = intersect_scene<COUNT, false>(S, xyz(o), xyz(d), 0.0f);
+        if (COUNT) {
+            pops += h.tot_pops;
+            inner += h.tot_inner;
+            tris += h.tot_tris;
+        }
         if (h.hit) {
             P.hitA[p] = make_float4(h.world_pos.x, h.world_pos.y, h.world_pos.z, h.dist);
             P.hitB[p] = make_uint4(h.inst, h.tri, __float_as_uint(h.u), __float_as_uint(h.v));
@@ -158,6 +190,7 @@ __global__ void __launch_bounds__(128) k_extend(DevScene S, PathState P,
             P.hitB[p] = make_uint4(MT_NO_HIT, 0u, 0u, 0u);
         }
     }
+    if (COUNT) flush_counts(cnt, pops, inner, tris);
 }
 
 __device__ __forceinline__ f3 ld4(const float4* p, uint32_t i)
@@ -330,15 +363,23 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, PathState P, ShadowQu
     }
 }
 
+template <bool COUNT>
 __global__ void __launch_bounds__(128) k_shadow(DevScene S, PathState P, ShadowQueue SQ,
                                                 const uint32_t* counts,
-                                                unsigned long long* rays)
+                                                unsigned long long* rays,
+                                                unsigned long long* cnt)
 {
     const uint32_t n = counts[2];
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(rays, static_cast<unsigned long long>(n));
+    uint32_t pops = 0, inner = 0, tris = 0;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const float4 o = SQ.o[i], d = SQ.d[i];
-        const SceneHit h = intersect_scene<false, true>(S, xyz(o), xyz(d), o.w);
+        const SceneHit h = intersect_scene<COUNT, true>(S, xyz(o), xyz(d), o.w);
+        if (COUNT) {
+            pops += h.tot_pops;
+            inner += h.tot_inner;
+            tris += h.tot_tris;
+        }
         if (h.hit) continue;
         const float4 c = SQ.c[i];
         const uint32_t p = __float_as_uint(d.w);
@@ -346,6 +387,7 @@ __global__ void __launch_bounds__(128) k_shadow(DevScene S, PathState P, ShadowQ
         const float4 a = acc[p];
         acc[p] = make_float4(__fadd_rn(a.x, c.x), __fadd_rn(a.y, c.y), __fadd_rn(a.z, c.z), 0.0f);
     }
+    if (COUNT) flush_counts(cnt, pops, inner, tris);
 }
 
 __global__ void __launch_bounds__(256) k_finalize(DevScene S, PathState P, BatchInfo B,
@@ -441,6 +483,7 @@ cudaError_t launch_trace(const DevScene& S, const mt_ray* rays, uint64_t n, mt_h
     switch (query) {
         case MT_QUERY_ANY: k_trace<MT_QUERY_ANY><<<g, 128, 0, st>>>(S, rays, n, hits); break;
         case MT_QUERY_CLOSEST_COUNT: k_trace<MT_QUERY_CLOSEST_COUNT><<<g, 128, 0, st>>>(S, rays, n, hits); break;
+        case MT_QUERY_CLOSEST_TOTALS: k_trace<MT_QUERY_CLOSEST_TOTALS><<<g, 128, 0, st>>>(S, rays, n, hits); break;
         default: k_trace<MT_QUERY_CLOSEST><<<g, 128, 0, st>>>(S, rays, n, hits); break;
     }
     return cudaGetLastError();
@@ -453,33 +496,98 @@ cudaError_t launch_brdf(const mt_brdf_query* q, uint64_t n, mt_brdf_result* out,
     return cudaGetLastError();
 }
 
+void Profiler::begin(int stage, cudaStream_t st)
+{
+    if (!timing) return;
+    if (used + 2 > pool.size()) {
+        cudaEvent_t a, b;
+        cudaEventCreate(&a);
+        cudaEventCreate(&b);
+        pool.push_back(a);
+        pool.push_back(b);
+    }
+    cudaEventRecord(pool[used], st);
+    marks.push_back({stage, used});
+    used += 2;
+}
+
+void Profiler::end(int stage, cudaStream_t st)
+{
+    (void)stage;
+    if (!timing) return;
+    cudaEventRecord(pool[marks.back().second + 1], st);
+}
+
+cudaError_t Profiler::collect(double* ms, uint64_t* launches)
+{
+    for (const auto& m : marks) {
+        cudaError_t e = cudaEventSynchronize(pool[m.second + 1]);
+        if (e != cudaSuccess) return e;
+        float t = 0.0f;
+        e = cudaEventElapsedTime(&t, pool[m.second], pool[m.second + 1]);
+        if (e != cudaSuccess) return e;
+        ms[m.first] += t;
+        launches[m.first] += 1;
+    }
+    marks.clear();
+    used = 0;
+    return cudaSuccess;
+}
+
+Profiler::~Profiler()
+{
+    for (cudaEvent_t e : pool) cudaEventDestroy(e);
+}
+
 cudaError_t launch_batch(const DevScene& S, const PathState& P, const ShadowQueue& SQ,
                          const WaveBuffers& W, uint64_t g0, uint32_t n, uint32_t band_pix,
-                         uint32_t pix_base, cudaStream_t st, uint64_t* launches)
+                         uint32_t pix_base, cudaStream_t st, uint64_t* launches, Profiler* prof)
 {
     BatchInfo B{g0, n, band_pix, pix_base};
     const unsigned gw = grid_for(n, 128, 16);
+    const bool count = prof && prof->counting;
+    unsigned long long* cnt = prof ? prof->d_counts : nullptr;
+    auto begin = [&](int s) { if (prof) prof->begin(s, st); };
+    auto end = [&](int s) { if (prof) prof->end(s, st); };
+    begin(MT_STAGE_RAYGEN);
     k_raygen<<<grid_for(n, 256, 8), 256, 0, st>>>(S, P, B, W.q[0], W.counts);
+    end(MT_STAGE_RAYGEN);
     uint64_t l = 1;
     int cur = 0;
     for (uint32_t b = 0; b < S.bounces; ++b) {
-        k_extend<<<gw, 128, 0, st>>>(S, P, W.q[cur], W.counts, cur, W.rays);
+        begin(MT_STAGE_EXTEND);
+        if (count)
+            k_extend<true><<<gw, 128, 0, st>>>(S, P, W.q[cur], W.counts, cur, W.rays, cnt);
+        else
+            k_extend<false><<<gw, 128, 0, st>>>(S, P, W.q[cur], W.counts, cur, W.rays, cnt);
+        end(MT_STAGE_EXTEND);
+        begin(MT_STAGE_SHADE);
         k_shade<<<gw, 128, 0, st>>>(S, P, SQ, B, b, W.q[cur], W.q[cur ^ 1], W.counts, cur);
-        k_shadow<<<gw, 128, 0, st>>>(S, P, SQ, W.counts, W.rays);
+        end(MT_STAGE_SHADE);
+        begin(MT_STAGE_SHADOW);
+        if (count)
+            k_shadow<true><<<gw, 128, 0, st>>>(S, P, SQ, W.counts, W.rays + 1, cnt ? cnt + 3 : nullptr);
+        else
+            k_shadow<false><<<gw, 128, 0, st>>>(S, P, SQ, W.counts, W.rays + 1, nullptr);
+        end(MT_STAGE_SHADOW);
         l += 3;
         cur ^= 1;
     }
+    begin(MT_STAGE_FINALIZE);
     k_finalize<<<grid_for(n, 256, 8), 256, 0, st>>>(S, P, B, W.sr, W.sg, W.sb);
+    end(MT_STAGE_FINALIZE);
     ++l;
     if (launches) *launches += l;
     return cudaGetLastError();
 }
 
 cudaError_t launch_resolve(const DevScene& S, const WaveBuffers& W, uint32_t band_pix, uint32_t pix_base,
-                           float* out, cudaStream_t st)
+                           float* out, cudaStream_t st, Profiler* prof)
 {
+    if (prof) prof->begin(MT_STAGE_RESOLVE, st);
     k_resolve<<<grid_for(band_pix, 256, 8), 256, 0, st>>>(W.sr, W.sg, W.sb, band_pix, S.spp, pix_base,
                                                           S.firefly_enable, S.firefly_k, out);
+    if (prof) prof->end(MT_STAGE_RESOLVE, st);
     return cudaGetLastError();
 }
 

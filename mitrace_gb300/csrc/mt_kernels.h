@@ -5,6 +5,7 @@
 
 #include <cstdint>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/mitrace_gpu.h"
@@ -39,10 +40,24 @@ struct ShadowQueue {
 struct WaveBuffers {
     uint32_t* q[2];                // ping-pong queues of live path indices
     uint32_t* counts;              // [0],[1] queue sizes, [2] shadow-queue size
-    unsigned long long* rays;      // rays traced (extension + shadow)
+    unsigned long long* rays;      // [0] extension rays, [1] shadow rays traced
     float* sr;                     // per-sample tonemapped R, sample-major in a band
     float* sg;
     float* sb;
+};
+
+// Optional per-stage CUDA-event timing and traversal counters of a render.
+struct Profiler {
+    bool timing = false;
+    bool counting = false;
+    unsigned long long* d_counts = nullptr;  // [extend pops, inner, tris, shadow pops, inner, tris]
+    std::vector<cudaEvent_t> pool;
+    std::vector<std::pair<int, size_t>> marks;  // (stage, index of start event in pool)
+    size_t used = 0;
+    void begin(int stage, cudaStream_t st);
+    void end(int stage, cudaStream_t st);
+    cudaError_t collect(double* ms, uint64_t* launches);
+    ~Profiler();
 };
 
 cudaError_t launch_trace(const DevScene& S, const mt_ray* rays, uint64_t n, mt_hit* hits, int query,
@@ -50,9 +65,9 @@ cudaError_t launch_trace(const DevScene& S, const mt_ray* rays, uint64_t n, mt_h
 cudaError_t launch_brdf(const mt_brdf_query* q, uint64_t n, mt_brdf_result* out, cudaStream_t st);
 cudaError_t launch_batch(const DevScene& S, const PathState& P, const ShadowQueue& SQ,
                          const WaveBuffers& W, uint64_t g0, uint32_t n, uint32_t band_pix,
-                         uint32_t pix_base, cudaStream_t st, uint64_t* launches);
+                         uint32_t pix_base, cudaStream_t st, uint64_t* launches, Profiler* prof);
 cudaError_t launch_resolve(const DevScene& S, const WaveBuffers& W, uint32_t band_pix,
-                           uint32_t pix_base, float* out, cudaStream_t st);
+                           uint32_t pix_base, float* out, cudaStream_t st, Profiler* prof);
 
 // Host BVH builder (mt_bvh.cpp).
 int build_bvh(const float* positions, uint32_t num_triangles, uint32_t max_triangles,

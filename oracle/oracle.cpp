@@ -557,7 +557,7 @@ void tris_linear(const Mesh& m, V3 o, V3 d, float& dist, float& bu, float& bv, u
 // IntersectTrianglesBVH, Intersect.cpp:47-141.  Stack DFS keyed on the box
 // EXIT distance with 0.1 slack; the nearer child is pushed last.
 void tris_bvh(const Mesh& m, V3 o, V3 d, float& dist, float& bu, float& bv, uint32_t& bvIdx,
-              uint32_t& tri, uint32_t& bvhTests, uint32_t& triTests,
+              uint32_t& tri, uint32_t& bvhTests, uint32_t& triTests, uint32_t& innerPops,
               std::vector<StackEntry>& stack)
 {
     const float minDelta = 0.1f;
@@ -593,6 +593,7 @@ void tris_bvh(const Mesh& m, V3 o, V3 d, float& dist, float& bu, float& bv, uint
                 }
             }
         } else {
+            ++innerPops;
             const float da = box(nodes[n.a]);
             const float db = box(nodes[n.b]);
             const bool pa = da >= 0.0f && da <= dist + minDelta;
@@ -616,7 +617,7 @@ void tris_bvh(const Mesh& m, V3 o, V3 d, float& dist, float& bu, float& bv, uint
 
 // IntersectMeshInstance, Intersect.cpp:143-199
 bool intersect_instance(const orc_scene& s, uint32_t ii, V3 o, V3 d, Hit& h,
-                        std::vector<StackEntry>& stack, uint32_t* totB, uint32_t* totT)
+                        std::vector<StackEntry>& stack, uint32_t* totB, uint32_t* totT, uint32_t* totI)
 {
     const Instance& in = s.instances[ii];
     if (ray_aabb(o, d, in.wlo, in.whi) < 0.0f) return false;
@@ -630,13 +631,14 @@ bool intersect_instance(const orc_scene& s, uint32_t ii, V3 o, V3 d, Hit& h,
     const Mesh& m = s.meshes[in.mesh];
     float dist = std::numeric_limits<float>::max();
     float bu = 0, bv = 0;
-    uint32_t bvIdx = 0, tri = 0, bvhTests = 0, triTests = 0;
+    uint32_t bvIdx = 0, tri = 0, bvhTests = 0, triTests = 0, innerPops = 0;
     if (m.hasBVH)
-        tris_bvh(m, lo, ld, dist, bu, bv, bvIdx, tri, bvhTests, triTests, stack);
+        tris_bvh(m, lo, ld, dist, bu, bv, bvIdx, tri, bvhTests, triTests, innerPops, stack);
     else
         tris_linear(m, lo, ld, dist, bu, bv, tri, triTests);
     if (totB) *totB += bvhTests;
     if (totT) *totT += triTests;
+    if (totI) *totI += innerPops;
     if (!(dist < std::numeric_limits<float>::max())) return false;
     const V3 lp = lo + dist * ld;
     h.worldPos = xyz(mul(in.model, V4{lp.x, lp.y, lp.z, 1.0f}));
@@ -654,14 +656,14 @@ bool intersect_instance(const orc_scene& s, uint32_t ii, V3 o, V3 d, Hit& h,
 
 // IntersectScene, Intersect.cpp:201-219: strict '<' keeps the first instance.
 Hit intersect_scene(const orc_scene& s, V3 o, V3 d, std::vector<StackEntry>& stack,
-                    uint32_t* totB = nullptr, uint32_t* totT = nullptr)
+                    uint32_t* totB = nullptr, uint32_t* totT = nullptr, uint32_t* totI = nullptr)
 {
     float best = std::numeric_limits<float>::max();
     Hit bestHit;
     const uint32_t n = static_cast<uint32_t>(s.instances.size());
     for (uint32_t i = 0; i < n; ++i) {
         Hit h;
-        if (intersect_instance(s, i, o, d, h, stack, totB, totT)) {
+        if (intersect_instance(s, i, o, d, h, stack, totB, totT, totI)) {
             if (h.dist < best) {
                 best = h.dist;
                 bestHit = h;
@@ -1340,8 +1342,8 @@ int orc_trace_rays(const orc_scene* s, const mt_ray* rays, uint64_t n, mt_hit* h
         const mt_ray& r = rays[i];
         const V3 o{r.origin[0], r.origin[1], r.origin[2]};
         const V3 d{r.direction[0], r.direction[1], r.direction[2]};
-        uint32_t tb = 0, tt = 0;
-        const Hit h = intersect_scene(*s, o, d, stacks[t], &tb, &tt);
+        uint32_t tb = 0, tt = 0, ti = 0;
+        const Hit h = intersect_scene(*s, o, d, stacks[t], &tb, &tt, &ti);
         mt_hit& o_ = hits[i];
         if (query == MT_QUERY_ANY) {
             std::memset(&o_, 0, sizeof(o_));
@@ -1361,8 +1363,9 @@ int orc_trace_rays(const orc_scene* s, const mt_ray* rays, uint64_t n, mt_hit* h
             o_.tri_tests = query == MT_QUERY_CLOSEST_COUNT ? h.triTests : 0;
         }
         if (totals) {
-            totals[2 * i] = tb;
-            totals[2 * i + 1] = tt;
+            totals[3 * i] = tb;
+            totals[3 * i + 1] = ti;
+            totals[3 * i + 2] = tt;
         }
     });
     return MT_OK;

@@ -49,8 +49,8 @@ int orc_scene_mesh_bvh(const orc_scene* s, uint32_t mesh, const mt_bvh_node** no
  * query: MT_QUERY_CLOSEST / MT_QUERY_CLOSEST_COUNT fill the hit record with the
  * winning instance's counters; MT_QUERY_ANY writes 1 into hit.instance when the
  * closest hit lies at world distance <= ray.tmax, else 0.
- * totals (optional, 2 x n): bvh tests and triangle tests summed over ALL
- * instances the ray visited. */
+ * totals (optional, 3 x n): bvh tests (pops), inner-node expansions and
+ * triangle tests summed over ALL instances the ray visited. */
 int orc_trace_rays(const orc_scene* s, const mt_ray* rays, uint64_t n, mt_hit* hits, int query,
                    uint32_t* totals, int threads);
 

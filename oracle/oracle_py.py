@@ -163,7 +163,7 @@ class OracleScene:
     def trace(self, rays: np.ndarray, query=0, totals=False, threads=0):
         rays = np.ascontiguousarray(rays, dtype=np.float32)
         hits = np.zeros((rays.shape[0], 8), dtype=np.uint32)
-        tot = np.zeros((rays.shape[0], 2), dtype=np.uint32) if totals else None
+        tot = np.zeros((rays.shape[0], 3), dtype=np.uint32) if totals else None
         _check(self.L.orc_trace_rays(self.h, _p(rays), rays.shape[0], _p(hits), query,
                                      _p(tot) if totals else None, threads), self.L, "orc_trace_rays")
         return (hits, tot) if totals else hits
