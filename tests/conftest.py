@@ -12,8 +12,11 @@ if str(ROOT) not in sys.path:
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
-    from mitrace_gb300 import build as b
+    import importlib.util
 
-    if not b.LIB.exists():
-        b.build_product()
+    # by path: importing the package would load the library before it is built
+    spec = importlib.util.spec_from_file_location("mitrace_gb300_build", ROOT / "mitrace_gb300" / "build.py")
+    b = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(b)
+    b.build_product()
     b.build_oracle()
