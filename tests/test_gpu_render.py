@@ -56,18 +56,27 @@ def test_counter_rng_render_matches_oracle(name):
 
 @pytest.mark.parametrize("name", ["box_room", "material_grid"])
 def test_ztest_against_reference_rng(name):
+    """Equal spp (256), GPU counter-RNG image vs the reference-faithful oracle
+    (mt19937 per tile): per pixel and channel |a - b| / sqrt(2 var / n) <= 3
+    for >= 99% of values, var estimated from 256 per-sample values.  The clamp
+    is off here (its exact parity is covered above) so both sides are plain
+    means and the normal approximation applies."""
     scene, cfg = CASES[name]()
-    cfg.samples = 32
-    cfg.firefly_enable = 0  # the z-test compares plain means; the clamp is covered above
+    cfg.samples = 256
+    cfg.firefly_enable = 0
+    if name == "material_grid":
+        cfg.width, cfg.height = 64, 36
     img, _ = gpu_render(scene, cfg)
     o = orc.OracleScene(mt.PackedScene(scene), cfg)
     ref, _, _ = o.render(orc.RNG_MT19937)
-    s = o.render_samples()  # per-sample values (counter RNG) give the per-pixel variance
+    s = o.render_samples()
     var = s.var(axis=0, ddof=1)
     se = np.sqrt(2.0 * var / cfg.samples) + 1e-6
     z = np.abs(img - ref) / se
-    frac = np.mean(np.all(z <= 3.0, axis=-1))
-    assert frac >= 0.99, f"{name}: {frac:.4f} of pixels within 3 sigma"
+    frac = np.mean(z <= 3.0)
+    assert frac >= 0.99, f"{name}: {frac:.4f} of pixel channels within 3 sigma"
+    # and no systematic offset: mean signed difference far below the noise
+    assert abs(float((img - ref).mean())) < 4.0 * float(np.sqrt((se ** 2).mean() / se.size)) + 1e-4
 
 
 def test_render_device_matches_async_path():
