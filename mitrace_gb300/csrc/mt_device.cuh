@@ -235,119 +235,6 @@ struct LocalHit {
 
 __device__ __forceinline__ uint32_t f2u(float f) { return __float_as_uint(f); }
 
-// IntersectTrianglesBVH (Intersect.cpp:47-141): explicit stack of
-// {node, exit distance}; pops skip boxes with exit < 0 or exit > best + 0.1;
-// the nearer child (by exit distance) is pushed last.  Returns true when a
-// hit at t < FLT_MAX was found.  ANY_TMAX >= 0 stops at the first accepted hit
-// for which stop(t) says so (any-hit shadow query).
-template <bool COUNT, class StopFn>
-__device__ __forceinline__ void traverse_bvh(const DevScene& S, const DevMesh& m, f3 o, f3 d,
-                                             LocalHit& h, StopFn stop, bool& stopped)
-{
-    const float4* __restrict__ nodes = S.nodes + 2ull * m.node_off;
-    const float4* __restrict__ slots = S.slots + 3ull * m.slot_off;
-    const f3 inv = {__fdiv_rn(1.0f, d.x), __fdiv_rn(1.0f, d.y), __fdiv_rn(1.0f, d.z)};
-    uint32_t stk_node[MT_STACK_SIZE];
-    float stk_dist[MT_STACK_SIZE];
-    int sp = 0;
-    {
-        const float4 a = __ldg(nodes + 0), b = __ldg(nodes + 1);
-        stk_node[0] = 0;
-        stk_dist[0] = slab(o, inv, xyz(a), xyz(b));
-        sp = 1;
-    }
-    const float minDelta = 0.1f;
-    while (sp > 0) {
-        --sp;
-        const uint32_t ni = stk_node[sp];
-        const float nd = stk_dist[sp];
-        if (COUNT) ++h.bvh_tests;
-        if (nd < 0.0f) continue;
-        if (nd > __fadd_rn(h.t, minDelta)) continue;
-        const uint32_t na = f2u(__ldg(&nodes[2 * ni].w));
-        const uint32_t nb = f2u(__ldg(&nodes[2 * ni + 1].w));
-        if (na & MT_BVH_LEAF_BIT) {
-            const uint32_t first = na & ~MT_BVH_LEAF_BIT;
-            const uint32_t count = nb & ~MT_BVH_LEAF_BIT;
-            for (uint32_t i = first; i < first + count; ++i) {
-                const float4 A = __ldg(slots + 3 * i);
-                const float4 B = __ldg(slots + 3 * i + 1);
-                const float4 C = __ldg(slots + 3 * i + 2);
-                float t, u, v, det;
-                if (COUNT) ++h.tri_tests;
-                if (tri_test(o, d, xyz(A), xyz(B), xyz(C), t, u, v, det)) {
-                    if (t > 0.0f && t < h.t) {
-                        const float id = __fdiv_rn(1.0f, det);
-                        h.t = t;
-                        h.u = __fmul_rn(u, id);
-                        h.v = __fmul_rn(v, id);
-                        h.slot = i;
-                        h.bv = ni;
-                        if (stop(t)) {
-                            stopped = true;
-                            return;
-                        }
-                    }
-                }
-            }
-        } else {
-            if (COUNT) ++h.inner;
-            const float4 a0 = __ldg(nodes + 2 * na), a1 = __ldg(nodes + 2 * na + 1);
-            const float4 b0 = __ldg(nodes + 2 * nb), b1 = __ldg(nodes + 2 * nb + 1);
-            const float da = slab(o, inv, xyz(a0), xyz(a1));
-            const float db = slab(o, inv, xyz(b0), xyz(b1));
-            const float lim = __fadd_rn(h.t, minDelta);
-            const bool pa = da >= 0.0f && da <= lim;
-            const bool pb = db >= 0.0f && db <= lim;
-            if (sp + 2 > MT_STACK_SIZE) {
-                atomicOr(S.error_flag, MT_ERRBIT_STACK);
-                return;
-            }
-            if (pa && pb) {
-                if (da < db) {
-                    stk_node[sp] = nb; stk_dist[sp] = db; ++sp;
-                    stk_node[sp] = na; stk_dist[sp] = da; ++sp;
-                } else {
-                    stk_node[sp] = na; stk_dist[sp] = da; ++sp;
-                    stk_node[sp] = nb; stk_dist[sp] = db; ++sp;
-                }
-            } else if (pa) {
-                stk_node[sp] = na; stk_dist[sp] = da; ++sp;
-            } else if (pb) {
-                stk_node[sp] = nb; stk_dist[sp] = db; ++sp;
-            }
-        }
-    }
-}
-
-// IntersectTrianglesLinear (Intersect.cpp:20-45).
-template <bool COUNT, class StopFn>
-__device__ __forceinline__ void traverse_linear(const DevScene& S, const DevMesh& m, f3 o, f3 d,
-                                                LocalHit& h, StopFn stop, bool& stopped)
-{
-    const float4* __restrict__ slots = S.slots + 3ull * m.slot_off;
-    for (uint32_t i = 0; i < m.num_slots; ++i) {
-        const float4 A = __ldg(slots + 3 * i);
-        const float4 B = __ldg(slots + 3 * i + 1);
-        const float4 C = __ldg(slots + 3 * i + 2);
-        float t, u, v, det;
-        if (COUNT) ++h.tri_tests;
-        if (tri_test(o, d, xyz(A), xyz(B), xyz(C), t, u, v, det)) {
-            if (t > 0.0f && t < h.t) {
-                const float id = __fdiv_rn(1.0f, det);
-                h.t = t;
-                h.u = __fmul_rn(u, id);
-                h.v = __fmul_rn(v, id);
-                h.slot = i;
-                if (stop(t)) {
-                    stopped = true;
-                    return;
-                }
-            }
-        }
-    }
-}
-
 struct SceneHit {
     bool hit;
     uint32_t inst, tri, bv, bvh_tests, tri_tests;
@@ -356,14 +243,32 @@ struct SceneHit {
     f3 world_pos;
 };
 
-// IntersectScene + IntersectMeshInstance (Intersect.cpp:143-219).
-// ANY: stops at the first accepted hit whose world distance is <= tmax and
-// reports it; the visit order up to that point is the closest-hit order, so the
-// verdict equals "closest hit distance <= tmax" (Tracer.cpp:322) whenever the
-// world distance is monotone in local t (rigid/affine instance transforms).
-template <bool COUNT, bool ANY>
-__device__ __forceinline__ SceneHit intersect_scene(const DevScene& S, f3 o, f3 d, float tmax)
+// ---------------------------------------------------------------------------
+// Scene traversal: IntersectScene / IntersectMeshInstance / IntersectTrianglesBVH
+// (Intersect.cpp:20-219), warp-cooperative
+// ---------------------------------------------------------------------------
+// Every lane owns one ray and pops its own BVH nodes, but all lanes run one
+// loop whatever instance they are in, and a leaf reached by any lane is tested
+// by the whole warp: lane j tests triangle first + j (coalesced 48-byte slots)
+// and a (t, index) arg-min picks the winner.  The reference tests a leaf's
+// triangles in order, accepting t > 0 && t < dist with dist shrinking as it
+// goes (Intersect.cpp:84-105); the survivor of that scan is the triangle with
+// the smallest valid t, the first one on ties, which is exactly the
+// lexicographic minimum, so the result (and every counter) is unchanged.
+// Meshes without a BVH are one leaf holding all their triangles
+// (IntersectTrianglesLinear, Intersect.cpp:20-45).
+// Must be called by all 32 lanes of a warp together; inactive lanes help.
+#define MT_FULL 0xffffffffu
+
+__device__ __forceinline__ bool key_less(float ta, uint32_t ia, float tb, uint32_t ib)
 {
+    return ta < tb || (ta == tb && ia < ib);
+}
+
+template <bool COUNT, bool ANY>
+__device__ __forceinline__ SceneHit trace_warp(const DevScene& S, f3 o, f3 d, float tmax, bool active)
+{
+    const uint32_t lane = threadIdx.x & 31;
     SceneHit best;
     best.hit = false;
     best.dist = FLT_MAX;
@@ -373,62 +278,226 @@ __device__ __forceinline__ SceneHit intersect_scene(const DevScene& S, f3 o, f3 
     best.u = best.v = 0.0f;
     best.world_pos = splat(0.0f);
     const f3 winv = {__fdiv_rn(1.0f, d.x), __fdiv_rn(1.0f, d.y), __fdiv_rn(1.0f, d.z)};
-    for (uint32_t ii = 0; ii < S.num_instances; ++ii) {
-        const DevInstance& I = S.instances[ii];
-        const f3 wlo = {__ldg(&I.wlo[0]), __ldg(&I.wlo[1]), __ldg(&I.wlo[2])};
-        const f3 whi = {__ldg(&I.whi[0]), __ldg(&I.whi[1]), __ldg(&I.whi[2])};
-        if (slab(o, winv, wlo, whi) < 0.0f) continue;
-        float inv[16], model[16];
-#pragma unroll
-        for (int k = 0; k < 16; ++k) inv[k] = __ldg(&I.inv[k]);
-        const f3 lo = xform_point(inv, o);
-        const f3 ld = normalize(xform_dir(inv, d));
-        const DevMesh m = S.meshes[__ldg(&I.mesh)];
+    bool stopped = false;  // ANY: a blocking hit was found
+
+    uint32_t stk_node[MT_STACK_SIZE];
+    float stk_dist[MT_STACK_SIZE];
+
+    for (uint32_t c0 = 0; c0 < S.num_instances; c0 += 32) {
+        // instance boxes the ray meets (IntersectMeshInstance's first test)
+        uint32_t mask = 0;
+        const uint32_t cn = min(32u, S.num_instances - c0);
+        for (uint32_t k = 0; k < cn; ++k) {
+            const DevInstance& I = S.instances[c0 + k];
+            const f3 wlo = {__ldg(&I.wlo[0]), __ldg(&I.wlo[1]), __ldg(&I.wlo[2])};
+            const f3 whi = {__ldg(&I.whi[0]), __ldg(&I.whi[1]), __ldg(&I.whi[2])};
+            if (slab(o, winv, wlo, whi) >= 0.0f) mask |= 1u << k;
+        }
+        if (!active || stopped) mask = 0;
+
+        bool in_inst = false;
+        uint32_t ii = 0;
+        f3 lo = splat(0.0f), ld = splat(0.0f), linv = splat(0.0f);
+        const float4* nodes = S.nodes;
+        uint32_t slot_base = 0;
         LocalHit h;
         h.t = FLT_MAX;
         h.u = h.v = 0.0f;
-        h.slot = 0;
-        h.bv = 0;
+        h.slot = h.bv = 0;
         h.bvh_tests = h.tri_tests = h.inner = 0;
-        bool stopped = false;
-        auto stop = [&](float t) -> bool {
-            if (!ANY) return false;
+        int sp = 0;
+        bool pending = false;
+        uint32_t pfirst = 0, pcount = 0, pnode = 0;
+
+        while (true) {
+            // 1. a lane whose stack ran dry closes its instance and opens the next
+            if (in_inst && sp == 0 && !pending) {
+                if (COUNT) {
+                    best.tot_pops += h.bvh_tests;
+                    best.tot_inner += h.inner;
+                    best.tot_tris += h.tri_tests;
+                }
+                if (!ANY && h.t < FLT_MAX) {
+                    const DevInstance& I = S.instances[ii];
+                    float model[16];
 #pragma unroll
-            for (int k = 0; k < 16; ++k) model[k] = __ldg(&I.model[k]);
-            const f3 wp = xform_point(model, lo + t * ld);
-            return !(length(wp - o) > tmax);
-        };
-        if (m.has_bvh)
-            traverse_bvh<COUNT>(S, m, lo, ld, h, stop, stopped);
-        else
-            traverse_linear<COUNT>(S, m, lo, ld, h, stop, stopped);
-        if (COUNT) {
-            best.tot_pops += h.bvh_tests;
-            best.tot_inner += h.inner;
-            best.tot_tris += h.tri_tests;
-        }
-        if (ANY && stopped) {
-            best.hit = true;
-            best.inst = ii;
-            return best;
-        }
-        if (ANY || !(h.t < FLT_MAX)) continue;
+                    for (int k = 0; k < 16; ++k) model[k] = __ldg(&I.model[k]);
+                    const f3 wp = xform_point(model, lo + h.t * ld);
+                    const float wd = length(wp - o);
+                    if (wd < best.dist) {
+                        best.hit = true;
+                        best.dist = wd;
+                        best.world_pos = wp;
+                        best.inst = ii;
+                        best.tri = f2u(__ldg(&S.slots[3ull * (slot_base + h.slot)].w));
+                        best.bv = h.bv;
+                        best.u = h.u;
+                        best.v = h.v;
+                        best.bvh_tests = h.bvh_tests;
+                        best.tri_tests = h.tri_tests;
+                    }
+                }
+                in_inst = false;
+            }
+            if (!in_inst && mask != 0) {
+                const uint32_t k = __ffs(mask) - 1;
+                mask &= mask - 1;
+                ii = c0 + k;
+                const DevInstance& I = S.instances[ii];
+                float inv[16];
 #pragma unroll
-        for (int k = 0; k < 16; ++k) model[k] = __ldg(&I.model[k]);
-        const f3 wp = xform_point(model, lo + h.t * ld);
-        const float wd = length(wp - o);
-        if (wd < best.dist) {
-            best.hit = true;
-            best.dist = wd;
-            best.world_pos = wp;
-            best.inst = ii;
-            best.tri = f2u(__ldg(&S.slots[3ull * (m.slot_off + h.slot)].w));
-            best.bv = h.bv;
-            best.u = h.u;
-            best.v = h.v;
-            best.bvh_tests = h.bvh_tests;
-            best.tri_tests = h.tri_tests;
+                for (int q = 0; q < 16; ++q) inv[q] = __ldg(&I.inv[q]);
+                lo = xform_point(inv, o);
+                ld = normalize(xform_dir(inv, d));
+                linv = {__fdiv_rn(1.0f, ld.x), __fdiv_rn(1.0f, ld.y), __fdiv_rn(1.0f, ld.z)};
+                const DevMesh m = S.meshes[__ldg(&I.mesh)];
+                nodes = S.nodes + 2ull * m.node_off;
+                slot_base = m.slot_off;
+                h.t = FLT_MAX;
+                h.u = h.v = 0.0f;
+                h.slot = h.bv = 0;
+                h.bvh_tests = h.tri_tests = h.inner = 0;
+                in_inst = true;
+                if (m.has_bvh) {
+                    const float4 a = __ldg(nodes + 0), b = __ldg(nodes + 1);
+                    stk_node[0] = 0;
+                    stk_dist[0] = slab(lo, linv, xyz(a), xyz(b));
+                    sp = 1;
+                } else {
+                    pending = true;
+                    pfirst = 0;
+                    pcount = m.num_slots;
+                    pnode = 0;
+                }
+            }
+            const bool work = in_inst && (sp > 0 || pending);
+            if (!__any_sync(MT_FULL, work)) break;
+
+            // 2. one node pop per lane (IntersectTrianglesBVH's loop body)
+            if (work && !pending) {
+                --sp;
+                const uint32_t ni = stk_node[sp];
+                const float nd = stk_dist[sp];
+                if (COUNT) ++h.bvh_tests;
+                if (!(nd < 0.0f) && !(nd > __fadd_rn(h.t, 0.1f))) {
+                    const uint32_t na = f2u(__ldg(&nodes[2 * ni].w));
+                    const uint32_t nb = f2u(__ldg(&nodes[2 * ni + 1].w));
+                    if (na & MT_BVH_LEAF_BIT) {
+                        pending = true;
+                        pfirst = na & ~MT_BVH_LEAF_BIT;
+                        pcount = nb & ~MT_BVH_LEAF_BIT;
+                        pnode = ni;
+                    } else {
+                        if (COUNT) ++h.inner;
+                        const float4 a0 = __ldg(nodes + 2 * na), a1 = __ldg(nodes + 2 * na + 1);
+                        const float4 b0 = __ldg(nodes + 2 * nb), b1 = __ldg(nodes + 2 * nb + 1);
+                        const float da = slab(lo, linv, xyz(a0), xyz(a1));
+                        const float db = slab(lo, linv, xyz(b0), xyz(b1));
+                        const float lim = __fadd_rn(h.t, 0.1f);
+                        const bool pa = da >= 0.0f && da <= lim;
+                        const bool pb = db >= 0.0f && db <= lim;
+                        if (sp + 2 > MT_STACK_SIZE) {
+                            atomicOr(S.error_flag, MT_ERRBIT_STACK);
+                            sp = 0;
+                        } else if (pa && pb) {
+                            if (da < db) {
+                                stk_node[sp] = nb; stk_dist[sp] = db; ++sp;
+                                stk_node[sp] = na; stk_dist[sp] = da; ++sp;
+                            } else {
+                                stk_node[sp] = na; stk_dist[sp] = da; ++sp;
+                                stk_node[sp] = nb; stk_dist[sp] = db; ++sp;
+                            }
+                        } else if (pa) {
+                            stk_node[sp] = na; stk_dist[sp] = da; ++sp;
+                        } else if (pb) {
+                            stk_node[sp] = nb; stk_dist[sp] = db; ++sp;
+                        }
+                    }
+                }
+            }
+
+            // 3. the warp tests every pending leaf together
+            uint32_t pm = __ballot_sync(MT_FULL, pending);
+            while (pm) {
+                const uint32_t L = __ffs(pm) - 1;
+                pm &= pm - 1;
+                const f3 ro = {__shfl_sync(MT_FULL, lo.x, L), __shfl_sync(MT_FULL, lo.y, L),
+                               __shfl_sync(MT_FULL, lo.z, L)};
+                const f3 rd = {__shfl_sync(MT_FULL, ld.x, L), __shfl_sync(MT_FULL, ld.y, L),
+                               __shfl_sync(MT_FULL, ld.z, L)};
+                const float dist = __shfl_sync(MT_FULL, h.t, L);
+                const uint32_t base = __shfl_sync(MT_FULL, slot_base + pfirst, L);
+                const uint32_t count = __shfl_sync(MT_FULL, pcount, L);
+                float bt = FLT_MAX, bu = 0.0f, bv = 0.0f;
+                uint32_t bi = 0xffffffffu;
+                for (uint32_t c = 0; c < count; c += 32) {
+                    const uint32_t i = c + lane;
+                    float t = FLT_MAX, u = 0.0f, v = 0.0f, det = 1.0f;
+                    bool ok = false;
+                    if (i < count) {
+                        const float4* sl = S.slots + 3ull * (base + i);
+                        const float4 A = __ldg(sl), B = __ldg(sl + 1), C = __ldg(sl + 2);
+                        ok = tri_test(ro, rd, xyz(A), xyz(B), xyz(C), t, u, v, det) && t > 0.0f && t < dist;
+                    }
+                    float kt = ok ? t : FLT_MAX;
+                    uint32_t ki = ok ? i : 0xffffffffu;
+#pragma unroll
+                    for (int off = 16; off > 0; off >>= 1) {
+                        const float ot = __shfl_xor_sync(MT_FULL, kt, off);
+                        const uint32_t oi = __shfl_xor_sync(MT_FULL, ki, off);
+                        if (key_less(ot, oi, kt, ki)) {
+                            kt = ot;
+                            ki = oi;
+                        }
+                    }
+                    if (ki != 0xffffffffu && key_less(kt, ki, bt, bi)) {
+                        const uint32_t w = ki - c;
+                        float uu = 0.0f, vv = 0.0f;
+                        if (ok) {
+                            const float id = __fdiv_rn(1.0f, det);
+                            uu = __fmul_rn(u, id);
+                            vv = __fmul_rn(v, id);
+                        }
+                        bt = kt;
+                        bi = ki;
+                        bu = __shfl_sync(MT_FULL, uu, w);
+                        bv = __shfl_sync(MT_FULL, vv, w);
+                    }
+                }
+                if (lane == L) {
+                    if (COUNT) h.tri_tests += count;
+                    if (bi != 0xffffffffu) {
+                        h.t = bt;
+                        h.u = bu;
+                        h.v = bv;
+                        h.slot = pfirst + bi;
+                        h.bv = pnode;
+                        if (ANY) {
+                            const DevInstance& I = S.instances[ii];
+                            float model[16];
+#pragma unroll
+                            for (int k = 0; k < 16; ++k) model[k] = __ldg(&I.model[k]);
+                            const f3 wp = xform_point(model, lo + bt * ld);
+                            if (!(length(wp - o) > tmax)) {
+                                stopped = true;
+                                best.hit = true;
+                                best.inst = ii;
+                                if (COUNT) {
+                                    best.tot_pops += h.bvh_tests;
+                                    best.tot_inner += h.inner;
+                                    best.tot_tris += h.tri_tests;
+                                }
+                                sp = 0;
+                                mask = 0;
+                                in_inst = false;
+                            }
+                        }
+                    }
+                    pending = false;
+                }
+            }
         }
+        if (ANY && __all_sync(MT_FULL, stopped || !active)) break;
     }
     return best;
 }

@@ -33,24 +33,36 @@ __device__ __forceinline__ uint32_t warp_append(uint32_t* counter)
 // ---------------------------------------------------------------------------
 // Ray queries
 // ---------------------------------------------------------------------------
+// Warp-uniform loop over a range: every lane of a warp calls trace_warp together.
+#define MT_WARP_LOOP(n)                                                                             \
+    const uint32_t lane_ = threadIdx.x & 31;                                                        \
+    const uint64_t warp0_ = (blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x) >> 5;    \
+    const uint64_t nwarps_ = (static_cast<uint64_t>(gridDim.x) * blockDim.x) >> 5;                  \
+    for (uint64_t base_ = warp0_ * 32; base_ < (n); base_ += nwarps_ * 32)
+
 template <int QUERY>
 __global__ void __launch_bounds__(128) k_trace(DevScene S, const mt_ray* __restrict__ rays,
                                                uint64_t n, mt_hit* __restrict__ hits)
 {
-    for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < n;
-         i += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
-        const float4 a = __ldg(reinterpret_cast<const float4*>(rays + i));
-        const float4 b = __ldg(reinterpret_cast<const float4*>(rays + i) + 1);
+    MT_WARP_LOOP(n)
+    {
+        const uint64_t i = base_ + lane_;
+        const bool active = i < n;
+        float4 a = make_float4(0, 0, 0, 0), b = make_float4(0, 0, 1, 0);
+        if (active) {
+            a = __ldg(reinterpret_cast<const float4*>(rays + i));
+            b = __ldg(reinterpret_cast<const float4*>(rays + i) + 1);
+        }
         mt_hit h;
         if (QUERY == MT_QUERY_ANY) {
-            const SceneHit sh = intersect_scene<false, true>(S, xyz(a), xyz(b), a.w);
+            const SceneHit sh = trace_warp<false, true>(S, xyz(a), xyz(b), a.w, active);
             h.distance = 0.0f;
             h.u = h.v = 0.0f;
             h.instance = sh.hit ? 1u : 0u;
             h.triangle = h.bv_index = h.bvh_tests = h.tri_tests = 0;
         } else {
             constexpr bool kCount = QUERY == MT_QUERY_CLOSEST_COUNT || QUERY == MT_QUERY_CLOSEST_TOTALS;
-            const SceneHit sh = intersect_scene<kCount, false>(S, xyz(a), xyz(b), 0.0f);
+            const SceneHit sh = trace_warp<kCount, false>(S, xyz(a), xyz(b), 0.0f, active);
             if (sh.hit) {
                 h.distance = sh.dist;
                 h.u = sh.u;
@@ -71,10 +83,12 @@ __global__ void __launch_bounds__(128) k_trace(DevScene S, const mt_ray* __restr
                 h.tri_tests = sh.tot_tris;
             }
         }
-        float4* dst = reinterpret_cast<float4*>(hits + i);
-        dst[0] = make_float4(h.distance, h.u, h.v, __uint_as_float(h.instance));
-        dst[1] = make_float4(__uint_as_float(h.triangle), __uint_as_float(h.bv_index),
-                             __uint_as_float(h.bvh_tests), __uint_as_float(h.tri_tests));
+        if (active) {
+            float4* dst = reinterpret_cast<float4*>(hits + i);
+            dst[0] = make_float4(h.distance, h.u, h.v, __uint_as_float(h.instance));
+            dst[1] = make_float4(__uint_as_float(h.triangle), __uint_as_float(h.bv_index),
+                                 __uint_as_float(h.bvh_tests), __uint_as_float(h.tri_tests));
+        }
     }
 }
 
@@ -174,10 +188,19 @@ __global__ void __launch_bounds__(128) k_extend(DevScene S, PathState P,
         atomicAdd(rays, static_cast<unsigned long long>(n));
     }
     uint32_t pops = 0, inner = 0, tris = 0;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const uint32_t p = q[i];
-        const float4 o = P.ro[p], d = P.rd[p];
-        const SceneHit h = intersect_scene<COUNT, false>(S, xyz(o), xyz(d), 0.0f);
+    MT_WARP_LOOP(n)
+    {
+        const uint64_t i = base_ + lane_;
+        const bool active = i < n;
+        uint32_t p = 0;
+        float4 o = make_float4(0, 0, 0, 0), d = make_float4(0, 0, 1, 0);
+        if (active) {
+            p = q[i];
+            o = P.ro[p];
+            d = P.rd[p];
+        }
+        const SceneHit h = trace_warp<COUNT, false>(S, xyz(o), xyz(d), 0.0f, active);
+        if (!active) continue;
         if (COUNT) {
             pops += h.tot_pops;
             inner += h.tot_inner;
@@ -372,9 +395,17 @@ __global__ void __launch_bounds__(128) k_shadow(DevScene S, PathState P, ShadowQ
     const uint32_t n = counts[2];
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(rays, static_cast<unsigned long long>(n));
     uint32_t pops = 0, inner = 0, tris = 0;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const float4 o = SQ.o[i], d = SQ.d[i];
-        const SceneHit h = intersect_scene<COUNT, true>(S, xyz(o), xyz(d), o.w);
+    MT_WARP_LOOP(n)
+    {
+        const uint64_t i = base_ + lane_;
+        const bool active = i < n;
+        float4 o = make_float4(0, 0, 0, 0), d = make_float4(0, 0, 1, 0);
+        if (active) {
+            o = SQ.o[i];
+            d = SQ.d[i];
+        }
+        const SceneHit h = trace_warp<COUNT, true>(S, xyz(o), xyz(d), o.w, active);
+        if (!active) continue;
         if (COUNT) {
             pops += h.tot_pops;
             inner += h.tot_inner;
