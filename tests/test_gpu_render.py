@@ -101,19 +101,29 @@ def test_small_batches_and_bands_give_same_image(monkeypatch):
 
 
 def test_kill_render_and_state_errors():
-    scene, cfg = mt.material_grid(width=640, height=360, samples=64)
+    # long enough (about 1 s, ~250 batches) that the kill lands mid-render
+    scene, cfg = mt.material_grid(width=1920, height=1080, samples=512)
     with mt.Tracer(scene, cfg) as tr:
         tr.StartRender()
         with pytest.raises(mt.MTError) as e:
             tr.StartRender()
         assert e.value.code == A.MT_ERR_STATE
-        time.sleep(0.05)
+        time.sleep(0.02)
         tr.KillRender()
         with pytest.raises(mt.MTError) as e:
             tr.WaitForRender()
         assert e.value.code in (A.MT_ERR_KILLED,)
         assert tr.IsDone()
-        # the handle stays usable after a kill
+        assert tr.GetStats().progress < 1.0
+    # the handle stays usable after a kill
+    scene, cfg = mt.material_grid(width=320, height=180, samples=16)
+    with mt.Tracer(scene, cfg) as tr:
+        tr.StartRender()
+        tr.KillRender()
+        try:
+            tr.WaitForRender()
+        except mt.MTError as e:
+            assert e.code == A.MT_ERR_KILLED
         tr.StartRender()
         tr.WaitForRender()
         st = tr.GetStats()
