@@ -211,6 +211,7 @@ struct mt_handle {
     // query scratch
     DevArray<mt_ray> qrays;
     DevArray<mt_hit> qhits;
+    DevArray<uint32_t> qfetch;  // ray fetch counter of the query kernels
     // async render
     std::mutex mu;
     std::thread worker;
@@ -435,6 +436,7 @@ mt_status upload_scene(mt_handle* h, const mt_scene_desc* d)
     MT_CUDA(h->textures.upload(texs.data(), texs.size(), st));
     MT_CUDA(h->lights.upload(lights.data(), lights.size(), st));
     MT_CUDA(h->error_flag.alloc(1));
+    MT_CUDA(h->qfetch.alloc(1));
     MT_CUDA(cudaMemsetAsync(h->error_flag.p, 0, sizeof(int), st));
     h->scene_bytes += nodes.size() * 16 + slots.size() * 16 + normals.size() * 4 + uvs.size() * 4 +
                       insts.size() * sizeof(DevInstance);
@@ -505,7 +507,8 @@ mt_status ensure_wave(mt_handle* h)
     MT_CUDA(h->phit.alloc(batch));
     MT_CUDA(h->sq.alloc(3ull * batch));
     MT_CUDA(h->queues.alloc(2ull * batch));
-    MT_CUDA(h->counts.alloc(4));
+    MT_CUDA(h->counts.alloc(8));
+    MT_CUDA(cudaMemset(h->counts.p, 0, 8 * sizeof(uint32_t)));
     MT_CUDA(h->rays.alloc(2));
     MT_CUDA(h->samples.alloc(3ull * h->band_capacity));
     MT_CUDA(h->image.alloc(npix * 3));
@@ -850,7 +853,7 @@ mt_status mt_trace_rays_device(mt_handle* h, const mt_ray* d_rays, uint64_t n, m
     if ((reinterpret_cast<uintptr_t>(d_rays) | reinterpret_cast<uintptr_t>(d_hits)) & 15)
         return set_err(MT_ERR_INVALID, "ray and hit buffers must be 16-byte aligned");
     cudaStream_t st = cuda_stream ? static_cast<cudaStream_t>(cuda_stream) : h->stream;
-    MT_CUDA(launch_trace(h->S, d_rays, n, d_hits, query, st));
+    MT_CUDA(launch_trace(h->S, d_rays, n, d_hits, query, h->qfetch.p, st));
     h->launches += n ? 1 : 0;
     return MT_OK;
 }

@@ -265,53 +265,99 @@ __device__ __forceinline__ bool key_less(float ta, uint32_t ia, float tb, uint32
     return ta < tb || (ta == tb && ia < ib);
 }
 
-template <bool COUNT, bool ANY>
-__device__ __forceinline__ SceneHit trace_warp(const DevScene& S, f3 o, f3 d, float tmax, bool active)
+// Persistent form: the warp keeps running until the work source is empty.  A
+// lane whose ray is finished takes the next one (one atomic per warp), so no
+// lane idles while its neighbours finish long rays.  The instance boxes a new
+// ray meets are tested 32 at a time by the whole warp (one box per lane, then
+// a ballot), the same test IntersectMeshInstance starts with.
+//
+// Work must provide, per lane:
+//   bool fetch(uint32_t index, f3& o, f3& d, float& tmax)  (false: index past the end)
+//   void finish(const SceneHit& h)
+template <bool COUNT, bool ANY, class Work>
+__device__ __forceinline__ void trace_persistent(const DevScene& S, Work& W, uint32_t* fetch_counter)
 {
     const uint32_t lane = threadIdx.x & 31;
+    const uint32_t lane_lt = (1u << lane) - 1u;
+    bool has_ray = false, exhausted = false;
+    f3 o = splat(0.0f), d = splat(0.0f), winv = splat(0.0f);
+    float tmax = 0.0f;
     SceneHit best;
-    best.hit = false;
-    best.dist = FLT_MAX;
-    best.bvh_tests = best.tri_tests = 0;
-    best.tot_pops = best.tot_inner = best.tot_tris = 0;
-    best.inst = best.tri = best.bv = 0;
-    best.u = best.v = 0.0f;
-    best.world_pos = splat(0.0f);
-    const f3 winv = {__fdiv_rn(1.0f, d.x), __fdiv_rn(1.0f, d.y), __fdiv_rn(1.0f, d.z)};
-    bool stopped = false;  // ANY: a blocking hit was found
-
+    bool stopped = false;
+    uint32_t chunk = 0, mask = 0;
+    bool need_mask = false;
+    bool in_inst = false;
+    uint32_t ii = 0;
+    f3 lo = splat(0.0f), ld = splat(0.0f), linv = splat(0.0f);
+    const float4* nodes = S.nodes;
+    uint32_t slot_base = 0;
+    LocalHit h;
+    int sp = 0;
+    bool pending = false;
+    uint32_t pfirst = 0, pcount = 0, pnode = 0;
     uint32_t stk_node[MT_STACK_SIZE];
     float stk_dist[MT_STACK_SIZE];
 
-    for (uint32_t c0 = 0; c0 < S.num_instances; c0 += 32) {
-        // instance boxes the ray meets (IntersectMeshInstance's first test)
-        uint32_t mask = 0;
-        const uint32_t cn = min(32u, S.num_instances - c0);
-        for (uint32_t k = 0; k < cn; ++k) {
-            const DevInstance& I = S.instances[c0 + k];
-            const f3 wlo = {__ldg(&I.wlo[0]), __ldg(&I.wlo[1]), __ldg(&I.wlo[2])};
-            const f3 whi = {__ldg(&I.whi[0]), __ldg(&I.whi[1]), __ldg(&I.whi[2])};
-            if (slab(o, winv, wlo, whi) >= 0.0f) mask |= 1u << k;
+    while (true) {
+        // A. lanes without a ray take the next ones
+        const bool want = !has_ray && !exhausted;
+        const uint32_t wm = __ballot_sync(MT_FULL, want);
+        if (wm) {
+            const uint32_t leader = __ffs(wm) - 1;
+            uint32_t first = 0;
+            if (lane == leader) first = atomicAdd(fetch_counter, static_cast<uint32_t>(__popc(wm)));
+            first = __shfl_sync(MT_FULL, first, leader);
+            if (want) {
+                if (W.fetch(first + __popc(wm & lane_lt), o, d, tmax)) {
+                    has_ray = true;
+                    winv = {__fdiv_rn(1.0f, d.x), __fdiv_rn(1.0f, d.y), __fdiv_rn(1.0f, d.z)};
+                    best.hit = false;
+                    best.dist = FLT_MAX;
+                    best.bvh_tests = best.tri_tests = 0;
+                    best.tot_pops = best.tot_inner = best.tot_tris = 0;
+                    best.inst = best.tri = best.bv = 0;
+                    best.u = best.v = 0.0f;
+                    best.world_pos = splat(0.0f);
+                    stopped = false;
+                    chunk = 0;
+                    mask = 0;
+                    need_mask = S.num_instances > 0;
+                    in_inst = false;
+                    sp = 0;
+                    pending = false;
+                } else {
+                    exhausted = true;
+                }
+            }
         }
-        if (!active || stopped) mask = 0;
+        if (!__any_sync(MT_FULL, has_ray)) break;
 
-        bool in_inst = false;
-        uint32_t ii = 0;
-        f3 lo = splat(0.0f), ld = splat(0.0f), linv = splat(0.0f);
-        const float4* nodes = S.nodes;
-        uint32_t slot_base = 0;
-        LocalHit h;
-        h.t = FLT_MAX;
-        h.u = h.v = 0.0f;
-        h.slot = h.bv = 0;
-        h.bvh_tests = h.tri_tests = h.inner = 0;
-        int sp = 0;
-        bool pending = false;
-        uint32_t pfirst = 0, pcount = 0, pnode = 0;
+        // B. instance boxes of the current chunk, one warp pass per requesting lane
+        uint32_t nm = __ballot_sync(MT_FULL, need_mask);
+        while (nm) {
+            const uint32_t L = __ffs(nm) - 1;
+            nm &= nm - 1;
+            const f3 bo = {__shfl_sync(MT_FULL, o.x, L), __shfl_sync(MT_FULL, o.y, L), __shfl_sync(MT_FULL, o.z, L)};
+            const f3 bi = {__shfl_sync(MT_FULL, winv.x, L), __shfl_sync(MT_FULL, winv.y, L),
+                           __shfl_sync(MT_FULL, winv.z, L)};
+            const uint32_t k = __shfl_sync(MT_FULL, chunk, L) + lane;
+            bool meets = false;
+            if (k < S.num_instances) {
+                const DevInstance& I = S.instances[k];
+                const f3 wlo = {__ldg(&I.wlo[0]), __ldg(&I.wlo[1]), __ldg(&I.wlo[2])};
+                const f3 whi = {__ldg(&I.whi[0]), __ldg(&I.whi[1]), __ldg(&I.whi[2])};
+                meets = slab(bo, bi, wlo, whi) >= 0.0f;
+            }
+            const uint32_t m = __ballot_sync(MT_FULL, meets);
+            if (lane == L) {
+                mask = m;
+                need_mask = false;
+            }
+        }
 
-        while (true) {
-            // 1. a lane whose stack ran dry closes its instance and opens the next
-            if (in_inst && sp == 0 && !pending) {
+        // C. close the instance whose stack ran dry; open the next; finish the ray
+        if (has_ray && !need_mask && !pending && sp == 0) {
+            if (in_inst) {
                 if (COUNT) {
                     best.tot_pops += h.bvh_tests;
                     best.tot_inner += h.inner;
@@ -321,7 +367,7 @@ __device__ __forceinline__ SceneHit trace_warp(const DevScene& S, f3 o, f3 d, fl
                     const DevInstance& I = S.instances[ii];
                     float model[16];
 #pragma unroll
-                    for (int k = 0; k < 16; ++k) model[k] = __ldg(&I.model[k]);
+                    for (int q = 0; q < 16; ++q) model[q] = __ldg(&I.model[q]);
                     const f3 wp = xform_point(model, lo + h.t * ld);
                     const float wd = length(wp - o);
                     if (wd < best.dist) {
@@ -339,10 +385,16 @@ __device__ __forceinline__ SceneHit trace_warp(const DevScene& S, f3 o, f3 d, fl
                 }
                 in_inst = false;
             }
-            if (!in_inst && mask != 0) {
+            if (mask == 0 && !stopped && chunk + 32 < S.num_instances) {
+                chunk += 32;
+                need_mask = true;
+            } else if (mask == 0 || stopped) {
+                W.finish(best);
+                has_ray = false;
+            } else {
                 const uint32_t k = __ffs(mask) - 1;
                 mask &= mask - 1;
-                ii = c0 + k;
+                ii = chunk + k;
                 const DevInstance& I = S.instances[ii];
                 float inv[16];
 #pragma unroll
@@ -370,136 +422,132 @@ __device__ __forceinline__ SceneHit trace_warp(const DevScene& S, f3 o, f3 d, fl
                     pnode = 0;
                 }
             }
-            const bool work = in_inst && (sp > 0 || pending);
-            if (!__any_sync(MT_FULL, work)) break;
+        }
 
-            // 2. one node pop per lane (IntersectTrianglesBVH's loop body)
-            if (work && !pending) {
-                --sp;
-                const uint32_t ni = stk_node[sp];
-                const float nd = stk_dist[sp];
-                if (COUNT) ++h.bvh_tests;
-                if (!(nd < 0.0f) && !(nd > __fadd_rn(h.t, 0.1f))) {
-                    const uint32_t na = f2u(__ldg(&nodes[2 * ni].w));
-                    const uint32_t nb = f2u(__ldg(&nodes[2 * ni + 1].w));
-                    if (na & MT_BVH_LEAF_BIT) {
-                        pending = true;
-                        pfirst = na & ~MT_BVH_LEAF_BIT;
-                        pcount = nb & ~MT_BVH_LEAF_BIT;
-                        pnode = ni;
-                    } else {
-                        if (COUNT) ++h.inner;
-                        const float4 a0 = __ldg(nodes + 2 * na), a1 = __ldg(nodes + 2 * na + 1);
-                        const float4 b0 = __ldg(nodes + 2 * nb), b1 = __ldg(nodes + 2 * nb + 1);
-                        const float da = slab(lo, linv, xyz(a0), xyz(a1));
-                        const float db = slab(lo, linv, xyz(b0), xyz(b1));
-                        const float lim = __fadd_rn(h.t, 0.1f);
-                        const bool pa = da >= 0.0f && da <= lim;
-                        const bool pb = db >= 0.0f && db <= lim;
-                        if (sp + 2 > MT_STACK_SIZE) {
-                            atomicOr(S.error_flag, MT_ERRBIT_STACK);
-                            sp = 0;
-                        } else if (pa && pb) {
-                            if (da < db) {
-                                stk_node[sp] = nb; stk_dist[sp] = db; ++sp;
-                                stk_node[sp] = na; stk_dist[sp] = da; ++sp;
-                            } else {
-                                stk_node[sp] = na; stk_dist[sp] = da; ++sp;
-                                stk_node[sp] = nb; stk_dist[sp] = db; ++sp;
-                            }
-                        } else if (pa) {
+        // D. one node pop per lane (IntersectTrianglesBVH's loop body)
+        if (in_inst && !pending && sp > 0) {
+            --sp;
+            const uint32_t ni = stk_node[sp];
+            const float nd = stk_dist[sp];
+            if (COUNT) ++h.bvh_tests;
+            if (!(nd < 0.0f) && !(nd > __fadd_rn(h.t, 0.1f))) {
+                const uint32_t na = f2u(__ldg(&nodes[2 * ni].w));
+                const uint32_t nb = f2u(__ldg(&nodes[2 * ni + 1].w));
+                if (na & MT_BVH_LEAF_BIT) {
+                    pending = true;
+                    pfirst = na & ~MT_BVH_LEAF_BIT;
+                    pcount = nb & ~MT_BVH_LEAF_BIT;
+                    pnode = ni;
+                } else {
+                    if (COUNT) ++h.inner;
+                    const float4 a0 = __ldg(nodes + 2 * na), a1 = __ldg(nodes + 2 * na + 1);
+                    const float4 b0 = __ldg(nodes + 2 * nb), b1 = __ldg(nodes + 2 * nb + 1);
+                    const float da = slab(lo, linv, xyz(a0), xyz(a1));
+                    const float db = slab(lo, linv, xyz(b0), xyz(b1));
+                    const float lim = __fadd_rn(h.t, 0.1f);
+                    const bool pa = da >= 0.0f && da <= lim;
+                    const bool pb = db >= 0.0f && db <= lim;
+                    if (sp + 2 > MT_STACK_SIZE) {
+                        atomicOr(S.error_flag, MT_ERRBIT_STACK);
+                        sp = 0;
+                    } else if (pa && pb) {
+                        if (da < db) {
+                            stk_node[sp] = nb; stk_dist[sp] = db; ++sp;
                             stk_node[sp] = na; stk_dist[sp] = da; ++sp;
-                        } else if (pb) {
+                        } else {
+                            stk_node[sp] = na; stk_dist[sp] = da; ++sp;
                             stk_node[sp] = nb; stk_dist[sp] = db; ++sp;
                         }
+                    } else if (pa) {
+                        stk_node[sp] = na; stk_dist[sp] = da; ++sp;
+                    } else if (pb) {
+                        stk_node[sp] = nb; stk_dist[sp] = db; ++sp;
                     }
-                }
-            }
-
-            // 3. the warp tests every pending leaf together
-            uint32_t pm = __ballot_sync(MT_FULL, pending);
-            while (pm) {
-                const uint32_t L = __ffs(pm) - 1;
-                pm &= pm - 1;
-                const f3 ro = {__shfl_sync(MT_FULL, lo.x, L), __shfl_sync(MT_FULL, lo.y, L),
-                               __shfl_sync(MT_FULL, lo.z, L)};
-                const f3 rd = {__shfl_sync(MT_FULL, ld.x, L), __shfl_sync(MT_FULL, ld.y, L),
-                               __shfl_sync(MT_FULL, ld.z, L)};
-                const float dist = __shfl_sync(MT_FULL, h.t, L);
-                const uint32_t base = __shfl_sync(MT_FULL, slot_base + pfirst, L);
-                const uint32_t count = __shfl_sync(MT_FULL, pcount, L);
-                float bt = FLT_MAX, bu = 0.0f, bv = 0.0f;
-                uint32_t bi = 0xffffffffu;
-                for (uint32_t c = 0; c < count; c += 32) {
-                    const uint32_t i = c + lane;
-                    float t = FLT_MAX, u = 0.0f, v = 0.0f, det = 1.0f;
-                    bool ok = false;
-                    if (i < count) {
-                        const float4* sl = S.slots + 3ull * (base + i);
-                        const float4 A = __ldg(sl), B = __ldg(sl + 1), C = __ldg(sl + 2);
-                        ok = tri_test(ro, rd, xyz(A), xyz(B), xyz(C), t, u, v, det) && t > 0.0f && t < dist;
-                    }
-                    float kt = ok ? t : FLT_MAX;
-                    uint32_t ki = ok ? i : 0xffffffffu;
-#pragma unroll
-                    for (int off = 16; off > 0; off >>= 1) {
-                        const float ot = __shfl_xor_sync(MT_FULL, kt, off);
-                        const uint32_t oi = __shfl_xor_sync(MT_FULL, ki, off);
-                        if (key_less(ot, oi, kt, ki)) {
-                            kt = ot;
-                            ki = oi;
-                        }
-                    }
-                    if (ki != 0xffffffffu && key_less(kt, ki, bt, bi)) {
-                        const uint32_t w = ki - c;
-                        float uu = 0.0f, vv = 0.0f;
-                        if (ok) {
-                            const float id = __fdiv_rn(1.0f, det);
-                            uu = __fmul_rn(u, id);
-                            vv = __fmul_rn(v, id);
-                        }
-                        bt = kt;
-                        bi = ki;
-                        bu = __shfl_sync(MT_FULL, uu, w);
-                        bv = __shfl_sync(MT_FULL, vv, w);
-                    }
-                }
-                if (lane == L) {
-                    if (COUNT) h.tri_tests += count;
-                    if (bi != 0xffffffffu) {
-                        h.t = bt;
-                        h.u = bu;
-                        h.v = bv;
-                        h.slot = pfirst + bi;
-                        h.bv = pnode;
-                        if (ANY) {
-                            const DevInstance& I = S.instances[ii];
-                            float model[16];
-#pragma unroll
-                            for (int k = 0; k < 16; ++k) model[k] = __ldg(&I.model[k]);
-                            const f3 wp = xform_point(model, lo + bt * ld);
-                            if (!(length(wp - o) > tmax)) {
-                                stopped = true;
-                                best.hit = true;
-                                best.inst = ii;
-                                if (COUNT) {
-                                    best.tot_pops += h.bvh_tests;
-                                    best.tot_inner += h.inner;
-                                    best.tot_tris += h.tri_tests;
-                                }
-                                sp = 0;
-                                mask = 0;
-                                in_inst = false;
-                            }
-                        }
-                    }
-                    pending = false;
                 }
             }
         }
-        if (ANY && __all_sync(MT_FULL, stopped || !active)) break;
+
+        // E. the warp tests every pending leaf together
+        uint32_t pm = __ballot_sync(MT_FULL, pending);
+        while (pm) {
+            const uint32_t L = __ffs(pm) - 1;
+            pm &= pm - 1;
+            const f3 ro = {__shfl_sync(MT_FULL, lo.x, L), __shfl_sync(MT_FULL, lo.y, L),
+                           __shfl_sync(MT_FULL, lo.z, L)};
+            const f3 rd = {__shfl_sync(MT_FULL, ld.x, L), __shfl_sync(MT_FULL, ld.y, L),
+                           __shfl_sync(MT_FULL, ld.z, L)};
+            const float dist = __shfl_sync(MT_FULL, h.t, L);
+            const uint32_t base = __shfl_sync(MT_FULL, slot_base + pfirst, L);
+            const uint32_t count = __shfl_sync(MT_FULL, pcount, L);
+            float bt = FLT_MAX, bu = 0.0f, bv = 0.0f;
+            uint32_t bidx = 0xffffffffu;
+            for (uint32_t c = 0; c < count; c += 32) {
+                const uint32_t i = c + lane;
+                float t = FLT_MAX, u = 0.0f, v = 0.0f, det = 1.0f;
+                bool ok = false;
+                if (i < count) {
+                    const float4* sl = S.slots + 3ull * (base + i);
+                    const float4 A = __ldg(sl), B = __ldg(sl + 1), C = __ldg(sl + 2);
+                    ok = tri_test(ro, rd, xyz(A), xyz(B), xyz(C), t, u, v, det) && t > 0.0f && t < dist;
+                }
+                float kt = ok ? t : FLT_MAX;
+                uint32_t ki = ok ? i : 0xffffffffu;
+#pragma unroll
+                for (int off = 16; off > 0; off >>= 1) {
+                    const float ot = __shfl_xor_sync(MT_FULL, kt, off);
+                    const uint32_t oi = __shfl_xor_sync(MT_FULL, ki, off);
+                    if (key_less(ot, oi, kt, ki)) {
+                        kt = ot;
+                        ki = oi;
+                    }
+                }
+                if (ki != 0xffffffffu && key_less(kt, ki, bt, bidx)) {
+                    const uint32_t w = ki - c;
+                    float uu = 0.0f, vv = 0.0f;
+                    if (ok) {
+                        const float id = __fdiv_rn(1.0f, det);
+                        uu = __fmul_rn(u, id);
+                        vv = __fmul_rn(v, id);
+                    }
+                    bt = kt;
+                    bidx = ki;
+                    bu = __shfl_sync(MT_FULL, uu, w);
+                    bv = __shfl_sync(MT_FULL, vv, w);
+                }
+            }
+            if (lane == L) {
+                if (COUNT) h.tri_tests += count;
+                pending = false;
+                if (bidx != 0xffffffffu) {
+                    h.t = bt;
+                    h.u = bu;
+                    h.v = bv;
+                    h.slot = pfirst + bidx;
+                    h.bv = pnode;
+                    if (ANY) {
+                        const DevInstance& I = S.instances[ii];
+                        float model[16];
+#pragma unroll
+                        for (int q = 0; q < 16; ++q) model[q] = __ldg(&I.model[q]);
+                        const f3 wp = xform_point(model, lo + bt * ld);
+                        if (!(length(wp - o) > tmax)) {
+                            stopped = true;
+                            best.hit = true;
+                            best.inst = ii;
+                            if (COUNT) {
+                                best.tot_pops += h.bvh_tests;
+                                best.tot_inner += h.inner;
+                                best.tot_tris += h.tri_tests;
+                            }
+                            sp = 0;
+                            mask = 0;
+                            in_inst = false;
+                        }
+                    }
+                }
+            }
+        }
     }
-    return best;
 }
 
 // ---------------------------------------------------------------------------

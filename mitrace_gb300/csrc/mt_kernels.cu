@@ -33,63 +33,64 @@ __device__ __forceinline__ uint32_t warp_append(uint32_t* counter)
 // ---------------------------------------------------------------------------
 // Ray queries
 // ---------------------------------------------------------------------------
-// Warp-uniform loop over a range: every lane of a warp calls trace_warp together.
-#define MT_WARP_LOOP(n)                                                                             \
-    const uint32_t lane_ = threadIdx.x & 31;                                                        \
-    const uint64_t warp0_ = (blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x) >> 5;    \
-    const uint64_t nwarps_ = (static_cast<uint64_t>(gridDim.x) * blockDim.x) >> 5;                  \
-    for (uint64_t base_ = warp0_ * 32; base_ < (n); base_ += nwarps_ * 32)
-
+// Ray-query work for trace_persistent: rays in, mt_hit records out.
 template <int QUERY>
-__global__ void __launch_bounds__(128) k_trace(DevScene S, const mt_ray* __restrict__ rays,
-                                               uint64_t n, mt_hit* __restrict__ hits)
-{
-    MT_WARP_LOOP(n)
+struct QueryWork {
+    const mt_ray* rays;
+    mt_hit* hits;
+    uint32_t n;
+    uint32_t idx;
+    __device__ bool fetch(uint32_t i, f3& o, f3& d, float& tmax)
     {
-        const uint64_t i = base_ + lane_;
-        const bool active = i < n;
-        float4 a = make_float4(0, 0, 0, 0), b = make_float4(0, 0, 1, 0);
-        if (active) {
-            a = __ldg(reinterpret_cast<const float4*>(rays + i));
-            b = __ldg(reinterpret_cast<const float4*>(rays + i) + 1);
-        }
+        if (i >= n) return false;
+        idx = i;
+        const float4 a = __ldg(reinterpret_cast<const float4*>(rays + i));
+        const float4 b = __ldg(reinterpret_cast<const float4*>(rays + i) + 1);
+        o = xyz(a);
+        d = xyz(b);
+        tmax = a.w;
+        return true;
+    }
+    __device__ void finish(const SceneHit& sh)
+    {
         mt_hit h;
         if (QUERY == MT_QUERY_ANY) {
-            const SceneHit sh = trace_warp<false, true>(S, xyz(a), xyz(b), a.w, active);
-            h.distance = 0.0f;
-            h.u = h.v = 0.0f;
+            h.distance = h.u = h.v = 0.0f;
             h.instance = sh.hit ? 1u : 0u;
             h.triangle = h.bv_index = h.bvh_tests = h.tri_tests = 0;
+        } else if (sh.hit) {
+            h.distance = sh.dist;
+            h.u = sh.u;
+            h.v = sh.v;
+            h.instance = sh.inst;
+            h.triangle = sh.tri;
+            h.bv_index = sh.bv;
+            h.bvh_tests = sh.bvh_tests;
+            h.tri_tests = sh.tri_tests;
         } else {
-            constexpr bool kCount = QUERY == MT_QUERY_CLOSEST_COUNT || QUERY == MT_QUERY_CLOSEST_TOTALS;
-            const SceneHit sh = trace_warp<kCount, false>(S, xyz(a), xyz(b), 0.0f, active);
-            if (sh.hit) {
-                h.distance = sh.dist;
-                h.u = sh.u;
-                h.v = sh.v;
-                h.instance = sh.inst;
-                h.triangle = sh.tri;
-                h.bv_index = sh.bv;
-                h.bvh_tests = sh.bvh_tests;
-                h.tri_tests = sh.tri_tests;
-            } else {
-                h.distance = h.u = h.v = 0.0f;
-                h.instance = MT_NO_HIT;
-                h.triangle = h.bv_index = h.bvh_tests = h.tri_tests = 0;
-            }
-            if (QUERY == MT_QUERY_CLOSEST_TOTALS) {
-                h.bv_index = sh.tot_inner;
-                h.bvh_tests = sh.tot_pops;
-                h.tri_tests = sh.tot_tris;
-            }
+            h.distance = h.u = h.v = 0.0f;
+            h.instance = MT_NO_HIT;
+            h.triangle = h.bv_index = h.bvh_tests = h.tri_tests = 0;
         }
-        if (active) {
-            float4* dst = reinterpret_cast<float4*>(hits + i);
-            dst[0] = make_float4(h.distance, h.u, h.v, __uint_as_float(h.instance));
-            dst[1] = make_float4(__uint_as_float(h.triangle), __uint_as_float(h.bv_index),
-                                 __uint_as_float(h.bvh_tests), __uint_as_float(h.tri_tests));
+        if (QUERY == MT_QUERY_CLOSEST_TOTALS) {
+            h.bv_index = sh.tot_inner;
+            h.bvh_tests = sh.tot_pops;
+            h.tri_tests = sh.tot_tris;
         }
+        float4* dst = reinterpret_cast<float4*>(hits + idx);
+        dst[0] = make_float4(h.distance, h.u, h.v, __uint_as_float(h.instance));
+        dst[1] = make_float4(__uint_as_float(h.triangle), __uint_as_float(h.bv_index),
+                             __uint_as_float(h.bvh_tests), __uint_as_float(h.tri_tests));
     }
+};
+
+template <int QUERY>
+__global__ void __launch_bounds__(128) k_trace(DevScene S, const mt_ray* __restrict__ rays, uint32_t n,
+                                               mt_hit* __restrict__ hits, uint32_t* fetch)
+{
+    QueryWork<QUERY> W{rays, hits, n, 0};
+    constexpr bool kCount = QUERY == MT_QUERY_CLOSEST_COUNT || QUERY == MT_QUERY_CLOSEST_TOTALS;
+    trace_persistent<kCount, QUERY == MT_QUERY_ANY>(S, W, fetch);
 }
 
 __global__ void k_brdf(const mt_brdf_query* __restrict__ q, uint64_t n, mt_brdf_result* __restrict__ out)
@@ -130,7 +131,10 @@ __device__ __forceinline__ void path_coords(const DevScene& S, const BatchInfo& 
 __global__ void __launch_bounds__(256) k_raygen(DevScene S, PathState P, BatchInfo B,
                                                 uint32_t* __restrict__ q0, uint32_t* counts)
 {
-    if (blockIdx.x == 0 && threadIdx.x == 0) counts[0] = B.n;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        counts[0] = B.n;
+        counts[3] = 0;  // ray fetch counter of the first extend
+    }
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < B.n; p += gridDim.x * blockDim.x) {
         uint32_t pixel, sample;
         path_coords(S, B, p, pixel, sample);
@@ -174,33 +178,25 @@ __device__ __forceinline__ void flush_counts(unsigned long long* cnt, uint32_t p
     }
 }
 
+// Extension rays of the live paths (queue q) -> hit records per path.
 template <bool COUNT>
-__global__ void __launch_bounds__(128) k_extend(DevScene S, PathState P,
-                                                const uint32_t* __restrict__ q,
-                                                uint32_t* counts, int cur,
-                                                unsigned long long* rays,
-                                                unsigned long long* cnt)
-{
-    const uint32_t n = counts[cur];
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        counts[cur ^ 1] = 0;
-        counts[2] = 0;
-        atomicAdd(rays, static_cast<unsigned long long>(n));
-    }
-    uint32_t pops = 0, inner = 0, tris = 0;
-    MT_WARP_LOOP(n)
+struct ExtendWork {
+    PathState P;
+    const uint32_t* q;
+    uint32_t n;
+    uint32_t p;
+    uint32_t pops, inner, tris;
+    __device__ bool fetch(uint32_t i, f3& o, f3& d, float& tmax)
     {
-        const uint64_t i = base_ + lane_;
-        const bool active = i < n;
-        uint32_t p = 0;
-        float4 o = make_float4(0, 0, 0, 0), d = make_float4(0, 0, 1, 0);
-        if (active) {
-            p = q[i];
-            o = P.ro[p];
-            d = P.rd[p];
-        }
-        const SceneHit h = trace_warp<COUNT, false>(S, xyz(o), xyz(d), 0.0f, active);
-        if (!active) continue;
+        if (i >= n) return false;
+        p = q[i];
+        o = xyz(P.ro[p]);
+        d = xyz(P.rd[p]);
+        tmax = 0.0f;
+        return true;
+    }
+    __device__ void finish(const SceneHit& h)
+    {
         if (COUNT) {
             pops += h.tot_pops;
             inner += h.tot_inner;
@@ -213,7 +209,25 @@ __global__ void __launch_bounds__(128) k_extend(DevScene S, PathState P,
             P.hitB[p] = make_uint4(MT_NO_HIT, 0u, 0u, 0u);
         }
     }
-    if (COUNT) flush_counts(cnt, pops, inner, tris);
+};
+
+template <bool COUNT>
+__global__ void __launch_bounds__(128) k_extend(DevScene S, PathState P,
+                                                const uint32_t* __restrict__ q,
+                                                uint32_t* counts, int cur,
+                                                unsigned long long* rays,
+                                                unsigned long long* cnt)
+{
+    const uint32_t n = counts[cur];
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        counts[cur ^ 1] = 0;
+        counts[2] = 0;
+        counts[4] = 0;  // ray fetch counter of this bounce's shadow stage
+        atomicAdd(rays, static_cast<unsigned long long>(n));
+    }
+    ExtendWork<COUNT> W{P, q, n, 0, 0, 0, 0};
+    trace_persistent<COUNT, false>(S, W, &counts[3]);
+    if (COUNT) flush_counts(cnt, W.pops, W.inner, W.tris);
 }
 
 __device__ __forceinline__ f3 ld4(const float4* p, uint32_t i)
@@ -386,39 +400,55 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, PathState P, ShadowQu
     }
 }
 
+// Shadow rays queued by k_shade: an unoccluded ray adds its contribution to
+// the owning path's direct (first vertex) or indirect light (Tracer.cpp:322-336).
 template <bool COUNT>
-__global__ void __launch_bounds__(128) k_shadow(DevScene S, PathState P, ShadowQueue SQ,
-                                                const uint32_t* counts,
-                                                unsigned long long* rays,
-                                                unsigned long long* cnt)
-{
-    const uint32_t n = counts[2];
-    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(rays, static_cast<unsigned long long>(n));
-    uint32_t pops = 0, inner = 0, tris = 0;
-    MT_WARP_LOOP(n)
+struct ShadowWork {
+    PathState P;
+    ShadowQueue SQ;
+    uint32_t n;
+    uint32_t i;
+    uint32_t pops, inner, tris;
+    __device__ bool fetch(uint32_t k, f3& o, f3& d, float& tmax)
     {
-        const uint64_t i = base_ + lane_;
-        const bool active = i < n;
-        float4 o = make_float4(0, 0, 0, 0), d = make_float4(0, 0, 1, 0);
-        if (active) {
-            o = SQ.o[i];
-            d = SQ.d[i];
-        }
-        const SceneHit h = trace_warp<COUNT, true>(S, xyz(o), xyz(d), o.w, active);
-        if (!active) continue;
+        if (k >= n) return false;
+        i = k;
+        const float4 a = SQ.o[k], b = SQ.d[k];
+        o = xyz(a);
+        d = xyz(b);
+        tmax = a.w;
+        return true;
+    }
+    __device__ void finish(const SceneHit& h)
+    {
         if (COUNT) {
             pops += h.tot_pops;
             inner += h.tot_inner;
             tris += h.tot_tris;
         }
-        if (h.hit) continue;
+        if (h.hit) return;
         const float4 c = SQ.c[i];
-        const uint32_t p = __float_as_uint(d.w);
+        const uint32_t p = __float_as_uint(SQ.d[i].w);
         float4* acc = c.w != 0.0f ? P.direct : P.indirect;
         const float4 a = acc[p];
         acc[p] = make_float4(__fadd_rn(a.x, c.x), __fadd_rn(a.y, c.y), __fadd_rn(a.z, c.z), 0.0f);
     }
-    if (COUNT) flush_counts(cnt, pops, inner, tris);
+};
+
+template <bool COUNT>
+__global__ void __launch_bounds__(128) k_shadow(DevScene S, PathState P, ShadowQueue SQ,
+                                                uint32_t* counts,
+                                                unsigned long long* rays,
+                                                unsigned long long* cnt)
+{
+    const uint32_t n = counts[2];
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        counts[3] = 0;  // ray fetch counter of the next bounce's extend
+        atomicAdd(rays, static_cast<unsigned long long>(n));
+    }
+    ShadowWork<COUNT> W{P, SQ, n, 0, 0, 0, 0};
+    trace_persistent<COUNT, true>(S, W, &counts[4]);
+    if (COUNT) flush_counts(cnt, W.pops, W.inner, W.tris);
 }
 
 __global__ void __launch_bounds__(256) k_finalize(DevScene S, PathState P, BatchInfo B,
@@ -506,18 +536,44 @@ static unsigned grid_for(uint64_t n, unsigned block, unsigned per_sm)
     return static_cast<unsigned>(need < cap ? (need ? need : 1) : cap);
 }
 
+// One resident wave of blocks for a persistent kernel.
+template <class K>
+static unsigned persistent_grid(K kernel, int block)
+{
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, 0) != cudaSuccess || per_sm < 1)
+        per_sm = 1;
+    return static_cast<unsigned>(per_sm * sm_count());
+}
+
+template <int Q>
+static cudaError_t trace_chunks(const DevScene& S, const mt_ray* rays, uint64_t n, mt_hit* hits,
+                                uint32_t* fetch, cudaStream_t st)
+{
+    static unsigned grid = 0;
+    if (!grid) grid = persistent_grid(k_trace<Q>, 128);
+    const uint64_t chunk = 1ull << 30;
+    for (uint64_t b = 0; b < n; b += chunk) {
+        const uint32_t m = static_cast<uint32_t>(n - b < chunk ? n - b : chunk);
+        cudaError_t e = cudaMemsetAsync(fetch, 0, sizeof(uint32_t), st);
+        if (e != cudaSuccess) return e;
+        k_trace<Q><<<grid, 128, 0, st>>>(S, rays + b, m, hits + b, fetch);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
 cudaError_t launch_trace(const DevScene& S, const mt_ray* rays, uint64_t n, mt_hit* hits, int query,
-                         cudaStream_t st)
+                         uint32_t* fetch, cudaStream_t st)
 {
     if (n == 0) return cudaSuccess;
-    const unsigned g = grid_for(n, 128, 64);
     switch (query) {
-        case MT_QUERY_ANY: k_trace<MT_QUERY_ANY><<<g, 128, 0, st>>>(S, rays, n, hits); break;
-        case MT_QUERY_CLOSEST_COUNT: k_trace<MT_QUERY_CLOSEST_COUNT><<<g, 128, 0, st>>>(S, rays, n, hits); break;
-        case MT_QUERY_CLOSEST_TOTALS: k_trace<MT_QUERY_CLOSEST_TOTALS><<<g, 128, 0, st>>>(S, rays, n, hits); break;
-        default: k_trace<MT_QUERY_CLOSEST><<<g, 128, 0, st>>>(S, rays, n, hits); break;
+        case MT_QUERY_ANY: return trace_chunks<MT_QUERY_ANY>(S, rays, n, hits, fetch, st);
+        case MT_QUERY_CLOSEST_COUNT: return trace_chunks<MT_QUERY_CLOSEST_COUNT>(S, rays, n, hits, fetch, st);
+        case MT_QUERY_CLOSEST_TOTALS: return trace_chunks<MT_QUERY_CLOSEST_TOTALS>(S, rays, n, hits, fetch, st);
+        default: return trace_chunks<MT_QUERY_CLOSEST>(S, rays, n, hits, fetch, st);
     }
-    return cudaGetLastError();
 }
 
 cudaError_t launch_brdf(const mt_brdf_query* q, uint64_t n, mt_brdf_result* out, cudaStream_t st)
@@ -576,6 +632,13 @@ cudaError_t launch_batch(const DevScene& S, const PathState& P, const ShadowQueu
 {
     BatchInfo B{g0, n, band_pix, pix_base};
     const unsigned gw = grid_for(n, 128, 16);
+    static unsigned g_ext[2] = {0, 0}, g_sh[2] = {0, 0};
+    if (!g_ext[0]) {
+        g_ext[0] = persistent_grid(k_extend<false>, 128);
+        g_ext[1] = persistent_grid(k_extend<true>, 128);
+        g_sh[0] = persistent_grid(k_shadow<false>, 128);
+        g_sh[1] = persistent_grid(k_shadow<true>, 128);
+    }
     const bool count = prof && prof->counting;
     unsigned long long* cnt = prof ? prof->d_counts : nullptr;
     auto begin = [&](int s) { if (prof) prof->begin(s, st); };
@@ -588,18 +651,18 @@ cudaError_t launch_batch(const DevScene& S, const PathState& P, const ShadowQueu
     for (uint32_t b = 0; b < S.bounces; ++b) {
         begin(MT_STAGE_EXTEND);
         if (count)
-            k_extend<true><<<gw, 128, 0, st>>>(S, P, W.q[cur], W.counts, cur, W.rays, cnt);
+            k_extend<true><<<g_ext[1], 128, 0, st>>>(S, P, W.q[cur], W.counts, cur, W.rays, cnt);
         else
-            k_extend<false><<<gw, 128, 0, st>>>(S, P, W.q[cur], W.counts, cur, W.rays, cnt);
+            k_extend<false><<<g_ext[0], 128, 0, st>>>(S, P, W.q[cur], W.counts, cur, W.rays, cnt);
         end(MT_STAGE_EXTEND);
         begin(MT_STAGE_SHADE);
         k_shade<<<gw, 128, 0, st>>>(S, P, SQ, B, b, W.q[cur], W.q[cur ^ 1], W.counts, cur);
         end(MT_STAGE_SHADE);
         begin(MT_STAGE_SHADOW);
         if (count)
-            k_shadow<true><<<gw, 128, 0, st>>>(S, P, SQ, W.counts, W.rays + 1, cnt ? cnt + 3 : nullptr);
+            k_shadow<true><<<g_sh[1], 128, 0, st>>>(S, P, SQ, W.counts, W.rays + 1, cnt ? cnt + 3 : nullptr);
         else
-            k_shadow<false><<<gw, 128, 0, st>>>(S, P, SQ, W.counts, W.rays + 1, nullptr);
+            k_shadow<false><<<g_sh[0], 128, 0, st>>>(S, P, SQ, W.counts, W.rays + 1, nullptr);
         end(MT_STAGE_SHADOW);
         l += 3;
         cur ^= 1;

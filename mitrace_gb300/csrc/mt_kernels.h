@@ -39,7 +39,8 @@ struct ShadowQueue {
 
 struct WaveBuffers {
     uint32_t* q[2];                // ping-pong queues of live path indices
-    uint32_t* counts;              // [0],[1] queue sizes, [2] shadow-queue size
+    uint32_t* counts;              // [0],[1] queue sizes, [2] shadow-queue size,
+                                   // [3] extend / [4] shadow ray fetch counters
     unsigned long long* rays;      // [0] extension rays, [1] shadow rays traced
     float* sr;                     // per-sample tonemapped R, sample-major in a band
     float* sg;
@@ -61,7 +62,7 @@ struct Profiler {
 };
 
 cudaError_t launch_trace(const DevScene& S, const mt_ray* rays, uint64_t n, mt_hit* hits, int query,
-                         cudaStream_t st);
+                         uint32_t* fetch, cudaStream_t st);
 cudaError_t launch_brdf(const mt_brdf_query* q, uint64_t n, mt_brdf_result* out, cudaStream_t st);
 cudaError_t launch_batch(const DevScene& S, const PathState& P, const ShadowQueue& SQ,
                          const WaveBuffers& W, uint64_t g0, uint32_t n, uint32_t band_pix,

@@ -98,14 +98,20 @@ def test_against_fp64(setup):
     # grazing hits: single-precision t is ill-conditioned there (0.13% of hits on the spheres)
     assert (t_rel <= 1e-5).mean() >= 0.998, f"{name}: t rel error quantiles {np.quantile(t_rel, [0.99, 1])}"
     bary = np.abs(f[hit, 1:3] - ref[hit, 1:3]).max(axis=1)
-    # per-triangle scale: the longest edge of the hit triangle in world units
+    # single-precision Moller-Trumbore error bound: eps * distance / (smallest
+    # altitude of the triangle * |cos| of the incidence angle), times 32
     pos = {i: scene.meshes[it.mesh].positions for i, it in enumerate(scene.instances)}
-    tri = np.stack([pos[int(i)][int(t)] for i, t in zip(g[hit, 3], g[hit, 4])])
-    h = np.max(np.linalg.norm(tri[:, [1, 2, 0]] - tri, axis=-1), axis=1)
-    bound = 1e-5 + 4 * np.finfo(np.float32).eps * (ref[hit, 0] + 1.0) / h
-    frac = (bary <= bound).mean()
-    assert frac >= 0.999, f"{name}: {frac:.5f} of barycentrics within the float32 bound"
-    big = h >= 0.5
+    tri = np.stack([pos[int(i)][int(t)] for i, t in zip(g[hit, 3], g[hit, 4])]).astype(np.float64)
+    e = tri[:, [1, 2, 0]] - tri
+    n = np.cross(tri[:, 1] - tri[:, 0], tri[:, 2] - tri[:, 0])
+    area2 = np.linalg.norm(n, axis=1)
+    alt = area2 / np.linalg.norm(e, axis=-1).max(axis=1)
+    cosg = np.abs((n / area2[:, None] * rays[hit, 4:7]).sum(axis=1))
+    bound = 32 * np.finfo(np.float32).eps * (ref[hit, 0] + 1.0) / alt / np.maximum(cosg, 1e-3)
+    worst = np.argmax(bary / bound)
+    assert np.all(bary <= bound), f"{name}: barycentric error {bary[worst]:.3g} above bound {bound[worst]:.3g}"
+    # large triangles (walls, ground, terrain cells seen head-on) meet 1e-5 outright
+    big = (alt >= 0.25) & (cosg > 0.2)
     if big.any():
         assert (bary[big] <= 1e-5).mean() >= 0.999
 
