@@ -260,11 +260,6 @@ struct SceneHit {
 // Must be called by all 32 lanes of a warp together; inactive lanes help.
 #define MT_FULL 0xffffffffu
 
-__device__ __forceinline__ bool key_less(float ta, uint32_t ia, float tb, uint32_t ib)
-{
-    return ta < tb || (ta == tb && ia < ib);
-}
-
 // Persistent form: the warp keeps running until the work source is empty.  A
 // lane whose ray is finished takes the next one (one atomic per warp), so no
 // lane idles while its neighbours finish long rays.  The instance boxes a new
@@ -490,27 +485,21 @@ __device__ __forceinline__ void trace_persistent(const DevScene& S, Work& W, uin
                     const float4 A = __ldg(sl), B = __ldg(sl + 1), C = __ldg(sl + 2);
                     ok = tri_test(ro, rd, xyz(A), xyz(B), xyz(C), t, u, v, det) && t > 0.0f && t < dist;
                 }
-                float kt = ok ? t : FLT_MAX;
-                uint32_t ki = ok ? i : 0xffffffffu;
-#pragma unroll
-                for (int off = 16; off > 0; off >>= 1) {
-                    const float ot = __shfl_xor_sync(MT_FULL, kt, off);
-                    const uint32_t oi = __shfl_xor_sync(MT_FULL, ki, off);
-                    if (key_less(ot, oi, kt, ki)) {
-                        kt = ot;
-                        ki = oi;
-                    }
-                }
-                if (ki != 0xffffffffu && key_less(kt, ki, bt, bidx)) {
-                    const uint32_t w = ki - c;
+                // valid t are > 0, whose IEEE bit patterns order like the values, so
+                // one unsigned min finds the smallest t and the lowest lane holding it
+                // is the first such triangle of this chunk
+                const uint32_t key = ok ? __float_as_uint(t) : 0xffffffffu;
+                const uint32_t kmin = __reduce_min_sync(MT_FULL, key);
+                if (kmin != 0xffffffffu && __uint_as_float(kmin) < bt) {
+                    const uint32_t w = __ffs(__ballot_sync(MT_FULL, key == kmin)) - 1;
                     float uu = 0.0f, vv = 0.0f;
-                    if (ok) {
+                    if (lane == w) {
                         const float id = __fdiv_rn(1.0f, det);
                         uu = __fmul_rn(u, id);
                         vv = __fmul_rn(v, id);
                     }
-                    bt = kt;
-                    bidx = ki;
+                    bt = __uint_as_float(kmin);
+                    bidx = c + w;
                     bu = __shfl_sync(MT_FULL, uu, w);
                     bv = __shfl_sync(MT_FULL, vv, w);
                 }
