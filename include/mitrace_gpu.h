@@ -226,6 +226,25 @@ int mt_is_done(const mt_handle* h);
  * enqueued; rays/samples are added to the handle's counters. */
 mt_status mt_render_device(mt_handle* h, float* d_rgb_out, void* cuda_stream);
 
+/* Allocation-free render of rows [row0, row1) into a caller-owned DEVICE
+ * buffer holding the whole W*H*3 image (only those rows are written), enqueued
+ * on cuda_stream (0 = the legacy default stream).  No counterpart in the
+ * reference: it exists for callers that must not allocate GPU memory while
+ * they render (a fixed memory budget reserved up front, a frame loop or host
+ * callback that must not block in the allocator, an allocator hooked by
+ * another library).  All scratch lives in one static device array of
+ * MT_NOALLOC_SCRATCH_BYTES that every GPU loading the library keeps until
+ * exit; one call renders at most MT_NOALLOC_MAX_PATHS paths
+ * ((row1 - row0) * width * samples), larger requests return MT_ERR_INVALID.
+ * Calls share that array: work of two calls that overlaps on the GPU races, so
+ * serialise them.  The first call on a device looks up the array's address;
+ * make it before any stream capture.  Same kernels and results as
+ * mt_render_device for those rows. */
+#define MT_NOALLOC_MAX_PATHS 65536u
+#define MT_NOALLOC_SCRATCH_BYTES (16u << 20)
+mt_status mt_render_rows_noalloc(mt_handle* h, uint32_t row0, uint32_t row1, float* d_rgb_out,
+                                 void* cuda_stream);
+
 /* ------------------------------------------------------------------------ */
 /* Ray queries (test and microbench entry points).                          */
 /* ------------------------------------------------------------------------ */

@@ -182,6 +182,8 @@ class mt_stage_profile(C.Structure):
 MT_STAGE_RAYGEN, MT_STAGE_EXTEND, MT_STAGE_SHADE, MT_STAGE_SHADOW, MT_STAGE_FINALIZE, MT_STAGE_RESOLVE = range(6)
 MT_NUM_STAGES = 6
 MT_QUERY_CLOSEST_TOTALS = 3
+MT_NOALLOC_MAX_PATHS = 65536
+MT_NOALLOC_SCRATCH_BYTES = 16 << 20
 
 
 class mt_profile(C.Structure):
@@ -215,6 +217,7 @@ PROTOTYPES = [
     ("mt_get_stats", C.c_int, [_VP, C.POINTER(mt_stats)]),
     ("mt_is_done", C.c_int, [_VP]),
     ("mt_render_device", C.c_int, [_VP, _VP, _VP]),
+    ("mt_render_rows_noalloc", C.c_int, [_VP, C.c_uint32, C.c_uint32, _VP, _VP]),
     ("mt_trace_rays", C.c_int, [_VP, _VP, C.c_uint64, _VP, C.c_int]),
     ("mt_trace_rays_device", C.c_int, [_VP, _VP, C.c_uint64, _VP, C.c_int, _VP]),
     ("mt_brdf_batch", C.c_int, [_VP, C.c_uint64, _VP]),

@@ -20,6 +20,7 @@
 
 #include "../../include/mitrace_gpu.h"
 #include "mt_device.cuh"
+#include "mt_internal.h"
 #include "mt_kernels.h"
 
 using namespace mt;
@@ -643,6 +644,14 @@ mt_status check_handle(const mt_handle* h)
 }
 
 }  // namespace
+
+namespace mt {
+
+const DevScene* internal_scene(const mt_handle* h) { return h ? &h->S : nullptr; }
+bool internal_busy(const mt_handle* h) { return h && h->running.load() != 0; }
+mt_status internal_error(mt_status code, const std::string& msg) { return set_err(code, msg); }
+
+}  // namespace mt
 
 extern "C" {
 
