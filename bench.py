@@ -56,6 +56,9 @@ def parse():
     p.add_argument("--e2e-steps", type=int, default=None)
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-microbench", action="store_true",
+                   help="skip the 16M incoherent-ray closest/any-hit microbench on the large scene")
+    p.add_argument("--microbench-rays", type=int, default=1 << 24)
     return p.parse_args()
 
 
@@ -197,6 +200,63 @@ def run_reference(a):
         "e2e": {"value": v, "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+# --------------------------------------------------------------------------- microbench
+def microbench(a, dev, peak):
+    """Incoherent rays (origins uniform in the scene box, directions uniform on
+    the sphere, seed 0) against the large scene: fBm terrain of 2 * 1023^2
+    triangles plus 50k icospheres of 80 triangles, each set one mesh.  Closest
+    hit and any hit through mt_trace_rays_device; device-resident rays and
+    hits (> L2), CUDA events on the launching stream."""
+    import ctypes as C
+
+    import numpy as np
+    import torch
+
+    import mitrace_gb300 as mt
+    from mitrace_gb300 import _abi as A
+
+    scene, cfg = mt.large_scene(samples=1)
+    lo, hi = mt.scene_bounds(scene)
+    n = a.microbench_rays
+    rays = mt.incoherent_rays(lo, hi, n, seed=0)
+    t0 = time.perf_counter()
+    tr = mt.Tracer(scene, cfg)
+    create_s = time.perf_counter() - t0
+    stream = torch.cuda.current_stream(dev)
+    d_rays = torch.from_numpy(rays).to(dev)
+    d_hits = torch.empty((n, 8), dtype=torch.int32, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    out = {"scene": "fBm terrain 2x1023^2 tris + 50k icospheres x 80 tris (merged meshes)",
+           "triangles": scene.num_triangles, "rays": n, "create_s": create_s}
+    # traversal work of the closest-hit query (untimed counting pass)
+    tr.trace_device(d_rays.data_ptr(), n, d_hits.data_ptr(), A.MT_QUERY_CLOSEST_TOTALS, stream.cuda_stream)
+    torch.cuda.synchronize()
+    h = d_hits.cpu().numpy().view(np.uint32)
+    inner, tris = int(h[:, 5].astype(np.uint64).sum()), int(h[:, 7].astype(np.uint64).sum())
+    alg_bytes = 64 * inner + 40 * tris + 64 * n
+    out["hit_fraction"] = float((h[:, 3] != A.MT_NO_HIT).mean())
+    out["per_ray"] = {"inner_pops": inner / n, "tri_tests": tris / n, "node_pops": float(h[:, 6].mean())}
+    for name, q in (("closest", A.MT_QUERY_CLOSEST), ("any", A.MT_QUERY_ANY)):
+        tr.trace_device(d_rays.data_ptr(), n, d_hits.data_ptr(), q, stream.cuda_stream)  # warm-up
+        ms = []
+        for i in range(3):
+            flush.fill_(i)
+            s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s0.record(stream)
+            tr.trace_device(d_rays.data_ptr(), n, d_hits.data_ptr(), q, stream.cuda_stream)
+            s1.record(stream)
+            torch.cuda.synchronize()
+            ms.append(s0.elapsed_time(s1))
+        t = statistics.median(ms)
+        out[f"{name}_mrays_s"] = n / (t / 1e3) / 1e6
+        out[f"{name}_ms"] = t
+    achieved = alg_bytes / (out["closest_ms"] / 1e3) / 1e9
+    out["roofline_closest"] = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                               "frac": achieved / peak, "alg_bytes": alg_bytes}
+    tr.close()
+    return out
 
 
 # --------------------------------------------------------------------------- GPU arm
@@ -357,6 +417,9 @@ def run_ours(a):
         "stage_ms_per_step": stage_ms,
         "clocks": clk,
     }
+    if not a.no_microbench:
+        torch.cuda.empty_cache()
+        line["incoherent"] = microbench(a, dev, peak)
     if not a.no_cpu_baseline:
         cb = cpu_baseline(scene, cfg, a.cpu_seconds)
         line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}

@@ -61,7 +61,12 @@ def _run_parallel(cmds):
 
 
 def build_product(force: bool = False, verbose: bool = False) -> Path:
+    """Compiles and links the library.  MT_NVCC_EXTRA (whitespace-separated
+    flags, e.g. -DMT_TRAVERSE_MIN_BLOCKS=5) is appended for tuning builds."""
     nvcc = nvcc_path()
+    extra = os.environ.get("MT_NVCC_EXTRA", "").split()
+    if extra:
+        force = True
     BUILD.mkdir(exist_ok=True)
     headers = list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.h")) + [ROOT / "include" / "mitrace_gpu.h"]
     objs, cmds = [], []
@@ -70,7 +75,7 @@ def build_product(force: bool = False, verbose: bool = False) -> Path:
         o = BUILD / (src + ".o")
         objs.append(o)
         if force or not _newer(o, [s, *headers]):
-            cmds.append([nvcc, *ARCH, *NVCC_FLAGS, "-c", str(s), "-o", str(o)])
+            cmds.append([nvcc, *ARCH, *NVCC_FLAGS, *extra, "-c", str(s), "-o", str(o)])
     if cmds:
         if verbose:
             for c in cmds:

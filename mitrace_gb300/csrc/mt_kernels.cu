@@ -17,6 +17,12 @@
 #include "mt_device.cuh"
 #include "mt_kernels.h"
 
+// Occupancy hint of the traversal kernels: blocks of 128 threads per SM that
+// the register allocation must allow (8 -> at most 64 registers per thread).
+#ifndef MT_TRAVERSE_MIN_BLOCKS
+#define MT_TRAVERSE_MIN_BLOCKS 8
+#endif
+
 namespace mt {
 
 __device__ __forceinline__ uint32_t warp_append(uint32_t* counter)
@@ -85,7 +91,7 @@ struct QueryWork {
 };
 
 template <int QUERY>
-__global__ void __launch_bounds__(128) k_trace(DevScene S, const mt_ray* __restrict__ rays, uint32_t n,
+__global__ void __launch_bounds__(128, MT_TRAVERSE_MIN_BLOCKS) k_trace(DevScene S, const mt_ray* __restrict__ rays, uint32_t n,
                                                mt_hit* __restrict__ hits, uint32_t* fetch)
 {
     QueryWork<QUERY> W{rays, hits, n, 0};
@@ -212,7 +218,7 @@ struct ExtendWork {
 };
 
 template <bool COUNT>
-__global__ void __launch_bounds__(128) k_extend(DevScene S, PathState P,
+__global__ void __launch_bounds__(128, MT_TRAVERSE_MIN_BLOCKS) k_extend(DevScene S, PathState P,
                                                 const uint32_t* __restrict__ q,
                                                 uint32_t* counts, int cur,
                                                 unsigned long long* rays,
@@ -436,7 +442,7 @@ struct ShadowWork {
 };
 
 template <bool COUNT>
-__global__ void __launch_bounds__(128) k_shadow(DevScene S, PathState P, ShadowQueue SQ,
+__global__ void __launch_bounds__(128, MT_TRAVERSE_MIN_BLOCKS) k_shadow(DevScene S, PathState P, ShadowQueue SQ,
                                                 uint32_t* counts,
                                                 unsigned long long* rays,
                                                 unsigned long long* cnt)
