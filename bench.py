@@ -59,6 +59,10 @@ def parse():
     p.add_argument("--no-microbench", action="store_true",
                    help="skip the 16M incoherent-ray closest/any-hit microbench on the large scene")
     p.add_argument("--microbench-rays", type=int, default=1 << 24)
+    p.add_argument("--time-to-relmse", action="store_true",
+                   help="instead of the throughput line: time to relMSE 0.01 against a high-spp reference")
+    p.add_argument("--ref-spp", type=int, default=16384)
+    p.add_argument("--relmse-target", type=float, default=0.01)
     return p.parse_args()
 
 
@@ -225,6 +229,7 @@ def microbench(a, dev, peak):
     tr = mt.Tracer(scene, cfg)
     create_s = time.perf_counter() - t0
     stream = torch.cuda.current_stream(dev)
+    assert stream.cuda_stream != 0
     d_rays = torch.from_numpy(rays).to(dev)
     d_hits = torch.empty((n, 8), dtype=torch.int32, device=dev)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
@@ -279,8 +284,12 @@ def run_ours(a):
 
     scene, cfg = mt.material_grid(width=a.width, height=a.height, samples=a.spp)
     tr = mt.Tracer(scene, cfg)
-    stream = torch.cuda.current_stream(dev)
+    # an explicit non-default stream: the library enqueues on exactly this
+    # stream, so the CUDA events below bracket its kernels
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
     sptr = stream.cuda_stream
+    assert sptr != 0
     out = torch.empty((a.height, a.width, 3), dtype=torch.float32, device=dev)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)  # 256 MiB > 129 MB L2
 
@@ -429,8 +438,84 @@ def run_ours(a):
         torch.distributed.destroy_process_group()
 
 
+# --------------------------------------------------------------------------- time to relMSE
+def relmse(x, r):
+    """Mean over pixels and channels of (x - r)^2 / (r^2 + 1e-2), on the
+    tonemapped images the renderer outputs."""
+    return float(((x - r) ** 2 / (r * r + 1e-2)).mean())
+
+
+def run_time_to_relmse(a):
+    """Renders the material grid at an spp ladder (seed 0) and a reference at
+    --ref-spp (seed 1); reports relMSE per rung, the GPU time to reach the
+    target (first rung at or below it, and the 1/spp fit), and the CPU oracle's
+    time for the same spp extrapolated from its measured samples/s."""
+    import numpy as np
+    import torch
+
+    import mitrace_gb300 as mt
+
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
+
+    def render(spp, seed):
+        scene, cfg = mt.material_grid(width=a.width, height=a.height, samples=spp, seed=0)
+        cfg.seed = seed
+        out = torch.empty((a.height, a.width, 3), dtype=torch.float32, device=dev)
+        with mt.Tracer(scene, cfg) as tr:
+            tr.render_device(out.data_ptr(), stream.cuda_stream)  # warm-up
+            torch.cuda.synchronize()
+            s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s0.record(stream)
+            tr.render_device(out.data_ptr(), stream.cuda_stream)
+            s1.record(stream)
+            torch.cuda.synchronize()
+            rays = tr.GetStats().rays
+        return out.cpu().numpy(), s0.elapsed_time(s1) / 1e3, rays, scene, cfg
+
+    t0 = time.perf_counter()
+    ref, ref_s, ref_rays, scene, cfg = render(a.ref_spp, 1)
+    ladder = []
+    spp = 1
+    while spp <= 1024:
+        img, sec, rays, _, _ = render(spp, 0)
+        ladder.append({"spp": spp, "seconds": sec, "relmse": relmse(img, ref), "mrays_s": rays / sec / 1e6})
+        spp *= 2
+    hit = next((r for r in ladder if r["relmse"] <= a.relmse_target), None)
+    # relMSE ~ c / spp on the rungs above 8 spp
+    xs = np.array([r["spp"] for r in ladder if r["spp"] >= 8], dtype=np.float64)
+    ys = np.array([r["relmse"] for r in ladder if r["spp"] >= 8], dtype=np.float64)
+    c = float(np.exp(np.mean(np.log(ys * xs))))
+    spp_fit = c / a.relmse_target
+    sec_per_spp = statistics.median(r["seconds"] / r["spp"] for r in ladder if r["spp"] >= 8)
+    cb = cpu_baseline(scene, cfg, a.cpu_seconds) if not a.no_cpu_baseline else None
+    line = {
+        "metric": "time-to-relMSE 0.01 @1080p", "unit": "s", "higher_is_better": False,
+        "config": {"workload": workload_name(a), "ref_spp": a.ref_spp, "ref_seed": 1, "seed": 0,
+                   "relmse": "mean over pixels/channels of (x-r)^2/(r^2+1e-2) on the tonemapped output"},
+        "gpu_first_rung": hit, "gpu_fit": {"c": c, "spp": spp_fit, "seconds": spp_fit * sec_per_spp},
+        "ladder": ladder, "reference_seconds": ref_s, "reference_rays": ref_rays,
+        "wall_s": time.perf_counter() - t0,
+    }
+    if cb:
+        cpu_sps = cb["msamples_s"] * 1e6
+        line["cpu_extrapolated"] = {
+            "seconds_at_gpu_first_rung": (hit["spp"] * a.width * a.height / cpu_sps) if hit else None,
+            "seconds_at_fit": spp_fit * a.width * a.height / cpu_sps,
+            "msamples_s": cb["msamples_s"], "cores": cb["cores"], "cpu": cb["cpu"], "sample": cb["sample"],
+            "note": "extrapolated from the oracle's measured samples/s on a band of the same image",
+        }
+        if hit:
+            line["speedup_vs_cpu_at_target"] = line["cpu_extrapolated"]["seconds_at_gpu_first_rung"] / hit["seconds"]
+    print(json.dumps(line), flush=True)
+
+
 def main():
     a = parse()
+    if a.time_to_relmse:
+        run_time_to_relmse(a)
+        return
     if a.impl == "reference":
         run_reference(a)
     else:

@@ -221,9 +221,9 @@ mt_status mt_get_stats(const mt_handle* h, mt_stats* out);
 /* 1 when a render was started and has finished, else 0. */
 int mt_is_done(const mt_handle* h);
 
-/* Synchronous render into a caller-owned DEVICE buffer (W*H*3 floats) on the
- * given CUDA stream (0 = the handle's stream).  Returns when the work is
- * enqueued; rays/samples are added to the handle's counters. */
+/* Render into a caller-owned DEVICE buffer (W*H*3 floats) enqueued on the
+ * given CUDA stream (0 = the legacy default stream).  Returns when the work is
+ * enqueued; mt_get_stats reports its rays once the stream has finished it. */
 mt_status mt_render_device(mt_handle* h, float* d_rgb_out, void* cuda_stream);
 
 /* Allocation-free render of rows [row0, row1) into a caller-owned DEVICE
@@ -286,7 +286,7 @@ typedef struct mt_hit {
 
 /* Host buffers: copies rays in, runs the query, copies hits out (blocking). */
 mt_status mt_trace_rays(mt_handle* h, const mt_ray* rays, uint64_t n, mt_hit* hits, int query);
-/* Device buffers on a caller stream (0 = handle stream); does not block. */
+/* Device buffers on a caller stream (0 = the legacy default stream); does not block. */
 mt_status mt_trace_rays_device(mt_handle* h, const mt_ray* d_rays, uint64_t n, mt_hit* d_hits,
                                int query, void* cuda_stream);
 

@@ -845,7 +845,7 @@ mt_status mt_render_device(mt_handle* h, float* d_rgb_out, void* cuda_stream)
 {
     if (check_handle(h) != MT_OK || !d_rgb_out) return set_err(MT_ERR_INVALID, "null argument");
     if (h->running) return set_err(MT_ERR_STATE, "an asynchronous render is running");
-    cudaStream_t st = cuda_stream ? static_cast<cudaStream_t>(cuda_stream) : h->stream;
+    cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);  // 0: the legacy default stream
     h->kill = 0;
     const mt_status rc = render_into(h, d_rgb_out, st, false);
     if (rc == MT_OK) h->stat_samples += static_cast<uint64_t>(h->cfg.width) * h->cfg.height * h->cfg.samples;
@@ -861,7 +861,7 @@ mt_status mt_trace_rays_device(mt_handle* h, const mt_ray* d_rays, uint64_t n, m
         return set_err(MT_ERR_INVALID, "unknown query");
     if ((reinterpret_cast<uintptr_t>(d_rays) | reinterpret_cast<uintptr_t>(d_hits)) & 15)
         return set_err(MT_ERR_INVALID, "ray and hit buffers must be 16-byte aligned");
-    cudaStream_t st = cuda_stream ? static_cast<cudaStream_t>(cuda_stream) : h->stream;
+    cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);  // 0: the legacy default stream
     MT_CUDA(launch_trace(h->S, d_rays, n, d_hits, query, h->qfetch.p, st));
     h->launches += n ? 1 : 0;
     return MT_OK;
