@@ -246,6 +246,34 @@ mt_status mt_render_rows_noalloc(mt_handle* h, uint32_t row0, uint32_t row1, flo
                                  void* cuda_stream);
 
 /* ------------------------------------------------------------------------ */
+/* Path-replay adjoint (no reference counterpart: gradient of an image loss). */
+/* ------------------------------------------------------------------------ */
+
+/* Device buffers of mt_render_grad.  Gradients are ADDED to d_* (zero them
+ * first).  d_texels covers the texels of every RGB32F texture that some
+ * material uses as its base-colour texture, W*H*3 floats each, concatenated in
+ * texture-index order; pass NULL to skip texel gradients. */
+typedef struct mt_grad_buffers {
+    const float* target; /* W*H*3 target image                                  */
+    float* image;        /* W*H*3 out: the rendered image                       */
+    float* loss;         /* 1 float out: sum over pixels/channels of (image-target)^2 */
+    float* d_base;       /* num_materials*3: dL/d base_color_factor rgb          */
+    float* d_roughness;  /* num_materials: dL/d roughness_factor                 */
+    float* d_metallic;   /* num_materials: dL/d metallic_factor                  */
+    float* d_light;      /* num_lights: dL/d s, light colour scaled by s at s=1  */
+    float* d_texels;     /* see above, or NULL                                   */
+} mt_grad_buffers;
+
+#define MT_GRAD_MAX_BOUNCES 16
+
+/* Renders the image (same estimator and counter RNG as mt_render_device) and
+ * accumulates dL/dparameters by replaying every path from its seed.  Sampling
+ * decisions and pdfs, light-pick probabilities, the energy cut-off and the
+ * firefly mask are held constant.  Needs bounces <= MT_GRAD_MAX_BOUNCES.
+ * Enqueued on cuda_stream (0 = the legacy default stream). */
+mt_status mt_render_grad(mt_handle* h, const mt_grad_buffers* g, void* cuda_stream);
+
+/* ------------------------------------------------------------------------ */
 /* Ray queries (test and microbench entry points).                          */
 /* ------------------------------------------------------------------------ */
 

@@ -190,6 +190,22 @@ class mt_profile(C.Structure):
     _fields_ = [("stage", mt_stage_profile * MT_NUM_STAGES)]
 
 
+class mt_grad_buffers(C.Structure):
+    _fields_ = [
+        ("target", C.c_void_p),
+        ("image", C.c_void_p),
+        ("loss", C.c_void_p),
+        ("d_base", C.c_void_p),
+        ("d_roughness", C.c_void_p),
+        ("d_metallic", C.c_void_p),
+        ("d_light", C.c_void_p),
+        ("d_texels", C.c_void_p),
+    ]
+
+
+MT_GRAD_MAX_BOUNCES = 16
+
+
 class mt_brdf_query(C.Structure):
     _fields_ = [
         ("L", C.c_float * 3),
@@ -218,6 +234,7 @@ PROTOTYPES = [
     ("mt_is_done", C.c_int, [_VP]),
     ("mt_render_device", C.c_int, [_VP, _VP, _VP]),
     ("mt_render_rows_noalloc", C.c_int, [_VP, C.c_uint32, C.c_uint32, _VP, _VP]),
+    ("mt_render_grad", C.c_int, [_VP, C.POINTER(mt_grad_buffers), _VP]),
     ("mt_trace_rays", C.c_int, [_VP, _VP, C.c_uint64, _VP, C.c_int]),
     ("mt_trace_rays_device", C.c_int, [_VP, _VP, C.c_uint64, _VP, C.c_int, _VP]),
     ("mt_brdf_batch", C.c_int, [_VP, C.c_uint64, _VP]),

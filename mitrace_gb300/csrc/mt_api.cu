@@ -20,6 +20,7 @@
 
 #include "../../include/mitrace_gpu.h"
 #include "mt_device.cuh"
+#include "mt_adjoint.h"
 #include "mt_internal.h"
 #include "mt_kernels.h"
 
@@ -209,6 +210,11 @@ struct mt_handle {
     double prof_ms[MT_NUM_STAGES] = {};
     uint64_t prof_launches[MT_NUM_STAGES] = {};
     uint64_t prof_rays[2] = {};
+    // adjoint
+    uint32_t grad_batch = 0;
+    DevArray<float4> rec_vert, rec_path, grad_pix;
+    DevArray<long long> texel_off;
+    uint64_t grad_texels = 0;
     // query scratch
     DevArray<mt_ray> qrays;
     DevArray<mt_hit> qhits;
@@ -426,6 +432,21 @@ mt_status upload_scene(mt_handle* h, const mt_scene_desc* d)
     }
     if (d->env_texture >= static_cast<int>(d->num_textures))
         return set_err(MT_ERR_INVALID, "env texture index out of range");
+    // gradient layout: RGB32F textures used as a base colour, in texture order
+    {
+        std::vector<long long> off(std::max<uint32_t>(1, d->num_textures), -1);
+        std::vector<char> used(d->num_textures, 0);
+        for (uint32_t i = 0; i < d->num_materials; ++i)
+            if (d->materials[i].base_color_tex >= 0) used[d->materials[i].base_color_tex] = 1;
+        uint64_t total = 0;
+        for (uint32_t ti = 0; ti < d->num_textures; ++ti)
+            if (used[ti] && d->textures[ti].rgb32f) {
+                off[ti] = static_cast<long long>(total);
+                total += 3ull * d->textures[ti].width * d->textures[ti].height;
+            }
+        h->grad_texels = total;
+        MT_CUDA(h->texel_off.upload(off.data(), off.size(), st));
+    }
 
     MT_CUDA(h->nodes.upload(nodes.data(), nodes.size(), st));
     MT_CUDA(h->slots.upload(slots.data(), slots.size(), st));
@@ -850,6 +871,70 @@ mt_status mt_render_device(mt_handle* h, float* d_rgb_out, void* cuda_stream)
     const mt_status rc = render_into(h, d_rgb_out, st, false);
     if (rc == MT_OK) h->stat_samples += static_cast<uint64_t>(h->cfg.width) * h->cfg.height * h->cfg.samples;
     return rc;
+}
+
+mt_status mt_render_grad(mt_handle* h, const mt_grad_buffers* g, void* cuda_stream)
+{
+    if (check_handle(h) != MT_OK || !g) return set_err(MT_ERR_INVALID, "null argument");
+    if (!g->target || !g->image || !g->loss || !g->d_base || !g->d_roughness || !g->d_metallic ||
+        (!g->d_light && h->S.num_lights))
+        return set_err(MT_ERR_INVALID, "target, image, loss and the material/light gradient buffers are required");
+    if (h->running) return set_err(MT_ERR_STATE, "an asynchronous render is running");
+    if (h->cfg.bounces > MT_GRAD_MAX_BOUNCES)
+        return set_err(MT_ERR_INVALID, "mt_render_grad supports at most MT_GRAD_MAX_BOUNCES bounces");
+    mt_status rc = ensure_wave(h);
+    if (rc != MT_OK) return rc;
+    const mt_config& c = h->cfg;
+    const uint64_t rows_per_band = h->band_capacity / (static_cast<uint64_t>(c.width) * c.samples);
+    if (!h->grad_batch) {
+        const uint64_t gb = std::min<uint64_t>(h->batch, env_u64("MT_GRAD_BATCH_PATHS", 1ull << 20));
+        h->grad_batch = static_cast<uint32_t>(gb);
+        MT_CUDA(h->rec_vert.alloc(gb * std::max<uint32_t>(1, c.bounces) * 5));
+        MT_CUDA(h->rec_path.alloc(gb * 2));
+        MT_CUDA(h->grad_pix.alloc(2 * rows_per_band * c.width));
+    }
+    cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
+    const WaveViews v = views(h);
+    GradParams G{};
+    G.target = g->target;
+    G.loss = g->loss;
+    G.d_base = g->d_base;
+    G.d_rough = g->d_roughness;
+    G.d_metal = g->d_metallic;
+    G.d_light = g->d_light;
+    G.d_texels = h->grad_texels ? g->d_texels : nullptr;
+    G.texel_off = h->texel_off.p;
+    G.pix = h->grad_pix.p;
+    const uint32_t nmat = static_cast<uint32_t>(h->materials.n);
+    G.smem_materials = nmat <= 1024 ? nmat : 0;
+    G.smem_lights = h->S.num_lights <= 256 ? h->S.num_lights : 0;
+    RecordBuffers R;
+    R.vert = h->rec_vert.p;
+    R.path = h->rec_path.p;
+    MT_CUDA(cudaMemsetAsync(g->loss, 0, sizeof(float), st));
+    MT_CUDA(cudaMemsetAsync(h->rays.p, 0, 2 * sizeof(unsigned long long), st));
+    uint64_t launches = 0;
+    for (uint64_t r0 = 0; r0 < c.height; r0 += rows_per_band) {
+        const uint64_t rows = std::min<uint64_t>(rows_per_band, c.height - r0);
+        const uint32_t band_pix = static_cast<uint32_t>(rows * c.width);
+        const uint32_t pix_base = static_cast<uint32_t>(r0 * c.width);
+        const uint64_t paths = static_cast<uint64_t>(band_pix) * c.samples;
+        for (uint64_t g0 = 0; g0 < paths; g0 += h->batch) {
+            const uint32_t n = static_cast<uint32_t>(std::min<uint64_t>(h->batch, paths - g0));
+            MT_CUDA(launch_batch(h->S, v.P, v.SQ, v.W, g0, n, band_pix, pix_base, st, &launches, nullptr));
+        }
+        MT_CUDA(launch_resolve(h->S, v.W, band_pix, pix_base, g->image, st, nullptr));
+        MT_CUDA(launch_grad_pixel(h->S, v.W, band_pix, pix_base, g->image, G, st));
+        launches += 2;
+        for (uint64_t g0 = 0; g0 < paths; g0 += h->grad_batch) {
+            const uint32_t n = static_cast<uint32_t>(std::min<uint64_t>(h->grad_batch, paths - g0));
+            MT_CUDA(launch_batch(h->S, v.P, v.SQ, v.W, g0, n, band_pix, pix_base, st, &launches, nullptr, &R));
+            MT_CUDA(launch_adjoint(h->S, G, R, v.W, g0, n, band_pix, st));
+            ++launches;
+        }
+    }
+    h->launches += launches;
+    return MT_OK;
 }
 
 mt_status mt_trace_rays_device(mt_handle* h, const mt_ray* d_rays, uint64_t n, mt_hit* d_hits, int query,

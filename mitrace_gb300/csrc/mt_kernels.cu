@@ -136,7 +136,8 @@ __device__ __forceinline__ void path_coords(const DevScene& S, const BatchInfo& 
 }
 
 __global__ void __launch_bounds__(256) k_raygen(DevScene S, PathState P, BatchInfo B,
-                                                uint32_t* __restrict__ q0, uint32_t* counts)
+                                                uint32_t* __restrict__ q0, uint32_t* counts,
+                                                RecordBuffers R)
 {
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         counts[0] = B.n;
@@ -163,6 +164,10 @@ __global__ void __launch_bounds__(256) k_raygen(DevScene S, PathState P, BatchIn
         P.indirect[p] = zero;
         P.sky[p] = zero;
         q0[p] = p;
+        if (R.path) {
+            R.path[2 * p] = zero;
+            R.path[2 * p + 1] = make_float4(0.0f, 0.0f, 0.0f, -1.0f);
+        }
     }
 }
 
@@ -251,7 +256,7 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, PathState P, ShadowQu
                                                BatchInfo B, uint32_t bounce,
                                                const uint32_t* __restrict__ q,
                                                uint32_t* __restrict__ nq, uint32_t* counts,
-                                               int cur)
+                                               int cur, RecordBuffers R)
 {
     const uint32_t n = counts[cur];
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -262,7 +267,9 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, PathState P, ShadowQu
         if (hb.x == MT_NO_HIT) {
             // Tracer.cpp:244-252: previous vertex's base colour times energy times sky.
             const f3 color = bounce > 0 ? ld4(P.prev, p) : splat(1.0f);
-            st4(P.sky, p, ld4(P.sky, p) + (color * cur_e) * sample_sky(S, rd, bounce == 0));
+            const f3 sky = sample_sky(S, rd, bounce == 0);
+            st4(P.sky, p, ld4(P.sky, p) + (color * cur_e) * sky);
+            if (R.path) R.path[2 * p + 1] = make_float4(sky.x, sky.y, sky.z, static_cast<float>(bounce));
             continue;
         }
         uint32_t pixel, sample;
@@ -307,6 +314,15 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, PathState P, ShadowQu
 
         // Emission (Tracer.cpp:255)
         st4(P.emit, p, ld4(P.emit, p) + (cur_e * S.emission_base) * mp.emission);
+        float4* vr = R.vert ? R.vert + (static_cast<uint64_t>(p) * S.bounces + bounce) * 5 : nullptr;
+        if (vr) {
+            vr[0] = make_float4(N.x, N.y, N.z, __uint_as_float(__ldg(&I.material)));
+            vr[1] = make_float4(view.x, view.y, view.z, __uint_as_float(MT_VREC_HIT));
+            vr[2] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            vr[3] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            vr[4] = make_float4(tu, tv, __uint_as_float(0u), 0.0f);
+            R.path[2 * p].w = static_cast<float>(bounce + 1);
+        }
 
         // Weighted reservoir light pick (Tracer.cpp:257-279)
         int chosen = -1;
@@ -340,12 +356,14 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, PathState P, ShadowQu
             const f3 lvec = lpos - hit_pos;
             const f3 ldir = normalize(lvec);
             f3 lcol = {__ldg(&L.color[0]), __ldg(&L.color[1]), __ldg(&L.color[2])};
+            float spot = 1.0f;
             if (type == MT_LIGHT_SPOT) {
                 const f3 sd = {__ldg(&L.dir[0]), __ldg(&L.dir[1]), __ldg(&L.dir[2])};
                 const float dd = dot(-ldir, sd);
                 const float inten = __fdiv_rn(__fsub_rn(dd, __ldg(&L.outer_cos)),
                                               __fsub_rn(__ldg(&L.inner_cos), __ldg(&L.outer_cos)));
-                lcol = lcol * gclamp(inten, 0.0f, 1.0f);
+                spot = gclamp(inten, 0.0f, 1.0f);
+                lcol = lcol * spot;
             }
             const float llen = length(lvec);
             const f3 brdf = eval_brdf(ldir, view, N, base, mp.roughness, mp.metallic);
@@ -357,7 +375,13 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, PathState P, ShadowQu
             const f3 so = hit_pos + lvec * 0.0001f;
             SQ.o[slot] = make_float4(so.x, so.y, so.z, llen);
             SQ.d[slot] = make_float4(ldir.x, ldir.y, ldir.z, __uint_as_float(p));
-            SQ.c[slot] = make_float4(contrib.x, contrib.y, contrib.z, bounce == 0 ? 1.0f : 0.0f);
+            SQ.c[slot] = make_float4(contrib.x, contrib.y, contrib.z, static_cast<float>(bounce));
+            if (vr) {
+                vr[1].w = __uint_as_float(MT_VREC_HIT | MT_VREC_CHOSEN);
+                vr[3] = make_float4(ldir.x, ldir.y, ldir.z, nl * fall / pick);
+                vr[4].z = __uint_as_float(static_cast<uint32_t>(chosen));
+                vr[4].w = spot;
+            }
         }
 
         // Bounce sampling (Tracer.cpp:177-208); the last vertex never extends.
@@ -395,6 +419,10 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, PathState P, ShadowQu
         const float nl = gmax(dot(N, nd), 0.0f);
         const f3 energy = pdf > 0.0f ? brdf * __fdiv_rn(nl, pdf) : splat(0.0f);
         if (chosen >= 0) st4(P.cur, p, cur_e * energy);  // Tracer.cpp:339
+        if (vr) {
+            vr[1].w = __uint_as_float(__float_as_uint(vr[1].w) | MT_VREC_NEXT);
+            vr[2] = make_float4(nd.x, nd.y, nd.z, pdf > 0.0f ? nl / pdf : 0.0f);
+        }
         const f3 tot = ld4(P.tot, p) * energy;
         st4(P.tot, p, tot);
         if (length(tot) < S.terminate_energy) continue;  // Tracer.cpp:207-208
@@ -413,6 +441,8 @@ template <bool COUNT>
 struct ShadowWork {
     PathState P;
     ShadowQueue SQ;
+    RecordBuffers R;
+    uint32_t bounces;
     uint32_t n;
     uint32_t i;
     uint32_t pops, inner, tris;
@@ -436,7 +466,11 @@ struct ShadowWork {
         if (h.hit) return;
         const float4 c = SQ.c[i];
         const uint32_t p = __float_as_uint(SQ.d[i].w);
-        float4* acc = c.w != 0.0f ? P.direct : P.indirect;
+        if (R.vert) {
+            float4* vr = R.vert + (static_cast<uint64_t>(p) * bounces + static_cast<uint32_t>(c.w)) * 5;
+            vr[1].w = __uint_as_float(__float_as_uint(vr[1].w) | MT_VREC_VISIBLE);
+        }
+        float4* acc = c.w == 0.0f ? P.direct : P.indirect;
         const float4 a = acc[p];
         acc[p] = make_float4(__fadd_rn(a.x, c.x), __fadd_rn(a.y, c.y), __fadd_rn(a.z, c.z), 0.0f);
     }
@@ -446,24 +480,30 @@ template <bool COUNT>
 __global__ void __launch_bounds__(128, MT_TRAVERSE_MIN_BLOCKS) k_shadow(DevScene S, PathState P, ShadowQueue SQ,
                                                 uint32_t* counts,
                                                 unsigned long long* rays,
-                                                unsigned long long* cnt)
+                                                unsigned long long* cnt,
+                                                RecordBuffers R)
 {
     const uint32_t n = counts[2];
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         counts[3] = 0;  // ray fetch counter of the next bounce's extend
         atomicAdd(rays, static_cast<unsigned long long>(n));
     }
-    ShadowWork<COUNT> W{P, SQ, n, 0, 0, 0, 0};
+    ShadowWork<COUNT> W{P, SQ, R, S.bounces, n, 0, 0, 0, 0};
     trace_persistent<COUNT, true>(S, W, &counts[4]);
     if (COUNT) flush_counts(cnt, W.pops, W.inner, W.tris);
 }
 
 __global__ void __launch_bounds__(256) k_finalize(DevScene S, PathState P, BatchInfo B,
                                                   float* __restrict__ sr, float* __restrict__ sg,
-                                                  float* __restrict__ sb)
+                                                  float* __restrict__ sb, RecordBuffers R)
 {
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < B.n; p += gridDim.x * blockDim.x) {
         const f3 total = ((ld4(P.emit, p) + ld4(P.direct, p)) + ld4(P.indirect, p)) + ld4(P.sky, p);
+        if (R.path) {
+            R.path[2 * p].x = total.x;
+            R.path[2 * p].y = total.y;
+            R.path[2 * p].z = total.z;
+        }
         const f3 c = aces(total, S.exposure);
         const uint64_t g = B.g0 + p;
         sr[g] = c.x;
@@ -635,8 +675,10 @@ Profiler::~Profiler()
 
 cudaError_t launch_batch(const DevScene& S, const PathState& P, const ShadowQueue& SQ,
                          const WaveBuffers& W, uint64_t g0, uint32_t n, uint32_t band_pix,
-                         uint32_t pix_base, cudaStream_t st, uint64_t* launches, Profiler* prof)
+                         uint32_t pix_base, cudaStream_t st, uint64_t* launches, Profiler* prof,
+                         const RecordBuffers* rec)
 {
+    const RecordBuffers R = rec ? *rec : RecordBuffers{};
     BatchInfo B{g0, n, band_pix, pix_base};
     const unsigned gw = grid_for(n, 128, 16);
     static unsigned g_ext[2] = {0, 0}, g_sh[2] = {0, 0};
@@ -651,7 +693,7 @@ cudaError_t launch_batch(const DevScene& S, const PathState& P, const ShadowQueu
     auto begin = [&](int s) { if (prof) prof->begin(s, st); };
     auto end = [&](int s) { if (prof) prof->end(s, st); };
     begin(MT_STAGE_RAYGEN);
-    k_raygen<<<grid_for(n, 256, 8), 256, 0, st>>>(S, P, B, W.q[0], W.counts);
+    k_raygen<<<grid_for(n, 256, 8), 256, 0, st>>>(S, P, B, W.q[0], W.counts, R);
     end(MT_STAGE_RAYGEN);
     uint64_t l = 1;
     int cur = 0;
@@ -663,19 +705,19 @@ cudaError_t launch_batch(const DevScene& S, const PathState& P, const ShadowQueu
             k_extend<false><<<g_ext[0], 128, 0, st>>>(S, P, W.q[cur], W.counts, cur, W.rays, cnt);
         end(MT_STAGE_EXTEND);
         begin(MT_STAGE_SHADE);
-        k_shade<<<gw, 128, 0, st>>>(S, P, SQ, B, b, W.q[cur], W.q[cur ^ 1], W.counts, cur);
+        k_shade<<<gw, 128, 0, st>>>(S, P, SQ, B, b, W.q[cur], W.q[cur ^ 1], W.counts, cur, R);
         end(MT_STAGE_SHADE);
         begin(MT_STAGE_SHADOW);
         if (count)
-            k_shadow<true><<<g_sh[1], 128, 0, st>>>(S, P, SQ, W.counts, W.rays + 1, cnt ? cnt + 3 : nullptr);
+            k_shadow<true><<<g_sh[1], 128, 0, st>>>(S, P, SQ, W.counts, W.rays + 1, cnt ? cnt + 3 : nullptr, R);
         else
-            k_shadow<false><<<g_sh[0], 128, 0, st>>>(S, P, SQ, W.counts, W.rays + 1, nullptr);
+            k_shadow<false><<<g_sh[0], 128, 0, st>>>(S, P, SQ, W.counts, W.rays + 1, nullptr, R);
         end(MT_STAGE_SHADOW);
         l += 3;
         cur ^= 1;
     }
     begin(MT_STAGE_FINALIZE);
-    k_finalize<<<grid_for(n, 256, 8), 256, 0, st>>>(S, P, B, W.sr, W.sg, W.sb);
+    k_finalize<<<grid_for(n, 256, 8), 256, 0, st>>>(S, P, B, W.sr, W.sg, W.sb, R);
     end(MT_STAGE_FINALIZE);
     ++l;
     if (launches) *launches += l;

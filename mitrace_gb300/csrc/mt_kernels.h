@@ -47,6 +47,25 @@ struct WaveBuffers {
     float* sb;
 };
 
+// Per-vertex records written by a recording (path-replay) pass of the render
+// stages; null pointers in ordinary renders.  Vertex record of path p, bounce b:
+// vert[(p * bounces + b) * 5 + k]
+//   k=0  shading normal N, material index (bits)
+//   k=1  view direction V = -ray, flags (bits, MT_VREC_*)
+//   k=2  sampled next direction, NL / pdf (energy = brdf * this)
+//   k=3  light direction, NL * falloff / pick (NEE = cur * brdf * lightColor * this)
+//   k=4  uv, chosen light index (bits), spot factor
+// Path record: path[2p] = (total radiance before ACES, hit vertices),
+//              path[2p+1] = (sky sample, bounce of the miss or -1).
+struct RecordBuffers {
+    float4* vert = nullptr;
+    float4* path = nullptr;
+};
+#define MT_VREC_HIT 1u
+#define MT_VREC_CHOSEN 2u
+#define MT_VREC_VISIBLE 4u
+#define MT_VREC_NEXT 8u
+
 // Optional per-stage CUDA-event timing and traversal counters of a render.
 struct Profiler {
     bool timing = false;
@@ -66,7 +85,8 @@ cudaError_t launch_trace(const DevScene& S, const mt_ray* rays, uint64_t n, mt_h
 cudaError_t launch_brdf(const mt_brdf_query* q, uint64_t n, mt_brdf_result* out, cudaStream_t st);
 cudaError_t launch_batch(const DevScene& S, const PathState& P, const ShadowQueue& SQ,
                          const WaveBuffers& W, uint64_t g0, uint32_t n, uint32_t band_pix,
-                         uint32_t pix_base, cudaStream_t st, uint64_t* launches, Profiler* prof);
+                         uint32_t pix_base, cudaStream_t st, uint64_t* launches, Profiler* prof,
+                         const RecordBuffers* rec = nullptr);
 cudaError_t launch_resolve(const DevScene& S, const WaveBuffers& W, uint32_t band_pix,
                            uint32_t pix_base, float* out, cudaStream_t st, Profiler* prof);
 

@@ -413,6 +413,35 @@ def material_grid(width=1920, height=1080, samples=256, seed=0, segments=64, rin
     return scene, cfg
 
 
+def num_grad_texels(s: SceneData) -> int:
+    """Length of the texel-gradient buffer: RGB32F textures used as a base
+    colour, in texture order (the layout mt_render_grad writes)."""
+    used = {m.base_tex for m in s.materials if m.base_tex >= 0}
+    return sum(t.rgb32f.size for i, t in enumerate(s.textures) if i in used and t.rgb32f is not None)
+
+
+def adjoint_scene(width=512, height=512, samples=64, seed=0, texture_size=512, segments=64, rings=32):
+    """Inverse-materials scene: the 7x7 material grid at 512x512 with a
+    texture_size^2 RGB32F albedo texture on the ground plane (the parameters
+    are the 49 spheres' base colour, roughness and metallic, the ground's
+    texels and the two lights' intensities)."""
+    scene, cfg = material_grid(width=width, height=height, samples=samples, seed=seed, segments=segments,
+                               rings=rings)
+    rng = np.random.default_rng(seed + 7)
+    t = np.arange(texture_size)
+    X, Y = np.meshgrid(t, t)
+    checker = ((X // (texture_size // 8) + Y // (texture_size // 8)) % 2).astype(np.float32)
+    albedo = np.stack([0.3 + 0.4 * checker, 0.35 + 0.1 * rng.random((texture_size, texture_size)),
+                       0.5 - 0.3 * checker], -1).astype(np.float32)
+    scene.textures.append(TextureData(rgb32f=albedo, filter=A.MT_FILTER_NEAREST, scale=(6.0, 6.0)))
+    ground = scene.materials[49]
+    ground.base_tex = len(scene.textures) - 1
+    ground.base_color = (1.0, 1.0, 1.0, 1.0)
+    cfg.width, cfg.height = width, height
+    scene.camera.aspect = width / height
+    return scene, cfg
+
+
 def _value_noise(n, cells, rng):
     g = rng.random((cells + 1, cells + 1))
     x = np.linspace(0, cells, n, endpoint=False)

@@ -75,6 +75,14 @@ class Tracer:
                                     hits.ctypes.data_as(C.c_void_p), query), "mt_trace_rays")
         return hits
 
+    def render_grad_device(self, target_ptr: int, image_ptr: int, loss_ptr: int, d_base_ptr: int,
+                           d_rough_ptr: int, d_metal_ptr: int, d_light_ptr: int, d_texels_ptr: int = 0,
+                           stream_ptr: int = 0):
+        """mt_render_grad on device buffers (gradients are added to the d_* buffers)."""
+        g = A.mt_grad_buffers(target_ptr, image_ptr, loss_ptr, d_base_ptr, d_rough_ptr, d_metal_ptr,
+                              d_light_ptr or None, d_texels_ptr or None)
+        A.check(A.lib.mt_render_grad(self.handle, C.byref(g), C.c_void_p(stream_ptr)), "mt_render_grad")
+
     def kernel_launches(self) -> int:
         return int(A.lib.mt_kernel_launches(self.handle))
 

@@ -941,6 +941,17 @@ struct PathStep {
     V3 hitPos, base, normal, energy, emission;
     float metallic, roughness;
     bool didHit;
+    // kept for the adjoint replay
+    uint32_t mat = 0;
+    V2 uv{0.0f, 0.0f};
+    V3 nextDir{0, 0, 0};
+    float facNext = 0.0f;  // energy = brdf(nextDir) * facNext
+    bool chosen = false, visible = false;
+    uint32_t light = 0;
+    V3 ldir{0, 0, 0};
+    float facLight = 0.0f;  // NEE = cur * brdf(ldir) * color * spot * facLight
+    float spot = 1.0f;
+    V3 sky{0, 0, 0};       // sky sample of a miss step
 };
 
 struct Worker {
@@ -990,6 +1001,8 @@ void generate_path(const orc_scene& s, Worker& w, Rng& rng, V3 o0, V3 d0)
         st.normal = compute_normal(geomN, mp.normal);
         st.emission = mp.emission;
         st.didHit = true;
+        st.mat = in.material;
+        st.uv = uv;
 
         const V3 view = -d;
         const float ps = specular_probability(view, st.normal, st.base, st.metallic);
@@ -1005,6 +1018,8 @@ void generate_path(const orc_scene& s, Worker& w, Rng& rng, V3 o0, V3 d0)
         const V3 brdf = eval_brdf(nd, view, st.normal, st.base, st.roughness, st.metallic);
         const float nl = gmax(dot(st.normal, nd), 0.0f);
         st.energy = (pdf > 0.0f) ? brdf * (nl / pdf) : v3(0.0f);
+        st.nextDir = nd;
+        st.facNext = (pdf > 0.0f) ? nl / pdf : 0.0f;
         w.path.push_back(st);
         o = no;
         d = nd;
@@ -1014,18 +1029,20 @@ void generate_path(const orc_scene& s, Worker& w, Rng& rng, V3 o0, V3 d0)
     }
 }
 
-V3 process_ray_forward(const orc_scene& s, Worker& w, Rng& rng, V3 o, V3 d, float expo)
+V3 process_ray_forward(const orc_scene& s, Worker& w, Rng& rng, V3 o, V3 d, float expo,
+                       V3* total_out = nullptr)
 {
     const mt_config& cfg = s.cfg;
     generate_path(s, w, rng, o, d);
     V3 cur = v3(1.0f);
     V3 emitted = v3(0.0f), direct = v3(0.0f), indirect = v3(0.0f), sky = v3(0.0f);
     for (size_t i = 0; i < w.path.size(); ++i) {
-        const PathStep& st = w.path[i];
+        PathStep& st = w.path[i];
         const uint32_t bounce = static_cast<uint32_t>(i);
         if (!st.didHit) {
             const V3 color = (i > 0) ? w.path[i - 1].base : v3(1.0f);
-            sky = sky + color * cur * sample_sky(s, st.rayD, i == 0);
+            st.sky = sample_sky(s, st.rayD, i == 0);
+            sky = sky + color * cur * st.sky;
             break;
         }
         emitted = emitted + cur * cfg.emission_base_intensity * st.emission;
@@ -1054,13 +1071,18 @@ V3 process_ray_forward(const orc_scene& s, Worker& w, Rng& rng, V3 o, V3 d, floa
         const V3 lvec = lpos - st.hitPos;
         const V3 ldir = normalize(lvec);
         V3 lcol;
+        st.spot = 1.0f;
         if (L.type == MT_LIGHT_SPOT) {
             const float dd = dot(-ldir, L.dir);
             const float inten = (dd - L.outerCos) / (L.innerCos - L.outerCos);
-            lcol = L.color * gclamp(inten, 0.0f, 1.0f);
+            st.spot = gclamp(inten, 0.0f, 1.0f);
+            lcol = L.color * st.spot;
         } else {
             lcol = L.color;
         }
+        st.chosen = true;
+        st.light = static_cast<uint32_t>(chosen);
+        st.ldir = ldir;
         const V3 so = st.hitPos + lvec * 0.0001f;
         const Hit sh = intersect_scene(s, so, ldir, w.stack);
         ++w.rays;
@@ -1070,6 +1092,8 @@ V3 process_ray_forward(const orc_scene& s, Worker& w, Rng& rng, V3 o, V3 d, floa
             const float fall = 1.0f / (length(lvec) * length(lvec) + 1.0f);
             const V3 le = brdf * nl * fall;
             const V3 c = cur * le * lcol / pickPdf;
+            st.visible = true;
+            st.facLight = nl * fall / pickPdf;
             if (i == 0)
                 direct = direct + c;
             else
@@ -1078,6 +1102,7 @@ V3 process_ray_forward(const orc_scene& s, Worker& w, Rng& rng, V3 o, V3 d, floa
         cur = cur * st.energy;
     }
     const V3 total = ((emitted + direct) + indirect) + sky;
+    if (total_out) *total_out = total;
     return aces(total, expo);
 }
 
@@ -1162,6 +1187,200 @@ void seed_counter(Rng& rng, const orc_scene& s)
     rng.mode = ORC_RNG_COUNTER;
     rng.key[0] = static_cast<uint32_t>(s.cfg.seed);
     rng.key[1] = static_cast<uint32_t>(s.cfg.seed >> 32);
+}
+
+// ----------------------------------------------------------------------------
+// Adjoint check: derivatives of EvaluateBRDF (BRDF.hpp:52-77) by forward-mode
+// dual numbers over (base r, g, b, roughness, metallic).
+// ----------------------------------------------------------------------------
+struct Dual {
+    float v;
+    float d[5];
+    static Dual c(float x)
+    {
+        Dual r{x, {0, 0, 0, 0, 0}};
+        return r;
+    }
+    static Dual var(float x, int k)
+    {
+        Dual r = c(x);
+        r.d[k] = 1.0f;
+        return r;
+    }
+};
+Dual operator+(const Dual& a, const Dual& b)
+{
+    Dual r{a.v + b.v, {}};
+    for (int k = 0; k < 5; ++k) r.d[k] = a.d[k] + b.d[k];
+    return r;
+}
+Dual operator-(const Dual& a, const Dual& b)
+{
+    Dual r{a.v - b.v, {}};
+    for (int k = 0; k < 5; ++k) r.d[k] = a.d[k] - b.d[k];
+    return r;
+}
+Dual operator*(const Dual& a, const Dual& b)
+{
+    Dual r{a.v * b.v, {}};
+    for (int k = 0; k < 5; ++k) r.d[k] = a.d[k] * b.v + a.v * b.d[k];
+    return r;
+}
+Dual operator/(const Dual& a, const Dual& b)
+{
+    Dual r{a.v / b.v, {}};
+    for (int k = 0; k < 5; ++k) r.d[k] = (a.d[k] * b.v - a.v * b.d[k]) / (b.v * b.v);
+    return r;
+}
+
+void brdf_grad(V3 L, V3 V, V3 N, V3 base, float rough, float metal, V3 adj, double* g)
+{
+    const float nl = gmax(dot(N, L), 0.0f), nv = gmax(dot(N, V), 0.0f);
+    if (nl <= 0.0f || nv <= 0.0f) return;
+    const V3 h = normalize(V + L);
+    const float nh = gclamp(gmax(dot(N, h), 0.0f), 0.0f, 1.0f);
+    const float hv = gclamp(gmax(dot(h, V), 0.0f), 0.0f, 1.0f);
+    const Dual one = Dual::c(1.0f);
+    const Dual r = rough < 0.05f ? Dual::c(0.05f) : Dual::var(rough, 3);
+    const Dual m = Dual::var(metal, 4);
+    const Dual mc = metal < 0.0f ? Dual::c(0.0f) : (metal > 1.0f ? Dual::c(1.0f) : m);
+    const Dual p5 = Dual::c(std::pow(1.0f - hv, 5.0f));
+    const Dual a = r * r, a2 = a * a;
+    const Dual q = Dual::c(nh * nh) * (a2 - one) + one;
+    const Dual D = a2 / (Dual::c(kPi) * q * q);
+    const Dual rr = r + one;
+    const Dual k = rr * rr / Dual::c(8.0f);
+    const Dual G = (Dual::c(nv) / (Dual::c(nv) * (one - k) + k)) * (Dual::c(nl) / (Dual::c(nl) * (one - k) + k));
+    const Dual sden = Dual::c(gmax(4.0f * nv * nl, 0.001f));
+    const float b[3] = {base.x, base.y, base.z}, ad[3] = {adj.x, adj.y, adj.z};
+    for (int ch = 0; ch < 3; ++ch) {
+        const Dual bc = Dual::var(b[ch], ch);
+        const Dual f0 = Dual::c(0.04f) * (one - mc) + bc * mc;
+        const Dual F = f0 + (one - f0) * p5;
+        const Dual f = (one - F) * (one - m) * bc / Dual::c(kPi) + D * G * F / sden;
+        if (f.v < 0.0f) continue;
+        for (int kk = 0; kk < 5; ++kk) g[kk] += static_cast<double>(ad[ch]) * f.d[kk];
+    }
+}
+
+// Texel indices and weights Image::Sample blends (Image.cpp:17-61).
+int texel_taps(const Texture& t, float uvx, float uvy, long long idx[4], float w[4])
+{
+    const float u = uvx - std::floor(uvx), v = uvy - std::floor(uvy);
+    const int W = static_cast<int>(t.w), H = static_cast<int>(t.h);
+    const long long maxIdx = static_cast<long long>(t.w) * t.h - 1;
+    auto at = [&](int x, int y) {
+        const long long i = static_cast<long long>(y) * t.w + x;
+        return i < 0 ? 0 : (i > maxIdx ? maxIdx : i);
+    };
+    if (t.filter == MT_FILTER_LINEAR) {
+        const int x0 = static_cast<int>(std::floor(u * static_cast<float>(W)));
+        const int x1 = std::min(x0 + 1, W - 1);
+        const int y0 = static_cast<int>(std::floor(v * static_cast<float>(H)));
+        const int y1 = std::min(y0 + 1, H - 1);
+        const float sx = u - static_cast<float>(x0) / static_cast<float>(W);
+        const float sy = v - static_cast<float>(y0) / static_cast<float>(H);
+        idx[0] = at(x0, y0), w[0] = (1 - sx) * (1 - sy);
+        idx[1] = at(x1, y0), w[1] = sx * (1 - sy);
+        idx[2] = at(x0, y1), w[2] = (1 - sx) * sy;
+        idx[3] = at(x1, y1), w[3] = sx * sy;
+        return 4;
+    }
+    int ix = static_cast<int>(u * static_cast<float>(W)) % W;
+    int iy = static_cast<int>(v * static_cast<float>(H)) % H;
+    if (ix < 0) ix += W;
+    if (iy < 0) iy += H;
+    idx[0] = at(ix, iy);
+    w[0] = 1.0f;
+    return 1;
+}
+
+float aces_slope(float x)
+{
+    const double a = 2.51, b = 0.03, c = 2.43, d = 0.59, e = 0.14, X = x;
+    const double n = X * (a * X + b), dn = X * (c * X + d) + e;
+    return static_cast<float>(((2 * a * X + b) * dn - n * (2 * c * X + d)) / (dn * dn));
+}
+
+struct GradAcc {
+    std::vector<double> mat;  // materials * 5
+    std::vector<double> light;
+    std::vector<double> texel;
+    double loss = 0.0;
+};
+
+// Replays one kept sample's recorded path backwards (adjoint of
+// ProcessRayForward with the path's decisions held fixed).
+void sample_backward(const orc_scene& s, const std::vector<PathStep>& path, V3 gv,
+                     const std::vector<long long>& texOff, GradAcc& acc)
+{
+    size_t nv = 0;
+    while (nv < path.size() && path[nv].didHit) ++nv;
+    const bool miss = nv < path.size();
+    std::vector<V3> cur(nv + 1, v3(1.0f));
+    for (size_t i = 0; i < nv; ++i) cur[i + 1] = path[i].chosen ? cur[i] * path[i].energy : cur[i];
+    V3 adj = v3(0.0f), adjBaseSky = v3(0.0f);
+    if (miss && nv > 0) {
+        adj = gv * path[nv - 1].base * path[nv].sky;
+        adjBaseSky = gv * cur[nv] * path[nv].sky;
+    }
+    for (size_t ii = nv; ii-- > 0;) {
+        const PathStep& st = path[ii];
+        double g[5] = {0, 0, 0, 0, 0};
+        if (ii + 1 == nv) {
+            g[0] += adjBaseSky.x;
+            g[1] += adjBaseSky.y;
+            g[2] += adjBaseSky.z;
+        }
+        const V3 adjNext = adj;
+        const V3 V = -st.rayD;
+        if (st.chosen) {
+            adj = adjNext * st.energy;
+            brdf_grad(st.nextDir, V, st.normal, st.base, st.roughness, st.metallic,
+                      adjNext * cur[ii] * st.facNext, g);
+        }
+        adj = adj + gv * s.cfg.emission_base_intensity * st.emission;
+        if (st.chosen && st.visible) {
+            const Light& L = s.lights[st.light];
+            const V3 lc = L.color * (st.spot * st.facLight);
+            const V3 fl = eval_brdf(st.ldir, V, st.normal, st.base, st.roughness, st.metallic);
+            adj = adj + gv * fl * lc;
+            brdf_grad(st.ldir, V, st.normal, st.base, st.roughness, st.metallic, gv * cur[ii] * lc, g);
+            const V3 c = cur[ii] * fl * lc;
+            acc.light[st.light] += static_cast<double>(gv.x) * c.x + static_cast<double>(gv.y) * c.y +
+                                   static_cast<double>(gv.z) * c.z;
+        }
+        const Material& M = s.materials[st.mat];
+        V3 tb = v3(1.0f);
+        float tr = 1.0f, tm = 1.0f;
+        if (M.baseTex >= 0) {
+            const V4 t = tex_sample(s, M.baseTex, st.uv);
+            tb = {t.x, t.y, t.z};
+        }
+        if (M.mrTex >= 0) {
+            const V4 t = tex_sample(s, M.mrTex, st.uv);
+            tr = t.y;
+            tm = t.z;
+        }
+        double* dm = &acc.mat[5 * st.mat];
+        dm[0] += g[0] * 0.96 * tb.x;
+        dm[1] += g[1] * 0.96 * tb.y;
+        dm[2] += g[2] * 0.96 * tb.z;
+        dm[3] += g[3] * tr;
+        dm[4] += g[4] * tm;
+        if (M.baseTex >= 0 && texOff[M.baseTex] >= 0) {
+            const Texture& t = s.textures[M.baseTex];
+            long long idx[4];
+            float w[4];
+            const int n = texel_taps(t, st.uv.x * t.scale.x + t.offset.x, st.uv.y * t.scale.y + t.offset.y, idx, w);
+            double* dt = &acc.texel[texOff[M.baseTex]];
+            for (int q = 0; q < n; ++q) {
+                dt[3 * idx[q]] += g[0] * 0.96 * M.baseFactor.x * w[q];
+                dt[3 * idx[q] + 1] += g[1] * 0.96 * M.baseFactor.y * w[q];
+                dt[3 * idx[q] + 2] += g[2] * 0.96 * M.baseFactor.z * w[q];
+            }
+        }
+    }
 }
 
 }  // namespace
@@ -1577,6 +1796,114 @@ int orc_render_samples(const orc_scene* s, int threads, uint32_t row0, uint32_t 
             dst[2] = c.z;
         }
     });
+    return MT_OK;
+}
+
+int orc_render_grad(const orc_scene* s, const float* target, float* image, float* loss, float* d_base,
+                    float* d_rough, float* d_metal, float* d_light, float* d_texels, int threads)
+{
+    if (!s || !target || !image || !loss || !d_base || !d_rough || !d_metal) return fail("null arg");
+    const mt_config& cfg = s->cfg;
+    const uint32_t W = cfg.width, H = cfg.height, S = cfg.samples;
+    const float aspect = static_cast<float>(W) / static_cast<float>(H);
+    const float pxW = 1.0f / static_cast<float>(W), pxH = 1.0f / static_cast<float>(H);
+    const float expo = std::pow(2.0f, -cfg.ev_exposure);
+    // RGB32F textures used as a base colour, in texture order
+    std::vector<long long> texOff(s->textures.size(), -1);
+    std::vector<char> used(s->textures.size(), 0);
+    for (const Material& m : s->materials)
+        if (m.baseTex >= 0) used[m.baseTex] = 1;
+    long long ntex = 0;
+    for (size_t i = 0; i < s->textures.size(); ++i)
+        if (used[i] && !s->textures[i].rgbf.empty()) {
+            texOff[i] = ntex;
+            ntex += 3ll * s->textures[i].w * s->textures[i].h;
+        }
+    const unsigned T = hw_threads(threads);
+    std::vector<GradAcc> acc(T);
+    for (GradAcc& a : acc) {
+        a.mat.assign(5 * s->materials.size(), 0.0);
+        a.light.assign(s->lights.size(), 0.0);
+        a.texel.assign(static_cast<size_t>(ntex), 0.0);
+    }
+    std::vector<Worker> workers(T);
+    parallel_for(static_cast<uint64_t>(W) * H, threads, [&](uint64_t p, unsigned t) {
+        const uint32_t y = static_cast<uint32_t>(p / W), x = static_cast<uint32_t>(p % W);
+        Worker& w = workers[t];
+        Rng rng;
+        seed_counter(rng, *s);
+        rng.pixel = y * W + x;
+        std::vector<std::vector<PathStep>> paths(S);
+        std::vector<V3> vals(S), totals(S);
+        for (uint32_t sm = 0; sm < S; ++sm) {
+            rng.sample = sm;
+            const float u = static_cast<float>(x) * pxW + rng.uniform(0.0f, pxW, 0, SLOT_JITTER, 0);
+            const float v = static_cast<float>(y) * pxH + rng.uniform(0.0f, pxH, 0, SLOT_JITTER, 1);
+            V3 o, d;
+            camera_ray(s->cam, u, v, aspect, o, d);
+            vals[sm] = process_ray_forward(*s, w, rng, o, d, expo, &totals[sm]);
+            paths[sm] = w.path;
+        }
+        std::vector<V3> buf = vals;
+        const V3 img = resolve_pixel(buf, cfg.firefly_enable != 0, cfg.firefly_threshold);
+        float* ip = image + 3 * p;
+        ip[0] = img.x, ip[1] = img.y, ip[2] = img.z;
+        const V3 r{img.x - target[3 * p], img.y - target[3 * p + 1], img.z - target[3 * p + 2]};
+        acc[t].loss += static_cast<double>(r.x) * r.x + static_cast<double>(r.y) * r.y +
+                       static_cast<double>(r.z) * r.z;
+        // firefly mask (CleanupFireflies, Tracer.cpp:490-548)
+        auto inten = [](V3 c) { return (c.x + c.y + c.z) / 3.0f; };
+        float mean = 0.0f, thr = std::numeric_limits<float>::max();
+        uint32_t kept = S;
+        if (cfg.firefly_enable) {
+            float sum = 0.0f;
+            for (const V3& c : vals) sum = sum + inten(c);
+            mean = sum / static_cast<float>(S);
+            float var = 0.0f;
+            for (const V3& c : vals) {
+                const float df = inten(c) - mean;
+                var = var + df * df;
+            }
+            var = var / static_cast<float>(S);
+            thr = cfg.firefly_threshold * std::sqrt(var);
+            for (const V3& c : vals)
+                if (std::fabs(inten(c) - mean) > thr) --kept;
+            if (kept == 0) kept = 1;
+        }
+        const float scale = 2.0f / static_cast<float>(kept);
+        for (uint32_t sm = 0; sm < S; ++sm) {
+            if (cfg.firefly_enable && std::fabs(inten(vals[sm]) - mean) > thr) continue;
+            const V3 tt = totals[sm];
+            const V3 gv{r.x * scale * aces_slope(tt.x * expo) * expo, r.y * scale * aces_slope(tt.y * expo) * expo,
+                        r.z * scale * aces_slope(tt.z * expo) * expo};
+            sample_backward(*s, paths[sm], gv, texOff, acc[t]);
+        }
+    });
+    double L = 0.0;
+    for (const GradAcc& a : acc) L += a.loss;
+    *loss = static_cast<float>(L);
+    for (size_t m = 0; m < s->materials.size(); ++m) {
+        double g[5] = {0, 0, 0, 0, 0};
+        for (const GradAcc& a : acc)
+            for (int k = 0; k < 5; ++k) g[k] += a.mat[5 * m + k];
+        d_base[3 * m] += static_cast<float>(g[0]);
+        d_base[3 * m + 1] += static_cast<float>(g[1]);
+        d_base[3 * m + 2] += static_cast<float>(g[2]);
+        d_rough[m] += static_cast<float>(g[3]);
+        d_metal[m] += static_cast<float>(g[4]);
+    }
+    if (d_light)
+        for (size_t l = 0; l < s->lights.size(); ++l) {
+            double g = 0;
+            for (const GradAcc& a : acc) g += a.light[l];
+            d_light[l] += static_cast<float>(g);
+        }
+    if (d_texels)
+        for (long long i = 0; i < ntex; ++i) {
+            double g = 0;
+            for (const GradAcc& a : acc) g += a.texel[static_cast<size_t>(i)];
+            d_texels[i] += static_cast<float>(g);
+        }
     return MT_OK;
 }
 

@@ -85,6 +85,13 @@ int orc_render_samples(const orc_scene* s, int threads, uint32_t row0, uint32_t 
 int orc_resolve_pixel(const float* samples_rgb, uint32_t n, int firefly_enable, float k,
                       float out_rgb[3]);
 
+/* Adjoint check: renders with the counter RNG, and adds dL/dparameters for
+ * L = sum over pixels/channels of (image - target)^2, replaying each kept
+ * sample's path with its decisions held fixed (same convention and gradient
+ * layout as mt_render_grad). */
+int orc_render_grad(const orc_scene* s, const float* target, float* image, float* loss, float* d_base,
+                    float* d_rough, float* d_metal, float* d_light, float* d_texels, int threads);
+
 /* ACES fit (Tracer.cpp:212-222). */
 void orc_aces(const float in_rgb[3], float exposure_mul, float out_rgb[3]);
 

@@ -49,6 +49,7 @@ def load(fast: bool = False):
         "orc_render_samples": (C.c_int, [vp, C.c_int, C.c_uint32, C.c_uint32, vp]),
         "orc_resolve_pixel": (C.c_int, [vp, C.c_uint32, C.c_int, C.c_float, vp]),
         "orc_aces": (None, [vp, C.c_float, vp]),
+        "orc_render_grad": (C.c_int, [vp, vp, vp, vp, vp, vp, vp, vp, vp, C.c_int]),
         "orc_last_error": (C.c_char_p, []),
     }
     for k, (r, a) in protos.items():
@@ -189,6 +190,31 @@ class OracleScene:
         _check(self.L.orc_render(self.h, rng, threads, row0, row1, _p(img), C.byref(rays), C.byref(samples)),
                self.L, "orc_render")
         return img, rays.value, samples.value
+
+    def render_grad(self, target: np.ndarray, num_texels: int = 0, threads=0):
+        """Counter-RNG render plus dL/dparameters of L = sum (image - target)^2.
+        Returns dict(image, loss, d_base (M,3), d_roughness (M,), d_metallic (M,),
+        d_light (Lights,), d_texels (num_texels,))."""
+        cfg = self.cfg
+        target = np.ascontiguousarray(target, dtype=np.float32).reshape(cfg.height, cfg.width, 3)
+        nm = self.packed.desc.num_materials
+        nl = self.packed.desc.num_lights
+        out = {
+            "image": np.zeros((cfg.height, cfg.width, 3), np.float32),
+            "loss": np.zeros(1, np.float32),
+            "d_base": np.zeros((nm, 3), np.float32),
+            "d_roughness": np.zeros(nm, np.float32),
+            "d_metallic": np.zeros(nm, np.float32),
+            "d_light": np.zeros(max(nl, 1), np.float32),
+            "d_texels": np.zeros(max(num_texels, 1), np.float32),
+        }
+        _check(self.L.orc_render_grad(self.h, _p(target), _p(out["image"]), _p(out["loss"]), _p(out["d_base"]),
+                                      _p(out["d_roughness"]), _p(out["d_metallic"]), _p(out["d_light"]),
+                                      _p(out["d_texels"]), threads), self.L, "orc_render_grad")
+        out["loss"] = float(out["loss"][0])
+        out["d_light"] = out["d_light"][:nl]
+        out["d_texels"] = out["d_texels"][:num_texels]
+        return out
 
     def render_samples(self, row0=0, row1=None, threads=0):
         W, H, S = self.cfg.width, self.cfg.height, self.cfg.samples
