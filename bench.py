@@ -63,6 +63,9 @@ def parse():
                    help="instead of the throughput line: time to relMSE 0.01 against a high-spp reference")
     p.add_argument("--ref-spp", type=int, default=16384)
     p.add_argument("--relmse-target", type=float, default=0.01)
+    p.add_argument("--no-nrc", action="store_true", help="time-to-relMSE: skip the radiance-cache leg")
+    p.add_argument("--nrc-warmup", type=int, default=8, help="training-only frames before the first cached frame")
+    p.add_argument("--nrc-frames", type=int, default=48, help="cached frames at most")
     return p.parse_args()
 
 
@@ -512,8 +515,58 @@ def run_time_to_relmse(a):
                        "cpu": cpu_model(), "mrays_s": rays_c / cpu_s / 1e6,
                        "note": "measured: full image at the GPU's first passing spp, same reference"}
         line["speedup_vs_cpu_at_target"] = cpu_s / hit["seconds"]
+    if not a.no_nrc:
+        line["nrc"] = nrc_time_to_relmse(a, ref, dev, stream)
+        if line["nrc"].get("seconds_to_target") and hit:
+            line["nrc_vs_plain_time"] = line["nrc"]["seconds_to_target"] / hit["seconds"]
     line["wall_s"] = time.perf_counter() - t0
     print(json.dumps(line), flush=True)
+
+
+def nrc_time_to_relmse(a, ref, dev, stream):
+    """The radiance-cache renderer on the same scene: --nrc-warmup training-only
+    frames, then cached frames (mt_nrc_config defaults: 4 spp, 65,536 training
+    paths and 4 Adam steps of 16,384 per frame) folded into a running mean.
+    Every frame is timed with CUDA events on the render stream; relMSE of the
+    running mean against the plain reference is evaluated between frames,
+    outside the timed spans."""
+    import torch
+
+    import mitrace_gb300 as mt
+
+    scene, cfg = mt.material_grid(width=a.width, height=a.height, samples=4, seed=0)
+    cfg.seed = 0
+    refd = torch.from_numpy(ref).to(dev)
+    acc = torch.zeros_like(refd)
+    out = {"warmup_frames": a.nrc_warmup, "frames": []}
+    with mt.Tracer(scene, cfg) as tr:
+        c = tr.nrc_enable()
+        out["config"] = {"spp_per_frame": c.spp, "train_paths": c.train_paths, "train_batch": c.train_batch,
+                         "train_steps": c.train_steps, "lr": c.learning_rate, "rough_min": c.rough_min}
+        ev = []
+        total = 0.0
+        for f in range(a.nrc_warmup + a.nrc_frames):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            cached = f >= a.nrc_warmup
+            k = f - a.nrc_warmup
+            tr.nrc_frame(acc.data_ptr() if cached else 0, max(k, 0), stream.cuda_stream)
+            e1.record(stream)
+            e1.synchronize()
+            ms = e0.elapsed_time(e1)
+            total += ms / 1e3
+            if not cached:
+                out.setdefault("warmup_ms", []).append(ms)
+                continue
+            r = float(((acc - refd) ** 2 / (refd * refd + 1e-2)).mean().item())
+            out["frames"].append({"frame": k, "ms": ms, "cum_s": total, "relmse": r})
+            if r <= a.relmse_target and "seconds_to_target" not in out:
+                out["seconds_to_target"] = total
+                out["frames_to_target"] = k + 1
+                if k >= 3:
+                    break
+    out["best_relmse"] = min(x["relmse"] for x in out["frames"]) if out["frames"] else None
+    return out
 
 
 def main():

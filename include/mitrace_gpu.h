@@ -274,6 +274,76 @@ typedef struct mt_grad_buffers {
 mt_status mt_render_grad(mt_handle* h, const mt_grad_buffers* g, void* cuda_stream);
 
 /* ------------------------------------------------------------------------ */
+/* Neural radiance cache (no reference counterpart).                        */
+/* ------------------------------------------------------------------------ */
+
+/* The cache is an MLP, MT_NRC_INPUTS -> 4 hidden layers of MT_NRC_WIDTH (ReLU)
+ * -> RGB, without bias terms (the constant-1 input lanes act as biases), BF16
+ * weights and activations with FP32 accumulation.  Its input is the encoding
+ * of a 20-float feature record (five float4):
+ *   f0 = (position normalised to the scene's world box, roughness)
+ *   f1 = (outgoing direction wo = -ray direction, unused)
+ *   f2 = (shading normal, unused)
+ *   f3 = (diffuse albedo base*(1-metallic), unused)
+ *   f4 = (specular albedo mix(0.04, base, metallic), unused)
+ * Encoding (80 lanes): 12 triangle-wave octaves per position axis (36),
+ * real spherical harmonics through band 3 of wo (16) and of the normal (16),
+ * roughness (1), diffuse (3) and specular (3) albedo, five constant 1s.
+ * Parameters, FP32 master copy: W0 (64 x 80), W1, W2, W3 (64 x 64), W4 (3 x
+ * 64), each row-major [out][in] like a torch Linear weight, concatenated. */
+#define MT_NRC_INPUTS 80u
+#define MT_NRC_WIDTH 64u
+#define MT_NRC_FEATURES 20u
+#define MT_NRC_PARAMS (80u * 64u + 3u * 64u * 64u + 64u * 3u) /* 17,600 */
+
+typedef struct mt_nrc_config {
+    uint32_t train_paths;  /* full-length training paths traced per frame (65,536) */
+    uint32_t train_batch;  /* training samples (path vertices) per Adam step (16,384) */
+    uint32_t train_steps;  /* Adam steps per frame (4) */
+    uint32_t spp;          /* cached-render samples per pixel per frame (4) */
+    float learning_rate;   /* Adam step size (1e-2) */
+    float beta1, beta2;    /* Adam moment decays (0.9, 0.99) */
+    float epsilon;         /* Adam denominator guard (1e-15) */
+    float rough_min;       /* a vertex with roughness >= this is diffuse-ish (0.3) */
+    uint32_t seed;         /* weight initialisation and training-path seed */
+    uint32_t reserved[6];
+} mt_nrc_config;
+
+void mt_nrc_config_defaults(mt_nrc_config* c);
+/* Allocates the cache on the handle and initialises its weights (Xavier
+ * uniform from seed) and Adam state.  Calling it again re-initialises. */
+mt_status mt_nrc_enable(mt_handle* h, const mt_nrc_config* c);
+/* One frame of the cached renderer, enqueued on cuda_stream:
+ *  1. trace train_paths full-length plain paths from random pixels, record
+ *     every vertex's features and the radiance the rest of its path carried
+ *     back ((path total - total before the vertex's NEE) / throughput);
+ *  2. take train_steps Adam steps on batches of those vertices (relative L2
+ *     loss |y - t|^2 / (y^2 + 0.01), y held constant in the denominator);
+ *  3. if d_accum is not NULL, render spp samples per pixel in which a path
+ *     ends at the first vertex after a diffuse-ish one (bounce >= 1) and adds
+ *     throughput * max(cache(vertex), 0) instead of tracing on; resolve them
+ *     like mt_render_device (per-sample ACES, firefly clamp over the frame's
+ *     spp) and fold the frame into d_accum (W*H*3) as a running mean:
+ *     accum += (frame - accum) / (accum_index + 1).
+ * Frames draw distinct random numbers (sample indices continue across frames). */
+mt_status mt_nrc_frame(mt_handle* h, float* d_accum, uint32_t accum_index, void* cuda_stream);
+/* Copies the FP32 master parameters out / in (MT_NRC_PARAMS floats, host).
+ * Setting them resets the Adam moments and step count. */
+mt_status mt_nrc_get_params(mt_handle* h, float* params);
+mt_status mt_nrc_set_params(mt_handle* h, const float* params);
+/* Cache outputs for n feature records (device buffers: n*20 floats in, n*3 out). */
+mt_status mt_nrc_infer(mt_handle* h, const float* d_features, uint32_t n, float* d_rgb, void* cuda_stream);
+/* One Adam step on n samples (device buffers: n*20 feature floats, n*3 target
+ * floats).  d_loss (1 float, may be NULL) receives the batch's mean relative
+ * L2 loss before the step; d_grad (MT_NRC_PARAMS floats, may be NULL) the
+ * gradient the step used.  n <= 4 * train_batch. */
+mt_status mt_nrc_train_step(mt_handle* h, const float* d_features, const float* d_targets, uint32_t n,
+                            float* d_loss, float* d_grad, void* cuda_stream);
+/* The FP32 input encoding of n feature records (n*20 floats in, n*80 out); no
+ * handle needed. */
+mt_status mt_nrc_encode(const float* d_features, uint32_t n, float* d_encoded, void* cuda_stream);
+
+/* ------------------------------------------------------------------------ */
 /* Ray queries (test and microbench entry points).                          */
 /* ------------------------------------------------------------------------ */
 

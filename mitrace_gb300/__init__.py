@@ -23,7 +23,7 @@ from .scenes import (
     incoherent_rays,
     scene_bounds,
 )
-from .tracer import Tracer, Stats, brdf_batch, bvh_build
+from .tracer import Tracer, Stats, brdf_batch, bvh_build, nrc_encode_device
 
 __all__ = [
     "MTError",
@@ -45,4 +45,5 @@ __all__ = [
     "Stats",
     "brdf_batch",
     "bvh_build",
+    "nrc_encode_device",
 ]

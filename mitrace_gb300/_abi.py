@@ -205,6 +205,27 @@ class mt_grad_buffers(C.Structure):
 
 MT_GRAD_MAX_BOUNCES = 16
 
+MT_NRC_INPUTS = 80
+MT_NRC_WIDTH = 64
+MT_NRC_FEATURES = 20
+MT_NRC_PARAMS = 80 * 64 + 3 * 64 * 64 + 64 * 3
+
+
+class mt_nrc_config(C.Structure):
+    _fields_ = [
+        ("train_paths", C.c_uint32),
+        ("train_batch", C.c_uint32),
+        ("train_steps", C.c_uint32),
+        ("spp", C.c_uint32),
+        ("learning_rate", C.c_float),
+        ("beta1", C.c_float),
+        ("beta2", C.c_float),
+        ("epsilon", C.c_float),
+        ("rough_min", C.c_float),
+        ("seed", C.c_uint32),
+        ("reserved", C.c_uint32 * 6),
+    ]
+
 
 class mt_brdf_query(C.Structure):
     _fields_ = [
@@ -235,6 +256,14 @@ PROTOTYPES = [
     ("mt_render_device", C.c_int, [_VP, _VP, _VP]),
     ("mt_render_rows_noalloc", C.c_int, [_VP, C.c_uint32, C.c_uint32, _VP, _VP]),
     ("mt_render_grad", C.c_int, [_VP, C.POINTER(mt_grad_buffers), _VP]),
+    ("mt_nrc_config_defaults", None, [C.POINTER(mt_nrc_config)]),
+    ("mt_nrc_enable", C.c_int, [_VP, C.POINTER(mt_nrc_config)]),
+    ("mt_nrc_frame", C.c_int, [_VP, _VP, C.c_uint32, _VP]),
+    ("mt_nrc_get_params", C.c_int, [_VP, _VP]),
+    ("mt_nrc_set_params", C.c_int, [_VP, _VP]),
+    ("mt_nrc_infer", C.c_int, [_VP, _VP, C.c_uint32, _VP, _VP]),
+    ("mt_nrc_train_step", C.c_int, [_VP, _VP, _VP, C.c_uint32, _VP, _VP, _VP]),
+    ("mt_nrc_encode", C.c_int, [_VP, C.c_uint32, _VP, _VP]),
     ("mt_trace_rays", C.c_int, [_VP, _VP, C.c_uint64, _VP, C.c_int]),
     ("mt_trace_rays_device", C.c_int, [_VP, _VP, C.c_uint64, _VP, C.c_int, _VP]),
     ("mt_brdf_batch", C.c_int, [_VP, C.c_uint64, _VP]),

@@ -23,6 +23,7 @@
 #include "mt_adjoint.h"
 #include "mt_internal.h"
 #include "mt_kernels.h"
+#include "mt_nrc.h"
 
 using namespace mt;
 
@@ -190,6 +191,10 @@ struct mt_handle {
     std::vector<DevArray<float>> texf;
     DevArray<int> error_flag;
     uint64_t scene_bytes = 0;
+    float world_lo[3] = {std::numeric_limits<float>::max(), std::numeric_limits<float>::max(),
+                         std::numeric_limits<float>::max()};
+    float world_hi[3] = {std::numeric_limits<float>::lowest(), std::numeric_limits<float>::lowest(),
+                         std::numeric_limits<float>::lowest()};
     // wavefront storage (allocated on first render)
     uint32_t batch = 0;
     uint64_t band_capacity = 0;  // samples the band planes hold
@@ -215,6 +220,20 @@ struct mt_handle {
     DevArray<float4> rec_vert, rec_path, grad_pix;
     DevArray<long long> texel_off;
     uint64_t grad_texels = 0;
+    // neural radiance cache (mt_nrc_enable)
+    struct Nrc {
+        bool on = false;
+        mt_nrc_config cfg{};
+        DevArray<float> master, m, v, partial, planes, frame;
+        DevArray<uint16_t> fwd, bwd, acts;
+        DevArray<float4> qrec, trec, samples;
+        DevArray<uint32_t> counters;  // [0] cache queries, [1] training samples
+        NrcOptimizer opt{};
+        uint64_t frames = 0;          // frames rendered (sample indices continue)
+        uint64_t plane_capacity = 0;  // samples the cached render's band planes hold
+        uint32_t train_chunk = 0;     // training paths per wavefront batch
+        uint32_t sample_cap = 0;
+    } nrc;
     // query scratch
     DevArray<mt_ray> qrays;
     DevArray<mt_hit> qhits;
@@ -414,6 +433,10 @@ mt_status upload_scene(mt_handle* h, const mt_scene_desc* d)
             }
         }
         insts[i] = x;
+        for (int k = 0; k < 3; ++k) {
+            h->world_lo[k] = std::min(h->world_lo[k], x.wlo[k]);
+            h->world_hi[k] = std::max(h->world_hi[k], x.whi[k]);
+        }
     }
 
     std::vector<DevLight> lights(d->num_lights);
@@ -673,6 +696,121 @@ bool internal_busy(const mt_handle* h) { return h && h->running.load() != 0; }
 mt_status internal_error(mt_status code, const std::string& msg) { return set_err(code, msg); }
 
 }  // namespace mt
+
+namespace {
+
+// Xavier-uniform initial weights, bound sqrt(6 / (fan_in + fan_out)), from a
+// splitmix64 stream of the seed.
+void nrc_init_weights(uint32_t seed, std::vector<float>& w)
+{
+    w.assign(kNrcParams, 0.0f);
+    uint64_t x = 0x9E3779B97F4A7C15ull ^ seed;
+    auto next = [&x]() {
+        x += 0x9E3779B97F4A7C15ull;
+        uint64_t z = x;
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        return z ^ (z >> 31);
+    };
+    const int ins[5] = {80, 64, 64, 64, 64}, outs[5] = {64, 64, 64, 64, 3};
+    size_t off = 0;
+    for (int l = 0; l < 5; ++l) {
+        const double bound = std::sqrt(6.0 / (ins[l] + outs[l]));
+        for (int k = 0; k < ins[l] * outs[l]; ++k) {
+            const double u = static_cast<double>(next() >> 11) * (1.0 / 9007199254740992.0);
+            w[off + k] = static_cast<float>((2.0 * u - 1.0) * bound);
+        }
+        off += static_cast<size_t>(ins[l]) * outs[l];
+    }
+}
+
+uint64_t gcd64(uint64_t a, uint64_t b)
+{
+    while (b) {
+        const uint64_t t = a % b;
+        a = b;
+        b = t;
+    }
+    return a;
+}
+
+mt_status nrc_alloc(mt_handle* h, const mt_nrc_config& c)
+{
+    auto& N = h->nrc;
+    N.on = false;
+    N.cfg = c;
+    const mt_config& cfg = h->cfg;
+    const cudaStream_t st = h->stream;
+    NrcOptimizer& O = N.opt;
+    O.max_splits = 128;
+    O.max_rows = static_cast<uint32_t>(((4ull * c.train_batch + 63) / 64) * 64 + 64ull * O.max_splits);
+    MT_CUDA(N.master.alloc(kNrcParams));
+    MT_CUDA(N.m.alloc(kNrcParams));
+    MT_CUDA(N.v.alloc(kNrcParams));
+    MT_CUDA(N.partial.alloc(static_cast<size_t>(O.max_splits) * kNrcParams));
+    MT_CUDA(N.fwd.alloc(kNrcFwdElems));
+    MT_CUDA(N.bwd.alloc(kNrcBwdElems));
+    MT_CUDA(cudaMemsetAsync(N.fwd.p, 0, kNrcFwdElems * 2, st));
+    MT_CUDA(cudaMemsetAsync(N.bwd.p, 0, kNrcBwdElems * 2, st));
+    const uint64_t R = O.max_rows;
+    MT_CUDA(N.acts.alloc(R * (80 + 8 * 64 + 8)));
+    O.acts.x = N.acts.p;
+    for (int l = 0; l < 4; ++l) {
+        O.acts.h[l] = N.acts.p + R * (80 + 64 * l);
+        O.acts.d[l] = N.acts.p + R * (80 + 256 + 64 * l);
+    }
+    O.acts.dy = N.acts.p + R * (80 + 512);
+    O.master = N.master.p;
+    O.m = N.m.p;
+    O.v = N.v.p;
+    O.partial = N.partial.p;
+    O.fwd = N.fwd.p;
+    O.bwd = N.bwd.p;
+    O.lr = c.learning_rate;
+    O.beta1 = c.beta1;
+    O.beta2 = c.beta2;
+    O.eps = c.epsilon;
+    O.step = 0;
+    // training paths and their samples
+    const uint32_t bounces = std::max<uint32_t>(1, cfg.bounces);
+    N.train_chunk = std::min<uint32_t>(c.train_paths, h->batch);
+    MT_CUDA(N.trec.alloc(static_cast<size_t>(N.train_chunk) * bounces * 6));
+    MT_CUDA(cudaMemsetAsync(N.trec.p, 0, N.trec.n * sizeof(float4), st));
+    N.sample_cap = c.train_paths * bounces;
+    MT_CUDA(N.samples.alloc(static_cast<size_t>(N.sample_cap) * 6));
+    MT_CUDA(N.qrec.alloc(static_cast<size_t>(h->batch) * 5));
+    MT_CUDA(N.counters.alloc(2));
+    MT_CUDA(cudaMemsetAsync(N.counters.p, 0, 2 * sizeof(uint32_t), st));
+    // band planes of the cached render and its frame image
+    const uint64_t npix = static_cast<uint64_t>(cfg.width) * cfg.height;
+    const uint64_t budget = env_u64("MT_SAMPLE_BUDGET_MB", 12288) << 20;
+    uint64_t rows = budget / (static_cast<uint64_t>(cfg.width) * c.spp * 12ull);
+    rows = std::max<uint64_t>(1, std::min<uint64_t>(rows, cfg.height));
+    N.plane_capacity = rows * cfg.width * c.spp;
+    MT_CUDA(N.planes.alloc(3 * N.plane_capacity));
+    MT_CUDA(N.frame.alloc(npix * 3));
+    // weights
+    std::vector<float> w;
+    nrc_init_weights(c.seed, w);
+    MT_CUDA(cudaMemcpyAsync(N.master.p, w.data(), kNrcParams * sizeof(float), cudaMemcpyHostToDevice, st));
+    MT_CUDA(cudaMemsetAsync(N.m.p, 0, kNrcParams * sizeof(float), st));
+    MT_CUDA(cudaMemsetAsync(N.v.p, 0, kNrcParams * sizeof(float), st));
+    MT_CUDA(launch_nrc_publish(O, st));
+    MT_CUDA(cudaStreamSynchronize(st));
+    N.frames = 0;
+    N.on = true;
+    return MT_OK;
+}
+
+mt_status nrc_ready(mt_handle* h)
+{
+    if (check_handle(h) != MT_OK) return MT_ERR_INVALID;
+    if (!h->nrc.on) return set_err(MT_ERR_STATE, "the radiance cache is not enabled (mt_nrc_enable)");
+    if (h->running) return set_err(MT_ERR_STATE, "an asynchronous render is running");
+    return MT_OK;
+}
+
+}  // namespace
 
 extern "C" {
 
@@ -1018,6 +1156,198 @@ void mt_bvh_free(mt_bvh_node* nodes, uint32_t* indices)
 {
     std::free(nodes);
     std::free(indices);
+}
+
+void mt_nrc_config_defaults(mt_nrc_config* c)
+{
+    if (!c) return;
+    std::memset(c, 0, sizeof(*c));
+    c->train_paths = 65536;
+    c->train_batch = 16384;
+    c->train_steps = 4;
+    c->spp = 4;
+    c->learning_rate = 1e-2f;
+    c->beta1 = 0.9f;
+    c->beta2 = 0.99f;
+    c->epsilon = 1e-15f;
+    c->rough_min = 0.3f;
+    c->seed = 1337;
+}
+
+mt_status mt_nrc_enable(mt_handle* h, const mt_nrc_config* c)
+{
+    if (check_handle(h) != MT_OK || !c) return set_err(MT_ERR_INVALID, "null argument");
+    if (h->running) return set_err(MT_ERR_STATE, "an asynchronous render is running");
+    if (c->train_paths == 0 || c->train_batch == 0 || c->train_batch > (1u << 24) || c->spp == 0 ||
+        !(c->learning_rate > 0.0f) || !(c->beta1 >= 0.0f && c->beta1 < 1.0f) || !(c->beta2 >= 0.0f && c->beta2 < 1.0f) ||
+        !(c->epsilon >= 0.0f))
+        return set_err(MT_ERR_INVALID, "invalid radiance-cache configuration");
+    if (static_cast<uint64_t>(c->train_paths) * std::max<uint32_t>(1, h->cfg.bounces) > 0xFFFFFFFFull)
+        return set_err(MT_ERR_INVALID, "train_paths * bounces exceeds 2^32");
+    mt_status rc = ensure_wave(h);
+    if (rc != MT_OK) return rc;
+    return nrc_alloc(h, *c);
+}
+
+mt_status mt_nrc_frame(mt_handle* h, float* d_accum, uint32_t accum_index, void* cuda_stream)
+{
+    mt_status rc = nrc_ready(h);
+    if (rc != MT_OK) return rc;
+    auto& N = h->nrc;
+    const mt_nrc_config& nc = N.cfg;
+    const mt_config& c = h->cfg;
+    cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);  // 0: the legacy default stream
+    const WaveViews v = views(h);
+    const uint64_t npix = static_cast<uint64_t>(c.width) * c.height;
+    NrcShade base;
+    base.rough_min = nc.rough_min;
+    for (int k = 0; k < 3; ++k) {
+        base.lo[k] = h->world_lo[k];
+        const float ext = h->world_hi[k] - h->world_lo[k];
+        base.inv_ext[k] = ext > 1e-12f ? 1.0f / ext : 1.0f;
+    }
+    uint64_t launches = 0;
+    // 1. full-length training paths from pixels spread over the image
+    DevScene St = h->S;
+    St.key0 ^= 0x85EBCA6Bu * static_cast<uint32_t>(N.frames + 1) + nc.seed;
+    St.key1 ^= 0xC2B2AE35u;
+    NrcShade T = base;
+    T.mode = MT_NRC_TRAIN;
+    T.rec = N.trec.p;
+    T.samples = N.samples.p;
+    T.sample_count = N.counters.p + 1;
+    T.sample_cap = N.sample_cap;
+    uint64_t mul = (0x9E3779B1ull + 2 * N.frames) % npix;
+    if (mul == 0) mul = 1;
+    while (gcd64(mul, npix) != 1) mul = (mul + 1) % npix ? (mul + 1) % npix : 1;
+    const uint64_t add0 = (N.frames * 0x632BE5ABull) % npix;
+    MT_CUDA(cudaMemsetAsync(N.counters.p + 1, 0, sizeof(uint32_t), st));
+    for (uint32_t c0 = 0; c0 < nc.train_paths; c0 += N.train_chunk) {
+        const uint32_t n = std::min<uint32_t>(N.train_chunk, nc.train_paths - c0);
+        BatchExtra X;
+        X.nrc = &T;
+        X.sample_base = 0;
+        X.scatter_mul = static_cast<uint32_t>(mul);
+        X.scatter_add = static_cast<uint32_t>((add0 + (static_cast<uint64_t>(c0) % npix) * mul) % npix);
+        MT_CUDA(launch_batch(St, v.P, v.SQ, v.W, 0, n, static_cast<uint32_t>(npix), 0, st, &launches, nullptr,
+                             nullptr, &X));
+    }
+    // 2. Adam steps on random vertices of those paths
+    for (uint32_t s = 0; s < nc.train_steps; ++s) {
+        NrcTrainArgs a{};
+        a.feat = N.samples.p;
+        a.fstride = 6;
+        a.targets = reinterpret_cast<const float*>(N.samples.p + 5);
+        a.tstride = 24;
+        a.count = N.counters.p + 1;
+        a.base = static_cast<uint32_t>((N.frames * nc.train_steps + s) * nc.train_batch);
+        a.rows = nc.train_batch;
+        MT_CUDA(launch_nrc_train_step(N.opt, a, nullptr, nullptr, st));
+        launches += 3;
+    }
+    // 3. the cached render
+    if (d_accum) {
+        DevScene Sr = h->S;
+        Sr.spp = nc.spp;
+        WaveBuffers Wr = v.W;
+        Wr.sr = N.planes.p;
+        Wr.sg = N.planes.p + N.plane_capacity;
+        Wr.sb = N.planes.p + 2 * N.plane_capacity;
+        NrcShade Q = base;
+        Q.mode = MT_NRC_QUERY;
+        Q.rec = N.qrec.p;
+        Q.count = N.counters.p;
+        Q.net = N.fwd.p;
+        const uint64_t rows_per_band = N.plane_capacity / (static_cast<uint64_t>(c.width) * nc.spp);
+        for (uint64_t r0 = 0; r0 < c.height; r0 += rows_per_band) {
+            const uint64_t rows = std::min<uint64_t>(rows_per_band, c.height - r0);
+            const uint32_t band_pix = static_cast<uint32_t>(rows * c.width);
+            const uint32_t pix_base = static_cast<uint32_t>(r0 * c.width);
+            const uint64_t paths = static_cast<uint64_t>(band_pix) * nc.spp;
+            for (uint64_t g0 = 0; g0 < paths; g0 += h->batch) {
+                const uint32_t n = static_cast<uint32_t>(std::min<uint64_t>(h->batch, paths - g0));
+                MT_CUDA(cudaMemsetAsync(N.counters.p, 0, sizeof(uint32_t), st));
+                BatchExtra X;
+                X.nrc = &Q;
+                X.sample_base = static_cast<uint32_t>(N.frames * nc.spp);
+                MT_CUDA(launch_batch(Sr, v.P, v.SQ, Wr, g0, n, band_pix, pix_base, st, &launches, nullptr, nullptr,
+                                     &X));
+            }
+            MT_CUDA(launch_resolve(Sr, Wr, band_pix, pix_base, N.frame.p, st, nullptr));
+            ++launches;
+        }
+        MT_CUDA(launch_nrc_blend(d_accum, N.frame.p, npix * 3, accum_index, st));
+        ++launches;
+    }
+    N.frames += 1;
+    h->launches += launches;
+    return MT_OK;
+}
+
+mt_status mt_nrc_get_params(mt_handle* h, float* params)
+{
+    mt_status rc = nrc_ready(h);
+    if (rc != MT_OK) return rc;
+    if (!params) return set_err(MT_ERR_INVALID, "null argument");
+    MT_CUDA(cudaDeviceSynchronize());
+    MT_CUDA(cudaMemcpy(params, h->nrc.master.p, kNrcParams * sizeof(float), cudaMemcpyDeviceToHost));
+    return MT_OK;
+}
+
+mt_status mt_nrc_set_params(mt_handle* h, const float* params)
+{
+    mt_status rc = nrc_ready(h);
+    if (rc != MT_OK) return rc;
+    if (!params) return set_err(MT_ERR_INVALID, "null argument");
+    auto& N = h->nrc;
+    MT_CUDA(cudaDeviceSynchronize());
+    MT_CUDA(cudaMemcpy(N.master.p, params, kNrcParams * sizeof(float), cudaMemcpyHostToDevice));
+    MT_CUDA(cudaMemset(N.m.p, 0, kNrcParams * sizeof(float)));
+    MT_CUDA(cudaMemset(N.v.p, 0, kNrcParams * sizeof(float)));
+    N.opt.step = 0;
+    MT_CUDA(launch_nrc_publish(N.opt, h->stream));
+    MT_CUDA(cudaStreamSynchronize(h->stream));
+    return MT_OK;
+}
+
+mt_status mt_nrc_infer(mt_handle* h, const float* d_features, uint32_t n, float* d_rgb, void* cuda_stream)
+{
+    mt_status rc = nrc_ready(h);
+    if (rc != MT_OK) return rc;
+    if (n && (!d_features || !d_rgb)) return set_err(MT_ERR_INVALID, "null argument");
+    MT_CUDA(launch_nrc_infer(h->nrc.fwd.p, d_features, n, d_rgb, static_cast<cudaStream_t>(cuda_stream)));
+    h->launches += n ? 1 : 0;
+    return MT_OK;
+}
+
+mt_status mt_nrc_train_step(mt_handle* h, const float* d_features, const float* d_targets, uint32_t n,
+                            float* d_loss, float* d_grad, void* cuda_stream)
+{
+    mt_status rc = nrc_ready(h);
+    if (rc != MT_OK) return rc;
+    if (!d_features || !d_targets) return set_err(MT_ERR_INVALID, "null argument");
+    if (n == 0 || static_cast<uint64_t>(n) > 4ull * h->nrc.cfg.train_batch)
+        return set_err(MT_ERR_INVALID, "n must be in [1, 4 * train_batch]");
+    cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
+    if (d_loss) MT_CUDA(cudaMemsetAsync(d_loss, 0, sizeof(float), st));
+    NrcTrainArgs a{};
+    a.feat = reinterpret_cast<const float4*>(d_features);
+    a.fstride = 5;
+    a.targets = d_targets;
+    a.tstride = 3;
+    a.count = nullptr;
+    a.base = 0;
+    a.rows = n;
+    MT_CUDA(launch_nrc_train_step(h->nrc.opt, a, d_loss, d_grad, st));
+    h->launches += 3;
+    return MT_OK;
+}
+
+mt_status mt_nrc_encode(const float* d_features, uint32_t n, float* d_encoded, void* cuda_stream)
+{
+    if (n && (!d_features || !d_encoded)) return set_err(MT_ERR_INVALID, "null argument");
+    MT_CUDA(launch_nrc_encode(d_features, n, d_encoded, static_cast<cudaStream_t>(cuda_stream)));
+    return MT_OK;
 }
 
 }  // extern "C"

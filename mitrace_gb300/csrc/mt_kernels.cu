@@ -16,6 +16,7 @@
 
 #include "mt_device.cuh"
 #include "mt_kernels.h"
+#include "mt_nrc.h"
 
 // Occupancy hint of the traversal kernels: blocks of 128 threads per SM that
 // the register allocation must allow (6 -> at most 80 registers per thread, no
@@ -125,14 +126,24 @@ struct BatchInfo {
     uint32_t n;         // paths in this batch
     uint32_t band_pix;  // pixels in the band
     uint32_t pix_base;  // first pixel (y*W+x) of the band
+    uint32_t sample_base;  // added to the sample index of every path
+    uint32_t scatter_mul;  // nonzero: path p is pixel (p * mul + add) mod W*H, sample sample_base
+    uint32_t scatter_add;
 };
 
 __device__ __forceinline__ void path_coords(const DevScene& S, const BatchInfo& B, uint32_t p,
                                             uint32_t& pixel, uint32_t& sample)
 {
+    if (B.scatter_mul) {
+        const uint64_t npix = static_cast<uint64_t>(S.width) * S.height;
+        pixel = static_cast<uint32_t>((static_cast<uint64_t>(p) * B.scatter_mul + B.scatter_add) % npix);
+        sample = B.sample_base;
+        return;
+    }
     const uint64_t g = B.g0 + p;
     sample = static_cast<uint32_t>(g / B.band_pix);
     pixel = B.pix_base + static_cast<uint32_t>(g - static_cast<uint64_t>(sample) * B.band_pix);
+    sample += B.sample_base;
 }
 
 __global__ void __launch_bounds__(256) k_raygen(DevScene S, PathState P, BatchInfo B,
@@ -256,7 +267,7 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, PathState P, ShadowQu
                                                BatchInfo B, uint32_t bounce,
                                                const uint32_t* __restrict__ q,
                                                uint32_t* __restrict__ nq, uint32_t* counts,
-                                               int cur, RecordBuffers R)
+                                               int cur, RecordBuffers R, NrcShade NC)
 {
     const uint32_t n = counts[cur];
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -313,7 +324,36 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, PathState P, ShadowQu
         const f3 view = -rd;
 
         // Emission (Tracer.cpp:255)
-        st4(P.emit, p, ld4(P.emit, p) + (cur_e * S.emission_base) * mp.emission);
+        const f3 emit_now = ld4(P.emit, p) + (cur_e * S.emission_base) * mp.emission;
+        st4(P.emit, p, emit_now);
+        float seen_diffuse = 0.0f;
+        if (NC.mode != MT_NRC_OFF) {
+            // Radiance-cache feature record of this vertex (mt_nrc.h)
+            seen_diffuse = P.prev[p].w;
+            const bool query = NC.mode == MT_NRC_QUERY && bounce >= 1 && seen_diffuse != 0.0f;
+            float4* fr = nullptr;
+            if (query)
+                fr = NC.rec + 5ull * warp_append(NC.count);
+            else if (NC.mode == MT_NRC_TRAIN)
+                fr = NC.rec + (static_cast<uint64_t>(p) * S.bounces + bounce) * 6;
+            if (fr) {
+                const f3 pn = {(hit_pos.x - NC.lo[0]) * NC.inv_ext[0], (hit_pos.y - NC.lo[1]) * NC.inv_ext[1],
+                               (hit_pos.z - NC.lo[2]) * NC.inv_ext[2]};
+                const float m = mp.metallic;
+                fr[0] = make_float4(pn.x, pn.y, pn.z, mp.roughness);
+                fr[1] = make_float4(view.x, view.y, view.z, __uint_as_float(p));
+                fr[2] = make_float4(N.x, N.y, N.z, cur_e.x);
+                fr[3] = make_float4(base.x * (1.0f - m), base.y * (1.0f - m), base.z * (1.0f - m), cur_e.y);
+                fr[4] = make_float4(0.04f * (1.0f - m) + base.x * m, 0.04f * (1.0f - m) + base.y * m,
+                                    0.04f * (1.0f - m) + base.z * m, cur_e.z);
+                if (!query) {
+                    const f3 pre = ((emit_now + ld4(P.direct, p)) + ld4(P.indirect, p)) + ld4(P.sky, p);
+                    fr[5] = make_float4(pre.x, pre.y, pre.z, 1.0f);
+                }
+            }
+            if (query) continue;  // the cache stands in for the rest of the path
+            if (mp.roughness >= NC.rough_min) seen_diffuse = 1.0f;
+        }
         float4* vr = R.vert ? R.vert + (static_cast<uint64_t>(p) * S.bounces + bounce) * 5 : nullptr;
         if (vr) {
             vr[0] = make_float4(N.x, N.y, N.z, __uint_as_float(__ldg(&I.material)));
@@ -430,7 +470,7 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, PathState P, ShadowQu
         const f3 no = (ro + rd * hit_dist) + N * 0.0001f;
         st4(P.ro, p, no);
         st4(P.rd, p, nd);
-        st4(P.prev, p, base);
+        st4(P.prev, p, base, seen_diffuse);
         nq[warp_append(&counts[cur ^ 1])] = p;
     }
 }
@@ -676,10 +716,12 @@ Profiler::~Profiler()
 cudaError_t launch_batch(const DevScene& S, const PathState& P, const ShadowQueue& SQ,
                          const WaveBuffers& W, uint64_t g0, uint32_t n, uint32_t band_pix,
                          uint32_t pix_base, cudaStream_t st, uint64_t* launches, Profiler* prof,
-                         const RecordBuffers* rec)
+                         const RecordBuffers* rec, const BatchExtra* extra)
 {
     const RecordBuffers R = rec ? *rec : RecordBuffers{};
-    BatchInfo B{g0, n, band_pix, pix_base};
+    const BatchExtra X = extra ? *extra : BatchExtra{};
+    const NrcShade NC = X.nrc ? *X.nrc : NrcShade{};
+    BatchInfo B{g0, n, band_pix, pix_base, X.sample_base, X.scatter_mul, X.scatter_add};
     const unsigned gw = grid_for(n, 128, 16);
     static unsigned g_ext[2] = {0, 0}, g_sh[2] = {0, 0};
     if (!g_ext[0]) {
@@ -705,7 +747,7 @@ cudaError_t launch_batch(const DevScene& S, const PathState& P, const ShadowQueu
             k_extend<false><<<g_ext[0], 128, 0, st>>>(S, P, W.q[cur], W.counts, cur, W.rays, cnt);
         end(MT_STAGE_EXTEND);
         begin(MT_STAGE_SHADE);
-        k_shade<<<gw, 128, 0, st>>>(S, P, SQ, B, b, W.q[cur], W.q[cur ^ 1], W.counts, cur, R);
+        k_shade<<<gw, 128, 0, st>>>(S, P, SQ, B, b, W.q[cur], W.q[cur ^ 1], W.counts, cur, R, NC);
         end(MT_STAGE_SHADE);
         begin(MT_STAGE_SHADOW);
         if (count)
@@ -715,6 +757,18 @@ cudaError_t launch_batch(const DevScene& S, const PathState& P, const ShadowQueu
         end(MT_STAGE_SHADOW);
         l += 3;
         cur ^= 1;
+    }
+    if (NC.mode == MT_NRC_TRAIN) {
+        // training paths feed the cache only; no image samples
+        const cudaError_t e = launch_nrc_targets(P, NC, n, S.bounces, st);
+        if (e != cudaSuccess) return e;
+        if (launches) *launches += l + 1;
+        return cudaSuccess;
+    }
+    if (NC.mode == MT_NRC_QUERY) {
+        const cudaError_t e = launch_nrc_query(NC.net, P, NC.rec, NC.count, n, st);
+        if (e != cudaSuccess) return e;
+        ++l;
     }
     begin(MT_STAGE_FINALIZE);
     k_finalize<<<grid_for(n, 256, 8), 256, 0, st>>>(S, P, B, W.sr, W.sg, W.sb, R);

@@ -83,10 +83,19 @@ struct Profiler {
 cudaError_t launch_trace(const DevScene& S, const mt_ray* rays, uint64_t n, mt_hit* hits, int query,
                          uint32_t* fetch, cudaStream_t st);
 cudaError_t launch_brdf(const mt_brdf_query* q, uint64_t n, mt_brdf_result* out, cudaStream_t st);
+struct NrcShade;
+// Optional batch settings beyond a plain band render.
+struct BatchExtra {
+    const NrcShade* nrc = nullptr;  // radiance-cache hooks of the shade stage
+    uint32_t sample_base = 0;       // added to every path's sample index
+    uint32_t scatter_mul = 0;       // nonzero: path p renders pixel (p * mul + add) mod W*H
+    uint32_t scatter_add = 0;
+};
+
 cudaError_t launch_batch(const DevScene& S, const PathState& P, const ShadowQueue& SQ,
                          const WaveBuffers& W, uint64_t g0, uint32_t n, uint32_t band_pix,
                          uint32_t pix_base, cudaStream_t st, uint64_t* launches, Profiler* prof,
-                         const RecordBuffers* rec = nullptr);
+                         const RecordBuffers* rec = nullptr, const BatchExtra* extra = nullptr);
 cudaError_t launch_resolve(const DevScene& S, const WaveBuffers& W, uint32_t band_pix,
                            uint32_t pix_base, float* out, cudaStream_t st, Profiler* prof);
 

@@ -1,0 +1,773 @@
+// mt_nrc.cu - neural radiance cache kernels.
+//
+// The cache maps a surface vertex (position, outgoing direction, normal,
+// roughness, albedos) to the radiance the rest of its path would carry back.
+// Network: 80 -> 64 -> 64 -> 64 -> 64 -> 3, ReLU, no biases; BF16 weights and
+// activations on the m16n8k16 tensor-core MMA with FP32 accumulation.
+//
+//   k_nrc_infer    fused encoding + 5 layers; a warp owns 16 rows, the
+//                  activations stay in registers between layers (the MMA
+//                  accumulator layout of one layer is the A-operand layout of
+//                  the next), the weights sit in shared memory.
+//   k_nrc_fwdbwd   the same forward pass, relative-L2 loss gradient, and the
+//                  backward pass through the activations; writes the layer
+//                  inputs and pre-activation gradients row-major (BF16).
+//   k_nrc_wgrad    dW_l = sum over rows of delta_l^T x input_l: 64-row chunks
+//                  staged in shared memory, transposed operands fetched with
+//                  ldmatrix.trans, one partial sum per block (fixed order).
+//   k_nrc_adam     sums the partials in block order, Adam, and rewrites the BF16
+//                  weight blobs.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+
+#include "mt_device.cuh"
+#include "mt_nrc.h"
+
+namespace mt {
+namespace {
+
+using bf16 = __nv_bfloat16;
+
+// ---------------------------------------------------------------------------
+// Layouts
+// ---------------------------------------------------------------------------
+__host__ __device__ constexpr int fwd_off(int l) { return l == 0 ? 0 : 64 * 88 + (l - 1) * 64 * 72; }
+__host__ __device__ constexpr int fwd_stride(int l) { return l == 0 ? 88 : 72; }
+__host__ __device__ constexpr int bwd_off(int l) { return (l - 1) * 64 * 72; }  // l = 1..4
+__host__ __device__ constexpr int bwd_stride(int l) { return l == 4 ? 24 : 72; }
+__host__ __device__ constexpr int master_off(int l) { return l == 0 ? 0 : 5120 + (l - 1) * 4096; }
+__host__ __device__ constexpr int layer_in(int l) { return l == 0 ? 80 : 64; }
+__host__ __device__ constexpr int layer_out(int l) { return l == 4 ? 3 : 64; }
+static_assert(fwd_off(4) + 8 * 72 == kNrcFwdElems, "forward blob size");
+static_assert(bwd_off(4) + 64 * 24 == kNrcBwdElems, "backward blob size");
+static_assert(master_off(4) + 3 * 64 == kNrcParams, "parameter count");
+
+__device__ __forceinline__ void param_coords(int q, int& l, int& o, int& i)
+{
+    if (q < 5120) {
+        l = 0;
+        o = q / 80;
+        i = q - o * 80;
+    } else if (q < 17408) {
+        const int r = q - 5120;
+        l = 1 + r / 4096;
+        const int s = r - (l - 1) * 4096;
+        o = s >> 6;
+        i = s & 63;
+    } else {
+        l = 4;
+        const int r = q - 17408;
+        o = r >> 6;
+        i = r & 63;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Input encoding
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float clamp01(float x) { return fminf(fmaxf(x, 0.0f), 1.0f); }
+
+// Triangle wave of period 1 with values in [-1, 1].
+__device__ __forceinline__ float tri_wave(float s)
+{
+    const float f = s - floorf(s);
+    return fabsf(4.0f * f - 2.0f) - 1.0f;
+}
+
+// Lanes [0,36) (12 octaves per position axis) and [68,80).
+template <class Out>
+__device__ __forceinline__ void encode_part0(float4 f0, float4 f3, float4 f4, Out out)
+{
+    const float p[3] = {clamp01(f0.x), clamp01(f0.y), clamp01(f0.z)};
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        float s = p[d];
+#pragma unroll
+        for (int j = 0; j < 12; ++j) {
+            out(d * 12 + j, tri_wave(s));
+            s *= 2.0f;
+        }
+    }
+    out(68, f0.w);
+    out(69, f3.x);
+    out(70, f3.y);
+    out(71, f3.z);
+    out(72, f4.x);
+    out(73, f4.y);
+    out(74, f4.z);
+#pragma unroll
+    for (int k = 75; k < 80; ++k) out(k, 1.0f);
+}
+
+// Real spherical harmonics of bands 0..3 of a unit vector (16 lanes from base).
+template <class Out>
+__device__ __forceinline__ void sh16(float x, float y, float z, int base, Out out)
+{
+    const float xx = x * x, yy = y * y, zz = z * z;
+    out(base + 0, 0.28209479177387814f);
+    out(base + 1, -0.48860251190291987f * y);
+    out(base + 2, 0.48860251190291987f * z);
+    out(base + 3, -0.48860251190291987f * x);
+    out(base + 4, 1.0925484305920792f * x * y);
+    out(base + 5, -1.0925484305920792f * y * z);
+    out(base + 6, 0.94617469575756f * zz - 0.31539156525252f);
+    out(base + 7, -1.0925484305920792f * x * z);
+    out(base + 8, 0.54627421529603959f * (xx - yy));
+    out(base + 9, 0.59004358992664352f * y * (yy - 3.0f * xx));
+    out(base + 10, 2.8906114426405538f * x * y * z);
+    out(base + 11, 0.45704579946446572f * y * (1.0f - 5.0f * zz));
+    out(base + 12, 0.3731763325901154f * z * (5.0f * zz - 3.0f));
+    out(base + 13, 0.45704579946446572f * x * (1.0f - 5.0f * zz));
+    out(base + 14, 1.4453057213202769f * z * (xx - yy));
+    out(base + 15, 0.59004358992664352f * x * (3.0f * yy - xx));
+}
+
+// Lanes [36,68): harmonics of wo and of the normal.
+template <class Out>
+__device__ __forceinline__ void encode_part1(float4 f1, float4 f2, Out out)
+{
+    sh16(f1.x, f1.y, f1.z, 36, out);
+    sh16(f2.x, f2.y, f2.z, 52, out);
+}
+
+// Encodes the 16 rows [r0, r0+16) of a feature array into a warp's staging
+// tile stg[16][88] (BF16); rows >= n become zeros (constant lanes included, so
+// their outputs and gradients are exactly zero).  Lanes 0-15 do part 0 of row
+// lane, lanes 16-31 part 1.
+__device__ __forceinline__ void stage_rows(const float4* __restrict__ feat, uint32_t fstride, uint32_t r0,
+                                           uint32_t n, const uint32_t* map, bf16* stg)
+{
+    const int lane = threadIdx.x & 31;
+    const int row = lane & 15;
+    const uint32_t r = r0 + row;
+    bf16* dst = stg + row * 88;
+    auto put = [&](int k, float v) { dst[k] = __float2bfloat16_rn(v); };
+    if (r < n) {
+        const float4* f = feat + static_cast<uint64_t>(map ? map[row] : r) * fstride;
+        if (lane < 16)
+            encode_part0(f[0], f[3], f[4], put);
+        else
+            encode_part1(f[1], f[2], put);
+    } else {
+        const bf16 z = __float2bfloat16_rn(0.0f);
+        if (lane < 16) {
+            for (int k = 0; k < 36; ++k) dst[k] = z;
+            for (int k = 68; k < 80; ++k) dst[k] = z;
+        } else {
+            for (int k = 36; k < 68; ++k) dst[k] = z;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Tensor-core helpers (mma.sync m16n8k16, BF16 in, FP32 accumulate)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t lds32(const bf16* p) { return *reinterpret_cast<const uint32_t*>(p); }
+
+__device__ __forceinline__ void mma16816(float* d, const uint32_t* a, uint32_t b0, uint32_t b1)
+{
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+__device__ __forceinline__ uint32_t pack2(float lo, float hi)
+{
+    const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<const uint32_t*>(&v);
+}
+
+__device__ __forceinline__ void ldsm_x4_trans(uint32_t* r, const bf16* p)
+{
+    const uint32_t a = static_cast<uint32_t>(__cvta_generic_to_shared(p));
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(a));
+}
+__device__ __forceinline__ void ldsm_x2_trans(uint32_t* r, const bf16* p)
+{
+    const uint32_t a = static_cast<uint32_t>(__cvta_generic_to_shared(p));
+    asm volatile("ldmatrix.sync.aligned.m8n8.x2.trans.shared.b16 {%0,%1}, [%2];\n"
+                 : "=r"(r[0]), "=r"(r[1])
+                 : "r"(a));
+}
+
+// acc[16 x 8*NT] = A[16 x 16*KT] * W^T, W given as rows [n][k] with stride.
+template <int KT, int NT>
+__device__ __forceinline__ void dense(const uint32_t (&a)[KT][4], const bf16* w, int stride, float (&acc)[NT][4])
+{
+    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+#pragma unroll
+    for (int j = 0; j < NT; ++j) {
+        acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.0f;
+        const bf16* row = w + (8 * j + g) * stride + 2 * t;
+#pragma unroll
+        for (int kt = 0; kt < KT; ++kt) mma16816(acc[j], a[kt], lds32(row + 16 * kt), lds32(row + 16 * kt + 8));
+    }
+}
+
+// Accumulator tiles -> A-operand fragments of the next layer (with ReLU).
+template <int NT>
+__device__ __forceinline__ void relu_pack(const float (&acc)[NT][4], uint32_t (&a)[NT / 2][4])
+{
+#pragma unroll
+    for (int kt = 0; kt < NT / 2; ++kt) {
+        a[kt][0] = pack2(fmaxf(acc[2 * kt][0], 0.0f), fmaxf(acc[2 * kt][1], 0.0f));
+        a[kt][1] = pack2(fmaxf(acc[2 * kt][2], 0.0f), fmaxf(acc[2 * kt][3], 0.0f));
+        a[kt][2] = pack2(fmaxf(acc[2 * kt + 1][0], 0.0f), fmaxf(acc[2 * kt + 1][1], 0.0f));
+        a[kt][3] = pack2(fmaxf(acc[2 * kt + 1][2], 0.0f), fmaxf(acc[2 * kt + 1][3], 0.0f));
+    }
+}
+
+// Zeroes gradient entries whose ReLU output was zero, then packs them as
+// A-operand fragments.
+template <int NT>
+__device__ __forceinline__ void mask_pack(float (&acc)[NT][4], const uint32_t (&h)[NT / 2][4],
+                                          uint32_t (&a)[NT / 2][4])
+{
+#pragma unroll
+    for (int j = 0; j < NT; ++j) {
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            const uint32_t hw = h[j >> 1][(j & 1) * 2 + (c >> 1)];
+            const uint32_t bits = (c & 1) ? (hw >> 16) : (hw & 0xffffu);
+            if ((bits & 0x7fffu) == 0) acc[j][c] = 0.0f;
+        }
+    }
+#pragma unroll
+    for (int kt = 0; kt < NT / 2; ++kt) {
+        a[kt][0] = pack2(acc[2 * kt][0], acc[2 * kt][1]);
+        a[kt][1] = pack2(acc[2 * kt][2], acc[2 * kt][3]);
+        a[kt][2] = pack2(acc[2 * kt + 1][0], acc[2 * kt + 1][1]);
+        a[kt][3] = pack2(acc[2 * kt + 1][2], acc[2 * kt + 1][3]);
+    }
+}
+
+__device__ __forceinline__ void load_x_frags(const bf16* stg, uint32_t (&ax)[5][4])
+{
+    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+#pragma unroll
+    for (int kt = 0; kt < 5; ++kt) {
+        ax[kt][0] = lds32(stg + g * 88 + 16 * kt + 2 * t);
+        ax[kt][1] = lds32(stg + (g + 8) * 88 + 16 * kt + 2 * t);
+        ax[kt][2] = lds32(stg + g * 88 + 16 * kt + 8 + 2 * t);
+        ax[kt][3] = lds32(stg + (g + 8) * 88 + 16 * kt + 8 + 2 * t);
+    }
+}
+
+struct Hidden {
+    uint32_t h[4][4][4];  // layer, k-tile, register
+};
+
+// Forward pass of one 16-row tile; returns the output accumulator y.
+__device__ __forceinline__ void forward(const bf16* W, const uint32_t (&ax)[5][4], Hidden& H, float (&y)[1][4])
+{
+    float acc[8][4];
+    dense<5, 8>(ax, W + fwd_off(0), fwd_stride(0), acc);
+    relu_pack<8>(acc, H.h[0]);
+    dense<4, 8>(H.h[0], W + fwd_off(1), fwd_stride(1), acc);
+    relu_pack<8>(acc, H.h[1]);
+    dense<4, 8>(H.h[1], W + fwd_off(2), fwd_stride(2), acc);
+    relu_pack<8>(acc, H.h[2]);
+    dense<4, 8>(H.h[2], W + fwd_off(3), fwd_stride(3), acc);
+    relu_pack<8>(acc, H.h[3]);
+    dense<4, 1>(H.h[3], W + fwd_off(4), fwd_stride(4), y);
+}
+
+__device__ __forceinline__ void copy_blob(bf16* dst, const bf16* __restrict__ src, int elems)
+{
+    const uint4* s = reinterpret_cast<const uint4*>(src);
+    uint4* d = reinterpret_cast<uint4*>(dst);
+    for (int i = threadIdx.x; i < elems / 8; i += blockDim.x) d[i] = s[i];
+}
+
+// ---------------------------------------------------------------------------
+// Inference
+// ---------------------------------------------------------------------------
+constexpr int kInferWarps = 8;
+
+// PATHS: rec are query records of a render batch (count on the device) and the
+// result goes to the owning path's indirect light; otherwise feat -> out.
+template <bool PATHS>
+__global__ void __launch_bounds__(kInferWarps * 32) k_nrc_infer(const bf16* __restrict__ blob,
+                                                                const float4* __restrict__ feat, uint32_t n_host,
+                                                                const uint32_t* __restrict__ count,
+                                                                float* __restrict__ out, PathState P)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    bf16* W = reinterpret_cast<bf16*>(smem);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    bf16* stg = W + kNrcFwdElems + warp * 16 * 88;
+    copy_blob(W, blob, kNrcFwdElems);
+    __syncthreads();
+    const uint32_t n = PATHS ? *count : n_host;
+    const uint32_t tiles = (n + 15) / 16;
+    for (uint32_t tile = blockIdx.x * kInferWarps + warp; tile < tiles; tile += gridDim.x * kInferWarps) {
+        const uint32_t r0 = tile * 16;
+        stage_rows(feat, 5, r0, n, nullptr, stg);
+        __syncwarp();
+        uint32_t ax[5][4];
+        load_x_frags(stg, ax);
+        __syncwarp();
+        Hidden H;
+        float y[1][4];
+        forward(W, ax, H, y);
+        // column 2 lives in the neighbouring lane (t = 1)
+        const float c2a = __shfl_down_sync(0xffffffffu, y[0][0], 1);
+        const float c2b = __shfl_down_sync(0xffffffffu, y[0][2], 1);
+        if (t == 0) {
+#pragma unroll
+            for (int half = 0; half < 2; ++half) {
+                const uint32_t r = r0 + g + 8 * half;
+                if (r >= n) continue;
+                const float v0 = half ? y[0][2] : y[0][0];
+                const float v1 = half ? y[0][3] : y[0][1];
+                const float v2 = half ? c2b : c2a;
+                if (PATHS) {
+                    const float4* q = feat + 5ull * r;
+                    const uint32_t p = __float_as_uint(q[1].w);
+                    const float4 a = P.indirect[p];
+                    P.indirect[p] = make_float4(a.x + q[2].w * fmaxf(v0, 0.0f), a.y + q[3].w * fmaxf(v1, 0.0f),
+                                                a.z + q[4].w * fmaxf(v2, 0.0f), a.w);
+                } else {
+                    out[3ull * r + 0] = v0;
+                    out[3ull * r + 1] = v1;
+                    out[3ull * r + 2] = v2;
+                }
+            }
+        }
+    }
+}
+
+__global__ void k_nrc_encode(const float4* __restrict__ feat, uint32_t n, float* __restrict__ out)
+{
+    for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+        const float4* f = feat + 5ull * r;
+        float* o = out + 80ull * r;
+        auto put = [&](int k, float v) { o[k] = v; };
+        encode_part0(f[0], f[3], f[4], put);
+        encode_part1(f[1], f[2], put);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Training: forward + backward through the activations
+// ---------------------------------------------------------------------------
+constexpr int kTrainWarps = 4;
+
+// 32-bit integer finaliser (MurmurHash3 fmix32): row -> pseudo-random sample.
+__device__ __forceinline__ uint32_t mix32(uint32_t h)
+{
+    h ^= h >> 16;
+    h *= 0x85EBCA6Bu;
+    h ^= h >> 13;
+    h *= 0xC2B2AE35u;
+    h ^= h >> 16;
+    return h;
+}
+
+__device__ __forceinline__ void st32(void* base, uint64_t idx, uint32_t v)
+{
+    reinterpret_cast<uint32_t*>(base)[idx] = v;
+}
+
+__global__ void __launch_bounds__(kTrainWarps * 32) k_nrc_fwdbwd(const bf16* __restrict__ fwd,
+                                                                 const bf16* __restrict__ bwd, NrcTrainArgs a,
+                                                                 uint32_t rows_pad, NrcActs A, float* loss)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    bf16* WF = reinterpret_cast<bf16*>(smem);
+    bf16* WB = WF + kNrcFwdElems;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    bf16* stg = WB + kNrcBwdElems + warp * 16 * 88;
+    uint32_t* map = reinterpret_cast<uint32_t*>(WB + kNrcBwdElems + kTrainWarps * 16 * 88) + warp * 16;
+    copy_blob(WF, fwd, kNrcFwdElems);
+    copy_blob(WB, bwd, kNrcBwdElems);
+    __syncthreads();
+    const uint32_t cnt = a.count ? *a.count : a.rows;
+    const uint32_t n = cnt ? a.rows : 0;  // valid rows
+    const float scale = n ? 1.0f / (3.0f * static_cast<float>(n)) : 0.0f;
+    float lsum = 0.0f;
+    for (uint32_t tile = blockIdx.x * kTrainWarps + warp; tile < rows_pad / 16; tile += gridDim.x * kTrainWarps) {
+        const uint32_t r0 = tile * 16;
+        if (lane < 16) map[lane] = a.count ? (n ? mix32(a.base + r0 + lane) % cnt : 0u) : r0 + lane;
+        __syncwarp();
+        stage_rows(a.feat, a.fstride, r0, n, map, stg);
+        __syncwarp();
+        uint32_t ax[5][4];
+        load_x_frags(stg, ax);
+        // layer input x: 16 rows x 160 B, copied as 16-byte pieces
+        for (int i = lane; i < 160; i += 32) {
+            const int row = i / 10, c = i - row * 10;
+            reinterpret_cast<uint4*>(A.x)[(static_cast<uint64_t>(r0 + row) * 80 + 8 * c) / 8] =
+                *reinterpret_cast<const uint4*>(stg + row * 88 + 8 * c);
+        }
+        __syncwarp();
+        Hidden H;
+        float y[1][4];
+        forward(WF, ax, H, y);
+        // hidden outputs
+#pragma unroll
+        for (int l = 0; l < 4; ++l)
+#pragma unroll
+            for (int kt = 0; kt < 4; ++kt)
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+                    st32(A.h[l], ((static_cast<uint64_t>(r0 + g + 8 * (q & 1)) * 64) + 16 * kt + 8 * (q >> 1) + 2 * t) / 2,
+                         H.h[l][kt][q]);
+        // relative L2 loss and its gradient (columns 2t, 2t+1 of rows g, g+8)
+        float dy[4];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            const uint32_t r = r0 + g + 8 * (c >> 1);
+            const int col = 2 * t + (c & 1);
+            dy[c] = 0.0f;
+            if (r < n && col < 3) {
+                const float target = a.targets[static_cast<uint64_t>(map[g + 8 * (c >> 1)]) * a.tstride + col];
+                const float diff = y[0][c] - target;
+                const float den = y[0][c] * y[0][c] + 0.01f;
+                lsum += diff * diff / den;
+                dy[c] = 2.0f * diff / den * scale;
+            }
+        }
+        st32(A.dy, (static_cast<uint64_t>(r0 + g) * 8 + 2 * t) / 2, pack2(dy[0], dy[1]));
+        st32(A.dy, (static_cast<uint64_t>(r0 + g + 8) * 8 + 2 * t) / 2, pack2(dy[2], dy[3]));
+        uint32_t ady[1][4] = {{pack2(dy[0], dy[1]), pack2(dy[2], dy[3]), 0u, 0u}};
+        float acc[8][4];
+        uint32_t ad[4][4];
+        dense<1, 8>(ady, WB + bwd_off(4), bwd_stride(4), acc);
+#pragma unroll
+        for (int l = 3; l >= 0; --l) {
+            mask_pack<8>(acc, H.h[l], ad);
+#pragma unroll
+            for (int kt = 0; kt < 4; ++kt)
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+                    st32(A.d[l], ((static_cast<uint64_t>(r0 + g + 8 * (q & 1)) * 64) + 16 * kt + 8 * (q >> 1) + 2 * t) / 2,
+                         ad[kt][q]);
+            if (l > 0) dense<4, 8>(ad, WB + bwd_off(l), bwd_stride(l), acc);
+        }
+        __syncwarp();
+    }
+    if (loss) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) lsum += __shfl_down_sync(0xffffffffu, lsum, o);
+        if (lane == 0) atomicAdd(loss, lsum * scale);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Training: weight gradients
+// ---------------------------------------------------------------------------
+constexpr int kWgWarps = 16;
+constexpr int kChunk = 64;
+// Shared tile strides (elements) and offsets: X, H1..H4, D1..D4, DY.
+constexpr int kSX = 88, kSH = 72, kSY = 24;
+__host__ __device__ constexpr int wg_off_h(int l) { return kChunk * kSX + l * kChunk * kSH; }
+__host__ __device__ constexpr int wg_off_d(int l) { return kChunk * kSX + (4 + l) * kChunk * kSH; }
+constexpr int kWgOffY = kChunk * kSX + 8 * kChunk * kSH;
+constexpr int kWgElems = kWgOffY + kChunk * kSY;
+constexpr int kWgTasks = 34;
+
+struct WgTask {
+    int l, m0, n0, nt;
+};
+__device__ __forceinline__ WgTask wg_task(int id)
+{
+    if (id < 8) return {0, (id >> 1) * 16, (id & 1) * 40, 5};
+    if (id < 32) {
+        const int r = (id - 8) & 7;
+        return {1 + (id - 8) / 8, (r >> 1) * 16, (r & 1) * 32, 4};
+    }
+    return {4, 0, (id - 32) * 32, 4};
+}
+
+__global__ void __launch_bounds__(kWgWarps * 32) k_nrc_wgrad(NrcActs A, uint32_t rows_per_split,
+                                                             float* __restrict__ partial)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    bf16* T = reinterpret_cast<bf16*>(smem);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    // DY columns 8..23 stay zero (the output layer's padded rows)
+    for (int i = threadIdx.x; i < kChunk * kSY; i += blockDim.x) T[kWgOffY + i] = __float2bfloat16_rn(0.0f);
+    const int ntask = warp + 32 < kWgTasks ? 3 : 2;
+    float acc[3][5][4];
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int j = 0; j < 5; ++j) acc[a][j][0] = acc[a][j][1] = acc[a][j][2] = acc[a][j][3] = 0.0f;
+    const uint64_t row_begin = static_cast<uint64_t>(blockIdx.x) * rows_per_split;
+    for (uint32_t c0 = 0; c0 < rows_per_split; c0 += kChunk) {
+        __syncthreads();
+        const uint64_t rb = row_begin + c0;
+        // stage the chunk: X (10 x 16 B per row), 8 x (8 x 16 B), DY (1 x 16 B)
+        for (int i = threadIdx.x; i < kChunk * 10; i += blockDim.x) {
+            const int row = i / 10, c = i - row * 10;
+            *reinterpret_cast<uint4*>(T + row * kSX + 8 * c) =
+                reinterpret_cast<const uint4*>(A.x)[((rb + row) * 80 + 8 * c) / 8];
+        }
+        for (int i = threadIdx.x; i < 8 * kChunk * 8; i += blockDim.x) {
+            const int m = i / (kChunk * 8), rem = i - m * kChunk * 8, row = rem >> 3, c = rem & 7;
+            const void* src = m < 4 ? A.h[m] : A.d[m - 4];
+            *reinterpret_cast<uint4*>(T + kChunk * kSX + m * kChunk * kSH + row * kSH + 8 * c) =
+                reinterpret_cast<const uint4*>(src)[((rb + row) * 64 + 8 * c) / 8];
+        }
+        for (int i = threadIdx.x; i < kChunk; i += blockDim.x)
+            *reinterpret_cast<uint4*>(T + kWgOffY + i * kSY) = reinterpret_cast<const uint4*>(A.dy)[rb + i];
+        __syncthreads();
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            if (a >= ntask) break;
+            const WgTask k = wg_task(warp + 16 * a);
+            // A = delta^T (rows: outputs of layer l), B = the layer input
+            const bf16* Dt = k.l == 4 ? T + kWgOffY : T + wg_off_d(k.l);
+            const int ds = k.l == 4 ? kSY : kSH;
+            const bf16* Bt = k.l == 0 ? T : T + wg_off_h(k.l - 1);
+            const int bs = k.l == 0 ? kSX : kSH;
+#pragma unroll
+            for (int ks = 0; ks < kChunk / 16; ++ks) {
+                uint32_t af[4];
+                ldsm_x4_trans(af, Dt + (ks * 16 + (lane & 7) + ((lane >> 4) << 3)) * ds + k.m0 + (((lane >> 3) & 1) << 3));
+                const int brow = ks * 16 + (lane & 7) + (((lane >> 3) & 1) << 3);
+#pragma unroll
+                for (int p = 0; p < 2; ++p) {
+                    uint32_t bf[4];
+                    ldsm_x4_trans(bf, Bt + brow * bs + k.n0 + 16 * p + ((lane >> 4) << 3));
+                    mma16816(acc[a][2 * p], af, bf[0], bf[1]);
+                    mma16816(acc[a][2 * p + 1], af, bf[2], bf[3]);
+                }
+                if (k.nt == 5) {
+                    uint32_t bf[2];
+                    ldsm_x2_trans(bf, Bt + brow * bs + k.n0 + 32);
+                    mma16816(acc[a][4], af, bf[0], bf[1]);
+                }
+            }
+        }
+    }
+    float* out = partial + static_cast<uint64_t>(blockIdx.x) * kNrcParams;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        if (a >= ntask) break;
+        const WgTask k = wg_task(warp + 16 * a);
+        const int in = layer_in(k.l), outs = layer_out(k.l);
+#pragma unroll
+        for (int j = 0; j < 5; ++j) {
+            if (j >= k.nt) break;
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                const int m = k.m0 + g + 8 * (c >> 1);
+                const int nn = k.n0 + 8 * j + 2 * t + (c & 1);
+                if (m < outs) out[master_off(k.l) + m * in + nn] = acc[a][j][c];
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Adam and weight publication
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void publish_param(bf16* fwd, bf16* bwd, int q, float w)
+{
+    int l, o, i;
+    param_coords(q, l, o, i);
+    const bf16 b = __float2bfloat16_rn(w);
+    fwd[fwd_off(l) + o * fwd_stride(l) + i] = b;
+    if (l >= 1) bwd[bwd_off(l) + i * bwd_stride(l) + o] = b;
+}
+
+__global__ void k_nrc_adam(float* __restrict__ master, float* __restrict__ m, float* __restrict__ v,
+                           const float* __restrict__ partial, uint32_t splits, float lr, float b1, float b2,
+                           float eps, float bc1, float bc2, bf16* fwd, bf16* bwd, float* grad_out)
+{
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= kNrcParams) return;
+    float gsum = 0.0f;
+    for (uint32_t s = 0; s < splits; ++s) gsum += partial[static_cast<uint64_t>(s) * kNrcParams + q];
+    if (grad_out) grad_out[q] = gsum;
+    const float mm = b1 * m[q] + (1.0f - b1) * gsum;
+    const float vv = b2 * v[q] + (1.0f - b2) * gsum * gsum;
+    m[q] = mm;
+    v[q] = vv;
+    const float w = master[q] - lr * (mm / bc1) / (sqrtf(vv / bc2) + eps);
+    master[q] = w;
+    publish_param(fwd, bwd, q, w);
+}
+
+__global__ void k_nrc_publish(const float* __restrict__ master, bf16* fwd, bf16* bwd)
+{
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q < kNrcParams) publish_param(fwd, bwd, q, master[q]);
+}
+
+__global__ void k_nrc_blend(float* __restrict__ accum, const float* __restrict__ frame, uint64_t n, float w)
+{
+    for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<uint64_t>(gridDim.x) * blockDim.x)
+        accum[i] += (frame[i] - accum[i]) * w;
+}
+
+// ---------------------------------------------------------------------------
+// Training targets from recorded training paths
+// ---------------------------------------------------------------------------
+__global__ void k_nrc_targets(PathState P, NrcShade N, uint32_t n, uint32_t bounces)
+{
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+        const float4 e = P.emit[p], d = P.direct[p], ind = P.indirect[p], s = P.sky[p];
+        const float tot[3] = {((e.x + d.x) + ind.x) + s.x, ((e.y + d.y) + ind.y) + s.y, ((e.z + d.z) + ind.z) + s.z};
+        for (uint32_t k = 0; k < bounces; ++k) {
+            float4* r = N.rec + (static_cast<uint64_t>(p) * bounces + k) * 6;
+            const float4 pre = r[5];
+            if (pre.w != 1.0f) break;  // vertices are recorded in bounce order
+            r[5].w = 0.0f;
+            const float cur[3] = {r[2].w, r[3].w, r[4].w};
+            const float prv[3] = {pre.x, pre.y, pre.z};
+            float tg[3];
+            bool ok = true;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                ok = ok && cur[c] > 1e-6f;
+                tg[c] = fmaxf(tot[c] - prv[c], 0.0f) / cur[c];
+                ok = ok && isfinite(tg[c]);
+            }
+            if (!ok) continue;
+            const uint32_t slot = atomicAdd(N.sample_count, 1u);
+            if (slot >= N.sample_cap) continue;
+            float4* o = N.samples + static_cast<uint64_t>(slot) * 6;
+#pragma unroll
+            for (int i = 0; i < 5; ++i) o[i] = r[i];
+            o[5] = make_float4(tg[0], tg[1], tg[2], 0.0f);
+        }
+    }
+}
+
+int g_sms_nrc = 0;
+int sms()
+{
+    if (!g_sms_nrc) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&g_sms_nrc, cudaDevAttrMultiProcessorCount, dev);
+        if (g_sms_nrc <= 0) g_sms_nrc = 1;
+    }
+    return g_sms_nrc;
+}
+
+constexpr size_t kInferSmem = (kNrcFwdElems + kInferWarps * 16 * 88) * sizeof(bf16);
+constexpr size_t kTrainSmem =
+    (kNrcFwdElems + kNrcBwdElems + kTrainWarps * 16 * 88) * sizeof(bf16) + kTrainWarps * 16 * sizeof(uint32_t);
+constexpr size_t kWgSmem = kWgElems * sizeof(bf16);
+
+template <class K>
+cudaError_t allow_smem(K kernel, size_t bytes, bool& done)
+{
+    if (done) return cudaSuccess;
+    const cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               static_cast<int>(bytes));
+    if (e == cudaSuccess) done = true;
+    return e;
+}
+
+template <bool PATHS>
+cudaError_t infer(const void* net, const float4* feat, uint32_t n_host, const uint32_t* count, uint32_t capacity,
+                  float* out, const PathState& P, cudaStream_t st)
+{
+    static bool ok = false;
+    cudaError_t e = allow_smem(k_nrc_infer<PATHS>, kInferSmem, ok);
+    if (e != cudaSuccess) return e;
+    const uint64_t tiles = (static_cast<uint64_t>(capacity) + 15) / 16;
+    uint64_t blocks = (tiles + kInferWarps - 1) / kInferWarps;
+    const uint64_t cap = static_cast<uint64_t>(sms()) * 3;
+    if (blocks > cap) blocks = cap;
+    if (blocks == 0) blocks = 1;
+    k_nrc_infer<PATHS><<<static_cast<unsigned>(blocks), kInferWarps * 32, kInferSmem, st>>>(
+        static_cast<const bf16*>(net), feat, n_host, count, out, P);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_nrc_query(const void* net, const PathState& P, const float4* rec, const uint32_t* count,
+                             uint32_t capacity, cudaStream_t st)
+{
+    return infer<true>(net, rec, 0, count, capacity, nullptr, P, st);
+}
+
+cudaError_t launch_nrc_infer(const void* net, const float* features, uint32_t n, float* out, cudaStream_t st)
+{
+    if (n == 0) return cudaSuccess;
+    return infer<false>(net, reinterpret_cast<const float4*>(features), n, nullptr, n, out, PathState{}, st);
+}
+
+cudaError_t launch_nrc_encode(const float* features, uint32_t n, float* out, cudaStream_t st)
+{
+    if (n == 0) return cudaSuccess;
+    const unsigned blocks = static_cast<unsigned>(std::min<uint64_t>((n + 127) / 128, 1024));
+    k_nrc_encode<<<blocks, 128, 0, st>>>(reinterpret_cast<const float4*>(features), n, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_nrc_targets(const PathState& P, const NrcShade& N, uint32_t n, uint32_t bounces,
+                               cudaStream_t st)
+{
+    const unsigned blocks = static_cast<unsigned>(std::min<uint64_t>((n + 255) / 256, 4096));
+    k_nrc_targets<<<blocks ? blocks : 1, 256, 0, st>>>(P, N, n, bounces);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_nrc_train_step(NrcOptimizer& O, const NrcTrainArgs& a, float* loss, float* grad_out,
+                                  cudaStream_t st)
+{
+    if (a.rows == 0 || a.rows > O.max_rows) return cudaErrorInvalidValue;
+    static bool ok_t = false, ok_w = false;
+    cudaError_t e = allow_smem(k_nrc_fwdbwd, kTrainSmem, ok_t);
+    if (e != cudaSuccess) return e;
+    e = allow_smem(k_nrc_wgrad, kWgSmem, ok_w);
+    if (e != cudaSuccess) return e;
+    // rows padded to whole chunks; split so that every block has whole chunks
+    const uint32_t chunks = (a.rows + kChunk - 1) / kChunk;
+    const uint32_t per = (chunks + O.max_splits - 1) / O.max_splits;
+    const uint32_t splits = (chunks + per - 1) / per;
+    const uint32_t rows_pad = splits * per * kChunk;
+    if (rows_pad > O.max_rows) return cudaErrorInvalidValue;
+    const uint64_t tiles = rows_pad / 16;
+    uint64_t blocks = (tiles + kTrainWarps - 1) / kTrainWarps;
+    const uint64_t cap = static_cast<uint64_t>(sms()) * 2;
+    if (blocks > cap) blocks = cap;
+    k_nrc_fwdbwd<<<static_cast<unsigned>(blocks), kTrainWarps * 32, kTrainSmem, st>>>(
+        static_cast<const bf16*>(O.fwd), static_cast<const bf16*>(O.bwd), a, rows_pad, O.acts, loss);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    k_nrc_wgrad<<<splits, kWgWarps * 32, kWgSmem, st>>>(O.acts, per * kChunk, O.partial);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    O.step += 1;
+    const double bc1 = 1.0 - std::pow(static_cast<double>(O.beta1), static_cast<double>(O.step));
+    const double bc2 = 1.0 - std::pow(static_cast<double>(O.beta2), static_cast<double>(O.step));
+    k_nrc_adam<<<(kNrcParams + 255) / 256, 256, 0, st>>>(O.master, O.m, O.v, O.partial, splits, O.lr, O.beta1,
+                                                        O.beta2, O.eps, static_cast<float>(bc1),
+                                                        static_cast<float>(bc2), static_cast<bf16*>(O.fwd),
+                                                        static_cast<bf16*>(O.bwd), grad_out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_nrc_publish(const NrcOptimizer& O, cudaStream_t st)
+{
+    k_nrc_publish<<<(kNrcParams + 255) / 256, 256, 0, st>>>(O.master, static_cast<bf16*>(O.fwd),
+                                                           static_cast<bf16*>(O.bwd));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_nrc_blend(float* accum, const float* frame, uint64_t n, uint32_t index, cudaStream_t st)
+{
+    const unsigned blocks = static_cast<unsigned>(std::min<uint64_t>((n + 255) / 256, 8192));
+    k_nrc_blend<<<blocks ? blocks : 1, 256, 0, st>>>(accum, frame, n, 1.0f / static_cast<float>(index + 1));
+    return cudaGetLastError();
+}
+
+}  // namespace mt

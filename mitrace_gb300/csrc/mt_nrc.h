@@ -1,0 +1,100 @@
+// mt_nrc.h - neural radiance cache: network buffers, the render-stage hooks and
+// the launchers of its BF16 tensor-core kernels (mt_nrc.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "mt_kernels.h"
+
+namespace mt {
+
+// Network dimensions.  The output layer is padded to 8 rows for the m16n8k16
+// tensor-core tiles; rows 3..7 of its weights stay zero.
+constexpr int kNrcIn = 80;
+constexpr int kNrcW = 64;
+constexpr int kNrcOutPad = 8;
+constexpr int kNrcParams = 80 * 64 + 3 * 64 * 64 + 64 * 3;
+// BF16 weight blobs in the padded layouts the kernels copy into shared memory:
+// forward: W_l as [out][in + 8]; backward: W_l^T as [in][out + 8] (l >= 1, the
+// output layer's transpose padded to 16 + 8 columns).
+constexpr int kNrcFwdElems = 64 * 88 + 3 * 64 * 72 + 8 * 72;  // 20,032
+constexpr int kNrcBwdElems = 3 * 64 * 72 + 64 * 24;           // 15,360
+
+// Render-stage hooks of one wavefront batch.
+#define MT_NRC_OFF 0
+#define MT_NRC_QUERY 1  // end paths at the first vertex after a diffuse-ish one, queue a cache query
+#define MT_NRC_TRAIN 2  // record every vertex of full-length training paths
+struct NrcShade {
+    int mode = MT_NRC_OFF;
+    float rough_min = 0.3f;
+    float lo[3] = {0, 0, 0};       // world box lower corner
+    float inv_ext[3] = {1, 1, 1};  // 1 / world box extent
+    // QUERY: query records, 5 float4 each (the feature record of the header,
+    //        with f1.w = path index bits and f2.w, f3.w, f4.w = throughput rgb).
+    // TRAIN: vertex records of path p, bounce k at rec[(p * bounces + k) * 6]:
+    //        the 5 feature float4 (f2.w, f3.w, f4.w = throughput) and
+    //        (radiance collected before the vertex's NEE, 1 = recorded).
+    float4* rec = nullptr;
+    uint32_t* count = nullptr;  // QUERY: queries appended
+    // QUERY: bf16 forward weight blob.
+    const void* net = nullptr;
+    // TRAIN: training samples (5 feature float4 + target float4 each).
+    float4* samples = nullptr;
+    uint32_t* sample_count = nullptr;
+    uint32_t sample_cap = 0;
+};
+
+// Transposable activations of one training batch, row-major BF16 per row.
+struct NrcActs {
+    void* x;      // [rows][80]
+    void* h[4];   // [rows][64] hidden outputs after ReLU
+    void* d[4];   // [rows][64] loss gradient w.r.t. the hidden pre-activations
+    void* dy;     // [rows][8]  loss gradient w.r.t. the outputs (cols 3..7 zero)
+};
+
+// Cache queries of a batch: adds throughput * max(cache, 0) to P.indirect.
+cudaError_t launch_nrc_query(const void* net, const PathState& P, const float4* rec, const uint32_t* count,
+                             uint32_t capacity, cudaStream_t st);
+// Training targets of a batch of training paths -> samples.
+cudaError_t launch_nrc_targets(const PathState& P, const NrcShade& N, uint32_t n, uint32_t bounces,
+                               cudaStream_t st);
+// Plain inference into out (n x 3).
+cudaError_t launch_nrc_infer(const void* net, const float* features, uint32_t n, float* out, cudaStream_t st);
+cudaError_t launch_nrc_encode(const float* features, uint32_t n, float* out, cudaStream_t st);
+
+// One training step.  Rows r < rows read sample fmix32(base + r) mod *count of
+// the (features, targets) arrays when count is not null (random draws with
+// replacement; an empty set trains on nothing), else sample r.  feat: the 5 feature float4 of sample
+// i start at feat[i * fstride]; targets: tstride floats per sample (rgb first).
+struct NrcTrainArgs {
+    const float4* feat;
+    uint32_t fstride;  // float4 per sample in feat
+    const float* targets;
+    uint32_t tstride;
+    const uint32_t* count;
+    uint32_t base;
+    uint32_t rows;
+};
+struct NrcOptimizer {
+    float* master;      // kNrcParams fp32 weights
+    float* m;           // Adam first moments
+    float* v;           // Adam second moments
+    float* partial;     // splits x kNrcParams weight-gradient partial sums
+    void* fwd;          // bf16 forward blob
+    void* bwd;          // bf16 backward blob
+    NrcActs acts;       // sized for max_rows
+    uint32_t max_rows;  // multiple of 64
+    uint32_t max_splits;
+    float lr, beta1, beta2, eps;
+    uint64_t step;      // Adam steps taken
+};
+cudaError_t launch_nrc_train_step(NrcOptimizer& O, const NrcTrainArgs& a, float* loss, float* grad_out,
+                                  cudaStream_t st);
+// Writes the bf16 blobs from the fp32 master weights.
+cudaError_t launch_nrc_publish(const NrcOptimizer& O, cudaStream_t st);
+// running mean: accum += (frame - accum) / (index + 1)
+cudaError_t launch_nrc_blend(float* accum, const float* frame, uint64_t n, uint32_t index, cudaStream_t st);
+
+}  // namespace mt

@@ -83,6 +83,43 @@ class Tracer:
                               d_light_ptr or None, d_texels_ptr or None)
         A.check(A.lib.mt_render_grad(self.handle, C.byref(g), C.c_void_p(stream_ptr)), "mt_render_grad")
 
+    # --- neural radiance cache ---------------------------------------------------
+    def nrc_enable(self, **overrides) -> A.mt_nrc_config:
+        """mt_nrc_enable with mt_nrc_config_defaults plus the given fields."""
+        c = A.mt_nrc_config()
+        A.lib.mt_nrc_config_defaults(C.byref(c))
+        for k, v in overrides.items():
+            setattr(c, k, v)
+        A.check(A.lib.mt_nrc_enable(self.handle, C.byref(c)), "mt_nrc_enable")
+        self.nrc_config = c
+        return c
+
+    def nrc_frame(self, accum_ptr: int = 0, accum_index: int = 0, stream_ptr: int = 0):
+        """One training iteration plus (accum_ptr != 0) one cached frame folded
+        into the running mean at accum_ptr (W*H*3 float32 on the device)."""
+        A.check(A.lib.mt_nrc_frame(self.handle, C.c_void_p(accum_ptr or None), accum_index,
+                                   C.c_void_p(stream_ptr)), "mt_nrc_frame")
+
+    def nrc_get_params(self) -> np.ndarray:
+        p = np.zeros(A.MT_NRC_PARAMS, dtype=np.float32)
+        A.check(A.lib.mt_nrc_get_params(self.handle, p.ctypes.data_as(C.c_void_p)), "mt_nrc_get_params")
+        return p
+
+    def nrc_set_params(self, params: np.ndarray):
+        p = np.ascontiguousarray(params, dtype=np.float32)
+        assert p.size == A.MT_NRC_PARAMS
+        A.check(A.lib.mt_nrc_set_params(self.handle, p.ctypes.data_as(C.c_void_p)), "mt_nrc_set_params")
+
+    def nrc_infer_device(self, feat_ptr: int, n: int, out_ptr: int, stream_ptr: int = 0):
+        A.check(A.lib.mt_nrc_infer(self.handle, C.c_void_p(feat_ptr), n, C.c_void_p(out_ptr),
+                                   C.c_void_p(stream_ptr)), "mt_nrc_infer")
+
+    def nrc_train_step_device(self, feat_ptr: int, target_ptr: int, n: int, loss_ptr: int = 0, grad_ptr: int = 0,
+                              stream_ptr: int = 0):
+        A.check(A.lib.mt_nrc_train_step(self.handle, C.c_void_p(feat_ptr), C.c_void_p(target_ptr), n,
+                                        C.c_void_p(loss_ptr or None), C.c_void_p(grad_ptr or None),
+                                        C.c_void_p(stream_ptr)), "mt_nrc_train_step")
+
     def kernel_launches(self) -> int:
         return int(A.lib.mt_kernel_launches(self.handle))
 
@@ -112,6 +149,12 @@ def brdf_batch(q: np.ndarray) -> np.ndarray:
     A.check(A.lib.mt_brdf_batch(q.ctypes.data_as(C.c_void_p), q.shape[0], out.ctypes.data_as(C.c_void_p)),
             "mt_brdf_batch")
     return out
+
+
+def nrc_encode_device(feat_ptr: int, n: int, out_ptr: int, stream_ptr: int = 0):
+    """The radiance cache's FP32 input encoding: n x 20 features -> n x 80 (device buffers)."""
+    A.check(A.lib.mt_nrc_encode(C.c_void_p(feat_ptr), n, C.c_void_p(out_ptr), C.c_void_p(stream_ptr)),
+            "mt_nrc_encode")
 
 
 def bvh_build(positions: np.ndarray, max_triangles=32, max_depth=32):

@@ -1,0 +1,157 @@
+"""The neural radiance cache on the GPU, through the C ABI.
+
+1. mt_nrc_encode equals the float32 reference encoding.
+2. mt_nrc_infer (fused BF16 tensor-core MLP) equals a plain PyTorch FP32
+   forward of the same weights with BF16 rounding of weights and activations,
+   to 1e-2 relative in norm; full and ragged row counts.
+3. mt_nrc_train_step's gradient equals PyTorch autograd of the relative L2
+   loss through that forward to 3e-2 relative per layer, its loss to 1e-3, and
+   its Adam update equals the float32 Adam formula applied to that gradient.
+4. Training on a smooth target lowers the loss tenfold.
+5. With no diffuse-ish vertex (rough_min > 1) a cached frame is bit-identical
+   to mt_render_device at the same samples: the cache hooks leave the plain
+   estimator untouched.
+6. Cached frames on the box room converge near the plain render.
+"""
+import numpy as np
+import pytest
+
+import mitrace_gb300 as mt
+from mitrace_gb300 import _abi as A
+from tests import nrc_reference as ref
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+def dev(a):
+    return torch.from_numpy(np.ascontiguousarray(a, np.float32)).cuda()
+
+
+def small_room(**kw):
+    return mt.box_room(width=48, height=48, samples=4, seed=2, **kw)
+
+
+@pytest.fixture(scope="module")
+def tracer():
+    scene, cfg = small_room()
+    tr = mt.Tracer(scene, cfg)
+    tr.nrc_enable(train_paths=4096, train_batch=4096, spp=4)
+    yield tr
+    tr.close()
+
+
+def test_encoding_matches_reference():
+    f = ref.random_features(3001, seed=4)
+    out = torch.zeros((3001, 80), device="cuda")
+    fd = dev(f)
+    mt.nrc_encode_device(fd.data_ptr(), 3001, out.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    np.testing.assert_allclose(out.cpu().numpy(), ref.encode(f), atol=2e-6, rtol=1e-6)
+
+
+@pytest.mark.parametrize("n", [4096, 1000, 17])
+def test_inference_matches_torch_fp32(tracer, n):
+    p = tracer.nrc_get_params()
+    f = ref.random_features(n, seed=n)
+    out = torch.zeros((n, 3), device="cuda")
+    fd = dev(f)
+    tracer.nrc_infer_device(fd.data_ptr(), n, out.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    y = out.cpu().numpy().astype(np.float64)
+    x = torch.tensor(ref.encode(f))
+    r = ref.torch_forward(x, torch.tensor(p)).numpy().astype(np.float64)
+    assert np.all(np.isfinite(y))
+    assert np.linalg.norm(y - r) <= 1e-2 * np.linalg.norm(r)
+    # and it is not the unrounded network either by accident: both close
+    r32 = ref.torch_forward(x, torch.tensor(p), bf16=False).numpy()
+    assert np.linalg.norm(y - r32) <= 5e-2 * np.linalg.norm(r32)
+
+
+def test_train_step_gradient_loss_and_adam(tracer):
+    n = 3000
+    rng = np.random.default_rng(5)
+    p0 = (rng.normal(size=A.MT_NRC_PARAMS) * 0.15).astype(np.float32)
+    tracer.nrc_set_params(p0)
+    f = ref.random_features(n, seed=6)
+    t = rng.uniform(0.0, 2.0, (n, 3)).astype(np.float32)
+    loss = torch.zeros(1, device="cuda")
+    grad = torch.zeros(A.MT_NRC_PARAMS, device="cuda")
+    fd, td = dev(f), dev(t)
+    tracer.nrc_train_step_device(fd.data_ptr(), td.data_ptr(), n, loss.data_ptr(), grad.data_ptr(),
+                                 torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    g = grad.cpu().numpy()
+    p1 = tracer.nrc_get_params()
+    # torch autograd through the BF16-rounded forward
+    pt = torch.tensor(p0, requires_grad=True)
+    y = ref.torch_forward(torch.tensor(ref.encode(f)), pt)
+    lt = ref.relative_l2(y, torch.tensor(t))
+    lt.backward()
+    gr = pt.grad.numpy()
+    assert abs(float(loss.item()) - float(lt.item())) <= 1e-3 * float(lt.item())
+    off = 0
+    for l, (o, i) in enumerate(ref.SHAPES):
+        a, b = g[off:off + o * i], gr[off:off + o * i]
+        assert np.linalg.norm(a - b) <= 3e-2 * np.linalg.norm(b), f"layer {l}"
+        off += o * i
+    w, _, _ = ref.adam_step(p0, g, np.zeros_like(g), np.zeros_like(g), 1)
+    np.testing.assert_allclose(p1, w, atol=1e-6, rtol=1e-6)
+
+
+def test_training_fits_a_smooth_target():
+    scene, cfg = small_room()
+    with mt.Tracer(scene, cfg) as tr:
+        tr.nrc_enable(train_batch=4096)
+        n = 8192
+        f = ref.random_features(n, seed=9)
+        ff = f.reshape(n, 5, 4)
+        t = np.stack([0.5 + 0.4 * np.sin(4 * ff[:, 0, 0]), 0.3 + 0.2 * ff[:, 2, 1], ff[:, 3, 0] + 0.1], 1)
+        fd, td = dev(f), dev(t.astype(np.float32))
+        loss = torch.zeros(1, device="cuda")
+        first = None
+        for k in range(300):
+            tr.nrc_train_step_device(fd.data_ptr(), td.data_ptr(), n, loss.data_ptr(), 0,
+                                     torch.cuda.current_stream().cuda_stream)
+            if k == 0:
+                torch.cuda.synchronize()
+                first = float(loss.item())
+        torch.cuda.synchronize()
+        last = float(loss.item())
+    assert np.isfinite(last) and last < first / 10, (first, last)
+
+
+def test_cache_hooks_leave_plain_paths_unchanged():
+    scene, cfg = small_room()
+    img = torch.zeros((cfg.height, cfg.width, 3), device="cuda")
+    acc = torch.zeros_like(img)
+    st = torch.cuda.current_stream().cuda_stream
+    with mt.Tracer(scene, cfg) as tr:
+        tr.render_device(img.data_ptr(), st)
+        tr.nrc_enable(train_paths=2048, train_batch=1024, spp=cfg.samples, rough_min=2.0)
+        tr.nrc_frame(acc.data_ptr(), 0, st)
+        torch.cuda.synchronize()
+    np.testing.assert_array_equal(acc.cpu().numpy(), img.cpu().numpy())
+
+
+def test_cached_frames_converge_near_plain_render():
+    scene, cfg = mt.box_room(width=64, height=64, samples=256, seed=2)
+    st = torch.cuda.current_stream().cuda_stream
+    plain = torch.zeros((cfg.height, cfg.width, 3), device="cuda")
+    with mt.Tracer(scene, cfg) as tr:
+        tr.render_device(plain.data_ptr(), st)
+        torch.cuda.synchronize()
+    scene, cfg = mt.box_room(width=64, height=64, samples=4, seed=2)
+    acc = torch.zeros_like(plain)
+    with mt.Tracer(scene, cfg) as tr:
+        tr.nrc_enable(train_paths=16384, train_batch=4096, spp=4)
+        for _ in range(30):  # training only
+            tr.nrc_frame(0, 0, st)
+        for k in range(64):
+            tr.nrc_frame(acc.data_ptr(), k, st)
+        torch.cuda.synchronize()
+    a, p = acc.cpu().numpy().astype(np.float64), plain.cpu().numpy().astype(np.float64)
+    assert np.all(np.isfinite(a))
+    rel = float(((a - p) ** 2 / (p * p + 1e-2)).mean())
+    assert rel < 0.02, rel
+    assert abs(a.mean() - p.mean()) <= 0.05 * p.mean(), (a.mean(), p.mean())
