@@ -28,6 +28,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import re
 import os
 import statistics
 import subprocess
@@ -40,7 +41,7 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 PEAKS_FILE = ROOT / "MEASURED_PEAKS.json"
-TRAFFIC_FILE = ROOT / "profiles" / "extend_traffic.json"
+TRAFFIC_FILE = ROOT / "profiles" / "k_extend_material_grid.md"
 FALLBACK_HBM_GBS = 6800.0
 
 
@@ -365,12 +366,13 @@ def run_ours(a):
             pass
     traffic = None
     if TRAFFIC_FILE.exists():
-        try:
-            t = json.loads(TRAFFIC_FILE.read_text())
-            if t.get("workload") == workload_name(a):
-                traffic = t.get("dram_bytes_per_launch")
-        except Exception:
-            pass
+        # DRAM bytes per extend launch from the ncu summary (a capture of a
+        # smaller render of the same scene, scaled by rays per launch)
+        text = TRAFFIC_FILE.read_text()
+        w = re.search(r"^traffic_workload: (\S+)$", text, re.M)
+        b = re.search(r"^traffic_per_launch_bytes: (\d+)$", text, re.M)
+        if w and b and w.group(1) == workload_name(a):
+            traffic = int(b.group(1))
     stage_ms = {n: round(prof.stage[i].milliseconds / a.steps, 3) for i, n in
                 enumerate(["raygen", "extend", "shade", "shadow", "finalize", "resolve"])}
 

@@ -1240,6 +1240,7 @@ mt_status mt_nrc_frame(mt_handle* h, float* d_accum, uint32_t accum_index, void*
         a.targets = reinterpret_cast<const float*>(N.samples.p + 5);
         a.tstride = 24;
         a.count = N.counters.p + 1;
+        a.count_cap = N.sample_cap;
         a.base = static_cast<uint32_t>((N.frames * nc.train_steps + s) * nc.train_batch);
         a.rows = nc.train_batch;
         MT_CUDA(launch_nrc_train_step(N.opt, a, nullptr, nullptr, st));

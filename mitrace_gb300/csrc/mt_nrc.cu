@@ -390,7 +390,7 @@ __global__ void __launch_bounds__(kTrainWarps * 32) k_nrc_fwdbwd(const bf16* __r
     copy_blob(WF, fwd, kNrcFwdElems);
     copy_blob(WB, bwd, kNrcBwdElems);
     __syncthreads();
-    const uint32_t cnt = a.count ? *a.count : a.rows;
+    const uint32_t cnt = a.count ? min(*a.count, a.count_cap) : a.rows;
     const uint32_t n = cnt ? a.rows : 0;  // valid rows
     const float scale = n ? 1.0f / (3.0f * static_cast<float>(n)) : 0.0f;
     float lsum = 0.0f;

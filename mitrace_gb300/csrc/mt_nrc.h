@@ -74,6 +74,7 @@ struct NrcTrainArgs {
     const float* targets;
     uint32_t tstride;
     const uint32_t* count;
+    uint32_t count_cap;  // samples the arrays hold (*count may run past it)
     uint32_t base;
     uint32_t rows;
 };
