@@ -306,8 +306,21 @@ typedef struct mt_nrc_config {
     float epsilon;         /* Adam denominator guard (1e-15) */
     float rough_min;       /* a vertex with roughness >= this is diffuse-ish (0.3) */
     uint32_t seed;         /* weight initialisation and training-path seed */
-    uint32_t reserved[6];
+    float ema_decay;       /* the renderer queries an exponential moving average
+                              of the trained weights (bias-corrected) with this
+                              decay; 0 queries the trained weights themselves (0.9) */
+    uint32_t reserved[5];
 } mt_nrc_config;
+
+/* Counters of the cache (mt_nrc_get_stats synchronizes the device). */
+typedef struct mt_nrc_stats {
+    uint64_t frames;        /* mt_nrc_frame calls since mt_nrc_enable */
+    uint64_t adam_steps;    /* optimizer steps since enable / set_params */
+    uint32_t train_samples; /* vertices recorded by the last frame's training paths */
+    uint32_t queries;       /* cache queries of the last frame's render */
+    float train_loss;       /* mean relative L2 loss of the last frame's steps */
+    float reserved[3];
+} mt_nrc_stats;
 
 void mt_nrc_config_defaults(mt_nrc_config* c);
 /* Allocates the cache on the handle and initialises its weights (Xavier
@@ -327,11 +340,13 @@ mt_status mt_nrc_enable(mt_handle* h, const mt_nrc_config* c);
  *     accum += (frame - accum) / (accum_index + 1).
  * Frames draw distinct random numbers (sample indices continue across frames). */
 mt_status mt_nrc_frame(mt_handle* h, float* d_accum, uint32_t accum_index, void* cuda_stream);
+mt_status mt_nrc_get_stats(mt_handle* h, mt_nrc_stats* out);
 /* Copies the FP32 master parameters out / in (MT_NRC_PARAMS floats, host).
- * Setting them resets the Adam moments and step count. */
+ * Setting them resets the Adam moments, the step count and the moving average. */
 mt_status mt_nrc_get_params(mt_handle* h, float* params);
 mt_status mt_nrc_set_params(mt_handle* h, const float* params);
-/* Cache outputs for n feature records (device buffers: n*20 floats in, n*3 out). */
+/* Cache outputs for n feature records (device buffers: n*20 floats in, n*3
+ * out), from the weights the renderer queries (see ema_decay). */
 mt_status mt_nrc_infer(mt_handle* h, const float* d_features, uint32_t n, float* d_rgb, void* cuda_stream);
 /* One Adam step on n samples (device buffers: n*20 feature floats, n*3 target
  * floats).  d_loss (1 float, may be NULL) receives the batch's mean relative

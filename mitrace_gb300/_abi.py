@@ -223,7 +223,19 @@ class mt_nrc_config(C.Structure):
         ("epsilon", C.c_float),
         ("rough_min", C.c_float),
         ("seed", C.c_uint32),
-        ("reserved", C.c_uint32 * 6),
+        ("ema_decay", C.c_float),
+        ("reserved", C.c_uint32 * 5),
+    ]
+
+
+class mt_nrc_stats(C.Structure):
+    _fields_ = [
+        ("frames", C.c_uint64),
+        ("adam_steps", C.c_uint64),
+        ("train_samples", C.c_uint32),
+        ("queries", C.c_uint32),
+        ("train_loss", C.c_float),
+        ("reserved", C.c_float * 3),
     ]
 
 
@@ -259,6 +271,7 @@ PROTOTYPES = [
     ("mt_nrc_config_defaults", None, [C.POINTER(mt_nrc_config)]),
     ("mt_nrc_enable", C.c_int, [_VP, C.POINTER(mt_nrc_config)]),
     ("mt_nrc_frame", C.c_int, [_VP, _VP, C.c_uint32, _VP]),
+    ("mt_nrc_get_stats", C.c_int, [_VP, C.POINTER(mt_nrc_stats)]),
     ("mt_nrc_get_params", C.c_int, [_VP, _VP]),
     ("mt_nrc_set_params", C.c_int, [_VP, _VP]),
     ("mt_nrc_infer", C.c_int, [_VP, _VP, C.c_uint32, _VP, _VP]),

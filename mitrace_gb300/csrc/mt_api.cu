@@ -225,9 +225,12 @@ struct mt_handle {
         bool on = false;
         mt_nrc_config cfg{};
         DevArray<float> master, m, v, partial, planes, frame;
-        DevArray<uint16_t> fwd, bwd, acts;
+        DevArray<uint16_t> fwd, bwd, infer, acts;
+        DevArray<float> ema;
         DevArray<float4> qrec, trec, samples;
-        DevArray<uint32_t> counters;  // [0] cache queries, [1] training samples
+        // [0] cache queries of a batch, [1] training samples, [2] queries of the
+        // frame, [3] summed step losses of the frame (float bits)
+        DevArray<uint32_t> counters;
         NrcOptimizer opt{};
         uint64_t frames = 0;          // frames rendered (sample indices continue)
         uint64_t plane_capacity = 0;  // samples the cached render's band planes hold
@@ -750,8 +753,11 @@ mt_status nrc_alloc(mt_handle* h, const mt_nrc_config& c)
     MT_CUDA(N.partial.alloc(static_cast<size_t>(O.max_splits) * kNrcParams));
     MT_CUDA(N.fwd.alloc(kNrcFwdElems));
     MT_CUDA(N.bwd.alloc(kNrcBwdElems));
+    MT_CUDA(N.infer.alloc(kNrcFwdElems));
+    MT_CUDA(N.ema.alloc(kNrcParams));
     MT_CUDA(cudaMemsetAsync(N.fwd.p, 0, kNrcFwdElems * 2, st));
     MT_CUDA(cudaMemsetAsync(N.bwd.p, 0, kNrcBwdElems * 2, st));
+    MT_CUDA(cudaMemsetAsync(N.infer.p, 0, kNrcFwdElems * 2, st));
     const uint64_t R = O.max_rows;
     MT_CUDA(N.acts.alloc(R * (80 + 8 * 64 + 8)));
     O.acts.x = N.acts.p;
@@ -766,6 +772,9 @@ mt_status nrc_alloc(mt_handle* h, const mt_nrc_config& c)
     O.partial = N.partial.p;
     O.fwd = N.fwd.p;
     O.bwd = N.bwd.p;
+    O.infer = N.infer.p;
+    O.ema = N.ema.p;
+    O.ema_decay = c.ema_decay;
     O.lr = c.learning_rate;
     O.beta1 = c.beta1;
     O.beta2 = c.beta2;
@@ -779,8 +788,8 @@ mt_status nrc_alloc(mt_handle* h, const mt_nrc_config& c)
     N.sample_cap = c.train_paths * bounces;
     MT_CUDA(N.samples.alloc(static_cast<size_t>(N.sample_cap) * 6));
     MT_CUDA(N.qrec.alloc(static_cast<size_t>(h->batch) * 5));
-    MT_CUDA(N.counters.alloc(2));
-    MT_CUDA(cudaMemsetAsync(N.counters.p, 0, 2 * sizeof(uint32_t), st));
+    MT_CUDA(N.counters.alloc(4));
+    MT_CUDA(cudaMemsetAsync(N.counters.p, 0, 4 * sizeof(uint32_t), st));
     // band planes of the cached render and its frame image
     const uint64_t npix = static_cast<uint64_t>(cfg.width) * cfg.height;
     const uint64_t budget = env_u64("MT_SAMPLE_BUDGET_MB", 12288) << 20;
@@ -1172,6 +1181,7 @@ void mt_nrc_config_defaults(mt_nrc_config* c)
     c->epsilon = 1e-15f;
     c->rough_min = 0.3f;
     c->seed = 1337;
+    c->ema_decay = 0.9f;
 }
 
 mt_status mt_nrc_enable(mt_handle* h, const mt_nrc_config* c)
@@ -1180,7 +1190,7 @@ mt_status mt_nrc_enable(mt_handle* h, const mt_nrc_config* c)
     if (h->running) return set_err(MT_ERR_STATE, "an asynchronous render is running");
     if (c->train_paths == 0 || c->train_batch == 0 || c->train_batch > (1u << 24) || c->spp == 0 ||
         !(c->learning_rate > 0.0f) || !(c->beta1 >= 0.0f && c->beta1 < 1.0f) || !(c->beta2 >= 0.0f && c->beta2 < 1.0f) ||
-        !(c->epsilon >= 0.0f))
+        !(c->epsilon >= 0.0f) || !(c->ema_decay >= 0.0f && c->ema_decay < 1.0f))
         return set_err(MT_ERR_INVALID, "invalid radiance-cache configuration");
     if (static_cast<uint64_t>(c->train_paths) * std::max<uint32_t>(1, h->cfg.bounces) > 0xFFFFFFFFull)
         return set_err(MT_ERR_INVALID, "train_paths * bounces exceeds 2^32");
@@ -1221,7 +1231,7 @@ mt_status mt_nrc_frame(mt_handle* h, float* d_accum, uint32_t accum_index, void*
     if (mul == 0) mul = 1;
     while (gcd64(mul, npix) != 1) mul = (mul + 1) % npix ? (mul + 1) % npix : 1;
     const uint64_t add0 = (N.frames * 0x632BE5ABull) % npix;
-    MT_CUDA(cudaMemsetAsync(N.counters.p + 1, 0, sizeof(uint32_t), st));
+    MT_CUDA(cudaMemsetAsync(N.counters.p + 1, 0, 3 * sizeof(uint32_t), st));
     for (uint32_t c0 = 0; c0 < nc.train_paths; c0 += N.train_chunk) {
         const uint32_t n = std::min<uint32_t>(N.train_chunk, nc.train_paths - c0);
         BatchExtra X;
@@ -1243,7 +1253,7 @@ mt_status mt_nrc_frame(mt_handle* h, float* d_accum, uint32_t accum_index, void*
         a.count_cap = N.sample_cap;
         a.base = static_cast<uint32_t>((N.frames * nc.train_steps + s) * nc.train_batch);
         a.rows = nc.train_batch;
-        MT_CUDA(launch_nrc_train_step(N.opt, a, nullptr, nullptr, st));
+        MT_CUDA(launch_nrc_train_step(N.opt, a, reinterpret_cast<float*>(N.counters.p + 3), nullptr, st));
         launches += 3;
     }
     // 3. the cached render
@@ -1258,7 +1268,8 @@ mt_status mt_nrc_frame(mt_handle* h, float* d_accum, uint32_t accum_index, void*
         Q.mode = MT_NRC_QUERY;
         Q.rec = N.qrec.p;
         Q.count = N.counters.p;
-        Q.net = N.fwd.p;
+        Q.net = N.infer.p;
+        Q.total = N.counters.p + 2;
         const uint64_t rows_per_band = N.plane_capacity / (static_cast<uint64_t>(c.width) * nc.spp);
         for (uint64_t r0 = 0; r0 < c.height; r0 += rows_per_band) {
             const uint64_t rows = std::min<uint64_t>(rows_per_band, c.height - r0);
@@ -1282,6 +1293,25 @@ mt_status mt_nrc_frame(mt_handle* h, float* d_accum, uint32_t accum_index, void*
     }
     N.frames += 1;
     h->launches += launches;
+    return MT_OK;
+}
+
+mt_status mt_nrc_get_stats(mt_handle* h, mt_nrc_stats* out)
+{
+    mt_status rc = nrc_ready(h);
+    if (rc != MT_OK) return rc;
+    if (!out) return set_err(MT_ERR_INVALID, "null argument");
+    uint32_t c[4];
+    MT_CUDA(cudaDeviceSynchronize());
+    MT_CUDA(cudaMemcpy(c, h->nrc.counters.p, sizeof(c), cudaMemcpyDeviceToHost));
+    std::memset(out, 0, sizeof(*out));
+    out->frames = h->nrc.frames;
+    out->adam_steps = h->nrc.opt.step;
+    out->train_samples = std::min(c[1], h->nrc.sample_cap);
+    out->queries = c[2];
+    float loss;
+    std::memcpy(&loss, &c[3], sizeof(loss));
+    out->train_loss = h->nrc.cfg.train_steps ? loss / static_cast<float>(h->nrc.cfg.train_steps) : 0.0f;
     return MT_OK;
 }
 
@@ -1316,7 +1346,7 @@ mt_status mt_nrc_infer(mt_handle* h, const float* d_features, uint32_t n, float*
     mt_status rc = nrc_ready(h);
     if (rc != MT_OK) return rc;
     if (n && (!d_features || !d_rgb)) return set_err(MT_ERR_INVALID, "null argument");
-    MT_CUDA(launch_nrc_infer(h->nrc.fwd.p, d_features, n, d_rgb, static_cast<cudaStream_t>(cuda_stream)));
+    MT_CUDA(launch_nrc_infer(h->nrc.infer.p, d_features, n, d_rgb, static_cast<cudaStream_t>(cuda_stream)));
     h->launches += n ? 1 : 0;
     return MT_OK;
 }

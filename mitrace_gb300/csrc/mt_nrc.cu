@@ -298,7 +298,8 @@ template <bool PATHS>
 __global__ void __launch_bounds__(kInferWarps * 32) k_nrc_infer(const bf16* __restrict__ blob,
                                                                 const float4* __restrict__ feat, uint32_t n_host,
                                                                 const uint32_t* __restrict__ count,
-                                                                float* __restrict__ out, PathState P)
+                                                                float* __restrict__ out, PathState P,
+                                                                uint32_t* total)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     bf16* W = reinterpret_cast<bf16*>(smem);
@@ -307,6 +308,7 @@ __global__ void __launch_bounds__(kInferWarps * 32) k_nrc_infer(const bf16* __re
     copy_blob(W, blob, kNrcFwdElems);
     __syncthreads();
     const uint32_t n = PATHS ? *count : n_host;
+    if (total && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(total, n);
     const uint32_t tiles = (n + 15) / 16;
     for (uint32_t tile = blockIdx.x * kInferWarps + warp; tile < tiles; tile += gridDim.x * kInferWarps) {
         const uint32_t r0 = tile * 16;
@@ -572,18 +574,21 @@ __global__ void __launch_bounds__(kWgWarps * 32) k_nrc_wgrad(NrcActs A, uint32_t
 // ---------------------------------------------------------------------------
 // Adam and weight publication
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void publish_param(bf16* fwd, bf16* bwd, int q, float w)
+__device__ __forceinline__ void publish_param(bf16* fwd, bf16* bwd, bf16* infer, int q, float w, float wi)
 {
     int l, o, i;
     param_coords(q, l, o, i);
     const bf16 b = __float2bfloat16_rn(w);
     fwd[fwd_off(l) + o * fwd_stride(l) + i] = b;
     if (l >= 1) bwd[bwd_off(l) + i * bwd_stride(l) + o] = b;
+    infer[fwd_off(l) + o * fwd_stride(l) + i] = __float2bfloat16_rn(wi);
 }
 
+// ema_bc = 1 - decay^step (bias correction of the zero-started average).
 __global__ void k_nrc_adam(float* __restrict__ master, float* __restrict__ m, float* __restrict__ v,
                            const float* __restrict__ partial, uint32_t splits, float lr, float b1, float b2,
-                           float eps, float bc1, float bc2, bf16* fwd, bf16* bwd, float* grad_out)
+                           float eps, float bc1, float bc2, bf16* fwd, bf16* bwd, float* grad_out,
+                           bf16* infer, float* __restrict__ ema, float decay, float ema_bc)
 {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= kNrcParams) return;
@@ -596,13 +601,22 @@ __global__ void k_nrc_adam(float* __restrict__ master, float* __restrict__ m, fl
     v[q] = vv;
     const float w = master[q] - lr * (mm / bc1) / (sqrtf(vv / bc2) + eps);
     master[q] = w;
-    publish_param(fwd, bwd, q, w);
+    float wi = w;
+    if (decay > 0.0f) {
+        const float e = decay * ema[q] + (1.0f - decay) * w;
+        ema[q] = e;
+        wi = e / ema_bc;
+    }
+    publish_param(fwd, bwd, infer, q, w, wi);
 }
 
-__global__ void k_nrc_publish(const float* __restrict__ master, bf16* fwd, bf16* bwd)
+__global__ void k_nrc_publish(const float* __restrict__ master, bf16* fwd, bf16* bwd, bf16* infer,
+                              float* __restrict__ ema)
 {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q < kNrcParams) publish_param(fwd, bwd, q, master[q]);
+    if (q >= kNrcParams) return;
+    ema[q] = 0.0f;
+    publish_param(fwd, bwd, infer, q, master[q], master[q]);
 }
 
 __global__ void k_nrc_blend(float* __restrict__ accum, const float* __restrict__ frame, uint64_t n, float w)
@@ -675,7 +689,7 @@ cudaError_t allow_smem(K kernel, size_t bytes, bool& done)
 
 template <bool PATHS>
 cudaError_t infer(const void* net, const float4* feat, uint32_t n_host, const uint32_t* count, uint32_t capacity,
-                  float* out, const PathState& P, cudaStream_t st)
+                  float* out, const PathState& P, uint32_t* total, cudaStream_t st)
 {
     static bool ok = false;
     cudaError_t e = allow_smem(k_nrc_infer<PATHS>, kInferSmem, ok);
@@ -686,22 +700,23 @@ cudaError_t infer(const void* net, const float4* feat, uint32_t n_host, const ui
     if (blocks > cap) blocks = cap;
     if (blocks == 0) blocks = 1;
     k_nrc_infer<PATHS><<<static_cast<unsigned>(blocks), kInferWarps * 32, kInferSmem, st>>>(
-        static_cast<const bf16*>(net), feat, n_host, count, out, P);
+        static_cast<const bf16*>(net), feat, n_host, count, out, P, total);
     return cudaGetLastError();
 }
 
 }  // namespace
 
 cudaError_t launch_nrc_query(const void* net, const PathState& P, const float4* rec, const uint32_t* count,
-                             uint32_t capacity, cudaStream_t st)
+                             uint32_t capacity, uint32_t* total, cudaStream_t st)
 {
-    return infer<true>(net, rec, 0, count, capacity, nullptr, P, st);
+    return infer<true>(net, rec, 0, count, capacity, nullptr, P, total, st);
 }
 
 cudaError_t launch_nrc_infer(const void* net, const float* features, uint32_t n, float* out, cudaStream_t st)
 {
     if (n == 0) return cudaSuccess;
-    return infer<false>(net, reinterpret_cast<const float4*>(features), n, nullptr, n, out, PathState{}, st);
+    return infer<false>(net, reinterpret_cast<const float4*>(features), n, nullptr, n, out, PathState{}, nullptr,
+                        st);
 }
 
 cudaError_t launch_nrc_encode(const float* features, uint32_t n, float* out, cudaStream_t st)
@@ -749,17 +764,19 @@ cudaError_t launch_nrc_train_step(NrcOptimizer& O, const NrcTrainArgs& a, float*
     O.step += 1;
     const double bc1 = 1.0 - std::pow(static_cast<double>(O.beta1), static_cast<double>(O.step));
     const double bc2 = 1.0 - std::pow(static_cast<double>(O.beta2), static_cast<double>(O.step));
-    k_nrc_adam<<<(kNrcParams + 255) / 256, 256, 0, st>>>(O.master, O.m, O.v, O.partial, splits, O.lr, O.beta1,
-                                                        O.beta2, O.eps, static_cast<float>(bc1),
-                                                        static_cast<float>(bc2), static_cast<bf16*>(O.fwd),
-                                                        static_cast<bf16*>(O.bwd), grad_out);
+    const double ema_bc = 1.0 - std::pow(static_cast<double>(O.ema_decay), static_cast<double>(O.step));
+    k_nrc_adam<<<(kNrcParams + 255) / 256, 256, 0, st>>>(
+        O.master, O.m, O.v, O.partial, splits, O.lr, O.beta1, O.beta2, O.eps, static_cast<float>(bc1),
+        static_cast<float>(bc2), static_cast<bf16*>(O.fwd), static_cast<bf16*>(O.bwd), grad_out,
+        static_cast<bf16*>(O.infer), O.ema, O.ema_decay, static_cast<float>(ema_bc));
     return cudaGetLastError();
 }
 
 cudaError_t launch_nrc_publish(const NrcOptimizer& O, cudaStream_t st)
 {
     k_nrc_publish<<<(kNrcParams + 255) / 256, 256, 0, st>>>(O.master, static_cast<bf16*>(O.fwd),
-                                                           static_cast<bf16*>(O.bwd));
+                                                           static_cast<bf16*>(O.bwd), static_cast<bf16*>(O.infer),
+                                                           O.ema);
     return cudaGetLastError();
 }
 

@@ -38,8 +38,9 @@ struct NrcShade {
     //        (radiance collected before the vertex's NEE, 1 = recorded).
     float4* rec = nullptr;
     uint32_t* count = nullptr;  // QUERY: queries appended
-    // QUERY: bf16 forward weight blob.
+    // QUERY: bf16 forward weight blob; queries are also added to *total.
     const void* net = nullptr;
+    uint32_t* total = nullptr;
     // TRAIN: training samples (5 feature float4 + target float4 each).
     float4* samples = nullptr;
     uint32_t* sample_count = nullptr;
@@ -56,7 +57,7 @@ struct NrcActs {
 
 // Cache queries of a batch: adds throughput * max(cache, 0) to P.indirect.
 cudaError_t launch_nrc_query(const void* net, const PathState& P, const float4* rec, const uint32_t* count,
-                             uint32_t capacity, cudaStream_t st);
+                             uint32_t capacity, uint32_t* total, cudaStream_t st);
 // Training targets of a batch of training paths -> samples.
 cudaError_t launch_nrc_targets(const PathState& P, const NrcShade& N, uint32_t n, uint32_t bounces,
                                cudaStream_t st);
@@ -83,8 +84,11 @@ struct NrcOptimizer {
     float* m;           // Adam first moments
     float* v;           // Adam second moments
     float* partial;     // splits x kNrcParams weight-gradient partial sums
-    void* fwd;          // bf16 forward blob
+    void* fwd;          // bf16 forward blob of the trained weights
     void* bwd;          // bf16 backward blob
+    void* infer;        // bf16 forward blob the renderer queries (moving average)
+    float* ema;         // fp32 moving average (zero-started, bias-corrected on use)
+    float ema_decay;    // 0: infer = trained weights
     NrcActs acts;       // sized for max_rows
     uint32_t max_rows;  // multiple of 64
     uint32_t max_splits;
@@ -93,7 +97,7 @@ struct NrcOptimizer {
 };
 cudaError_t launch_nrc_train_step(NrcOptimizer& O, const NrcTrainArgs& a, float* loss, float* grad_out,
                                   cudaStream_t st);
-// Writes the bf16 blobs from the fp32 master weights.
+// Writes the bf16 blobs from the fp32 master weights (and restarts the average).
 cudaError_t launch_nrc_publish(const NrcOptimizer& O, cudaStream_t st);
 // running mean: accum += (frame - accum) / (index + 1)
 cudaError_t launch_nrc_blend(float* accum, const float* frame, uint64_t n, uint32_t index, cudaStream_t st);

@@ -100,6 +100,12 @@ class Tracer:
         A.check(A.lib.mt_nrc_frame(self.handle, C.c_void_p(accum_ptr or None), accum_index,
                                    C.c_void_p(stream_ptr)), "mt_nrc_frame")
 
+    def nrc_get_stats(self) -> dict:
+        st = A.mt_nrc_stats()
+        A.check(A.lib.mt_nrc_get_stats(self.handle, C.byref(st)), "mt_nrc_get_stats")
+        return {"frames": st.frames, "adam_steps": st.adam_steps, "train_samples": st.train_samples,
+                "queries": st.queries, "train_loss": st.train_loss}
+
     def nrc_get_params(self) -> np.ndarray:
         p = np.zeros(A.MT_NRC_PARAMS, dtype=np.float32)
         A.check(A.lib.mt_nrc_get_params(self.handle, p.ctypes.data_as(C.c_void_p)), "mt_nrc_get_params")

@@ -86,6 +86,7 @@ def test_config_defaults():
     assert (c.train_paths, c.train_batch, c.train_steps, c.spp) == (65536, 16384, 4, 4)
     assert c.learning_rate == pytest.approx(1e-2) and c.beta1 == pytest.approx(0.9)
     assert c.beta2 == pytest.approx(0.99) and c.rough_min == pytest.approx(0.3)
+    assert c.ema_decay == pytest.approx(0.9)
 
 
 def test_argument_errors():
@@ -96,6 +97,7 @@ def test_argument_errors():
     assert A.lib.mt_nrc_infer(None, None, 0, None, None) == 3
     assert A.lib.mt_nrc_train_step(None, None, None, 1, None, None, None) == 3
     assert A.lib.mt_nrc_get_params(None, None) == 3
+    assert A.lib.mt_nrc_get_stats(None, None) == 3
     assert A.lib.mt_nrc_set_params(None, None) == 3
     assert A.lib.mt_nrc_encode(None, 4, None, None) == 3
     assert A.lib.mt_nrc_encode(None, 0, None, None) == 0  # nothing to do, no device touched
