@@ -178,11 +178,48 @@ typedef struct mt_config {
     int32_t firefly_enable;
     float firefly_threshold;
     float terminate_energy;
-    int32_t debug_mode; /* only 0 (DebugNone) is supported */
+    int32_t debug_mode; /* MT_DEBUG_* (Config::DebugMode), 0 = DebugNone */
     uint32_t reserved0;
     uint64_t seed;      /* seeds the counter-based RNG */
     uint32_t reserved[8];
 } mt_config;
+
+/* Debug render modes, the values of Config::DebugMode (src/CLI/Config.hpp:16-40).
+ * A sample of a debug render is ProcessDebugRay's value (Tracer.cpp:366-488)
+ * instead of the tonemapped radiance; samples are averaged (with the firefly
+ * clamp when enabled) as usual, and the modes marked (h) end with
+ * WaitForRender's heatmap post-processing over the whole image
+ * (Tracer.cpp:695-716: intensity / maximum intensity, colour ramp or grey).
+ * MT_DEBUG_COLOR_PER_MESH hashes the instance index (the reference hashes the
+ * low bits of the MeshInstance's address).  PIXEL_STANDARD_DEVIATION and
+ * FIREFLY_ELIMINATION render the normal image and then apply the heatmap, as
+ * the reference does.  Debug modes work with mt_render_device and
+ * mt_start/mt_wait; the adjoint, the radiance cache and the allocation-free
+ * entry point reject them. */
+#define MT_DEBUG_NONE 0
+#define MT_DEBUG_PRIMARY_BVH_TESTS 1          /* (h) */
+#define MT_DEBUG_TOTAL_BVH_TESTS 2            /* (h) */
+#define MT_DEBUG_PRIMARY_TRIANGLE_TESTS 3     /* (h) */
+#define MT_DEBUG_TOTAL_TRIANGLE_TESTS 4       /* (h) */
+#define MT_DEBUG_ALBEDO 5
+#define MT_DEBUG_METALLIC_ROUGHNESS 6
+#define MT_DEBUG_GEOMETRIC_NORMAL 7
+#define MT_DEBUG_SHADING_NORMAL 8
+#define MT_DEBUG_DIRECT_ONLY 9
+#define MT_DEBUG_INDIRECT_ONLY 10
+#define MT_DEBUG_EMISSION 11
+#define MT_DEBUG_COLOR_PER_MESH 12
+#define MT_DEBUG_COLOR_PER_TRIANGLE 13
+#define MT_DEBUG_COLOR_PER_BOUNDING_VOLUME 14
+#define MT_DEBUG_BOUNCES 15                   /* (h) */
+#define MT_DEBUG_DEPTH 16                     /* (h, grey) */
+#define MT_DEBUG_FIRST_HIT_FRESNEL 17
+#define MT_DEBUG_FIRST_HIT_BRDF 18            /* (h, grey) */
+#define MT_DEBUG_FIRST_HIT_PDF 19
+#define MT_DEBUG_REFLECTED_DIRECTION 20
+#define MT_DEBUG_PIXEL_STANDARD_DEVIATION 21  /* (h, grey) */
+#define MT_DEBUG_FIREFLY_ELIMINATION 22       /* (h) */
+#define MT_DEBUG_COUNT 23
 
 /* Fills *cfg with the reference defaults (Config.hpp:50-70). */
 void mt_config_defaults(mt_config* cfg);
@@ -282,13 +319,18 @@ mt_status mt_render_grad(mt_handle* h, const mt_grad_buffers* g, void* cuda_stre
  * weights and activations with FP32 accumulation.  Its input is the encoding
  * of a 20-float feature record (five float4):
  *   f0 = (position normalised to the scene's world box, roughness)
- *   f1 = (outgoing direction wo = -ray direction, unused)
- *   f2 = (shading normal, unused)
+ *   f1 = (outgoing direction wo = -ray direction,
+ *         bounce budget left (bounces - 1 - k) / (bounces - 1) at bounce k)
+ *   f2 = (shading normal,
+ *         cut-off headroom clamp(log2(|totalEnergy| / terminate_energy) / 16, 0, 1))
  *   f3 = (diffuse albedo base*(1-metallic), unused)
  *   f4 = (specular albedo mix(0.04, base, metallic), unused)
  * Encoding (80 lanes): 12 triangle-wave octaves per position axis (36),
  * real spherical harmonics through band 3 of wo (16) and of the normal (16),
- * roughness (1), diffuse (3) and specular (3) albedo, five constant 1s.
+ * roughness (1), diffuse (3) and specular (3) albedo, the bounce budget and
+ * the cut-off headroom (2), three constant 1s.  The two path-state lanes let
+ * one network serve vertices whose remaining paths the bounce limit and the
+ * energy cut-off truncate differently.
  * Parameters, FP32 master copy: W0 (64 x 80), W1, W2, W3 (64 x 64), W4 (3 x
  * 64), each row-major [out][in] like a torch Linear weight, concatenated. */
 #define MT_NRC_INPUTS 80u

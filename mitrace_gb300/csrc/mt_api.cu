@@ -205,6 +205,8 @@ struct mt_handle {
     DevArray<uint32_t> counts;
     DevArray<unsigned long long> rays;  // [0] extension, [1] shadow
     DevArray<float> samples;     // 3 planes
+    DevArray<float4> dval;       // debug render modes only
+    DevArray<uint4> dcnt;
     DevArray<float> image;
     unsigned long long* rays_host = nullptr;  // pinned, 2 words
     cudaEvent_t render_done = nullptr;        // end of the last synchronous render
@@ -526,6 +528,7 @@ mt_status upload_scene(mt_handle* h, const mt_scene_desc* d)
     S.firefly_enable = cfg.firefly_enable;
     S.firefly_k = cfg.firefly_threshold;
     S.error_flag = h->error_flag.p;
+    S.debug_mode = cfg.debug_mode;
     return MT_OK;
 }
 
@@ -560,6 +563,10 @@ mt_status ensure_wave(mt_handle* h)
     MT_CUDA(h->rays.alloc(2));
     MT_CUDA(h->samples.alloc(3ull * h->band_capacity));
     MT_CUDA(h->image.alloc(npix * 3));
+    if (c.debug_mode) {
+        MT_CUDA(h->dval.alloc(batch));
+        MT_CUDA(h->dcnt.alloc(batch));
+    }
     MT_CUDA(cudaMallocHost(reinterpret_cast<void**>(&h->rays_host), 2 * sizeof(unsigned long long)));
     h->rays_host[0] = h->rays_host[1] = 0;
     MT_CUDA(cudaEventCreateWithFlags(&h->render_done, cudaEventDisableTiming));
@@ -588,6 +595,8 @@ WaveViews views(mt_handle* h)
     v.P.sky = s + 8 * B;
     v.P.hitA = s + 9 * B;
     v.P.hitB = h->phit.p;
+    v.P.dval = h->dval.p;
+    v.P.dcnt = h->dcnt.p;
     v.SQ.o = h->sq.p;
     v.SQ.d = h->sq.p + B;
     v.SQ.c = h->sq.p + 2 * B;
@@ -643,6 +652,11 @@ mt_status render_into(mt_handle* h, float* out, cudaStream_t st, bool sync_each_
         }
         MT_CUDA(launch_resolve(h->S, v.W, band_pix, pix_base, out, st, prof));
         ++launches;
+    }
+    if (debug_needs_post(c.debug_mode)) {
+        // WaitForRender's post-processing (Tracer.cpp:781-799) over the whole image
+        MT_CUDA(launch_debug_post(out, static_cast<uint64_t>(c.width) * c.height, c.debug_mode, h->counts.p + 7, st));
+        launches += 2;
     }
     MT_CUDA(cudaMemcpyAsync(h->rays_host, h->rays.p, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
     MT_CUDA(cudaEventRecord(h->render_done, st));
@@ -783,11 +797,11 @@ mt_status nrc_alloc(mt_handle* h, const mt_nrc_config& c)
     // training paths and their samples
     const uint32_t bounces = std::max<uint32_t>(1, cfg.bounces);
     N.train_chunk = std::min<uint32_t>(c.train_paths, h->batch);
-    MT_CUDA(N.trec.alloc(static_cast<size_t>(N.train_chunk) * bounces * 6));
+    MT_CUDA(N.trec.alloc(static_cast<size_t>(N.train_chunk) * bounces * 7));
     MT_CUDA(cudaMemsetAsync(N.trec.p, 0, N.trec.n * sizeof(float4), st));
     N.sample_cap = c.train_paths * bounces;
     MT_CUDA(N.samples.alloc(static_cast<size_t>(N.sample_cap) * 6));
-    MT_CUDA(N.qrec.alloc(static_cast<size_t>(h->batch) * 5));
+    MT_CUDA(N.qrec.alloc(static_cast<size_t>(h->batch) * 6));
     MT_CUDA(N.counters.alloc(4));
     MT_CUDA(cudaMemsetAsync(N.counters.p, 0, 4 * sizeof(uint32_t), st));
     // band planes of the cached render and its frame image
@@ -857,7 +871,8 @@ mt_status mt_create(const mt_scene_desc* scene, const mt_config* cfg, mt_handle*
         return set_err(MT_ERR_INVALID, "width, height and samples must be positive");
     if (static_cast<uint64_t>(cfg->width) * cfg->height > 0xFFFFFFFFull / 2)
         return set_err(MT_ERR_INVALID, "image too large");
-    if (cfg->debug_mode != 0) return set_err(MT_ERR_INVALID, "debug modes are not supported");
+    if (cfg->debug_mode < 0 || cfg->debug_mode >= MT_DEBUG_COUNT)
+        return set_err(MT_ERR_INVALID, "debug_mode is not a Config::DebugMode value");
     if (scene->num_meshes && !scene->meshes) return set_err(MT_ERR_INVALID, "meshes is null");
     if (scene->num_instances && !scene->instances) return set_err(MT_ERR_INVALID, "instances is null");
     if (scene->num_materials && !scene->materials) return set_err(MT_ERR_INVALID, "materials is null");
@@ -1029,6 +1044,7 @@ mt_status mt_render_grad(mt_handle* h, const mt_grad_buffers* g, void* cuda_stre
     if (h->running) return set_err(MT_ERR_STATE, "an asynchronous render is running");
     if (h->cfg.bounces > MT_GRAD_MAX_BOUNCES)
         return set_err(MT_ERR_INVALID, "mt_render_grad supports at most MT_GRAD_MAX_BOUNCES bounces");
+    if (h->cfg.debug_mode) return set_err(MT_ERR_INVALID, "mt_render_grad needs debug_mode 0");
     mt_status rc = ensure_wave(h);
     if (rc != MT_OK) return rc;
     const mt_config& c = h->cfg;
@@ -1196,6 +1212,7 @@ mt_status mt_nrc_enable(mt_handle* h, const mt_nrc_config* c)
         return set_err(MT_ERR_INVALID, "train_paths * bounces exceeds 2^32");
     mt_status rc = ensure_wave(h);
     if (rc != MT_OK) return rc;
+    if (h->cfg.debug_mode) return set_err(MT_ERR_INVALID, "the radiance cache needs debug_mode 0");
     return nrc_alloc(h, *c);
 }
 

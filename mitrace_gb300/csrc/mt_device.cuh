@@ -181,6 +181,7 @@ struct DevScene {
     int32_t firefly_enable;
     float firefly_k;
     int* error_flag;
+    int32_t debug_mode;  // Config::DebugMode (MT_DEBUG_*), 0 = DebugNone
 };
 
 #define MT_STACK_SIZE 64
@@ -814,6 +815,35 @@ __device__ __forceinline__ f3 sample_sky(const DevScene& S, f3 d, bool primary)
     const DevTexture t = S.textures[S.env];
     const f4 c = image_sample(t, u, v);
     return f3{__fmul_rn(c.x, mult), __fmul_rn(c.y, mult), __fmul_rn(c.z, mult)};
+}
+
+// RandomColorFromU16 (Tracer.cpp:350-364): an integer hash of the low 16 bits,
+// 3 bits per channel.
+__device__ __forceinline__ f3 random_color_u16(uint32_t value)
+{
+    uint32_t x = value & 0xffffu;
+    x ^= x >> 7;
+    x *= 0x2C1B3C6Du;
+    x ^= x >> 12;
+    x *= 0x297A2D39u;
+    x ^= x >> 15;
+    const uint32_t v = x & 0xffffu;
+    return {__fdiv_rn(static_cast<float>((v & 0x01C0u) >> 6), 7.0f), __fdiv_rn(static_cast<float>((v & 0x0038u) >> 3), 7.0f),
+            __fdiv_rn(static_cast<float>(v & 0x0007u), 7.0f)};
+}
+
+// Heatmap (Tracer.cpp:650-670): blue, cyan, green, yellow, red; glm::mix(a, b, f)
+// = a * (1 - f) + b * f.
+__device__ __forceinline__ f3 heatmap(float t)
+{
+    t = fminf(fmaxf(t, 0.0f), 1.0f);
+    const float x = __fmul_rn(t, 4.0f);
+    const int i = min(static_cast<int>(x), 3);
+    const float fr = __fsub_rn(x, static_cast<float>(i));
+    const float r = __fsub_rn(1.0f, fr);
+    const float R[5] = {0, 0, 0, 1, 1}, G[5] = {0, 1, 1, 1, 0}, B[5] = {1, 1, 0, 0, 0};
+    return {__fadd_rn(__fmul_rn(R[i], r), __fmul_rn(R[i + 1], fr)), __fadd_rn(__fmul_rn(G[i], r), __fmul_rn(G[i + 1], fr)),
+            __fadd_rn(__fmul_rn(B[i], r), __fmul_rn(B[i + 1], fr))};
 }
 
 }  // namespace mt

@@ -175,6 +175,10 @@ __global__ void __launch_bounds__(256) k_raygen(DevScene S, PathState P, BatchIn
         P.indirect[p] = zero;
         P.sky[p] = zero;
         q0[p] = p;
+        if (P.dval) {
+            P.dval[p] = zero;
+            P.dcnt[p] = make_uint4(0u, 0u, 0u, 0u);
+        }
         if (R.path) {
             R.path[2 * p] = zero;
             R.path[2 * p + 1] = make_float4(0.0f, 0.0f, 0.0f, -1.0f);
@@ -194,7 +198,7 @@ __device__ __forceinline__ void flush_counts(unsigned long long* cnt, uint32_t p
         b += __shfl_down_sync(0xffffffffu, b, o);
         c += __shfl_down_sync(0xffffffffu, c, o);
     }
-    if ((threadIdx.x & 31) == 0) {
+    if ((threadIdx.x & 31) == 0 && cnt) {
         atomicAdd(cnt + 0, a);
         atomicAdd(cnt + 1, b);
         atomicAdd(cnt + 2, c);
@@ -209,6 +213,7 @@ struct ExtendWork {
     uint32_t n;
     uint32_t p;
     uint32_t pops, inner, tris;
+    int debug_mode;
     __device__ bool fetch(uint32_t i, f3& o, f3& d, float& tmax)
     {
         if (i >= n) return false;
@@ -231,6 +236,29 @@ struct ExtendWork {
         } else {
             P.hitB[p] = make_uint4(MT_NO_HIT, 0u, 0u, 0u);
         }
+        if (P.dcnt) {
+            // PathStep debug counters (Tracer.cpp:171-175); they are the winning
+            // instance's (COUNT traversals only), a miss step adds nothing
+            float4 v = P.dval[p];
+            uint4 c = P.dcnt[p];
+            if (h.hit) {
+                if (v.w == 0.0f) {
+                    c.x = h.bvh_tests | 0x80000000u;
+                    c.y = h.tri_tests;
+                    if (debug_mode == MT_DEBUG_COLOR_PER_BOUNDING_VOLUME) {
+                        const f3 col = random_color_u16(h.bv);
+                        v.x = col.x;
+                        v.y = col.y;
+                        v.z = col.z;
+                    }
+                }
+                c.z += h.bvh_tests;
+                c.w += h.tri_tests;
+                P.dcnt[p] = c;
+            }
+            v.w += 1.0f;
+            P.dval[p] = v;
+        }
     }
 };
 
@@ -248,7 +276,7 @@ __global__ void __launch_bounds__(128, MT_TRAVERSE_MIN_BLOCKS) k_extend(DevScene
         counts[4] = 0;  // ray fetch counter of this bounce's shadow stage
         atomicAdd(rays, static_cast<unsigned long long>(n));
     }
-    ExtendWork<COUNT> W{P, q, n, 0, 0, 0, 0};
+    ExtendWork<COUNT> W{P, q, n, 0, 0, 0, 0, S.debug_mode};
     trace_persistent<COUNT, false>(S, W, &counts[3]);
     if (COUNT) flush_counts(cnt, W.pops, W.inner, W.tris);
 }
@@ -333,22 +361,33 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, PathState P, ShadowQu
             const bool query = NC.mode == MT_NRC_QUERY && bounce >= 1 && seen_diffuse != 0.0f;
             float4* fr = nullptr;
             if (query)
-                fr = NC.rec + 5ull * warp_append(NC.count);
+                fr = NC.rec + 6ull * warp_append(NC.count);
             else if (NC.mode == MT_NRC_TRAIN)
-                fr = NC.rec + (static_cast<uint64_t>(p) * S.bounces + bounce) * 6;
+                fr = NC.rec + (static_cast<uint64_t>(p) * S.bounces + bounce) * 7;
             if (fr) {
                 const f3 pn = {(hit_pos.x - NC.lo[0]) * NC.inv_ext[0], (hit_pos.y - NC.lo[1]) * NC.inv_ext[1],
                                (hit_pos.z - NC.lo[2]) * NC.inv_ext[2]};
                 const float m = mp.metallic;
+                // what the rest of the path may still collect: the bounce budget
+                // left and the headroom above the energy cut-off
+                const float remaining = S.bounces > 1 ? static_cast<float>(S.bounces - 1 - bounce) /
+                                                            static_cast<float>(S.bounces - 1)
+                                                      : 0.0f;
+                float headroom = 1.0f;
+                if (S.terminate_energy > 0.0f) {
+                    const float te = length(ld4(P.tot, p));
+                    headroom = fminf(fmaxf(log2f(fmaxf(te, 1e-30f) / S.terminate_energy) * 0.0625f, 0.0f), 1.0f);
+                }
                 fr[0] = make_float4(pn.x, pn.y, pn.z, mp.roughness);
-                fr[1] = make_float4(view.x, view.y, view.z, __uint_as_float(p));
-                fr[2] = make_float4(N.x, N.y, N.z, cur_e.x);
-                fr[3] = make_float4(base.x * (1.0f - m), base.y * (1.0f - m), base.z * (1.0f - m), cur_e.y);
+                fr[1] = make_float4(view.x, view.y, view.z, remaining);
+                fr[2] = make_float4(N.x, N.y, N.z, headroom);
+                fr[3] = make_float4(base.x * (1.0f - m), base.y * (1.0f - m), base.z * (1.0f - m), 0.0f);
                 fr[4] = make_float4(0.04f * (1.0f - m) + base.x * m, 0.04f * (1.0f - m) + base.y * m,
-                                    0.04f * (1.0f - m) + base.z * m, cur_e.z);
+                                    0.04f * (1.0f - m) + base.z * m, 0.0f);
+                fr[5] = make_float4(cur_e.x, cur_e.y, cur_e.z, __uint_as_float(p));
                 if (!query) {
                     const f3 pre = ((emit_now + ld4(P.direct, p)) + ld4(P.indirect, p)) + ld4(P.sky, p);
-                    fr[5] = make_float4(pre.x, pre.y, pre.z, 1.0f);
+                    fr[6] = make_float4(pre.x, pre.y, pre.z, 1.0f);
                 }
             }
             if (query) continue;  // the cache stands in for the rest of the path
@@ -424,8 +463,35 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, PathState P, ShadowQu
             }
         }
 
-        // Bounce sampling (Tracer.cpp:177-208); the last vertex never extends.
-        if (bounce + 1 >= S.bounces) continue;
+        // First-hit debug values (ProcessDebugRay, Tracer.cpp:411-482)
+        const bool dbg0 = P.dval && bounce == 0;
+        if (dbg0) {
+            f3 dv = splat(0.0f);
+            bool set = true;
+            switch (S.debug_mode) {
+                case MT_DEBUG_ALBEDO: dv = base; break;
+                case MT_DEBUG_METALLIC_ROUGHNESS: dv = f3{0.0f, mp.metallic, mp.roughness}; break;
+                case MT_DEBUG_GEOMETRIC_NORMAL: dv = geom_n * 0.5f + splat(0.5f); break;
+                case MT_DEBUG_SHADING_NORMAL: dv = N * 0.5f + splat(0.5f); break;
+                case MT_DEBUG_COLOR_PER_MESH: dv = random_color_u16(hb.x); break;
+                case MT_DEBUG_COLOR_PER_TRIANGLE: dv = random_color_u16(hb.y); break;
+                case MT_DEBUG_DEPTH: dv = splat(length(hit_pos - ld4(P.ro, p))); break;
+                case MT_DEBUG_FIRST_HIT_FRESNEL:
+                    dv = fresnel_schlick(gmax(dot(N, -rd), 0.0f), base_reflectivity(base, mp.metallic));
+                    break;
+                default: set = false; break;
+            }
+            if (set) {
+                const float4 o = P.dval[p];
+                P.dval[p] = make_float4(dv.x, dv.y, dv.z, o.w);
+            }
+        }
+
+        // Bounce sampling (Tracer.cpp:177-208); the last vertex never extends
+        // (the debug modes that show the first vertex's sample draw it anyway).
+        const bool last = bounce + 1 >= S.bounces;
+        if (last && !(dbg0 && (S.debug_mode == MT_DEBUG_FIRST_HIT_BRDF || S.debug_mode == MT_DEBUG_FIRST_HIT_PDF)))
+            continue;
         const float ps = specular_probability(view, N, base, mp.metallic);
         const uint4 rl = draw(S, pixel, sample, bounce, SLOT_LOBE);
         f3 nd;
@@ -458,6 +524,12 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, PathState P, ShadowQu
         const f3 brdf = eval_brdf(nd, view, N, base, mp.roughness, mp.metallic);
         const float nl = gmax(dot(N, nd), 0.0f);
         const f3 energy = pdf > 0.0f ? brdf * __fdiv_rn(nl, pdf) : splat(0.0f);
+        if (dbg0 && (S.debug_mode == MT_DEBUG_FIRST_HIT_BRDF || S.debug_mode == MT_DEBUG_FIRST_HIT_PDF)) {
+            const float4 o = P.dval[p];
+            const float dv = S.debug_mode == MT_DEBUG_FIRST_HIT_PDF ? pdf : __fadd_rn(__fadd_rn(brdf.x, brdf.y), brdf.z);
+            P.dval[p] = make_float4(dv, dv, dv, o.w);
+        }
+        if (last) continue;
         if (chosen >= 0) st4(P.cur, p, cur_e * energy);  // Tracer.cpp:339
         if (vr) {
             vr[1].w = __uint_as_float(__float_as_uint(vr[1].w) | MT_VREC_NEXT);
@@ -466,6 +538,12 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, PathState P, ShadowQu
         const f3 tot = ld4(P.tot, p) * energy;
         st4(P.tot, p, tot);
         if (length(tot) < S.terminate_energy) continue;  // Tracer.cpp:207-208
+        if (dbg0 && S.debug_mode == MT_DEBUG_REFLECTED_DIRECTION) {
+            // path[1].ray.direction * 0.5 + 0.5: the path has a second step
+            const float4 o = P.dval[p];
+            const f3 dv = nd * 0.5f + splat(0.5f);
+            P.dval[p] = make_float4(dv.x, dv.y, dv.z, o.w);
+        }
         const f3 ro = xyz(P.ro[p]);
         const f3 no = (ro + rd * hit_dist) + N * 0.0001f;
         st4(P.ro, p, no);
@@ -533,6 +611,39 @@ __global__ void __launch_bounds__(128, MT_TRAVERSE_MIN_BLOCKS) k_shadow(DevScene
     if (COUNT) flush_counts(cnt, W.pops, W.inner, W.tris);
 }
 
+// The per-sample value of a debug render mode (ProcessDebugRay,
+// Tracer.cpp:366-488) from the path's debug planes and light accumulators.
+__device__ __forceinline__ f3 debug_sample(const DevScene& S, const PathState& P, uint32_t p, f3 total_aces)
+{
+    const float4 v = P.dval[p];
+    const uint4 c = P.dcnt[p];
+    const bool hit = (c.x & 0x80000000u) != 0;
+    const f3 black = splat(0.0f);
+    switch (S.debug_mode) {
+        case MT_DEBUG_PRIMARY_BVH_TESTS: return hit ? splat(static_cast<float>(c.x & 0x7fffffffu)) : black;
+        case MT_DEBUG_TOTAL_BVH_TESTS: return hit ? splat(static_cast<float>(c.z)) : black;
+        case MT_DEBUG_PRIMARY_TRIANGLE_TESTS: return hit ? splat(static_cast<float>(c.y)) : black;
+        case MT_DEBUG_TOTAL_TRIANGLE_TESTS: return hit ? splat(static_cast<float>(c.w)) : black;
+        case MT_DEBUG_BOUNCES: return hit ? splat(v.w) : black;
+        case MT_DEBUG_DIRECT_ONLY: return aces(ld4(P.direct, p), S.exposure);
+        case MT_DEBUG_INDIRECT_ONLY: return aces(ld4(P.indirect, p) + ld4(P.sky, p), S.exposure);
+        case MT_DEBUG_EMISSION: return aces(ld4(P.emit, p), S.exposure);
+        case MT_DEBUG_ALBEDO:
+        case MT_DEBUG_METALLIC_ROUGHNESS:
+        case MT_DEBUG_GEOMETRIC_NORMAL:
+        case MT_DEBUG_SHADING_NORMAL:
+        case MT_DEBUG_COLOR_PER_MESH:
+        case MT_DEBUG_COLOR_PER_TRIANGLE:
+        case MT_DEBUG_DEPTH:
+        case MT_DEBUG_FIRST_HIT_FRESNEL:
+        case MT_DEBUG_FIRST_HIT_BRDF:
+        case MT_DEBUG_FIRST_HIT_PDF:
+        case MT_DEBUG_REFLECTED_DIRECTION: return xyz(v);
+        case MT_DEBUG_COLOR_PER_BOUNDING_VOLUME: return xyz(v);
+        default: return total_aces;
+    }
+}
+
 __global__ void __launch_bounds__(256) k_finalize(DevScene S, PathState P, BatchInfo B,
                                                   float* __restrict__ sr, float* __restrict__ sg,
                                                   float* __restrict__ sb, RecordBuffers R)
@@ -544,7 +655,8 @@ __global__ void __launch_bounds__(256) k_finalize(DevScene S, PathState P, Batch
             R.path[2 * p].y = total.y;
             R.path[2 * p].z = total.z;
         }
-        const f3 c = aces(total, S.exposure);
+        f3 c = aces(total, S.exposure);
+        if (P.dval) c = debug_sample(S, P, p, c);
         const uint64_t g = B.g0 + p;
         sr[g] = c.x;
         sg[g] = c.y;
@@ -598,6 +710,37 @@ __global__ void __launch_bounds__(256) k_resolve(const float* __restrict__ sr, c
         o[0] = r.x;
         o[1] = r.y;
         o[2] = r.z;
+    }
+}
+
+// ApplyHeatMapPostProcessing (Tracer.cpp:672-693): the maximum of the pixel
+// intensities (r+g+b)/3 (non-negative floats compare like their bit patterns),
+// then every pixel mapped to the ramp of Heatmap (Tracer.cpp:650-670) or grey.
+__global__ void k_debug_max(const float* __restrict__ img, uint64_t npix, uint32_t* max_bits)
+{
+    float m = 0.0f;
+    for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < npix;
+         i += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+        const float in = __fdiv_rn(__fadd_rn(__fadd_rn(img[3 * i], img[3 * i + 1]), img[3 * i + 2]), 3.0f);
+        m = fmaxf(m, in);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_down_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(max_bits, __float_as_uint(m));
+}
+
+__global__ void k_debug_heatmap(float* __restrict__ img, uint64_t npix, const uint32_t* max_bits, int colorful)
+{
+    const float maxI = __uint_as_float(*max_bits);
+    for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < npix;
+         i += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+        const float in = __fdiv_rn(__fadd_rn(__fadd_rn(img[3 * i], img[3 * i + 1]), img[3 * i + 2]), 3.0f);
+        const float t = maxI > 0.0f ? __fdiv_rn(in, maxI) : 0.0f;
+        f3 c = splat(t);
+        if (colorful) c = heatmap(t);
+        img[3 * i] = c.x;
+        img[3 * i + 1] = c.y;
+        img[3 * i + 2] = c.z;
     }
 }
 
@@ -730,7 +873,10 @@ cudaError_t launch_batch(const DevScene& S, const PathState& P, const ShadowQueu
         g_sh[0] = persistent_grid(k_shadow<false>, 128);
         g_sh[1] = persistent_grid(k_shadow<true>, 128);
     }
-    const bool count = prof && prof->counting;
+    const bool count = (prof && prof->counting) ||
+                       (P.dcnt && (S.debug_mode == MT_DEBUG_PRIMARY_BVH_TESTS || S.debug_mode == MT_DEBUG_TOTAL_BVH_TESTS ||
+                                   S.debug_mode == MT_DEBUG_PRIMARY_TRIANGLE_TESTS ||
+                                   S.debug_mode == MT_DEBUG_TOTAL_TRIANGLE_TESTS));
     unsigned long long* cnt = prof ? prof->d_counts : nullptr;
     auto begin = [&](int s) { if (prof) prof->begin(s, st); };
     auto end = [&](int s) { if (prof) prof->end(s, st); };
@@ -750,7 +896,7 @@ cudaError_t launch_batch(const DevScene& S, const PathState& P, const ShadowQueu
         k_shade<<<gw, 128, 0, st>>>(S, P, SQ, B, b, W.q[cur], W.q[cur ^ 1], W.counts, cur, R, NC);
         end(MT_STAGE_SHADE);
         begin(MT_STAGE_SHADOW);
-        if (count)
+        if (prof && prof->counting)
             k_shadow<true><<<g_sh[1], 128, 0, st>>>(S, P, SQ, W.counts, W.rays + 1, cnt ? cnt + 3 : nullptr, R);
         else
             k_shadow<false><<<g_sh[0], 128, 0, st>>>(S, P, SQ, W.counts, W.rays + 1, nullptr, R);
@@ -775,6 +921,29 @@ cudaError_t launch_batch(const DevScene& S, const PathState& P, const ShadowQueu
     end(MT_STAGE_FINALIZE);
     ++l;
     if (launches) *launches += l;
+    return cudaGetLastError();
+}
+
+bool debug_needs_post(int mode)
+{
+    switch (mode) {
+        case MT_DEBUG_PRIMARY_BVH_TESTS: case MT_DEBUG_TOTAL_BVH_TESTS: case MT_DEBUG_PRIMARY_TRIANGLE_TESTS:
+        case MT_DEBUG_TOTAL_TRIANGLE_TESTS: case MT_DEBUG_BOUNCES: case MT_DEBUG_FIREFLY_ELIMINATION:
+        case MT_DEBUG_DEPTH: case MT_DEBUG_FIRST_HIT_BRDF: case MT_DEBUG_PIXEL_STANDARD_DEVIATION: return true;
+        default: return false;
+    }
+}
+
+cudaError_t launch_debug_post(float* img, uint64_t npix, int mode, uint32_t* scratch, cudaStream_t st)
+{
+    if (!debug_needs_post(mode) || npix == 0) return cudaSuccess;
+    cudaError_t e = cudaMemsetAsync(scratch, 0, sizeof(uint32_t), st);
+    if (e != cudaSuccess) return e;
+    const unsigned grid = grid_for(npix, 256, 8);
+    k_debug_max<<<grid, 256, 0, st>>>(img, npix, scratch);
+    const bool colorful = !(mode == MT_DEBUG_DEPTH || mode == MT_DEBUG_FIRST_HIT_BRDF ||
+                            mode == MT_DEBUG_PIXEL_STANDARD_DEVIATION);
+    k_debug_heatmap<<<grid, 256, 0, st>>>(img, npix, scratch, colorful ? 1 : 0);
     return cudaGetLastError();
 }
 

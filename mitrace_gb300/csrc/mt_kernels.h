@@ -28,6 +28,11 @@ struct PathState {
     float4* sky;       // LightOutput::skyLight
     float4* hitA;      // world position xyz, world distance
     uint4* hitB;       // instance (MT_NO_HIT on miss), triangle, u bits, v bits
+    // debug render modes only (null otherwise): first-hit value rgb and the
+    // number of path steps (w); first-hit BVH / triangle tests (x has bit 31
+    // set when the first step hit), summed BVH / triangle tests of all steps
+    float4* dval = nullptr;
+    uint4* dcnt = nullptr;
 };
 
 // Shadow rays queued by the shade stage.
@@ -40,7 +45,8 @@ struct ShadowQueue {
 struct WaveBuffers {
     uint32_t* q[2];                // ping-pong queues of live path indices
     uint32_t* counts;              // [0],[1] queue sizes, [2] shadow-queue size,
-                                   // [3] extend / [4] shadow ray fetch counters
+                                   // [3] extend / [4] shadow ray fetch counters,
+                                   // [7] debug heatmap maximum (scratch)
     unsigned long long* rays;      // [0] extension rays, [1] shadow rays traced
     float* sr;                     // per-sample tonemapped R, sample-major in a band
     float* sg;
@@ -98,6 +104,10 @@ cudaError_t launch_batch(const DevScene& S, const PathState& P, const ShadowQueu
                          const RecordBuffers* rec = nullptr, const BatchExtra* extra = nullptr);
 cudaError_t launch_resolve(const DevScene& S, const WaveBuffers& W, uint32_t band_pix,
                            uint32_t pix_base, float* out, cudaStream_t st, Profiler* prof);
+// True when S.debug_mode ends with WaitForRender's heatmap post-processing.
+bool debug_needs_post(int mode);
+// Heatmap post-processing of a whole W*H image (scratch: one device word).
+cudaError_t launch_debug_post(float* img, uint64_t npix, int mode, uint32_t* scratch, cudaStream_t st);
 
 // Host BVH builder (mt_bvh.cpp).
 int build_bvh(const float* positions, uint32_t num_triangles, uint32_t max_triangles,

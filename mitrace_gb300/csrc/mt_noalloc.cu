@@ -81,6 +81,7 @@ extern "C" mt_status mt_render_rows_noalloc(mt_handle* h, uint32_t row0, uint32_
     if (internal_busy(h)) return internal_error(MT_ERR_STATE, "an asynchronous render is running");
     if (row0 >= row1 || row1 > S->height)
         return internal_error(MT_ERR_INVALID, "rows must satisfy row0 < row1 <= height");
+    if (S->debug_mode) return internal_error(MT_ERR_INVALID, "debug render modes need mt_render_device");
     const uint64_t band_pix = static_cast<uint64_t>(row1 - row0) * S->width;
     const uint64_t paths = band_pix * S->spp;
     if (paths > kMaxPaths)

@@ -78,7 +78,7 @@ __device__ __forceinline__ float tri_wave(float s)
     return fabsf(4.0f * f - 2.0f) - 1.0f;
 }
 
-// Lanes [0,36) (12 octaves per position axis) and [68,80).
+// Lanes [0,36) (12 octaves per position axis), [68,75) and [77,80).
 template <class Out>
 __device__ __forceinline__ void encode_part0(float4 f0, float4 f3, float4 f4, Out out)
 {
@@ -100,7 +100,7 @@ __device__ __forceinline__ void encode_part0(float4 f0, float4 f3, float4 f4, Ou
     out(73, f4.y);
     out(74, f4.z);
 #pragma unroll
-    for (int k = 75; k < 80; ++k) out(k, 1.0f);
+    for (int k = 77; k < 80; ++k) out(k, 1.0f);
 }
 
 // Real spherical harmonics of bands 0..3 of a unit vector (16 lanes from base).
@@ -126,12 +126,15 @@ __device__ __forceinline__ void sh16(float x, float y, float z, int base, Out ou
     out(base + 15, 0.59004358992664352f * x * (3.0f * yy - xx));
 }
 
-// Lanes [36,68): harmonics of wo and of the normal.
+// Lanes [36,68): harmonics of wo and of the normal; 75, 76: the bounce budget
+// left and the cut-off headroom.
 template <class Out>
 __device__ __forceinline__ void encode_part1(float4 f1, float4 f2, Out out)
 {
     sh16(f1.x, f1.y, f1.z, 36, out);
     sh16(f2.x, f2.y, f2.z, 52, out);
+    out(75, f1.w);
+    out(76, f2.w);
 }
 
 // Encodes the 16 rows [r0, r0+16) of a feature array into a warp's staging
@@ -156,9 +159,12 @@ __device__ __forceinline__ void stage_rows(const float4* __restrict__ feat, uint
         const bf16 z = __float2bfloat16_rn(0.0f);
         if (lane < 16) {
             for (int k = 0; k < 36; ++k) dst[k] = z;
-            for (int k = 68; k < 80; ++k) dst[k] = z;
+            for (int k = 68; k < 75; ++k) dst[k] = z;
+            for (int k = 77; k < 80; ++k) dst[k] = z;
         } else {
             for (int k = 36; k < 68; ++k) dst[k] = z;
+            dst[75] = z;
+            dst[76] = z;
         }
     }
 }
@@ -312,7 +318,7 @@ __global__ void __launch_bounds__(kInferWarps * 32) k_nrc_infer(const bf16* __re
     const uint32_t tiles = (n + 15) / 16;
     for (uint32_t tile = blockIdx.x * kInferWarps + warp; tile < tiles; tile += gridDim.x * kInferWarps) {
         const uint32_t r0 = tile * 16;
-        stage_rows(feat, 5, r0, n, nullptr, stg);
+        stage_rows(feat, PATHS ? 6 : 5, r0, n, nullptr, stg);
         __syncwarp();
         uint32_t ax[5][4];
         load_x_frags(stg, ax);
@@ -332,11 +338,11 @@ __global__ void __launch_bounds__(kInferWarps * 32) k_nrc_infer(const bf16* __re
                 const float v1 = half ? y[0][3] : y[0][1];
                 const float v2 = half ? c2b : c2a;
                 if (PATHS) {
-                    const float4* q = feat + 5ull * r;
-                    const uint32_t p = __float_as_uint(q[1].w);
+                    const float4 q = feat[6ull * r + 5];  // throughput, path index
+                    const uint32_t p = __float_as_uint(q.w);
                     const float4 a = P.indirect[p];
-                    P.indirect[p] = make_float4(a.x + q[2].w * fmaxf(v0, 0.0f), a.y + q[3].w * fmaxf(v1, 0.0f),
-                                                a.z + q[4].w * fmaxf(v2, 0.0f), a.w);
+                    P.indirect[p] = make_float4(a.x + q.x * fmaxf(v0, 0.0f), a.y + q.y * fmaxf(v1, 0.0f),
+                                                a.z + q.z * fmaxf(v2, 0.0f), a.w);
                 } else {
                     out[3ull * r + 0] = v0;
                     out[3ull * r + 1] = v1;
@@ -635,11 +641,11 @@ __global__ void k_nrc_targets(PathState P, NrcShade N, uint32_t n, uint32_t boun
         const float4 e = P.emit[p], d = P.direct[p], ind = P.indirect[p], s = P.sky[p];
         const float tot[3] = {((e.x + d.x) + ind.x) + s.x, ((e.y + d.y) + ind.y) + s.y, ((e.z + d.z) + ind.z) + s.z};
         for (uint32_t k = 0; k < bounces; ++k) {
-            float4* r = N.rec + (static_cast<uint64_t>(p) * bounces + k) * 6;
-            const float4 pre = r[5];
+            float4* r = N.rec + (static_cast<uint64_t>(p) * bounces + k) * 7;
+            const float4 pre = r[6];
             if (pre.w != 1.0f) break;  // vertices are recorded in bounce order
-            r[5].w = 0.0f;
-            const float cur[3] = {r[2].w, r[3].w, r[4].w};
+            r[6].w = 0.0f;
+            const float cur[3] = {r[5].x, r[5].y, r[5].z};
             const float prv[3] = {pre.x, pre.y, pre.z};
             float tg[3];
             bool ok = true;

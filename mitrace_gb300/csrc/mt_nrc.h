@@ -31,11 +31,11 @@ struct NrcShade {
     float rough_min = 0.3f;
     float lo[3] = {0, 0, 0};       // world box lower corner
     float inv_ext[3] = {1, 1, 1};  // 1 / world box extent
-    // QUERY: query records, 5 float4 each (the feature record of the header,
-    //        with f1.w = path index bits and f2.w, f3.w, f4.w = throughput rgb).
-    // TRAIN: vertex records of path p, bounce k at rec[(p * bounces + k) * 6]:
-    //        the 5 feature float4 (f2.w, f3.w, f4.w = throughput) and
-    //        (radiance collected before the vertex's NEE, 1 = recorded).
+    // QUERY: query records, 6 float4 each: the 5 feature float4 of the header
+    //        and (throughput rgb, path index bits).
+    // TRAIN: vertex records of path p, bounce k at rec[(p * bounces + k) * 7]:
+    //        the 6 float4 of a query record and (radiance collected before the
+    //        vertex's NEE, 1 = recorded).
     float4* rec = nullptr;
     uint32_t* count = nullptr;  // QUERY: queries appended
     // QUERY: bf16 forward weight blob; queries are also added to *total.

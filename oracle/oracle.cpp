@@ -941,6 +941,11 @@ struct PathStep {
     V3 hitPos, base, normal, energy, emission;
     float metallic, roughness;
     bool didHit;
+    // debug information (Tracer.hpp:46-53); a miss step keeps zeros here, where
+    // the reference leaves these members uninitialised
+    V3 geomN{0, 0, 0};
+    float brdfIntensity = 0.0f, pdf = 0.0f;
+    uint32_t bvhTests = 0, triTests = 0, triIndex = 0, bvIndex = 0, inst = 0;
     // kept for the adjoint replay
     uint32_t mat = 0;
     V2 uv{0.0f, 0.0f};
@@ -1003,6 +1008,12 @@ void generate_path(const orc_scene& s, Worker& w, Rng& rng, V3 o0, V3 d0)
         st.didHit = true;
         st.mat = in.material;
         st.uv = uv;
+        st.geomN = geomN;
+        st.bvhTests = hit.bvhTests;
+        st.triTests = hit.triTests;
+        st.bvIndex = hit.bv & 0xffffu;
+        st.triIndex = hit.tri & 0xffffu;
+        st.inst = hit.inst;
 
         const V3 view = -d;
         const float ps = specular_probability(view, st.normal, st.base, st.metallic);
@@ -1018,6 +1029,8 @@ void generate_path(const orc_scene& s, Worker& w, Rng& rng, V3 o0, V3 d0)
         const V3 brdf = eval_brdf(nd, view, st.normal, st.base, st.roughness, st.metallic);
         const float nl = gmax(dot(st.normal, nd), 0.0f);
         st.energy = (pdf > 0.0f) ? brdf * (nl / pdf) : v3(0.0f);
+        st.brdfIntensity = (brdf.x + brdf.y) + brdf.z;
+        st.pdf = pdf;
         st.nextDir = nd;
         st.facNext = (pdf > 0.0f) ? nl / pdf : 0.0f;
         w.path.push_back(st);
@@ -1029,8 +1042,12 @@ void generate_path(const orc_scene& s, Worker& w, Rng& rng, V3 o0, V3 d0)
     }
 }
 
+struct LightOut {
+    V3 emitted, direct, indirect, sky;
+};
+
 V3 process_ray_forward(const orc_scene& s, Worker& w, Rng& rng, V3 o, V3 d, float expo,
-                       V3* total_out = nullptr)
+                       V3* total_out = nullptr, LightOut* parts = nullptr)
 {
     const mt_config& cfg = s.cfg;
     generate_path(s, w, rng, o, d);
@@ -1103,7 +1120,114 @@ V3 process_ray_forward(const orc_scene& s, Worker& w, Rng& rng, V3 o, V3 d, floa
     }
     const V3 total = ((emitted + direct) + indirect) + sky;
     if (total_out) *total_out = total;
+    if (parts) *parts = {emitted, direct, indirect, sky};
     return aces(total, expo);
+}
+
+// RandomColorFromU16, Tracer.cpp:350-364
+V3 random_color_u16(uint32_t value)
+{
+    uint32_t x = value & 0xffffu;
+    x ^= x >> 7;
+    x *= 0x2C1B3C6Du;
+    x ^= x >> 12;
+    x *= 0x297A2D39u;
+    x ^= x >> 15;
+    const uint32_t v = x & 0xffffu;
+    return {static_cast<float>((v & 0x01C0u) >> 6) / 7.0f, static_cast<float>((v & 0x0038u) >> 3) / 7.0f,
+            static_cast<float>(v & 0x0007u) / 7.0f};
+}
+
+// Config::DebugMode values (src/CLI/Config.hpp:16-40)
+enum DebugMode {
+    DBG_NONE = 0, DBG_PRIMARY_BVH, DBG_TOTAL_BVH, DBG_PRIMARY_TRI, DBG_TOTAL_TRI, DBG_ALBEDO,
+    DBG_METALLIC_ROUGHNESS, DBG_GEOM_NORMAL, DBG_SHADING_NORMAL, DBG_DIRECT, DBG_INDIRECT, DBG_EMISSION,
+    DBG_COLOR_MESH, DBG_COLOR_TRIANGLE, DBG_COLOR_BV, DBG_BOUNCES, DBG_DEPTH, DBG_FRESNEL, DBG_BRDF, DBG_PDF,
+    DBG_REFLECTED, DBG_PIXEL_STDDEV, DBG_FIREFLY, DBG_COUNT
+};
+
+// ProcessDebugRay, Tracer.cpp:366-488.  The colour per mesh is keyed by the
+// instance index: the reference keys it by the low 16 bits of the
+// MeshInstance's address, which change from run to run.
+V3 process_debug_ray(const orc_scene& s, Worker& w, Rng& rng, V3 o, V3 d, float expo, int mode)
+{
+    LightOut lo;
+    const V3 total = process_ray_forward(s, w, rng, o, d, expo, nullptr, &lo);
+    const PathStep& f = w.path.front();
+    const bool hit = f.didHit;
+    const V3 black = v3(0.0f);
+    auto sum_steps = [&](bool tris) {
+        float acc = 0.0f;
+        for (const PathStep& st : w.path) acc = acc + static_cast<float>(tris ? st.triTests : st.bvhTests);
+        return acc;
+    };
+    switch (mode) {
+        case DBG_PRIMARY_BVH: return hit ? v3(static_cast<float>(f.bvhTests)) : black;
+        case DBG_TOTAL_BVH: return hit ? v3(sum_steps(false)) : black;
+        case DBG_PRIMARY_TRI: return hit ? v3(static_cast<float>(f.triTests)) : black;
+        case DBG_TOTAL_TRI: return hit ? v3(sum_steps(true)) : black;
+        case DBG_BOUNCES: return hit ? v3(static_cast<float>(w.path.size())) : black;
+        case DBG_ALBEDO: return hit ? f.base : black;
+        case DBG_METALLIC_ROUGHNESS: return hit ? V3{0.0f, f.metallic, f.roughness} : black;
+        case DBG_GEOM_NORMAL: return hit ? f.geomN * 0.5f + v3(0.5f) : black;
+        case DBG_SHADING_NORMAL: return hit ? f.normal * 0.5f + v3(0.5f) : black;
+        case DBG_DIRECT: return aces(lo.direct, expo);
+        case DBG_INDIRECT: return aces(lo.indirect + lo.sky, expo);
+        case DBG_EMISSION: return aces(lo.emitted, expo);
+        case DBG_COLOR_MESH: return hit ? random_color_u16(f.inst) : black;
+        case DBG_COLOR_TRIANGLE: return hit ? random_color_u16(f.triIndex) : black;
+        case DBG_COLOR_BV: return hit ? random_color_u16(f.bvIndex) : black;
+        case DBG_DEPTH: return hit ? v3(length(f.hitPos - o)) : black;
+        case DBG_FRESNEL: {
+            const V3 f0 = base_reflectivity(f.base, f.metallic);
+            const float c = dot(f.normal, -d);
+            return hit ? fresnel_schlick(gmax(c, 0.0f), f0) : black;
+        }
+        case DBG_BRDF: return hit ? v3(f.brdfIntensity) : black;
+        case DBG_PDF: return hit ? v3(f.pdf) : black;
+        case DBG_REFLECTED: return w.path.size() > 1 ? w.path[1].rayD * 0.5f + v3(0.5f) : black;
+        default: return total;
+    }
+}
+
+// Heatmap, Tracer.cpp:650-670 (glm::mix(a, b, f) = a * (1 - f) + b * f)
+V3 heatmap(float t)
+{
+    t = gclamp(t, 0.0f, 1.0f);
+    static const V3 colors[5] = {{0, 0, 1}, {0, 1, 1}, {0, 1, 0}, {1, 1, 0}, {1, 0, 0}};
+    const float x = t * 4.0f;
+    const int i = std::min(static_cast<int>(x), 3);
+    const float fr = x - static_cast<float>(i);
+    const float r = 1.0f - fr;
+    const V3 a = colors[i], b = colors[i + 1];
+    return {a.x * r + b.x * fr, a.y * r + b.y * fr, a.z * r + b.z * fr};
+}
+
+// ApplyDebugPostProcessing, Tracer.cpp:695-716: heatmap modes map the image's
+// intensity (r+g+b)/3, divided by its maximum, to a colour ramp or to grey.
+void debug_postprocess(float* rgb, uint32_t W, uint32_t H, int mode)
+{
+    bool colorful;
+    switch (mode) {
+        case DBG_PRIMARY_BVH: case DBG_TOTAL_BVH: case DBG_PRIMARY_TRI: case DBG_TOTAL_TRI:
+        case DBG_BOUNCES: case DBG_FIREFLY: colorful = true; break;
+        case DBG_DEPTH: case DBG_BRDF: case DBG_PIXEL_STDDEV: colorful = false; break;
+        default: return;
+    }
+    const size_t n = static_cast<size_t>(W) * H;
+    float maxI = 0.0f;
+    for (size_t i = 0; i < n; ++i) {
+        const float in = ((rgb[3 * i] + rgb[3 * i + 1]) + rgb[3 * i + 2]) / 3.0f;
+        maxI = std::max(maxI, in);
+    }
+    for (size_t i = 0; i < n; ++i) {
+        const float in = ((rgb[3 * i] + rgb[3 * i + 1]) + rgb[3 * i + 2]) / 3.0f;
+        const float t = maxI > 0.0f ? in / maxI : 0.0f;
+        const V3 c = colorful ? heatmap(t) : v3(t);
+        rgb[3 * i] = c.x;
+        rgb[3 * i + 1] = c.y;
+        rgb[3 * i + 2] = c.z;
+    }
 }
 
 // CleanupFireflies (Tracer.cpp:490-548) + average (Tracer.cpp:598-600)
@@ -1740,7 +1864,9 @@ int orc_render(const orc_scene* s, int rng_mode, int threads, uint32_t row0, uin
                         const float v = bv + rng.uniform(0.0f, pxH, 0, SLOT_JITTER, 1);
                         V3 o, d;
                         camera_ray(s->cam, u, v, aspect, o, d);
-                        sampleBuf.push_back(process_ray_forward(*s, w, rng, o, d, expo));
+                        sampleBuf.push_back(cfg.debug_mode
+                                                ? process_debug_ray(*s, w, rng, o, d, expo, cfg.debug_mode)
+                                                : process_ray_forward(*s, w, rng, o, d, expo));
                         ++localSamples;
                     }
                     const V3 c = resolve_pixel(sampleBuf, cfg.firefly_enable != 0,
@@ -1761,6 +1887,8 @@ int orc_render(const orc_scene* s, int rng_mode, int threads, uint32_t row0, uin
     for (auto& th : pool) th.join();
     if (rays_out) *rays_out = rays.load();
     if (samples_out) *samples_out = samples.load();
+    // WaitForRender's post-processing needs the whole image
+    if (cfg.debug_mode && row0 == 0 && row1 == H) debug_postprocess(rgb_out, W, H, cfg.debug_mode);
     return MT_OK;
 }
 

@@ -43,7 +43,9 @@ def encode(feat):
     out[:, 68] = f[:, 0, 3]
     out[:, 69:72] = f[:, 3, :3]
     out[:, 72:75] = f[:, 4, :3]
-    out[:, 75:80] = 1.0
+    out[:, 75] = f[:, 1, 3]
+    out[:, 76] = f[:, 2, 3]
+    out[:, 77:80] = 1.0
     return out
 
 
@@ -69,6 +71,8 @@ def random_features(n, seed=0):
     m = rng.uniform(0, 1, (n, 1))
     f[:, 3, :3] = base * (1 - m)
     f[:, 4, :3] = 0.04 * (1 - m) + base * m
+    f[:, 1, 3] = rng.integers(0, 5, n) / 4.0  # bounce budget left
+    f[:, 2, 3] = rng.uniform(0, 1, n)        # cut-off headroom
     return f.reshape(n, 20)
 
 

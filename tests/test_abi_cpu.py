@@ -94,8 +94,9 @@ def test_argument_errors_are_status_codes():
     scene, _ = mt.box_room()
     ps = mt.PackedScene(scene)
     assert A.lib.mt_create(ps.ptr(), C.byref(cfg), C.byref(h)) == A.MT_ERR_INVALID
-    cfg = mt.make_config(debug_mode=3)
-    assert A.lib.mt_create(ps.ptr(), C.byref(cfg), C.byref(h)) == A.MT_ERR_INVALID
+    for bad in (-1, 23):  # Config::DebugMode has 23 values
+        cfg = mt.make_config(debug_mode=bad)
+        assert A.lib.mt_create(ps.ptr(), C.byref(cfg), C.byref(h)) == A.MT_ERR_INVALID
     assert A.lib.mt_start(None) == A.MT_ERR_INVALID
     assert A.lib.mt_is_done(None) == 0
     assert A.lib.mt_brdf_batch(None, 4, None) == A.MT_ERR_INVALID

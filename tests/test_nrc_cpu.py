@@ -57,8 +57,10 @@ def test_triangle_octaves():
     eg, eh = ref.encode(g.reshape(-1, 20)), ref.encode(h.reshape(-1, 20))
     # (x + 1/2 rounds away up to one low bit of x, which octave 11 scales by 2^13)
     np.testing.assert_allclose(eg[ok, 1:12], eh[ok, 1:12], atol=2e-3)
-    np.testing.assert_array_equal(e[:, 75:80], 1.0)
+    np.testing.assert_array_equal(e[:, 77:80], 1.0)
     np.testing.assert_array_equal(e[:, 69:75], f[:, 3:5, :3].reshape(-1, 6))
+    np.testing.assert_array_equal(e[:, 75], f[:, 1, 3])
+    np.testing.assert_array_equal(e[:, 76], f[:, 2, 3])
 
 
 def test_relative_l2_gradient_closed_form():
