@@ -135,23 +135,47 @@ def test_cache_hooks_leave_plain_paths_unchanged():
 
 
 def test_cached_frames_converge_near_plain_render():
-    scene, cfg = mt.box_room(width=64, height=64, samples=256, seed=2)
+    """Box room at +15 EV, where the per-sample ACES curve is linear (so the
+    cache's expectation and the plain estimator's agree; at normal exposure the
+    per-sample tonemap of a random suffix and of its mean differ by the Jensen
+    gap of the curve).  The cached frames' mean brightness matches the plain
+    render within 3% and their relative error is well below that of a render
+    whose cache returns zero (paths cut at the query vertex)."""
+    def room(spp):
+        scene, cfg = mt.box_room(width=64, height=64, samples=spp, seed=2)
+        cfg.ev_exposure = 15.0
+        return scene, cfg
+
     st = torch.cuda.current_stream().cuda_stream
+    scene, cfg = room(1024)
     plain = torch.zeros((cfg.height, cfg.width, 3), device="cuda")
     with mt.Tracer(scene, cfg) as tr:
         tr.render_device(plain.data_ptr(), st)
         torch.cuda.synchronize()
-    scene, cfg = mt.box_room(width=64, height=64, samples=4, seed=2)
-    acc = torch.zeros_like(plain)
-    with mt.Tracer(scene, cfg) as tr:
-        tr.nrc_enable(train_paths=16384, train_batch=4096, spp=4)
-        for _ in range(30):  # training only
-            tr.nrc_frame(0, 0, st)
-        for k in range(64):
-            tr.nrc_frame(acc.data_ptr(), k, st)
-        torch.cuda.synchronize()
-    a, p = acc.cpu().numpy().astype(np.float64), plain.cpu().numpy().astype(np.float64)
+    p = plain.cpu().numpy().astype(np.float64)
+    eps = (0.1 * p.mean()) ** 2
+
+    def cached(zero):
+        scene, cfg = room(4)
+        acc = torch.zeros_like(plain)
+        with mt.Tracer(scene, cfg) as tr:
+            tr.nrc_enable(train_paths=16384, train_batch=4096, spp=4, train_steps=8)
+            if zero:
+                tr.nrc_set_params(np.zeros(A.MT_NRC_PARAMS, np.float32))
+            for _ in range(0 if zero else 32):  # training only
+                tr.nrc_frame(0, 0, st)
+            for k in range(32):
+                tr.nrc_frame(acc.data_ptr(), k, st)
+            torch.cuda.synchronize()
+            stats = tr.nrc_get_stats()
+        return acc.cpu().numpy().astype(np.float64), stats
+
+    a, stats = cached(False)
+    z, _ = cached(True)
     assert np.all(np.isfinite(a))
-    rel = float(((a - p) ** 2 / (p * p + 1e-2)).mean())
-    assert rel < 0.02, rel
-    assert abs(a.mean() - p.mean()) <= 0.05 * p.mean(), (a.mean(), p.mean())
+    assert stats["frames"] == 64 and stats["queries"] > 0 and stats["train_samples"] > 0
+    assert np.isfinite(stats["train_loss"])
+    rel = float(((a - p) ** 2 / (p * p + eps)).mean())
+    rel0 = float(((z - p) ** 2 / (p * p + eps)).mean())
+    assert abs(a.mean() / p.mean() - 1) < 0.03, (a.mean(), p.mean())
+    assert rel < 0.5 * rel0, (rel, rel0)
