@@ -50,6 +50,30 @@ class RenderBuffer {
     float* Data() { return pixels_.data(); }
     const float* Data() const { return pixels_.data(); }
 
+    // GetPixelsRGB8 / SaveToFilePNG / SaveToFileHDR (RenderBuffer.cpp:37-84):
+    // bytes are clamp(v * 255, 0, 255) truncated; the HDR file holds the floats.
+    std::vector<uint8_t> GetPixelsRGB8() const
+    {
+        std::vector<uint8_t> out(pixels_.size());
+        for (size_t i = 0; i < pixels_.size(); ++i) {
+            float v = pixels_[i] * 255.0f;
+            v = v < 0.0f ? 0.0f : (v > 255.0f ? 255.0f : v);
+            out[i] = static_cast<uint8_t>(v);
+        }
+        return out;
+    }
+    void SaveToFilePNG(const std::string& filename) const
+    {
+        const std::vector<uint8_t> rgb = GetPixelsRGB8();
+        if (mt_write_png(filename.c_str(), rgb.data(), width_, height_) != MT_OK)
+            throw std::runtime_error("Failed to save image to file");
+    }
+    void SaveToFileHDR(const std::string& filename) const
+    {
+        if (mt_write_hdr(filename.c_str(), pixels_.data(), width_, height_) != MT_OK)
+            throw std::runtime_error("Failed to save image to file");
+    }
+
    private:
     unsigned width_, height_;
     std::vector<float> pixels_;

@@ -484,6 +484,21 @@ mt_status mt_bvh_build(const float* positions, uint32_t num_triangles, uint32_t 
 void mt_bvh_free(mt_bvh_node* nodes, uint32_t* indices);
 
 /* ------------------------------------------------------------------------ */
+/* Image output (RenderBuffer::GetPixelsRGB8 / SaveToFile*,                  */
+/* src/Tracer/RenderBuffer.cpp:37-84).                                      */
+/* ------------------------------------------------------------------------ */
+
+/* Device: W*H*3 floats -> W*H*3 bytes, clamp(v * 255, 0, 255) truncated, as
+ * FloatToU8 does (RenderBuffer.cpp:37-40).  Enqueued on cuda_stream. */
+mt_status mt_image_rgb8(const float* d_rgb, uint32_t width, uint32_t height, uint8_t* d_rgb8,
+                        void* cuda_stream);
+/* Host: an 8-bit RGB PNG of rgb8 (rows top to bottom, as the RenderBuffer). */
+mt_status mt_write_png(const char* path, const uint8_t* rgb8, uint32_t width, uint32_t height);
+/* Host: a Radiance .hdr (RGBE) of the float image, as SaveToFileHDR writes the
+ * RenderBuffer's (tonemapped) floats. */
+mt_status mt_write_hdr(const char* path, const float* rgb, uint32_t width, uint32_t height);
+
+/* ------------------------------------------------------------------------ */
 /* Diagnostics.                                                             */
 /* ------------------------------------------------------------------------ */
 

@@ -23,7 +23,7 @@ from .scenes import (
     incoherent_rays,
     scene_bounds,
 )
-from .tracer import Tracer, Stats, brdf_batch, bvh_build, nrc_encode_device
+from .tracer import Tracer, Stats, brdf_batch, bvh_build, image_rgb8_device, nrc_encode_device, write_hdr, write_png
 
 __all__ = [
     "MTError",
@@ -46,4 +46,7 @@ __all__ = [
     "brdf_batch",
     "bvh_build",
     "nrc_encode_device",
+    "image_rgb8_device",
+    "write_png",
+    "write_hdr",
 ]

@@ -283,6 +283,9 @@ PROTOTYPES = [
     ("mt_bvh_build", C.c_int, [_VP, C.c_uint32, C.c_uint32, C.c_uint32, C.POINTER(C.POINTER(mt_bvh_node)),
                                C.POINTER(C.c_uint32), C.POINTER(C.POINTER(C.c_uint32)), C.POINTER(C.c_uint32)]),
     ("mt_bvh_free", None, [_VP, _VP]),
+    ("mt_image_rgb8", C.c_int, [_VP, C.c_uint32, C.c_uint32, _VP, _VP]),
+    ("mt_write_png", C.c_int, [C.c_char_p, _VP, C.c_uint32, C.c_uint32]),
+    ("mt_write_hdr", C.c_int, [C.c_char_p, _VP, C.c_uint32, C.c_uint32]),
     ("mt_last_error", C.c_char_p, []),
     ("mt_abi_version", C.c_int, []),
     ("mt_kernel_launches", C.c_uint64, [_VP]),

@@ -31,7 +31,7 @@ NVCC_FLAGS = [
     "-Xcompiler",
     "-fPIC,-ffp-contract=off,-Wall",
 ]
-SOURCES = ["mt_api.cu", "mt_kernels.cu", "mt_bvh.cpp", "mt_noalloc.cu", "mt_adjoint.cu", "mt_nrc.cu"]
+SOURCES = ["mt_api.cu", "mt_kernels.cu", "mt_bvh.cpp", "mt_noalloc.cu", "mt_adjoint.cu", "mt_nrc.cu", "mt_image.cu"]
 
 
 def nvcc_path() -> str:

@@ -157,6 +157,26 @@ def brdf_batch(q: np.ndarray) -> np.ndarray:
     return out
 
 
+def image_rgb8_device(rgb_ptr: int, width: int, height: int, out_ptr: int, stream_ptr: int = 0):
+    """FloatToU8 of a device image (W*H*3 floats -> bytes) on the GPU."""
+    A.check(A.lib.mt_image_rgb8(C.c_void_p(rgb_ptr), width, height, C.c_void_p(out_ptr), C.c_void_p(stream_ptr)),
+            "mt_image_rgb8")
+
+
+def write_png(path, rgb8: np.ndarray):
+    """Writes an (H, W, 3) uint8 image as PNG."""
+    a = np.ascontiguousarray(rgb8, dtype=np.uint8)
+    A.check(A.lib.mt_write_png(str(path).encode(), a.ctypes.data_as(C.c_void_p), a.shape[1], a.shape[0]),
+            "mt_write_png")
+
+
+def write_hdr(path, rgb: np.ndarray):
+    """Writes an (H, W, 3) float32 image as Radiance HDR."""
+    a = np.ascontiguousarray(rgb, dtype=np.float32)
+    A.check(A.lib.mt_write_hdr(str(path).encode(), a.ctypes.data_as(C.c_void_p), a.shape[1], a.shape[0]),
+            "mt_write_hdr")
+
+
 def nrc_encode_device(feat_ptr: int, n: int, out_ptr: int, stream_ptr: int = 0):
     """The radiance cache's FP32 input encoding: n x 20 features -> n x 80 (device buffers)."""
     A.check(A.lib.mt_nrc_encode(C.c_void_p(feat_ptr), n, C.c_void_p(out_ptr), C.c_void_p(stream_ptr)),

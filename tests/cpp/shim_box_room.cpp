@@ -20,7 +20,7 @@ static void quad(std::vector<float>& p, std::vector<float>& n, const float a[3],
     }
 }
 
-int main()
+int main(int argc, char** argv)
 {
     std::vector<float> pos, nrm;
     const float f0[3] = {-1, 0, -1}, f1[3] = {-1, 0, 1}, f2[3] = {1, 0, 1}, f3[3] = {1, 0, -1}, up[3] = {0, 1, 0};
@@ -84,6 +84,10 @@ int main()
                 buffer->GetPixel(x, y, c);
                 for (int k = 0; k < 3; ++k) m[k] += c[k] / (64.0 * 64.0);
             }
+        if (argc > 1) {  // RenderBuffer::SaveToFilePNG / SaveToFileHDR
+            buffer->SaveToFilePNG(std::string(argv[1]) + ".png");
+            buffer->SaveToFileHDR(std::string(argv[1]) + ".hdr");
+        }
         std::printf("ok %.6f %.6f %.6f %zu %zu %.3f\n", m[0], m[1], m[2], st.rays, st.samples, st.progress);
     } catch (const std::exception& e) {
         std::printf("error %s\n", e.what());

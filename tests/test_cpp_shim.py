@@ -24,7 +24,7 @@ def test_shim_compiles(tmp_path):
 
 @pytest.mark.gpu
 def test_shim_renders(tmp_path):
-    out = subprocess.run([str(build(tmp_path))], capture_output=True, text=True, timeout=300)
+    out = subprocess.run([str(build(tmp_path)), str(tmp_path / "img")], capture_output=True, text=True, timeout=300)
     assert out.returncode == 0, out.stdout + out.stderr
     f = out.stdout.split()
     assert f[0] == "ok"
@@ -32,3 +32,8 @@ def test_shim_renders(tmp_path):
     rays, samples, progress = int(f[4]), int(f[5]), float(f[6])
     assert samples == 64 * 64 * 16 and rays > samples and progress == 1.0
     assert 0.05 < r < 1.0 and abs(r - g) < 1e-3
+    from mitrace_gb300 import gltf
+
+    png = gltf.decode_png((tmp_path / "img.png").read_bytes())
+    assert png.shape == (64, 64, 3) and abs(png[..., 0].mean() / 255.0 - r) < 0.01
+    assert (tmp_path / "img.hdr").stat().st_size > 64 * 64 * 4
