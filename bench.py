@@ -268,6 +268,100 @@ def microbench(a, dev, peak):
     return out
 
 
+# --------------------------------------------------------------------------- radiance cache kernels
+def nrc_microbench(dev):
+    """The cache's tensor-core kernels alone: inference over 1920x1080x4
+    feature records (one frame's worth of queries at most) and one training
+    step of 16,384 rows (forward, backward through the activations, weight
+    gradient, Adam).  Algorithmic flop: 2 * 17,600 per row forward; a training
+    row adds the backward data pass (2 * 12,480: no input gradient for the
+    first layer) and the weight gradient (2 * 17,600).  CUDA events on the
+    launching stream, median of 5 after warm-up."""
+    import numpy as np
+    import torch
+
+    import mitrace_gb300 as mt
+    from mitrace_gb300 import _abi as A
+
+    peak = None
+    if PEAKS_FILE.exists():
+        peak = float(json.loads(PEAKS_FILE.read_text())["bf16_tflops"])
+    stream = torch.cuda.current_stream(dev)
+    scene, cfg = mt.box_room(width=64, height=64, samples=1)
+    out = {}
+    with mt.Tracer(scene, cfg) as tr:
+        tr.nrc_enable()
+        rng = np.random.default_rng(0)
+        n = 1920 * 1080 * 4
+        f = np.zeros((n, 5, 4), np.float32)
+        f[:, 0, :] = rng.random((n, 4))
+        v = rng.normal(size=(n, 2, 3))
+        f[:, 1:3, :3] = v / np.linalg.norm(v, axis=2, keepdims=True)
+        f[:, 3:5, :3] = rng.random((n, 2, 3))
+        feat = torch.from_numpy(f.reshape(n, 20)).to(dev)
+        y = torch.empty((n, 3), device=dev)
+
+        def timed(fn):
+            fn()
+            ms = []
+            for _ in range(5):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                fn()
+                e1.record(stream)
+                torch.cuda.synchronize()
+                ms.append(e0.elapsed_time(e1))
+            return statistics.median(ms)
+
+        t = timed(lambda: tr.nrc_infer_device(feat.data_ptr(), n, y.data_ptr(), stream.cuda_stream))
+        fl = 2.0 * A.MT_NRC_PARAMS * n
+        out["infer"] = {"rows": n, "ms": t, "tflops": fl / t / 1e9, "mqueries_s": n / t / 1e3}
+        rows = 16384
+        tgt = torch.rand((rows, 3), device=dev)
+        t = timed(lambda: tr.nrc_train_step_device(feat.data_ptr(), tgt.data_ptr(), rows, 0, 0, stream.cuda_stream))
+        fl = (2.0 * A.MT_NRC_PARAMS * 2 + 2.0 * (3 * 64 * 64 + 64 * 3)) * rows
+        out["train_step"] = {"rows": rows, "ms": t, "tflops": fl / t / 1e9}
+    if peak:
+        for k in ("infer", "train_step"):
+            out[k]["frac_of_measured_bf16"] = out[k]["tflops"] / peak
+        out["peak_bf16_tflops"] = peak
+    return out
+
+
+def adjoint_bench(dev):
+    """mt_render_grad on the inverse-materials scene (7x7 material grid, 512x512,
+    64 spp, 512^2 RGB32F albedo texture): one gradient evaluation = the forward
+    render plus the path replay and the adjoint, timed with CUDA events."""
+    import numpy as np
+    import torch
+
+    import mitrace_gb300 as mt
+
+    stream = torch.cuda.current_stream(dev)
+    scene, cfg = mt.scenes.adjoint_scene()
+    nm, nl = len(scene.materials), len(scene.lights)
+    nt = mt.scenes.num_grad_texels(scene)
+    target = torch.full((cfg.height, cfg.width, 3), 0.3, device=dev)
+    bufs = [torch.zeros(k, device=dev) for k in (cfg.height * cfg.width * 3, 1, nm * 3, nm, nm, max(nl, 1), max(nt, 1))]
+    ms = []
+    with mt.Tracer(scene, cfg) as tr:
+        for i in range(4):
+            for b in bufs[2:]:
+                b.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            tr.render_grad_device(target.data_ptr(), *[b.data_ptr() for b in bufs], stream.cuda_stream)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            if i:
+                ms.append(e0.elapsed_time(e1))
+    t = statistics.median(ms)
+    samples = cfg.width * cfg.height * cfg.samples
+    return {"workload": f"adjoint_material_grid_{cfg.width}x{cfg.height}_{cfg.samples}spp",
+            "parameters": nm * 5 + nl + nt, "ms_per_gradient": t, "msamples_per_s": samples / t / 1e3,
+            "loss": float(bufs[1].item())}
+
+
 # --------------------------------------------------------------------------- GPU arm
 def run_ours(a):
     import ctypes as C
@@ -434,6 +528,10 @@ def run_ours(a):
     if not a.no_microbench:
         torch.cuda.empty_cache()
         line["incoherent"] = microbench(a, dev, peak)
+        torch.cuda.empty_cache()
+        line["nrc_kernels"] = nrc_microbench(dev)
+        torch.cuda.empty_cache()
+        line["adjoint"] = adjoint_bench(dev)
     if not a.no_cpu_baseline:
         cb = cpu_baseline(scene, cfg, a.cpu_seconds)
         line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
