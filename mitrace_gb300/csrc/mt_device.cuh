@@ -291,11 +291,12 @@ __device__ __forceinline__ void trace_persistent(const DevScene& S, Work& W, uin
     int sp = 0;
     bool pending = false;
     uint32_t pfirst = 0, pcount = 0, pnode = 0;
-    // stack entry: node, its two child words (a, b) and its box distance; the
-    // child words ride along from the parent's loads, so a pop needs no load
-    // of the popped node itself
-    uint32_t stk_node[MT_STACK_SIZE], stk_a[MT_STACK_SIZE], stk_b[MT_STACK_SIZE];
+    uint32_t stk_node[MT_STACK_SIZE];
     float stk_dist[MT_STACK_SIZE];
+    // child words (a, b) of the entry last pushed at top_sp: the near child is
+    // pushed last and usually popped next, so its words need no reload
+    int top_sp = -1;
+    uint32_t top_a = 0, top_b = 0;
 
     while (true) {
         // A. lanes without a ray take the next ones
@@ -412,10 +413,11 @@ __device__ __forceinline__ void trace_persistent(const DevScene& S, Work& W, uin
                 if (m.has_bvh) {
                     const float4 a = __ldg(nodes + 0), b = __ldg(nodes + 1);
                     stk_node[0] = 0;
-                    stk_a[0] = f2u(a.w);
-                    stk_b[0] = f2u(b.w);
                     stk_dist[0] = slab(lo, linv, xyz(a), xyz(b));
                     sp = 1;
+                    top_sp = 0;
+                    top_a = f2u(a.w);
+                    top_b = f2u(b.w);
                 } else {
                     pending = true;
                     pfirst = 0;
@@ -429,11 +431,13 @@ __device__ __forceinline__ void trace_persistent(const DevScene& S, Work& W, uin
         if (in_inst && !pending && sp > 0) {
             --sp;
             const uint32_t ni = stk_node[sp];
-            const uint32_t na = stk_a[sp];
-            const uint32_t nb = stk_b[sp];
             const float nd = stk_dist[sp];
+            const bool cached = sp == top_sp;
+            top_sp = -1;
             if (COUNT) ++h.bvh_tests;
             if (!(nd < 0.0f) && !(nd > __fadd_rn(h.t, 0.1f))) {
+                const uint32_t na = cached ? top_a : f2u(__ldg(&nodes[2 * ni].w));
+                const uint32_t nb = cached ? top_b : f2u(__ldg(&nodes[2 * ni + 1].w));
                 if (na & MT_BVH_LEAF_BIT) {
                     pending = true;
                     pfirst = na & ~MT_BVH_LEAF_BIT;
@@ -451,27 +455,29 @@ __device__ __forceinline__ void trace_persistent(const DevScene& S, Work& W, uin
                     if (sp + 2 > MT_STACK_SIZE) {
                         atomicOr(S.error_flag, MT_ERRBIT_STACK);
                         sp = 0;
-                    } else {
-                        // near child pushed last (popped first)
-                        const bool a_first = pa && pb && !(da < db);
-                        auto push = [&](uint32_t n, float4 x0, float4 x1, float dd) {
-                            stk_node[sp] = n;
-                            stk_a[sp] = f2u(x0.w);
-                            stk_b[sp] = f2u(x1.w);
-                            stk_dist[sp] = dd;
-                            ++sp;
-                        };
-                        if (pa && pb && !a_first) {
-                            push(nb, b0, b1, db);
-                            push(na, a0, a1, da);
-                        } else if (pa && pb) {
-                            push(na, a0, a1, da);
-                            push(nb, b0, b1, db);
-                        } else if (pa) {
-                            push(na, a0, a1, da);
-                        } else if (pb) {
-                            push(nb, b0, b1, db);
+                    } else if (pa && pb) {
+                        if (da < db) {
+                            stk_node[sp] = nb; stk_dist[sp] = db; ++sp;
+                            stk_node[sp] = na; stk_dist[sp] = da; ++sp;
+                            top_a = f2u(a0.w);
+                            top_b = f2u(a1.w);
+                        } else {
+                            stk_node[sp] = na; stk_dist[sp] = da; ++sp;
+                            stk_node[sp] = nb; stk_dist[sp] = db; ++sp;
+                            top_a = f2u(b0.w);
+                            top_b = f2u(b1.w);
                         }
+                        top_sp = sp - 1;
+                    } else if (pa) {
+                        stk_node[sp] = na; stk_dist[sp] = da; ++sp;
+                        top_a = f2u(a0.w);
+                        top_b = f2u(a1.w);
+                        top_sp = sp - 1;
+                    } else if (pb) {
+                        stk_node[sp] = nb; stk_dist[sp] = db; ++sp;
+                        top_a = f2u(b0.w);
+                        top_b = f2u(b1.w);
+                        top_sp = sp - 1;
                     }
                 }
             }

@@ -206,7 +206,7 @@ __device__ __forceinline__ void flush_counts(unsigned long long* cnt, uint32_t p
 }
 
 // Extension rays of the live paths (queue q) -> hit records per path.
-template <bool COUNT>
+template <bool COUNT, bool DBG>
 struct ExtendWork {
     PathState P;
     const uint32_t* q;
@@ -236,7 +236,7 @@ struct ExtendWork {
         } else {
             P.hitB[p] = make_uint4(MT_NO_HIT, 0u, 0u, 0u);
         }
-        if (P.dcnt) {
+        if (DBG && P.dcnt) {
             // PathStep debug counters (Tracer.cpp:171-175); they are the winning
             // instance's (COUNT traversals only), a miss step adds nothing
             float4 v = P.dval[p];
@@ -262,7 +262,7 @@ struct ExtendWork {
     }
 };
 
-template <bool COUNT>
+template <bool COUNT, bool DBG>
 __global__ void __launch_bounds__(128, MT_TRAVERSE_MIN_BLOCKS) k_extend(DevScene S, PathState P,
                                                 const uint32_t* __restrict__ q,
                                                 uint32_t* counts, int cur,
@@ -276,7 +276,7 @@ __global__ void __launch_bounds__(128, MT_TRAVERSE_MIN_BLOCKS) k_extend(DevScene
         counts[4] = 0;  // ray fetch counter of this bounce's shadow stage
         atomicAdd(rays, static_cast<unsigned long long>(n));
     }
-    ExtendWork<COUNT> W{P, q, n, 0, 0, 0, 0, S.debug_mode};
+    ExtendWork<COUNT, DBG> W{P, q, n, 0, 0, 0, 0, S.debug_mode};
     trace_persistent<COUNT, false>(S, W, &counts[3]);
     if (COUNT) flush_counts(cnt, W.pops, W.inner, W.tris);
 }
@@ -291,6 +291,9 @@ __device__ __forceinline__ void st4(float4* p, uint32_t i, f3 v, float w = 0.0f)
     p[i] = make_float4(v.x, v.y, v.z, w);
 }
 
+// HOOKS: the radiance-cache and debug-mode code paths; the plain render runs
+// the variant without them.
+template <bool HOOKS>
 __global__ void __launch_bounds__(128) k_shade(DevScene S, PathState P, ShadowQueue SQ,
                                                BatchInfo B, uint32_t bounce,
                                                const uint32_t* __restrict__ q,
@@ -355,7 +358,7 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, PathState P, ShadowQu
         const f3 emit_now = ld4(P.emit, p) + (cur_e * S.emission_base) * mp.emission;
         st4(P.emit, p, emit_now);
         float seen_diffuse = 0.0f;
-        if (NC.mode != MT_NRC_OFF) {
+        if (HOOKS && NC.mode != MT_NRC_OFF) {
             // Radiance-cache feature record of this vertex (mt_nrc.h)
             seen_diffuse = P.prev[p].w;
             const bool query = NC.mode == MT_NRC_QUERY && bounce >= 1 && seen_diffuse != 0.0f;
@@ -464,7 +467,7 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, PathState P, ShadowQu
         }
 
         // First-hit debug values (ProcessDebugRay, Tracer.cpp:411-482)
-        const bool dbg0 = P.dval && bounce == 0;
+        const bool dbg0 = HOOKS && P.dval && bounce == 0;
         if (dbg0) {
             f3 dv = splat(0.0f);
             bool set = true;
@@ -866,17 +869,15 @@ cudaError_t launch_batch(const DevScene& S, const PathState& P, const ShadowQueu
     const NrcShade NC = X.nrc ? *X.nrc : NrcShade{};
     BatchInfo B{g0, n, band_pix, pix_base, X.sample_base, X.scatter_mul, X.scatter_add};
     const unsigned gw = grid_for(n, 128, 16);
-    static unsigned g_ext[2] = {0, 0}, g_sh[2] = {0, 0};
+    static unsigned g_ext[3] = {0, 0, 0}, g_sh[2] = {0, 0};
     if (!g_ext[0]) {
-        g_ext[0] = persistent_grid(k_extend<false>, 128);
-        g_ext[1] = persistent_grid(k_extend<true>, 128);
+        g_ext[0] = persistent_grid(k_extend<false, false>, 128);
+        g_ext[1] = persistent_grid(k_extend<true, false>, 128);
+        g_ext[2] = persistent_grid(k_extend<true, true>, 128);
         g_sh[0] = persistent_grid(k_shadow<false>, 128);
         g_sh[1] = persistent_grid(k_shadow<true>, 128);
     }
-    const bool count = (prof && prof->counting) ||
-                       (P.dcnt && (S.debug_mode == MT_DEBUG_PRIMARY_BVH_TESTS || S.debug_mode == MT_DEBUG_TOTAL_BVH_TESTS ||
-                                   S.debug_mode == MT_DEBUG_PRIMARY_TRIANGLE_TESTS ||
-                                   S.debug_mode == MT_DEBUG_TOTAL_TRIANGLE_TESTS));
+    const bool count = prof && prof->counting;
     unsigned long long* cnt = prof ? prof->d_counts : nullptr;
     auto begin = [&](int s) { if (prof) prof->begin(s, st); };
     auto end = [&](int s) { if (prof) prof->end(s, st); };
@@ -887,13 +888,18 @@ cudaError_t launch_batch(const DevScene& S, const PathState& P, const ShadowQueu
     int cur = 0;
     for (uint32_t b = 0; b < S.bounces; ++b) {
         begin(MT_STAGE_EXTEND);
-        if (count)
-            k_extend<true><<<g_ext[1], 128, 0, st>>>(S, P, W.q[cur], W.counts, cur, W.rays, cnt);
+        if (P.dval)  // debug modes: counting traversal plus the per-path debug planes
+            k_extend<true, true><<<g_ext[2], 128, 0, st>>>(S, P, W.q[cur], W.counts, cur, W.rays, cnt);
+        else if (count)
+            k_extend<true, false><<<g_ext[1], 128, 0, st>>>(S, P, W.q[cur], W.counts, cur, W.rays, cnt);
         else
-            k_extend<false><<<g_ext[0], 128, 0, st>>>(S, P, W.q[cur], W.counts, cur, W.rays, cnt);
+            k_extend<false, false><<<g_ext[0], 128, 0, st>>>(S, P, W.q[cur], W.counts, cur, W.rays, cnt);
         end(MT_STAGE_EXTEND);
         begin(MT_STAGE_SHADE);
-        k_shade<<<gw, 128, 0, st>>>(S, P, SQ, B, b, W.q[cur], W.q[cur ^ 1], W.counts, cur, R, NC);
+        if (NC.mode != MT_NRC_OFF || P.dval)
+            k_shade<true><<<gw, 128, 0, st>>>(S, P, SQ, B, b, W.q[cur], W.q[cur ^ 1], W.counts, cur, R, NC);
+        else
+            k_shade<false><<<gw, 128, 0, st>>>(S, P, SQ, B, b, W.q[cur], W.q[cur ^ 1], W.counts, cur, R, NC);
         end(MT_STAGE_SHADE);
         begin(MT_STAGE_SHADOW);
         if (prof && prof->counting)
