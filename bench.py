@@ -65,6 +65,9 @@ def parse():
     p.add_argument("--ref-spp", type=int, default=16384)
     p.add_argument("--relmse-target", type=float, default=0.01)
     p.add_argument("--no-nrc", action="store_true", help="time-to-relMSE: skip the radiance-cache leg")
+    p.add_argument("--nrc-kernels-only", action="store_true",
+                   help="only time the radiance cache's inference and training kernels")
+    p.add_argument("--nrc-rows", type=int, default=1920 * 1080 * 4)
     p.add_argument("--nrc-warmup", type=int, default=8, help="training-only frames before the first cached frame")
     p.add_argument("--nrc-frames", type=int, default=48, help="cached frames at most")
     return p.parse_args()
@@ -269,7 +272,7 @@ def microbench(a, dev, peak):
 
 
 # --------------------------------------------------------------------------- radiance cache kernels
-def nrc_microbench(dev):
+def nrc_microbench(dev, rows=1920 * 1080 * 4):
     """The cache's tensor-core kernels alone: inference over 1920x1080x4
     feature records (one frame's worth of queries at most) and one training
     step of 16,384 rows (forward, backward through the activations, weight
@@ -292,7 +295,7 @@ def nrc_microbench(dev):
     with mt.Tracer(scene, cfg) as tr:
         tr.nrc_enable()
         rng = np.random.default_rng(0)
-        n = 1920 * 1080 * 4
+        n = rows
         f = np.zeros((n, 5, 4), np.float32)
         f[:, 0, :] = rng.random((n, 4))
         v = rng.normal(size=(n, 2, 3))
@@ -671,6 +674,13 @@ def nrc_time_to_relmse(a, ref, dev, stream):
 
 def main():
     a = parse()
+    if a.nrc_kernels_only:
+        import torch
+
+        dev = torch.device("cuda", 0)
+        torch.cuda.set_stream(torch.cuda.Stream(dev))
+        print(json.dumps({"nrc_kernels": nrc_microbench(dev, a.nrc_rows)}), flush=True)
+        return
     if a.time_to_relmse:
         run_time_to_relmse(a)
         return

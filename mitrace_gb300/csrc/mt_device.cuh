@@ -293,10 +293,6 @@ __device__ __forceinline__ void trace_persistent(const DevScene& S, Work& W, uin
     uint32_t pfirst = 0, pcount = 0, pnode = 0;
     uint32_t stk_node[MT_STACK_SIZE];
     float stk_dist[MT_STACK_SIZE];
-    // child words (a, b) of the entry last pushed at top_sp: the near child is
-    // pushed last and usually popped next, so its words need no reload
-    int top_sp = -1;
-    uint32_t top_a = 0, top_b = 0;
 
     while (true) {
         // A. lanes without a ray take the next ones
@@ -415,9 +411,6 @@ __device__ __forceinline__ void trace_persistent(const DevScene& S, Work& W, uin
                     stk_node[0] = 0;
                     stk_dist[0] = slab(lo, linv, xyz(a), xyz(b));
                     sp = 1;
-                    top_sp = 0;
-                    top_a = f2u(a.w);
-                    top_b = f2u(b.w);
                 } else {
                     pending = true;
                     pfirst = 0;
@@ -432,12 +425,10 @@ __device__ __forceinline__ void trace_persistent(const DevScene& S, Work& W, uin
             --sp;
             const uint32_t ni = stk_node[sp];
             const float nd = stk_dist[sp];
-            const bool cached = sp == top_sp;
-            top_sp = -1;
             if (COUNT) ++h.bvh_tests;
             if (!(nd < 0.0f) && !(nd > __fadd_rn(h.t, 0.1f))) {
-                const uint32_t na = cached ? top_a : f2u(__ldg(&nodes[2 * ni].w));
-                const uint32_t nb = cached ? top_b : f2u(__ldg(&nodes[2 * ni + 1].w));
+                const uint32_t na = f2u(__ldg(&nodes[2 * ni].w));
+                const uint32_t nb = f2u(__ldg(&nodes[2 * ni + 1].w));
                 if (na & MT_BVH_LEAF_BIT) {
                     pending = true;
                     pfirst = na & ~MT_BVH_LEAF_BIT;
@@ -459,25 +450,14 @@ __device__ __forceinline__ void trace_persistent(const DevScene& S, Work& W, uin
                         if (da < db) {
                             stk_node[sp] = nb; stk_dist[sp] = db; ++sp;
                             stk_node[sp] = na; stk_dist[sp] = da; ++sp;
-                            top_a = f2u(a0.w);
-                            top_b = f2u(a1.w);
                         } else {
                             stk_node[sp] = na; stk_dist[sp] = da; ++sp;
                             stk_node[sp] = nb; stk_dist[sp] = db; ++sp;
-                            top_a = f2u(b0.w);
-                            top_b = f2u(b1.w);
                         }
-                        top_sp = sp - 1;
                     } else if (pa) {
                         stk_node[sp] = na; stk_dist[sp] = da; ++sp;
-                        top_a = f2u(a0.w);
-                        top_b = f2u(a1.w);
-                        top_sp = sp - 1;
                     } else if (pb) {
                         stk_node[sp] = nb; stk_dist[sp] = db; ++sp;
-                        top_a = f2u(b0.w);
-                        top_b = f2u(b1.w);
-                        top_sp = sp - 1;
                     }
                 }
             }
