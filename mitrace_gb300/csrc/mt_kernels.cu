@@ -22,7 +22,7 @@
 // the register allocation must allow (6 -> at most 80 registers per thread, no
 // spills; 5, 6 and 8 were measured, 6 and 8 tie and 8 spills).
 #ifndef MT_TRAVERSE_MIN_BLOCKS
-#define MT_TRAVERSE_MIN_BLOCKS 6
+#define MT_TRAVERSE_MIN_BLOCKS 7
 #endif
 
 namespace mt {
