@@ -191,7 +191,6 @@ struct mt_handle {
     std::vector<DevArray<float>> texf;
     DevArray<int> error_flag;
     uint64_t scene_bytes = 0;
-    uint32_t num_world_boxes = 0;
     float world_lo[3] = {std::numeric_limits<float>::max(), std::numeric_limits<float>::max(),
                          std::numeric_limits<float>::max()};
     float world_hi[3] = {std::numeric_limits<float>::lowest(), std::numeric_limits<float>::lowest(),
@@ -203,7 +202,6 @@ struct mt_handle {
     DevArray<uint4> phit;
     DevArray<float4> sq;         // 3 float4 planes
     DevArray<uint32_t> queues;   // 2 planes
-    DevArray<uint32_t> bin_keys, bin_q, bins;  // extension-ray binning (MT_BIN_RAYS, default on)
     DevArray<uint32_t> counts;
     DevArray<unsigned long long> rays;  // [0] extension, [1] shadow
     DevArray<float> samples;     // 3 planes
@@ -440,7 +438,6 @@ mt_status upload_scene(mt_handle* h, const mt_scene_desc* d)
             }
         }
         insts[i] = x;
-        ++h->num_world_boxes;
         for (int k = 0; k < 3; ++k) {
             h->world_lo[k] = std::min(h->world_lo[k], x.wlo[k]);
             h->world_hi[k] = std::max(h->world_hi[k], x.whi[k]);
@@ -532,11 +529,6 @@ mt_status upload_scene(mt_handle* h, const mt_scene_desc* d)
     S.firefly_k = cfg.firefly_threshold;
     S.error_flag = h->error_flag.p;
     S.debug_mode = cfg.debug_mode;
-    for (int k = 0; k < 3; ++k) {
-        const float ext = h->world_hi[k] - h->world_lo[k];
-        S.box_lo[k] = h->num_world_boxes ? h->world_lo[k] : 0.0f;
-        S.box_scale[k] = (h->num_world_boxes && ext > 0.0f) ? 8.0f / ext : 0.0f;
-    }
     return MT_OK;
 }
 
@@ -566,11 +558,6 @@ mt_status ensure_wave(mt_handle* h)
     MT_CUDA(h->phit.alloc(batch));
     MT_CUDA(h->sq.alloc(3ull * batch));
     MT_CUDA(h->queues.alloc(2ull * batch));
-    if (env_u64("MT_BIN_RAYS", 1)) {
-        MT_CUDA(h->bin_keys.alloc(batch));
-        MT_CUDA(h->bin_q.alloc(batch));
-        MT_CUDA(h->bins.alloc(2 * 4096));
-    }
     MT_CUDA(h->counts.alloc(8));
     MT_CUDA(cudaMemset(h->counts.p, 0, 8 * sizeof(uint32_t)));
     MT_CUDA(h->rays.alloc(2));
@@ -615,9 +602,6 @@ WaveViews views(mt_handle* h)
     v.SQ.c = h->sq.p + 2 * B;
     v.W.q[0] = h->queues.p;
     v.W.q[1] = h->queues.p + B;
-    v.W.keys = h->bin_keys.p;
-    v.W.qs = h->bin_q.p;
-    v.W.bins = h->bins.p;
     v.W.counts = h->counts.p;
     v.W.rays = h->rays.p;
     v.W.sr = h->samples.p;

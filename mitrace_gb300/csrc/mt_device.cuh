@@ -182,8 +182,6 @@ struct DevScene {
     float firefly_k;
     int* error_flag;
     int32_t debug_mode;  // Config::DebugMode (MT_DEBUG_*), 0 = DebugNone
-    float box_lo[3];     // world box of the scene and 8 / its extent (ray-binning cells)
-    float box_scale[3];
 };
 
 #define MT_STACK_SIZE 64

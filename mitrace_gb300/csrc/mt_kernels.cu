@@ -291,68 +291,6 @@ __device__ __forceinline__ void st4(float4* p, uint32_t i, f3 v, float w = 0.0f)
     p[i] = make_float4(v.x, v.y, v.z, w);
 }
 
-// Bin of an extension ray: direction octant (major), then the Morton code of
-// its origin's cell in an 8x8x8 grid over the scene's world box.
-__device__ __forceinline__ uint32_t bin_key(const DevScene& S, f3 o, f3 d)
-{
-    const float c[3] = {(o.x - S.box_lo[0]) * S.box_scale[0], (o.y - S.box_lo[1]) * S.box_scale[1],
-                        (o.z - S.box_lo[2]) * S.box_scale[2]};
-    uint32_t m = 0;
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        const uint32_t ci = static_cast<uint32_t>(fminf(fmaxf(c[k], 0.0f), 7.0f));
-        m |= ((ci & 1u) << k) | (((ci >> 1) & 1u) << (3 + k)) | (((ci >> 2) & 1u) << (6 + k));
-    }
-    const uint32_t oct = (d.x < 0.0f ? 1u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 4u : 0u);
-    return (oct << 9) | m;
-}
-
-// Counting sort of the extension queue by bin: histogram, exclusive scan,
-// scatter into the scratch queue (order inside a bin is arbitrary; every ray's
-// result is independent of the order rays are traced in).
-__global__ void __launch_bounds__(256) k_bin_hist(const uint32_t* __restrict__ keys, const uint32_t* counts, int which,
-                                                  uint32_t* __restrict__ hist)
-{
-    __shared__ uint32_t h[4096];
-    for (int i = threadIdx.x; i < 4096; i += blockDim.x) h[i] = 0;
-    __syncthreads();
-    const uint32_t n = counts[which];
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        atomicAdd(&h[keys[i] & 4095u], 1u);
-    __syncthreads();
-    for (int i = threadIdx.x; i < 4096; i += blockDim.x)
-        if (h[i]) atomicAdd(&hist[i], h[i]);
-}
-
-__global__ void __launch_bounds__(1024) k_bin_scan(uint32_t* __restrict__ hist, uint32_t* __restrict__ offs)
-{
-    __shared__ uint32_t part[1024];
-    const int t = threadIdx.x;
-    const uint32_t a = hist[4 * t], b = hist[4 * t + 1], c = hist[4 * t + 2], d = hist[4 * t + 3];
-    part[t] = a + b + c + d;
-    __syncthreads();
-    for (int o = 1; o < 1024; o <<= 1) {  // inclusive Hillis-Steele scan
-        const uint32_t v = t >= o ? part[t - o] : 0u;
-        __syncthreads();
-        part[t] += v;
-        __syncthreads();
-    }
-    const uint32_t base = t ? part[t - 1] : 0u;
-    offs[4 * t] = base;
-    offs[4 * t + 1] = base + a;
-    offs[4 * t + 2] = base + a + b;
-    offs[4 * t + 3] = base + a + b + c;
-}
-
-__global__ void __launch_bounds__(256) k_bin_scatter(const uint32_t* __restrict__ q, const uint32_t* __restrict__ keys,
-                                                     const uint32_t* counts, int which, uint32_t* __restrict__ offs,
-                                                     uint32_t* __restrict__ out)
-{
-    const uint32_t n = counts[which];
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        out[atomicAdd(&offs[keys[i] & 4095u], 1u)] = q[i];
-}
-
 // HOOKS: the radiance-cache and debug-mode code paths; the plain render runs
 // the variant without them.
 template <bool HOOKS>
@@ -360,8 +298,7 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, PathState P, ShadowQu
                                                BatchInfo B, uint32_t bounce,
                                                const uint32_t* __restrict__ q,
                                                uint32_t* __restrict__ nq, uint32_t* counts,
-                                               int cur, RecordBuffers R, NrcShade NC,
-                                               uint32_t* __restrict__ nkeys)
+                                               int cur, RecordBuffers R, NrcShade NC)
 {
     const uint32_t n = counts[cur];
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -615,9 +552,7 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, PathState P, ShadowQu
         st4(P.ro, p, no);
         st4(P.rd, p, nd);
         st4(P.prev, p, base, seen_diffuse);
-        const uint32_t slot = warp_append(&counts[cur ^ 1]);
-        nq[slot] = p;
-        if (nkeys) nkeys[slot] = bin_key(S, no, nd);
+        nq[warp_append(&counts[cur ^ 1])] = p;
     }
 }
 
@@ -961,12 +896,10 @@ cudaError_t launch_batch(const DevScene& S, const PathState& P, const ShadowQueu
             k_extend<false, false><<<g_ext[0], 128, 0, st>>>(S, P, W.q[cur], W.counts, cur, W.rays, cnt);
         end(MT_STAGE_EXTEND);
         begin(MT_STAGE_SHADE);
-        const bool bin = W.keys && b + 1 < S.bounces;
-        uint32_t* nkeys = bin ? W.keys : nullptr;
         if (NC.mode != MT_NRC_OFF || P.dval)
-            k_shade<true><<<gw, 128, 0, st>>>(S, P, SQ, B, b, W.q[cur], W.q[cur ^ 1], W.counts, cur, R, NC, nkeys);
+            k_shade<true><<<gw, 128, 0, st>>>(S, P, SQ, B, b, W.q[cur], W.q[cur ^ 1], W.counts, cur, R, NC);
         else
-            k_shade<false><<<gw, 128, 0, st>>>(S, P, SQ, B, b, W.q[cur], W.q[cur ^ 1], W.counts, cur, R, NC, nkeys);
+            k_shade<false><<<gw, 128, 0, st>>>(S, P, SQ, B, b, W.q[cur], W.q[cur ^ 1], W.counts, cur, R, NC);
         end(MT_STAGE_SHADE);
         begin(MT_STAGE_SHADOW);
         if (prof && prof->counting)
@@ -975,19 +908,6 @@ cudaError_t launch_batch(const DevScene& S, const PathState& P, const ShadowQueu
             k_shadow<false><<<g_sh[0], 128, 0, st>>>(S, P, SQ, W.counts, W.rays + 1, nullptr, R);
         end(MT_STAGE_SHADOW);
         l += 3;
-        if (bin) {
-            // sort the next bounce's queue by bin (scratch, then back in place)
-            cudaError_t e = cudaMemsetAsync(W.bins, 0, 4096 * sizeof(uint32_t), st);
-            if (e != cudaSuccess) return e;
-            const unsigned gb = grid_for(n, 256, 4);
-            k_bin_hist<<<gb, 256, 0, st>>>(W.keys, W.counts, cur ^ 1, W.bins);
-            k_bin_scan<<<1, 1024, 0, st>>>(W.bins, W.bins + 4096);
-            k_bin_scatter<<<gb, 256, 0, st>>>(W.q[cur ^ 1], W.keys, W.counts, cur ^ 1, W.bins + 4096, W.qs);
-            e = cudaMemcpyAsync(W.q[cur ^ 1], W.qs, static_cast<size_t>(n) * sizeof(uint32_t),
-                                cudaMemcpyDeviceToDevice, st);
-            if (e != cudaSuccess) return e;
-            l += 3;
-        }
         cur ^= 1;
     }
     if (NC.mode == MT_NRC_TRAIN) {

@@ -51,12 +51,6 @@ struct WaveBuffers {
     float* sr;                     // per-sample tonemapped R, sample-major in a band
     float* sg;
     float* sb;
-    // Ray binning of the extension queue (null: off): per queue slot a 12-bit
-    // key (direction octant, Morton cell of the origin), a scratch queue and
-    // 2 x 4096 bin counters / offsets.
-    uint32_t* keys = nullptr;
-    uint32_t* qs = nullptr;
-    uint32_t* bins = nullptr;
 };
 
 // Per-vertex records written by a recording (path-replay) pass of the render
