@@ -1287,6 +1287,7 @@ mt_status mt_nrc_frame(mt_handle* h, float* d_accum, uint32_t accum_index, void*
         Q.count = N.counters.p;
         Q.net = N.infer.p;
         Q.total = N.counters.p + 2;
+        Q.err = h->error_flag.p;
         const uint64_t rows_per_band = N.plane_capacity / (static_cast<uint64_t>(c.width) * nc.spp);
         for (uint64_t r0 = 0; r0 < c.height; r0 += rows_per_band) {
             const uint64_t rows = std::min<uint64_t>(rows_per_band, c.height - r0);
@@ -1319,8 +1320,11 @@ mt_status mt_nrc_get_stats(mt_handle* h, mt_nrc_stats* out)
     if (rc != MT_OK) return rc;
     if (!out) return set_err(MT_ERR_INVALID, "null argument");
     uint32_t c[4];
+    int flag = 0;
     MT_CUDA(cudaDeviceSynchronize());
     MT_CUDA(cudaMemcpy(c, h->nrc.counters.p, sizeof(c), cudaMemcpyDeviceToHost));
+    MT_CUDA(cudaMemcpy(&flag, h->error_flag.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (flag & MT_ERRBIT_TIMEOUT) return set_err(MT_ERR_TIMEOUT, "a bounded wait on the tensor cores ran out");
     std::memset(out, 0, sizeof(*out));
     out->frames = h->nrc.frames;
     out->adam_steps = h->nrc.opt.step;
@@ -1363,7 +1367,8 @@ mt_status mt_nrc_infer(mt_handle* h, const float* d_features, uint32_t n, float*
     mt_status rc = nrc_ready(h);
     if (rc != MT_OK) return rc;
     if (n && (!d_features || !d_rgb)) return set_err(MT_ERR_INVALID, "null argument");
-    MT_CUDA(launch_nrc_infer(h->nrc.infer.p, d_features, n, d_rgb, static_cast<cudaStream_t>(cuda_stream)));
+    MT_CUDA(launch_nrc_infer(h->nrc.infer.p, d_features, n, d_rgb, h->error_flag.p,
+                             static_cast<cudaStream_t>(cuda_stream)));
     h->launches += n ? 1 : 0;
     return MT_OK;
 }

@@ -186,6 +186,7 @@ struct DevScene {
 
 #define MT_STACK_SIZE 64
 #define MT_ERRBIT_STACK 1
+#define MT_ERRBIT_TIMEOUT 2  // a bounded wait on the tensor cores ran out
 
 // ---------------------------------------------------------------------------
 // Intersection (restates src/Tracer/Intersect.cpp)

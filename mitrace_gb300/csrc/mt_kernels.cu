@@ -918,7 +918,7 @@ cudaError_t launch_batch(const DevScene& S, const PathState& P, const ShadowQueu
         return cudaSuccess;
     }
     if (NC.mode == MT_NRC_QUERY) {
-        const cudaError_t e = launch_nrc_query(NC.net, P, NC.rec, NC.count, n, NC.total, st);
+        const cudaError_t e = launch_nrc_query(NC.net, P, NC.rec, NC.count, n, NC.total, NC.err, st);
         if (e != cudaSuccess) return e;
         ++l;
     }

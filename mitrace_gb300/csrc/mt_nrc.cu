@@ -23,6 +23,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <cstdlib>
 
 #include "mt_device.cuh"
 #include "mt_nrc.h"
@@ -350,6 +351,260 @@ __global__ void __launch_bounds__(kInferWarps * 32) k_nrc_infer(const bf16* __re
                 }
             }
         }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Inference on the 5th-generation tensor cores (tcgen05, accumulators in TMEM)
+// ---------------------------------------------------------------------------
+// A CTA of 128 threads owns tiles of 128 rows; thread r owns row r of the tile
+// and TMEM lane r.  Per layer: the layer input sits in shared memory as a
+// K-major BF16 operand in the canonical no-swizzle layout (8-row x 16-byte
+// core matrices), one thread issues the layer's tcgen05.mma (M = 128, N = 64,
+// or 16 for the padded output layer; K in steps of 16) into a 64-column TMEM
+// accumulator and commits to an mbarrier; every thread waits (bounded), reads
+// its row back with tcgen05.ld, applies ReLU, rounds to BF16 and writes the
+// next layer's operand.  Weights are staged once per CTA in the same layout.
+constexpr int kTcRows = 128;
+constexpr int kTcW0 = 0;                          // 64 x 80: 8 n-groups x 10 k-chunks x 128 B
+constexpr int kTcW1 = kTcW0 + 64 * 80 * 2;        // 64 x 64 each
+constexpr int kTcW4 = kTcW1 + 3 * 64 * 64 * 2;    // 16 x 64 (rows 3..15 zero)
+constexpr int kTcA = kTcW4 + 16 * 64 * 2;         // 128 x 80 operand tile
+constexpr int kTcBar = kTcA + kTcRows * 80 * 2;   // mbarrier (8 B)
+constexpr int kTcTmem = kTcBar + 8;               // TMEM base address (4 B)
+constexpr int kTcFlag = kTcTmem + 4;              // timeout flag (4 B)
+constexpr int kTcSmem = kTcFlag + 4;
+constexpr uint32_t kTcCols = 64;                  // TMEM columns per CTA
+constexpr uint32_t kTcWaitLimit = 1u << 24;       // mbarrier polls before giving up
+
+// Element (row, k) of a K-major operand with kc 8-element k-chunks per row, in
+// bytes from the operand's start.
+__device__ __forceinline__ uint32_t canon_off(uint32_t row, uint32_t k, uint32_t kc)
+{
+    return (((row >> 3) * kc + (k >> 3)) * 64 + (row & 7) * 8 + (k & 7)) * 2;
+}
+
+// tcgen05 shared-memory matrix descriptor: start, leading-dimension byte offset
+// (next core matrix along K), stride byte offset (next 8-row group), version 1,
+// no swizzle.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo)
+{
+    return static_cast<uint64_t>((saddr & 0x3FFFFu) >> 4) | (static_cast<uint64_t>(lbo >> 4) << 16) |
+           (static_cast<uint64_t>(sbo >> 4) << 32) | (1ull << 46);
+}
+
+// Instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both
+// K-major, dense, M = 128.
+__host__ __device__ constexpr uint32_t tc_idesc(uint32_t n)
+{
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((n >> 3) << 17) | ((128u >> 4) << 24);
+}
+
+__device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc)
+{
+    asm volatile(
+        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+        "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+
+__device__ __forceinline__ void tc_commit(uint32_t bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(bar)
+                 : "memory");
+}
+
+// Waits for phase `parity` of the mbarrier; false when the bound ran out.
+__device__ __forceinline__ bool tc_wait(uint32_t bar, uint32_t parity)
+{
+    for (uint32_t i = 0; i < kTcWaitLimit; ++i) {
+        uint32_t done;
+        asm volatile(
+            "{\n.reg .pred q;\nmbarrier.try_wait.parity.shared::cta.b64 q, [%1], %2;\nselp.b32 %0, 1, 0, q;\n}\n"
+            : "=r"(done)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+// 16 consecutive FP32 columns of this thread's TMEM lane.
+__device__ __forceinline__ void tc_ld16(uint32_t taddr, float (&v)[16])
+{
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void tc_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
+
+// Issues one layer: D[128 x n] = A[128 x 8*kc] * W^T, W given as n x 8*kc.
+__device__ __forceinline__ void tc_layer(uint32_t tmem, uint32_t a_base, uint32_t w_base, uint32_t kc, uint32_t n,
+                                         uint32_t bar)
+{
+    const uint32_t idesc = tc_idesc(n);
+    for (uint32_t j = 0; j < kc / 2; ++j) {
+        const uint64_t a = smem_desc(a_base + j * 256, 128, kc * 128);
+        const uint64_t b = smem_desc(w_base + j * 256, 128, kc * 128);
+        tc_mma(tmem, a, b, idesc, j > 0 ? 1u : 0u);
+    }
+    tc_commit(bar);
+}
+
+template <bool PATHS>
+__global__ void __launch_bounds__(kTcRows) k_nrc_infer_tc(const bf16* __restrict__ blob, const float4* __restrict__ feat,
+                                                         uint32_t n_host, const uint32_t* __restrict__ count,
+                                                         float* __restrict__ out, PathState P, uint32_t* total,
+                                                         int* err)
+{
+    extern __shared__ __align__(1024) unsigned char tc_smem[];
+    unsigned char* smem = tc_smem;
+    const uint32_t s0 = static_cast<uint32_t>(__cvta_generic_to_shared(smem));
+    const uint32_t tid = threadIdx.x, warp = tid >> 5;
+    // weights: padded rows of the forward blob -> canonical K-major operands
+    for (uint32_t i = tid; i < 64 * 10 + 3 * 64 * 8 + 16 * 8; i += blockDim.x) {
+        uint32_t l, row, c;
+        if (i < 640) {
+            l = 0; row = i / 10; c = i % 10;
+        } else if (i < 640 + 1536) {
+            const uint32_t j = i - 640;
+            l = 1 + j / 512; row = (j % 512) / 8; c = j % 8;
+        } else {
+            const uint32_t j = i - 2176;
+            l = 4; row = j / 8; c = j % 8;
+        }
+        const uint32_t kc = l == 0 ? 10 : 8;
+        const uint32_t base = l == 0 ? kTcW0 : (l == 4 ? kTcW4 : kTcW1 + (l - 1) * 64 * 64 * 2);
+        uint4 v = make_uint4(0u, 0u, 0u, 0u);
+        if (l < 4 || row < 8)  // output rows 8..15 stay zero (the blob pads to 8)
+            v = *reinterpret_cast<const uint4*>(blob + fwd_off(l) + row * fwd_stride(l) + 8 * c);
+        *reinterpret_cast<uint4*>(smem + base + canon_off(row, 8 * c, kc)) = v;
+    }
+    const uint32_t bar = s0 + kTcBar;
+    int* flag = reinterpret_cast<int*>(smem + kTcFlag);
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar));
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        *flag = 0;
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(s0 + kTcTmem),
+                     "r"(kTcCols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+    }
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *reinterpret_cast<const uint32_t*>(smem + kTcTmem);
+    const uint32_t lane_addr = tmem + ((warp * 32u) << 16);
+
+    const uint32_t n = PATHS ? *count : n_host;
+    if (total && blockIdx.x == 0 && tid == 0) atomicAdd(total, n);
+    const uint32_t tiles = (n + kTcRows - 1) / kTcRows;
+    uint32_t phase = 0;
+    for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+        const uint32_t r = tile * kTcRows + tid;
+        // layer-0 operand: this thread's row, encoded
+        {
+            float e[80];
+            if (r < n) {
+                const float4* f = feat + static_cast<uint64_t>(r) * (PATHS ? 6 : 5);
+                auto put = [&](int k, float v) { e[k] = v; };
+                encode_part0(f[0], f[3], f[4], put);
+                encode_part1(f[1], f[2], put);
+            } else {
+#pragma unroll
+                for (int k = 0; k < 80; ++k) e[k] = 0.0f;
+            }
+#pragma unroll
+            for (int c = 0; c < 10; ++c) {
+                const uint4 v = make_uint4(pack2(e[8 * c], e[8 * c + 1]), pack2(e[8 * c + 2], e[8 * c + 3]),
+                                           pack2(e[8 * c + 4], e[8 * c + 5]), pack2(e[8 * c + 6], e[8 * c + 7]));
+                *reinterpret_cast<uint4*>(smem + kTcA + canon_off(tid, 8 * c, 10)) = v;
+            }
+        }
+        bool timed_out = false;
+        float y[16];
+#pragma unroll 1
+        for (uint32_t l = 0; l < 5; ++l) {
+            fence_async_smem();
+            tc_fence_before();
+            __syncthreads();
+            tc_fence_after();
+            if (tid == 0) {
+                const uint32_t w = l == 0 ? kTcW0 : (l == 4 ? kTcW4 : kTcW1 + (l - 1) * 64 * 64 * 2);
+                tc_layer(tmem, s0 + kTcA, s0 + w, l == 0 ? 10 : 8, l == 4 ? 16 : 64, bar);
+            }
+            const bool ok = tc_wait(bar, phase);
+            phase ^= 1;
+            if (__syncthreads_or(!ok)) {
+                timed_out = true;
+                break;
+            }
+            tc_fence_after();
+            if (l < 4) {
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    float v[16];
+                    tc_ld16(lane_addr + 16 * q, v);
+                    tc_wait_ld();
+#pragma unroll
+                    for (int c = 0; c < 2; ++c) {
+                        const float* x = v + 8 * c;
+                        const uint4 o = make_uint4(pack2(fmaxf(x[0], 0.0f), fmaxf(x[1], 0.0f)),
+                                                   pack2(fmaxf(x[2], 0.0f), fmaxf(x[3], 0.0f)),
+                                                   pack2(fmaxf(x[4], 0.0f), fmaxf(x[5], 0.0f)),
+                                                   pack2(fmaxf(x[6], 0.0f), fmaxf(x[7], 0.0f)));
+                        *reinterpret_cast<uint4*>(smem + kTcA + canon_off(tid, 16 * q + 8 * c, 8)) = o;
+                    }
+                }
+            } else {
+                tc_ld16(lane_addr, y);
+                tc_wait_ld();
+            }
+        }
+        if (timed_out) {
+            if (tid == 0) {
+                atomicOr(err, MT_ERRBIT_TIMEOUT);
+                *flag = 1;
+            }
+            break;
+        }
+        if (r < n) {
+            if (PATHS) {
+                const float4 q = feat[6ull * r + 5];  // throughput, path index
+                const uint32_t p = __float_as_uint(q.w);
+                const float4 a = P.indirect[p];
+                P.indirect[p] = make_float4(a.x + q.x * fmaxf(y[0], 0.0f), a.y + q.y * fmaxf(y[1], 0.0f),
+                                            a.z + q.z * fmaxf(y[2], 0.0f), a.w);
+            } else {
+                out[3ull * r + 0] = y[0];
+                out[3ull * r + 1] = y[1];
+                out[3ull * r + 2] = y[2];
+            }
+        }
+    }
+    // release TMEM only when no MMA of this CTA can still be in flight: after a
+    // timeout, wait (bounded) for the last commit before deallocating
+    tc_fence_before();
+    __syncthreads();
+    if (*flag) {
+        if (tid == 0) (void)tc_wait(bar, phase ^ 1);
+        __syncthreads();
+    }
+    if (warp == 0) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(kTcCols));
     }
 }
 
@@ -693,10 +948,31 @@ cudaError_t allow_smem(K kernel, size_t bytes, bool& done)
     return e;
 }
 
+bool use_tc()
+{
+    static const bool tc = [] {
+        const char* v = std::getenv("MT_NRC_TC");
+        return !(v && v[0] == '0');
+    }();
+    return tc;
+}
+
 template <bool PATHS>
 cudaError_t infer(const void* net, const float4* feat, uint32_t n_host, const uint32_t* count, uint32_t capacity,
-                  float* out, const PathState& P, uint32_t* total, cudaStream_t st)
+                  float* out, const PathState& P, uint32_t* total, int* err, cudaStream_t st)
 {
+    if (use_tc()) {
+        static bool ok_tc = false;
+        cudaError_t e = allow_smem(k_nrc_infer_tc<PATHS>, kTcSmem, ok_tc);
+        if (e != cudaSuccess) return e;
+        uint64_t blocks = (static_cast<uint64_t>(capacity) + kTcRows - 1) / kTcRows;
+        const uint64_t cap = static_cast<uint64_t>(sms()) * 3;  // 3 x 56 KB of shared memory per SM
+        if (blocks > cap) blocks = cap;
+        if (blocks == 0) blocks = 1;
+        k_nrc_infer_tc<PATHS><<<static_cast<unsigned>(blocks), kTcRows, kTcSmem, st>>>(
+            static_cast<const bf16*>(net), feat, n_host, count, out, P, total, err);
+        return cudaGetLastError();
+    }
     static bool ok = false;
     cudaError_t e = allow_smem(k_nrc_infer<PATHS>, kInferSmem, ok);
     if (e != cudaSuccess) return e;
@@ -713,16 +989,17 @@ cudaError_t infer(const void* net, const float4* feat, uint32_t n_host, const ui
 }  // namespace
 
 cudaError_t launch_nrc_query(const void* net, const PathState& P, const float4* rec, const uint32_t* count,
-                             uint32_t capacity, uint32_t* total, cudaStream_t st)
+                             uint32_t capacity, uint32_t* total, int* err, cudaStream_t st)
 {
-    return infer<true>(net, rec, 0, count, capacity, nullptr, P, total, st);
+    return infer<true>(net, rec, 0, count, capacity, nullptr, P, total, err, st);
 }
 
-cudaError_t launch_nrc_infer(const void* net, const float* features, uint32_t n, float* out, cudaStream_t st)
+cudaError_t launch_nrc_infer(const void* net, const float* features, uint32_t n, float* out, int* err,
+                             cudaStream_t st)
 {
     if (n == 0) return cudaSuccess;
     return infer<false>(net, reinterpret_cast<const float4*>(features), n, nullptr, n, out, PathState{}, nullptr,
-                        st);
+                        err, st);
 }
 
 cudaError_t launch_nrc_encode(const float* features, uint32_t n, float* out, cudaStream_t st)

@@ -41,6 +41,7 @@ struct NrcShade {
     // QUERY: bf16 forward weight blob; queries are also added to *total.
     const void* net = nullptr;
     uint32_t* total = nullptr;
+    int* err = nullptr;  // device error word (MT_ERRBIT_TIMEOUT)
     // TRAIN: training samples (5 feature float4 + target float4 each).
     float4* samples = nullptr;
     uint32_t* sample_count = nullptr;
@@ -57,12 +58,13 @@ struct NrcActs {
 
 // Cache queries of a batch: adds throughput * max(cache, 0) to P.indirect.
 cudaError_t launch_nrc_query(const void* net, const PathState& P, const float4* rec, const uint32_t* count,
-                             uint32_t capacity, uint32_t* total, cudaStream_t st);
+                             uint32_t capacity, uint32_t* total, int* err, cudaStream_t st);
 // Training targets of a batch of training paths -> samples.
 cudaError_t launch_nrc_targets(const PathState& P, const NrcShade& N, uint32_t n, uint32_t bounces,
                                cudaStream_t st);
 // Plain inference into out (n x 3).
-cudaError_t launch_nrc_infer(const void* net, const float* features, uint32_t n, float* out, cudaStream_t st);
+cudaError_t launch_nrc_infer(const void* net, const float* features, uint32_t n, float* out, int* err,
+                             cudaStream_t st);
 cudaError_t launch_nrc_encode(const float* features, uint32_t n, float* out, cudaStream_t st);
 
 // One training step.  Rows r < rows read sample fmix32(base + r) mod *count of
