@@ -357,25 +357,29 @@ __global__ void __launch_bounds__(kInferWarps * 32) k_nrc_infer(const bf16* __re
 // ---------------------------------------------------------------------------
 // Inference on the 5th-generation tensor cores (tcgen05, accumulators in TMEM)
 // ---------------------------------------------------------------------------
-// A CTA of 128 threads owns tiles of 128 rows; thread r owns row r of the tile
-// and TMEM lane r.  Per layer: the layer input sits in shared memory as a
-// K-major BF16 operand in the canonical no-swizzle layout (8-row x 16-byte
-// core matrices), one thread issues the layer's tcgen05.mma (M = 128, N = 64,
-// or 16 for the padded output layer; K in steps of 16) into a 64-column TMEM
-// accumulator and commits to an mbarrier; every thread waits (bounded), reads
-// its row back with tcgen05.ld, applies ReLU, rounds to BF16 and writes the
-// next layer's operand.  Weights are staged once per CTA in the same layout.
+// A CTA runs two warpgroups; each owns tiles of 128 rows (thread r of the
+// warpgroup owns row r and TMEM lane r) with its own operand buffer, mbarrier
+// and 64 TMEM columns, so one warpgroup's MMAs overlap the other's epilogue.
+// Per layer: the layer input sits in shared memory as a K-major BF16 operand in
+// the canonical no-swizzle layout (8-row x 16-byte core matrices); one thread
+// issues the layer's tcgen05.mma (M = 128, N = 64, or 16 for the padded output
+// layer; K in steps of 16) into the warpgroup's TMEM accumulator and commits to
+// its mbarrier; the warpgroup waits (bounded), reads its rows back with
+// tcgen05.ld, applies ReLU, rounds to BF16 and writes the next operand.  The
+// weights are staged once per CTA in the same layout.
 constexpr int kTcRows = 128;
+constexpr int kTcGroups = 2;
 constexpr int kTcW0 = 0;                          // 64 x 80: 8 n-groups x 10 k-chunks x 128 B
 constexpr int kTcW1 = kTcW0 + 64 * 80 * 2;        // 64 x 64 each
 constexpr int kTcW4 = kTcW1 + 3 * 64 * 64 * 2;    // 16 x 64 (rows 3..15 zero)
-constexpr int kTcA = kTcW4 + 16 * 64 * 2;         // 128 x 80 operand tile
-constexpr int kTcBar = kTcA + kTcRows * 80 * 2;   // mbarrier (8 B)
-constexpr int kTcTmem = kTcBar + 8;               // TMEM base address (4 B)
-constexpr int kTcFlag = kTcTmem + 4;              // timeout flag (4 B)
-constexpr int kTcSmem = kTcFlag + 4;
-constexpr uint32_t kTcCols = 64;                  // TMEM columns per CTA
-constexpr uint32_t kTcWaitLimit = 1u << 24;       // mbarrier polls before giving up
+constexpr int kTcA = kTcW4 + 16 * 64 * 2;         // per warpgroup: 128 x 80 operand tile
+constexpr int kTcABytes = kTcRows * 80 * 2;
+constexpr int kTcBar = kTcA + kTcGroups * kTcABytes;  // per warpgroup: mbarrier (8 B)
+constexpr int kTcTmem = kTcBar + 8 * kTcGroups;       // TMEM base address (4 B)
+constexpr int kTcFlag = kTcTmem + 4;                  // per warpgroup: timeout flag (4 B)
+constexpr int kTcSmem = kTcFlag + 4 * kTcGroups;
+constexpr uint32_t kTcCols = 64 * kTcGroups;          // TMEM columns per CTA
+constexpr uint32_t kTcWaitLimit = 1u << 24;           // mbarrier polls before giving up
 
 // Element (row, k) of a K-major operand with kc 8-element k-chunks per row, in
 // bytes from the operand's start.
@@ -446,6 +450,11 @@ __device__ __forceinline__ void tc_wait_ld() { asm volatile("tcgen05.wait::ld.sy
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory"); }
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
+// barrier of one warpgroup (named barrier 1 + group, 128 threads)
+__device__ __forceinline__ void group_sync(uint32_t group)
+{
+    asm volatile("bar.sync %0, 128;\n" ::"r"(1u + group) : "memory");
+}
 
 // Issues one layer: D[128 x n] = A[128 x 8*kc] * W^T, W given as n x 8*kc.
 __device__ __forceinline__ void tc_layer(uint32_t tmem, uint32_t a_base, uint32_t w_base, uint32_t kc, uint32_t n,
@@ -461,37 +470,39 @@ __device__ __forceinline__ void tc_layer(uint32_t tmem, uint32_t a_base, uint32_
 }
 
 template <bool PATHS>
-__global__ void __launch_bounds__(kTcRows) k_nrc_infer_tc(const bf16* __restrict__ blob, const float4* __restrict__ feat,
-                                                         uint32_t n_host, const uint32_t* __restrict__ count,
-                                                         float* __restrict__ out, PathState P, uint32_t* total,
-                                                         int* err)
+__global__ void __launch_bounds__(kTcRows * kTcGroups) k_nrc_infer_tc(const bf16* __restrict__ blob,
+                                                                      const float4* __restrict__ feat, uint32_t n_host,
+                                                                      const uint32_t* __restrict__ count,
+                                                                      float* __restrict__ out, PathState P,
+                                                                      uint32_t* total, int* err)
 {
     extern __shared__ __align__(1024) unsigned char tc_smem[];
     unsigned char* smem = tc_smem;
     const uint32_t s0 = static_cast<uint32_t>(__cvta_generic_to_shared(smem));
     const uint32_t tid = threadIdx.x, warp = tid >> 5;
+    const uint32_t group = tid >> 7, row = tid & 127;
     // weights: padded rows of the forward blob -> canonical K-major operands
     for (uint32_t i = tid; i < 64 * 10 + 3 * 64 * 8 + 16 * 8; i += blockDim.x) {
-        uint32_t l, row, c;
+        uint32_t l, r, c;
         if (i < 640) {
-            l = 0; row = i / 10; c = i % 10;
+            l = 0; r = i / 10; c = i % 10;
         } else if (i < 640 + 1536) {
             const uint32_t j = i - 640;
-            l = 1 + j / 512; row = (j % 512) / 8; c = j % 8;
+            l = 1 + j / 512; r = (j % 512) / 8; c = j % 8;
         } else {
             const uint32_t j = i - 2176;
-            l = 4; row = j / 8; c = j % 8;
+            l = 4; r = j / 8; c = j % 8;
         }
         const uint32_t kc = l == 0 ? 10 : 8;
         const uint32_t base = l == 0 ? kTcW0 : (l == 4 ? kTcW4 : kTcW1 + (l - 1) * 64 * 64 * 2);
         uint4 v = make_uint4(0u, 0u, 0u, 0u);
-        if (l < 4 || row < 8)  // output rows 8..15 stay zero (the blob pads to 8)
-            v = *reinterpret_cast<const uint4*>(blob + fwd_off(l) + row * fwd_stride(l) + 8 * c);
-        *reinterpret_cast<uint4*>(smem + base + canon_off(row, 8 * c, kc)) = v;
+        if (l < 4 || r < 8)  // output rows 8..15 stay zero (the blob pads to 8)
+            v = *reinterpret_cast<const uint4*>(blob + fwd_off(l) + r * fwd_stride(l) + 8 * c);
+        *reinterpret_cast<uint4*>(smem + base + canon_off(r, 8 * c, kc)) = v;
     }
-    const uint32_t bar = s0 + kTcBar;
-    int* flag = reinterpret_cast<int*>(smem + kTcFlag);
-    if (tid == 0) {
+    const uint32_t bar = s0 + kTcBar + 8 * group;
+    volatile int* flag = reinterpret_cast<volatile int*>(smem + kTcFlag) + group;
+    if (row == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar));
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
         *flag = 0;
@@ -505,15 +516,17 @@ __global__ void __launch_bounds__(kTcRows) k_nrc_infer_tc(const bf16* __restrict
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    const uint32_t tmem = *reinterpret_cast<const uint32_t*>(smem + kTcTmem);
-    const uint32_t lane_addr = tmem + ((warp * 32u) << 16);
+    const uint32_t tmem = *reinterpret_cast<const uint32_t*>(smem + kTcTmem) + 64u * group;
+    const uint32_t lane_addr = tmem + (((warp & 3u) * 32u) << 16);
+    unsigned char* A = smem + kTcA + group * kTcABytes;
+    const uint32_t a_s = s0 + kTcA + group * kTcABytes;
 
     const uint32_t n = PATHS ? *count : n_host;
     if (total && blockIdx.x == 0 && tid == 0) atomicAdd(total, n);
     const uint32_t tiles = (n + kTcRows - 1) / kTcRows;
     uint32_t phase = 0;
-    for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
-        const uint32_t r = tile * kTcRows + tid;
+    for (uint32_t tile = blockIdx.x * kTcGroups + group; tile < tiles; tile += gridDim.x * kTcGroups) {
+        const uint32_t r = tile * kTcRows + row;
         // layer-0 operand: this thread's row, encoded
         {
             float e[80];
@@ -530,7 +543,7 @@ __global__ void __launch_bounds__(kTcRows) k_nrc_infer_tc(const bf16* __restrict
             for (int c = 0; c < 10; ++c) {
                 const uint4 v = make_uint4(pack2(e[8 * c], e[8 * c + 1]), pack2(e[8 * c + 2], e[8 * c + 3]),
                                            pack2(e[8 * c + 4], e[8 * c + 5]), pack2(e[8 * c + 6], e[8 * c + 7]));
-                *reinterpret_cast<uint4*>(smem + kTcA + canon_off(tid, 8 * c, 10)) = v;
+                *reinterpret_cast<uint4*>(A + canon_off(row, 8 * c, 10)) = v;
             }
         }
         bool timed_out = false;
@@ -539,15 +552,16 @@ __global__ void __launch_bounds__(kTcRows) k_nrc_infer_tc(const bf16* __restrict
         for (uint32_t l = 0; l < 5; ++l) {
             fence_async_smem();
             tc_fence_before();
-            __syncthreads();
+            group_sync(group);
             tc_fence_after();
-            if (tid == 0) {
+            if (row == 0) {
                 const uint32_t w = l == 0 ? kTcW0 : (l == 4 ? kTcW4 : kTcW1 + (l - 1) * 64 * 64 * 2);
-                tc_layer(tmem, s0 + kTcA, s0 + w, l == 0 ? 10 : 8, l == 4 ? 16 : 64, bar);
+                tc_layer(tmem, a_s, s0 + w, l == 0 ? 10 : 8, l == 4 ? 16 : 64, bar);
             }
-            const bool ok = tc_wait(bar, phase);
+            if (!tc_wait(bar, phase)) *flag = 1;
             phase ^= 1;
-            if (__syncthreads_or(!ok)) {
+            group_sync(group);
+            if (*flag) {
                 timed_out = true;
                 break;
             }
@@ -565,7 +579,7 @@ __global__ void __launch_bounds__(kTcRows) k_nrc_infer_tc(const bf16* __restrict
                                                    pack2(fmaxf(x[2], 0.0f), fmaxf(x[3], 0.0f)),
                                                    pack2(fmaxf(x[4], 0.0f), fmaxf(x[5], 0.0f)),
                                                    pack2(fmaxf(x[6], 0.0f), fmaxf(x[7], 0.0f)));
-                        *reinterpret_cast<uint4*>(smem + kTcA + canon_off(tid, 16 * q + 8 * c, 8)) = o;
+                        *reinterpret_cast<uint4*>(A + canon_off(row, 16 * q + 8 * c, 8)) = o;
                     }
                 }
             } else {
@@ -574,10 +588,7 @@ __global__ void __launch_bounds__(kTcRows) k_nrc_infer_tc(const bf16* __restrict
             }
         }
         if (timed_out) {
-            if (tid == 0) {
-                atomicOr(err, MT_ERRBIT_TIMEOUT);
-                *flag = 1;
-            }
+            if (row == 0) atomicOr(err, MT_ERRBIT_TIMEOUT);
             break;
         }
         if (r < n) {
@@ -595,16 +606,14 @@ __global__ void __launch_bounds__(kTcRows) k_nrc_infer_tc(const bf16* __restrict
         }
     }
     // release TMEM only when no MMA of this CTA can still be in flight: after a
-    // timeout, wait (bounded) for the last commit before deallocating
+    // timeout, wait (bounded) for the warpgroup's last commit first
+    if (*flag && row == 0) (void)tc_wait(bar, phase ^ 1);
     tc_fence_before();
     __syncthreads();
-    if (*flag) {
-        if (tid == 0) (void)tc_wait(bar, phase ^ 1);
-        __syncthreads();
-    }
     if (warp == 0) {
         tc_fence_after();
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(kTcCols));
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem - 64u * group),
+                     "r"(kTcCols));
     }
 }
 
@@ -965,11 +974,11 @@ cudaError_t infer(const void* net, const float4* feat, uint32_t n_host, const ui
         static bool ok_tc = false;
         cudaError_t e = allow_smem(k_nrc_infer_tc<PATHS>, kTcSmem, ok_tc);
         if (e != cudaSuccess) return e;
-        uint64_t blocks = (static_cast<uint64_t>(capacity) + kTcRows - 1) / kTcRows;
-        const uint64_t cap = static_cast<uint64_t>(sms()) * 3;  // 3 x 56 KB of shared memory per SM
+        uint64_t blocks = (static_cast<uint64_t>(capacity) + kTcRows * kTcGroups - 1) / (kTcRows * kTcGroups);
+        const uint64_t cap = static_cast<uint64_t>(sms()) * 2;  // 2 x 77 KB of shared memory per SM
         if (blocks > cap) blocks = cap;
         if (blocks == 0) blocks = 1;
-        k_nrc_infer_tc<PATHS><<<static_cast<unsigned>(blocks), kTcRows, kTcSmem, st>>>(
+        k_nrc_infer_tc<PATHS><<<static_cast<unsigned>(blocks), kTcRows * kTcGroups, kTcSmem, st>>>(
             static_cast<const bf16*>(net), feat, n_host, count, out, P, total, err);
         return cudaGetLastError();
     }
