@@ -3,15 +3,16 @@
 // The cache maps a surface vertex (position, outgoing direction, normal,
 // roughness, albedos) to the radiance the rest of its path would carry back.
 // Network: 80 -> 64 -> 64 -> 64 -> 64 -> 3, ReLU, no biases; BF16 weights and
-// activations on the m16n8k16 tensor-core MMA with FP32 accumulation.
+// activations on the tensor cores with FP32 accumulation.
 //
-//   k_nrc_infer    fused encoding + 5 layers; a warp owns 16 rows, the
-//                  activations stay in registers between layers (the MMA
-//                  accumulator layout of one layer is the A-operand layout of
-//                  the next), the weights sit in shared memory.
-//   k_nrc_fwdbwd   the same forward pass, relative-L2 loss gradient, and the
-//                  backward pass through the activations; writes the layer
-//                  inputs and pre-activation gradients row-major (BF16).
+//   k_nrc_infer_tc fused encoding + 5 layers on tcgen05 (TMEM accumulators,
+//                  operands in shared memory), 128-row tiles per warpgroup.
+//   k_nrc_fwdbwd   forward pass on mma.sync m16n8k16 (a warp owns 16 rows,
+//                  the accumulator layout of one layer is the A-operand layout
+//                  of the next, so activations stay in registers), the
+//                  relative-L2 loss gradient and the backward pass through the
+//                  activations; writes the layer inputs and pre-activation
+//                  gradients row-major (BF16).
 //   k_nrc_wgrad    dW_l = sum over rows of delta_l^T x input_l: 64-row chunks
 //                  staged in shared memory, transposed operands fetched with
 //                  ldmatrix.trans, one partial sum per block (fixed order).
@@ -23,7 +24,6 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
-#include <cstdlib>
 
 #include "mt_device.cuh"
 #include "mt_nrc.h"
@@ -292,66 +292,6 @@ __device__ __forceinline__ void copy_blob(bf16* dst, const bf16* __restrict__ sr
     const uint4* s = reinterpret_cast<const uint4*>(src);
     uint4* d = reinterpret_cast<uint4*>(dst);
     for (int i = threadIdx.x; i < elems / 8; i += blockDim.x) d[i] = s[i];
-}
-
-// ---------------------------------------------------------------------------
-// Inference
-// ---------------------------------------------------------------------------
-constexpr int kInferWarps = 8;
-
-// PATHS: rec are query records of a render batch (count on the device) and the
-// result goes to the owning path's indirect light; otherwise feat -> out.
-template <bool PATHS>
-__global__ void __launch_bounds__(kInferWarps * 32) k_nrc_infer(const bf16* __restrict__ blob,
-                                                                const float4* __restrict__ feat, uint32_t n_host,
-                                                                const uint32_t* __restrict__ count,
-                                                                float* __restrict__ out, PathState P,
-                                                                uint32_t* total)
-{
-    extern __shared__ __align__(16) unsigned char smem[];
-    bf16* W = reinterpret_cast<bf16*>(smem);
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    bf16* stg = W + kNrcFwdElems + warp * 16 * 88;
-    copy_blob(W, blob, kNrcFwdElems);
-    __syncthreads();
-    const uint32_t n = PATHS ? *count : n_host;
-    if (total && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(total, n);
-    const uint32_t tiles = (n + 15) / 16;
-    for (uint32_t tile = blockIdx.x * kInferWarps + warp; tile < tiles; tile += gridDim.x * kInferWarps) {
-        const uint32_t r0 = tile * 16;
-        stage_rows(feat, PATHS ? 6 : 5, r0, n, nullptr, stg);
-        __syncwarp();
-        uint32_t ax[5][4];
-        load_x_frags(stg, ax);
-        __syncwarp();
-        Hidden H;
-        float y[1][4];
-        forward(W, ax, H, y);
-        // column 2 lives in the neighbouring lane (t = 1)
-        const float c2a = __shfl_down_sync(0xffffffffu, y[0][0], 1);
-        const float c2b = __shfl_down_sync(0xffffffffu, y[0][2], 1);
-        if (t == 0) {
-#pragma unroll
-            for (int half = 0; half < 2; ++half) {
-                const uint32_t r = r0 + g + 8 * half;
-                if (r >= n) continue;
-                const float v0 = half ? y[0][2] : y[0][0];
-                const float v1 = half ? y[0][3] : y[0][1];
-                const float v2 = half ? c2b : c2a;
-                if (PATHS) {
-                    const float4 q = feat[6ull * r + 5];  // throughput, path index
-                    const uint32_t p = __float_as_uint(q.w);
-                    const float4 a = P.indirect[p];
-                    P.indirect[p] = make_float4(a.x + q.x * fmaxf(v0, 0.0f), a.y + q.y * fmaxf(v1, 0.0f),
-                                                a.z + q.z * fmaxf(v2, 0.0f), a.w);
-                } else {
-                    out[3ull * r + 0] = v0;
-                    out[3ull * r + 1] = v1;
-                    out[3ull * r + 2] = v2;
-                }
-            }
-        }
-    }
 }
 
 // ---------------------------------------------------------------------------
@@ -942,7 +882,6 @@ int sms()
     return g_sms_nrc;
 }
 
-constexpr size_t kInferSmem = (kNrcFwdElems + kInferWarps * 16 * 88) * sizeof(bf16);
 constexpr size_t kTrainSmem =
     (kNrcFwdElems + kNrcBwdElems + kTrainWarps * 16 * 88) * sizeof(bf16) + kTrainWarps * 16 * sizeof(uint32_t);
 constexpr size_t kWgSmem = kWgElems * sizeof(bf16);
@@ -957,41 +896,19 @@ cudaError_t allow_smem(K kernel, size_t bytes, bool& done)
     return e;
 }
 
-bool use_tc()
-{
-    static const bool tc = [] {
-        const char* v = std::getenv("MT_NRC_TC");
-        return !(v && v[0] == '0');
-    }();
-    return tc;
-}
-
 template <bool PATHS>
 cudaError_t infer(const void* net, const float4* feat, uint32_t n_host, const uint32_t* count, uint32_t capacity,
                   float* out, const PathState& P, uint32_t* total, int* err, cudaStream_t st)
 {
-    if (use_tc()) {
-        static bool ok_tc = false;
-        cudaError_t e = allow_smem(k_nrc_infer_tc<PATHS>, kTcSmem, ok_tc);
-        if (e != cudaSuccess) return e;
-        uint64_t blocks = (static_cast<uint64_t>(capacity) + kTcRows * kTcGroups - 1) / (kTcRows * kTcGroups);
-        const uint64_t cap = static_cast<uint64_t>(sms()) * 2;  // 2 x 77 KB of shared memory per SM
-        if (blocks > cap) blocks = cap;
-        if (blocks == 0) blocks = 1;
-        k_nrc_infer_tc<PATHS><<<static_cast<unsigned>(blocks), kTcRows * kTcGroups, kTcSmem, st>>>(
-            static_cast<const bf16*>(net), feat, n_host, count, out, P, total, err);
-        return cudaGetLastError();
-    }
     static bool ok = false;
-    cudaError_t e = allow_smem(k_nrc_infer<PATHS>, kInferSmem, ok);
+    cudaError_t e = allow_smem(k_nrc_infer_tc<PATHS>, kTcSmem, ok);
     if (e != cudaSuccess) return e;
-    const uint64_t tiles = (static_cast<uint64_t>(capacity) + 15) / 16;
-    uint64_t blocks = (tiles + kInferWarps - 1) / kInferWarps;
-    const uint64_t cap = static_cast<uint64_t>(sms()) * 3;
+    uint64_t blocks = (static_cast<uint64_t>(capacity) + kTcRows * kTcGroups - 1) / (kTcRows * kTcGroups);
+    const uint64_t cap = static_cast<uint64_t>(sms()) * 2;  // 2 x 77 KB of shared memory per SM
     if (blocks > cap) blocks = cap;
     if (blocks == 0) blocks = 1;
-    k_nrc_infer<PATHS><<<static_cast<unsigned>(blocks), kInferWarps * 32, kInferSmem, st>>>(
-        static_cast<const bf16*>(net), feat, n_host, count, out, P, total);
+    k_nrc_infer_tc<PATHS><<<static_cast<unsigned>(blocks), kTcRows * kTcGroups, kTcSmem, st>>>(
+        static_cast<const bf16*>(net), feat, n_host, count, out, P, total, err);
     return cudaGetLastError();
 }
 
