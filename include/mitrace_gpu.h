@@ -289,7 +289,9 @@ mt_status mt_render_rows_noalloc(mt_handle* h, uint32_t row0, uint32_t row1, flo
 /* Device buffers of mt_render_grad.  Gradients are ADDED to d_* (zero them
  * first).  d_texels covers the texels of every RGB32F texture that some
  * material uses as its base-colour texture, W*H*3 floats each, concatenated in
- * texture-index order; pass NULL to skip texel gradients. */
+ * texture-index order; pass NULL to skip texel gradients.  With d_image set,
+ * the gradient that flows into the image is d_image itself (any loss of the
+ * caller's); target may then be NULL and loss is not written. */
 typedef struct mt_grad_buffers {
     const float* target; /* W*H*3 target image                                  */
     float* image;        /* W*H*3 out: the rendered image                       */
@@ -299,6 +301,7 @@ typedef struct mt_grad_buffers {
     float* d_metallic;   /* num_materials: dL/d metallic_factor                  */
     float* d_light;      /* num_lights: dL/d s, light colour scaled by s at s=1  */
     float* d_texels;     /* see above, or NULL                                   */
+    const float* d_image; /* W*H*3 dL/d(image), or NULL for the L2 loss above   */
 } mt_grad_buffers;
 
 #define MT_GRAD_MAX_BOUNCES 16
@@ -468,6 +471,31 @@ typedef struct mt_brdf_result {
 
 /* Host buffers; needs no scene (h may be NULL). */
 mt_status mt_brdf_batch(const mt_brdf_query* q, uint64_t n, mt_brdf_result* out);
+
+/* One bounce sample of GeneratePath (Tracer.cpp:177-203, SampleGGXDirection
+ * 49-72, cosine sampling 26-47) with its uniforms given: u[0] picks the lobe
+ * (GGX when below the specular probability), u[1], u[2] draw the direction,
+ * u[3], u[4] the cosine fallback of a GGX reflection below the surface. */
+typedef struct mt_brdf_sample_query {
+    float V[3];
+    float N[3];
+    float base_color[3];
+    float roughness;
+    float metallic;
+    float u[5];
+} mt_brdf_sample_query;
+
+/* Sampled direction L, the mixture pdf (1-ps) DiffusePdf + ps SpecularPdf,
+ * the specular probability ps, and the lobe: 0 cosine, 1 GGX, 2 GGX fell back
+ * to cosine. */
+typedef struct mt_brdf_sample_result {
+    float L[3];
+    float pdf;
+    float specular_probability;
+    int32_t lobe;
+} mt_brdf_sample_result;
+
+mt_status mt_brdf_sample_batch(const mt_brdf_sample_query* q, uint64_t n, mt_brdf_sample_result* out);
 
 /* ------------------------------------------------------------------------ */
 /* Host BVH builder.                                                        */

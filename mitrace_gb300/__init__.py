@@ -23,7 +23,7 @@ from .scenes import (
     incoherent_rays,
     scene_bounds,
 )
-from .tracer import Tracer, Stats, brdf_batch, bvh_build, image_rgb8_device, nrc_encode_device, write_hdr, write_png
+from .tracer import Tracer, Stats, brdf_batch, brdf_sample_batch, bvh_build, image_rgb8_device, nrc_encode_device, write_hdr, write_png
 
 __all__ = [
     "MTError",
@@ -44,6 +44,7 @@ __all__ = [
     "Tracer",
     "Stats",
     "brdf_batch",
+    "brdf_sample_batch",
     "bvh_build",
     "nrc_encode_device",
     "image_rgb8_device",

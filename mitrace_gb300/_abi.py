@@ -200,6 +200,7 @@ class mt_grad_buffers(C.Structure):
         ("d_metallic", C.c_void_p),
         ("d_light", C.c_void_p),
         ("d_texels", C.c_void_p),
+        ("d_image", C.c_void_p),
     ]
 
 
@@ -254,6 +255,16 @@ class mt_brdf_result(C.Structure):
     _fields_ = [("f", C.c_float * 3), ("diffuse_pdf", C.c_float), ("specular_pdf", C.c_float)]
 
 
+class mt_brdf_sample_query(C.Structure):
+    _fields_ = [("V", C.c_float * 3), ("N", C.c_float * 3), ("base_color", C.c_float * 3), ("roughness", C.c_float),
+                ("metallic", C.c_float), ("u", C.c_float * 5)]
+
+
+class mt_brdf_sample_result(C.Structure):
+    _fields_ = [("L", C.c_float * 3), ("pdf", C.c_float), ("specular_probability", C.c_float),
+                ("lobe", C.c_int32)]
+
+
 # Every entry point declared in include/mitrace_gpu.h: (name, restype, argtypes).
 _VP = C.c_void_p
 PROTOTYPES = [
@@ -280,6 +291,7 @@ PROTOTYPES = [
     ("mt_trace_rays", C.c_int, [_VP, _VP, C.c_uint64, _VP, C.c_int]),
     ("mt_trace_rays_device", C.c_int, [_VP, _VP, C.c_uint64, _VP, C.c_int, _VP]),
     ("mt_brdf_batch", C.c_int, [_VP, C.c_uint64, _VP]),
+    ("mt_brdf_sample_batch", C.c_int, [_VP, C.c_uint64, _VP]),
     ("mt_bvh_build", C.c_int, [_VP, C.c_uint32, C.c_uint32, C.c_uint32, C.POINTER(C.POINTER(mt_bvh_node)),
                                C.POINTER(C.c_uint32), C.POINTER(C.POINTER(C.c_uint32)), C.POINTER(C.c_uint32)]),
     ("mt_bvh_free", None, [_VP, _VP]),

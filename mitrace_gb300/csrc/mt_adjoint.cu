@@ -233,7 +233,8 @@ __device__ VertexMat vertex_material(const DevScene& S, uint32_t mi, float u, fl
 __global__ void k_grad_pixel(const float* __restrict__ sr, const float* __restrict__ sg,
                              const float* __restrict__ sb, uint32_t band_pix, uint32_t spp, uint32_t pix_base,
                              int enable, float kf, const float* __restrict__ image,
-                             const float* __restrict__ target, float4* __restrict__ pix, float* loss)
+                             const float* __restrict__ target, const float* __restrict__ dimg,
+                             float4* __restrict__ pix, float* loss)
 {
     float local = 0.0f;
     for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < band_pix; j += gridDim.x * blockDim.x) {
@@ -262,15 +263,22 @@ __global__ void k_grad_pixel(const float* __restrict__ sr, const float* __restri
             if (kept == 0) kept = 1;
         }
         const uint64_t px = pix_base + j;
-        const float rx = image[3 * px] - target[3 * px];
-        const float ry = image[3 * px + 1] - target[3 * px + 1];
-        const float rz = image[3 * px + 2] - target[3 * px + 2];
-        local += rx * rx + ry * ry + rz * rz;
+        float rx, ry, rz;  // half of dL/d(image)
+        if (dimg) {
+            rx = 0.5f * dimg[3 * px];
+            ry = 0.5f * dimg[3 * px + 1];
+            rz = 0.5f * dimg[3 * px + 2];
+        } else {
+            rx = image[3 * px] - target[3 * px];
+            ry = image[3 * px + 1] - target[3 * px + 1];
+            rz = image[3 * px + 2] - target[3 * px + 2];
+            local += rx * rx + ry * ry + rz * rz;
+        }
         pix[2 * j] = make_float4(mean, thr, 2.0f / static_cast<float>(kept), 0.0f);
         pix[2 * j + 1] = make_float4(rx, ry, rz, 0.0f);
     }
     for (int o = 16; o > 0; o >>= 1) local += __shfl_down_sync(0xffffffffu, local, o);
-    if ((threadIdx.x & 31) == 0) atomicAdd(loss, local);
+    if ((threadIdx.x & 31) == 0 && loss) atomicAdd(loss, local);
 }
 
 // One thread per path of a recorded batch.
@@ -413,7 +421,8 @@ cudaError_t launch_grad_pixel(const DevScene& S, const WaveBuffers& W, uint32_t 
 {
     const unsigned grid = static_cast<unsigned>((band_pix + 255) / 256 < 4096 ? (band_pix + 255) / 256 : 4096);
     k_grad_pixel<<<grid ? grid : 1, 256, 0, st>>>(W.sr, W.sg, W.sb, band_pix, S.spp, pix_base, S.firefly_enable,
-                                                   S.firefly_k, image, G.target, G.pix, G.loss);
+                                                   S.firefly_k, image, G.target, G.d_image, G.pix,
+                                                   G.d_image ? nullptr : G.loss);
     return cudaGetLastError();
 }
 

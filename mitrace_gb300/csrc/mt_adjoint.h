@@ -12,7 +12,8 @@
 namespace mt {
 
 struct GradParams {
-    const float* target;       // W*H*3
+    const float* target;       // W*H*3, or nullptr when d_image is given
+    const float* d_image;      // W*H*3 dL/d(image), or nullptr for the L2 loss
     float* loss;               // 1
     float* d_base;             // materials * 3
     float* d_rough;            // materials

@@ -1038,7 +1038,8 @@ mt_status mt_render_device(mt_handle* h, float* d_rgb_out, void* cuda_stream)
 mt_status mt_render_grad(mt_handle* h, const mt_grad_buffers* g, void* cuda_stream)
 {
     if (check_handle(h) != MT_OK || !g) return set_err(MT_ERR_INVALID, "null argument");
-    if (!g->target || !g->image || !g->loss || !g->d_base || !g->d_roughness || !g->d_metallic ||
+    if ((!g->target && !g->d_image) || !g->image || (!g->loss && !g->d_image) || !g->d_base || !g->d_roughness ||
+        !g->d_metallic ||
         (!g->d_light && h->S.num_lights))
         return set_err(MT_ERR_INVALID, "target, image, loss and the material/light gradient buffers are required");
     if (h->running) return set_err(MT_ERR_STATE, "an asynchronous render is running");
@@ -1060,6 +1061,7 @@ mt_status mt_render_grad(mt_handle* h, const mt_grad_buffers* g, void* cuda_stre
     const WaveViews v = views(h);
     GradParams G{};
     G.target = g->target;
+    G.d_image = g->d_image;
     G.loss = g->loss;
     G.d_base = g->d_base;
     G.d_rough = g->d_roughness;
@@ -1074,7 +1076,7 @@ mt_status mt_render_grad(mt_handle* h, const mt_grad_buffers* g, void* cuda_stre
     RecordBuffers R;
     R.vert = h->rec_vert.p;
     R.path = h->rec_path.p;
-    MT_CUDA(cudaMemsetAsync(g->loss, 0, sizeof(float), st));
+    if (!g->d_image) MT_CUDA(cudaMemsetAsync(g->loss, 0, sizeof(float), st));
     MT_CUDA(cudaMemsetAsync(h->rays.p, 0, 2 * sizeof(unsigned long long), st));
     uint64_t launches = 0;
     for (uint64_t r0 = 0; r0 < c.height; r0 += rows_per_band) {
@@ -1132,6 +1134,23 @@ mt_status mt_trace_rays(mt_handle* h, const mt_ray* rays, uint64_t n, mt_hit* hi
     int flag = 0;
     MT_CUDA(cudaMemcpy(&flag, h->error_flag.p, sizeof(int), cudaMemcpyDeviceToHost));
     if (flag) return set_err(MT_ERR_INVALID, "device error flag set (traversal stack overflow)");
+    return MT_OK;
+}
+
+mt_status mt_brdf_sample_batch(const mt_brdf_sample_query* q, uint64_t n, mt_brdf_sample_result* out)
+{
+    if (n == 0) return MT_OK;
+    if (!q || !out) return set_err(MT_ERR_INVALID, "null argument");
+    mt_brdf_sample_query* dq = nullptr;
+    mt_brdf_sample_result* dr = nullptr;
+    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(&dq), n * sizeof(mt_brdf_sample_query));
+    if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&dr), n * sizeof(mt_brdf_sample_result));
+    if (e == cudaSuccess) e = cudaMemcpy(dq, q, n * sizeof(mt_brdf_sample_query), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = launch_brdf_sample(dq, n, dr, 0);
+    if (e == cudaSuccess) e = cudaMemcpy(out, dr, n * sizeof(mt_brdf_sample_result), cudaMemcpyDeviceToHost);
+    if (dq) cudaFree(dq);
+    if (dr) cudaFree(dr);
+    if (e != cudaSuccess) return set_err(MT_ERR_CUDA, cudaGetErrorString(e));
     return MT_OK;
 }
 

@@ -698,6 +698,28 @@ __device__ __forceinline__ float specular_probability(f3 view, f3 n, f3 base, fl
     const float p = __fdiv_rn(__fadd_rn(__fadd_rn(f.x, f.y), f.z), 3.0f);
     return gclamp(p, 0.05f, 0.95f);
 }
+
+// SampleGGXDirection (Tracer.cpp:49-72) with its two uniforms given: the half
+// vector of the GGX lobe, flipped toward the viewer, and the reflection of the
+// incident direction rd about it.  False when the reflection points below the
+// surface (the caller then draws a cosine sample instead).
+__device__ __forceinline__ bool ggx_reflection(f3 rd, f3 N, float roughness, float u1, float u2, f3& out)
+{
+    const float alpha = gmax(__fmul_rn(roughness, roughness), 0.0025f);
+    const float alpha2 = __fmul_rn(alpha, alpha);
+    const float phi = __fmul_rn(__fmul_rn(2.0f, kPi), u2);
+    const float tan2 = __fdiv_rn(__fmul_rn(alpha2, u1), gmax(__fsub_rn(1.0f, u1), 0.0001f));
+    const float cosT = __fdiv_rn(1.0f, __fsqrt_rn(__fadd_rn(1.0f, tan2)));
+    const float sinT = __fsqrt_rn(gmax(0.0f, __fsub_rn(1.0f, __fmul_rn(cosT, cosT))));
+    f3 t, b;
+    build_tbn(N, t, b);
+    f3 h = normalize(t * __fmul_rn(sinT, cosf(phi)) + b * __fmul_rn(sinT, sinf(phi)) + N * cosT);
+    if (dot(h, -rd) < 0.0f) h = -h;
+    const f3 r = reflect(rd, h);
+    if (!(dot(r, N) > 0.0f)) return false;
+    out = normalize(r);
+    return true;
+}
 __device__ __forceinline__ f3 compute_normal(f3 surf, f3 tex)
 {
     const f3 n = normalize(surf);

@@ -118,6 +118,41 @@ __global__ void k_brdf(const mt_brdf_query* __restrict__ q, uint64_t n, mt_brdf_
     }
 }
 
+// The bounce sampling of GeneratePath (Tracer.cpp:177-203) with its uniforms
+// given: lobe choice, direction, and the mixture pdf.
+__global__ void k_brdf_sample(const mt_brdf_sample_query* __restrict__ q, uint64_t n,
+                              mt_brdf_sample_result* __restrict__ out)
+{
+    for (uint64_t i = blockIdx.x * static_cast<uint64_t>(blockDim.x) + threadIdx.x; i < n;
+         i += static_cast<uint64_t>(gridDim.x) * blockDim.x) {
+        const mt_brdf_sample_query x = q[i];
+        const f3 V = ld3(x.V), N = ld3(x.N), B = ld3(x.base_color);
+        const f3 rd = -V;
+        const float ps = specular_probability(V, N, B, x.metallic);
+        f3 nd;
+        int lobe = 0;
+        if (x.u[0] < ps) {
+            lobe = 1;
+            if (!ggx_reflection(rd, N, x.roughness, x.u[1], x.u[2], nd)) {
+                lobe = 2;
+                nd = cosine_hemisphere(x.u[3], x.u[4], N);
+            }
+        } else {
+            nd = cosine_hemisphere(x.u[1], x.u[2], N);
+        }
+        const float dp = diffuse_pdf(nd, N);
+        const float sp = specular_pdf(nd, V, N, x.roughness);
+        mt_brdf_sample_result r;
+        r.L[0] = nd.x;
+        r.L[1] = nd.y;
+        r.L[2] = nd.z;
+        r.pdf = __fadd_rn(__fmul_rn(__fsub_rn(1.0f, ps), dp), __fmul_rn(ps, sp));
+        r.specular_probability = ps;
+        r.lobe = lobe;
+        out[i] = r;
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Wavefront render stages
 // ---------------------------------------------------------------------------
@@ -499,22 +534,7 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, PathState P, ShadowQu
         const uint4 rl = draw(S, pixel, sample, bounce, SLOT_LOBE);
         f3 nd;
         if (urange(rl.x, 0.0f, 1.0f) < ps) {
-            // SampleGGXDirection (Tracer.cpp:49-72)
-            const float u1 = urange(rl.y, 0.0f, 1.0f), u2 = urange(rl.z, 0.0f, 1.0f);
-            const float alpha = gmax(__fmul_rn(mp.roughness, mp.roughness), 0.0025f);
-            const float alpha2 = __fmul_rn(alpha, alpha);
-            const float phi = __fmul_rn(__fmul_rn(2.0f, kPi), u2);
-            const float tan2 = __fdiv_rn(__fmul_rn(alpha2, u1), gmax(__fsub_rn(1.0f, u1), 0.0001f));
-            const float cosT = __fdiv_rn(1.0f, __fsqrt_rn(__fadd_rn(1.0f, tan2)));
-            const float sinT = __fsqrt_rn(gmax(0.0f, __fsub_rn(1.0f, __fmul_rn(cosT, cosT))));
-            f3 t, b;
-            build_tbn(N, t, b);
-            f3 h = normalize(t * __fmul_rn(sinT, cosf(phi)) + b * __fmul_rn(sinT, sinf(phi)) + N * cosT);
-            if (dot(h, -rd) < 0.0f) h = -h;
-            const f3 r = reflect(rd, h);
-            if (dot(r, N) > 0.0f) {
-                nd = normalize(r);
-            } else {
+            if (!ggx_reflection(rd, N, mp.roughness, urange(rl.y, 0.0f, 1.0f), urange(rl.z, 0.0f, 1.0f), nd)) {
                 const uint4 rf = draw(S, pixel, sample, bounce, SLOT_FALLBACK);
                 nd = cosine_hemisphere(urange(rf.x, 0.0f, 1.0f), urange(rf.y, 0.0f, 1.0f), N);
             }
@@ -813,6 +833,14 @@ cudaError_t launch_brdf(const mt_brdf_query* q, uint64_t n, mt_brdf_result* out,
 {
     if (n == 0) return cudaSuccess;
     k_brdf<<<grid_for(n, 128, 32), 128, 0, st>>>(q, n, out);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_brdf_sample(const mt_brdf_sample_query* q, uint64_t n, mt_brdf_sample_result* out,
+                               cudaStream_t st)
+{
+    if (n == 0) return cudaSuccess;
+    k_brdf_sample<<<grid_for(n, 128, 32), 128, 0, st>>>(q, n, out);
     return cudaGetLastError();
 }
 

@@ -89,6 +89,8 @@ struct Profiler {
 cudaError_t launch_trace(const DevScene& S, const mt_ray* rays, uint64_t n, mt_hit* hits, int query,
                          uint32_t* fetch, cudaStream_t st);
 cudaError_t launch_brdf(const mt_brdf_query* q, uint64_t n, mt_brdf_result* out, cudaStream_t st);
+cudaError_t launch_brdf_sample(const mt_brdf_sample_query* q, uint64_t n, mt_brdf_sample_result* out,
+                               cudaStream_t st);
 struct NrcShade;
 // Optional batch settings beyond a plain band render.
 struct BatchExtra {

@@ -77,10 +77,11 @@ class Tracer:
 
     def render_grad_device(self, target_ptr: int, image_ptr: int, loss_ptr: int, d_base_ptr: int,
                            d_rough_ptr: int, d_metal_ptr: int, d_light_ptr: int, d_texels_ptr: int = 0,
-                           stream_ptr: int = 0):
-        """mt_render_grad on device buffers (gradients are added to the d_* buffers)."""
-        g = A.mt_grad_buffers(target_ptr, image_ptr, loss_ptr, d_base_ptr, d_rough_ptr, d_metal_ptr,
-                              d_light_ptr or None, d_texels_ptr or None)
+                           stream_ptr: int = 0, d_image_ptr: int = 0):
+        """mt_render_grad on device buffers (gradients are added to the d_* buffers);
+        with d_image_ptr the image gradient is given instead of a target."""
+        g = A.mt_grad_buffers(target_ptr or None, image_ptr, loss_ptr or None, d_base_ptr, d_rough_ptr, d_metal_ptr,
+                              d_light_ptr or None, d_texels_ptr or None, d_image_ptr or None)
         A.check(A.lib.mt_render_grad(self.handle, C.byref(g), C.c_void_p(stream_ptr)), "mt_render_grad")
 
     # --- neural radiance cache ---------------------------------------------------
@@ -154,6 +155,17 @@ def brdf_batch(q: np.ndarray) -> np.ndarray:
     out = np.zeros((q.shape[0], 5), dtype=np.float32)
     A.check(A.lib.mt_brdf_batch(q.ctypes.data_as(C.c_void_p), q.shape[0], out.ctypes.data_as(C.c_void_p)),
             "mt_brdf_batch")
+    return out
+
+
+def brdf_sample_batch(q: np.ndarray) -> np.ndarray:
+    """q: (n, 16) float32 in mt_brdf_sample_query layout -> (n, 6) float32 rows
+    (L xyz, pdf, specular probability, lobe as int32 bits)."""
+    q = np.ascontiguousarray(q, dtype=np.float32)
+    assert q.ndim == 2 and q.shape[1] == 16
+    out = np.zeros((q.shape[0], 6), dtype=np.float32)
+    A.check(A.lib.mt_brdf_sample_batch(q.ctypes.data_as(C.c_void_p), q.shape[0], out.ctypes.data_as(C.c_void_p)),
+            "mt_brdf_sample_batch")
     return out
 
 

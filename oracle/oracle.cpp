@@ -881,10 +881,20 @@ V3 sample_cosine(Rng& rng, uint32_t bounce, uint32_t slot, uint32_t c0, V3 n)
     return cosine_hemisphere(u1, u2, n);
 }
 
+// SampleGGXDirection's reflection for given uniforms; false when it points
+// below the surface.
+bool ggx_reflection(V3 incident, V3 n, float roughness, float u1, float u2, V3& out);
+
 V3 sample_ggx(Rng& rng, uint32_t bounce, V3 incident, V3 n, float roughness)
 {
     const float u1 = rng.uniform(0.0f, 1.0f, bounce, SLOT_LOBE, 1);
     const float u2 = rng.uniform(0.0f, 1.0f, bounce, SLOT_LOBE, 2);
+    V3 r;
+    return ggx_reflection(incident, n, roughness, u1, u2, r) ? r : sample_cosine(rng, bounce, SLOT_FALLBACK, 0, n);
+}
+
+bool ggx_reflection(V3 incident, V3 n, float roughness, float u1, float u2, V3& out)
+{
     const float alpha = gmax(roughness * roughness, 0.0025f);
     const float alpha2 = alpha * alpha;
     const float phi = 2.0f * kPi * u2;
@@ -896,7 +906,9 @@ V3 sample_ggx(Rng& rng, uint32_t bounce, V3 incident, V3 n, float roughness)
     V3 h = normalize(t * (sinT * std::cos(phi)) + b * (sinT * std::sin(phi)) + n * cosT);
     if (dot(h, -incident) < 0.0f) h = -h;
     const V3 r = reflect(incident, h);
-    return (dot(r, n) > 0.0f) ? normalize(r) : sample_cosine(rng, bounce, SLOT_FALLBACK, 0, n);
+    if (!(dot(r, n) > 0.0f)) return false;
+    out = normalize(r);
+    return true;
 }
 
 float specular_probability(V3 view, V3 n, V3 base, float metallic)
@@ -1760,6 +1772,37 @@ int orc_trace_f64(const orc_scene* s, const mt_ray* rays, const mt_hit* hits, ui
         r[0] = std::sqrt(dx * dx + dy * dy + dz * dz);
         r[1] = u;
         r[2] = v;
+    }
+    return MT_OK;
+}
+
+// GeneratePath's bounce sampling (Tracer.cpp:177-203) with explicit uniforms.
+int orc_brdf_sample(const mt_brdf_sample_query* q, uint64_t n, mt_brdf_sample_result* out)
+{
+    if (!q || !out) return fail("null arg");
+    for (uint64_t i = 0; i < n; ++i) {
+        const mt_brdf_sample_query& x = q[i];
+        const V3 V{x.V[0], x.V[1], x.V[2]}, N{x.N[0], x.N[1], x.N[2]};
+        const V3 B{x.base_color[0], x.base_color[1], x.base_color[2]};
+        const float ps = specular_probability(V, N, B, x.metallic);
+        V3 nd;
+        int lobe = 0;
+        if (x.u[0] < ps) {
+            lobe = 1;
+            if (!ggx_reflection(-V, N, x.roughness, x.u[1], x.u[2], nd)) {
+                lobe = 2;
+                nd = cosine_hemisphere(x.u[3], x.u[4], N);
+            }
+        } else {
+            nd = cosine_hemisphere(x.u[1], x.u[2], N);
+        }
+        mt_brdf_sample_result& r = out[i];
+        r.L[0] = nd.x;
+        r.L[1] = nd.y;
+        r.L[2] = nd.z;
+        r.pdf = (1.0f - ps) * diffuse_pdf(nd, N) + ps * specular_pdf(nd, V, N, x.roughness);
+        r.specular_probability = ps;
+        r.lobe = lobe;
     }
     return MT_OK;
 }

@@ -62,6 +62,7 @@ int orc_trace_f64(const orc_scene* s, const mt_ray* rays, const mt_hit* hits, ui
 
 /* BRDF.hpp:52-97 on a batch. */
 int orc_brdf_batch(const mt_brdf_query* q, uint64_t n, mt_brdf_result* out);
+int orc_brdf_sample(const mt_brdf_sample_query* q, uint64_t n, mt_brdf_sample_result* out);
 
 /* Camera::GenerateCameraRay (src/Tracer/Camera.cpp:17-50) for (u, v) pairs. */
 int orc_camera_rays(const orc_scene* s, const float* uv, uint64_t n, mt_ray* out);

@@ -42,6 +42,7 @@ def load(fast: bool = False):
         "orc_trace_rays": (C.c_int, [vp, vp, C.c_uint64, vp, C.c_int, vp, C.c_int]),
         "orc_trace_f64": (C.c_int, [vp, vp, vp, C.c_uint64, vp]),
         "orc_brdf_batch": (C.c_int, [vp, C.c_uint64, vp]),
+        "orc_brdf_sample": (C.c_int, [vp, C.c_uint64, vp]),
         "orc_camera_rays": (C.c_int, [vp, vp, C.c_uint64, vp]),
         "orc_philox": (None, [vp, vp, vp]),
         "orc_render": (C.c_int, [vp, C.c_int, C.c_int, C.c_uint32, C.c_uint32, vp, C.POINTER(C.c_uint64),
@@ -107,6 +108,16 @@ def brdf_batch(q: np.ndarray) -> np.ndarray:
     q = np.ascontiguousarray(q, dtype=np.float32)
     out = np.zeros((q.shape[0], 5), dtype=np.float32)
     _check(L.orc_brdf_batch(_p(q), q.shape[0], _p(out)), L, "orc_brdf_batch")
+    return out
+
+
+def brdf_sample(q: np.ndarray) -> np.ndarray:
+    """q: (n, 16) float32 in mt_brdf_sample_query layout -> (n, 6) float32 rows
+    (L xyz, pdf, specular probability, lobe as int32 bits)."""
+    L = lib()
+    q = np.ascontiguousarray(q, dtype=np.float32)
+    out = np.zeros((q.shape[0], 6), dtype=np.float32)
+    _check(L.orc_brdf_sample(_p(q), q.shape[0], _p(out)), L, "orc_brdf_sample")
     return out
 
 

@@ -184,3 +184,26 @@ def test_autograd_function_backpropagates():
     g = gpu_grad(scene, cfg, target)
     np.testing.assert_allclose(base.grad.numpy(), g["d_base"], rtol=1e-6)
     assert np.abs(base.grad.numpy()).max() > 0
+
+
+def test_image_gradient_input_equals_l2_target_form():
+    """mt_render_grad with d_image = 2 (image - target) gives the same gradient
+    as the L2-loss form (any loss's image gradient can be supplied)."""
+    scene, cfg = CASES["box_room"]()
+    target = np.full((cfg.height, cfg.width, 3), 0.3, np.float32)
+    g = gpu_grad(scene, cfg, target)
+    nm, nl = len(scene.materials), len(scene.lights)
+    dimg = torch.from_numpy(2.0 * (g["image"] - target)).cuda()
+    out = {k: torch.zeros(v, device="cuda") for k, v in
+           (("image", cfg.height * cfg.width * 3), ("d_base", nm * 3), ("d_roughness", nm), ("d_metallic", nm),
+            ("d_light", max(nl, 1)))}
+    with mt.Tracer(scene, cfg) as tr:
+        tr.render_grad_device(0, out["image"].data_ptr(), 0, out["d_base"].data_ptr(), out["d_roughness"].data_ptr(),
+                              out["d_metallic"].data_ptr(), out["d_light"].data_ptr(), 0,
+                              torch.cuda.current_stream().cuda_stream, d_image_ptr=dimg.data_ptr())
+        torch.cuda.synchronize()
+    # equal up to the order of the atomic sums
+    np.testing.assert_allclose(out["d_base"].cpu().numpy().reshape(nm, 3), g["d_base"], rtol=1e-4, atol=1e-6)
+    np.testing.assert_allclose(out["d_roughness"].cpu().numpy(), g["d_roughness"], rtol=1e-4, atol=1e-6)
+    np.testing.assert_allclose(out["d_light"].cpu().numpy()[:nl], g["d_light"], rtol=1e-4, atol=1e-6)
+

@@ -271,3 +271,24 @@ def test_builder_rejects_empty_and_unsplittable():
             orc.bvh_build(pos, 32, 32)
         with pytest.raises(mt.MTError):
             mt.bvh_build(pos, 32, 32)
+
+
+def test_oracle_bounce_sampling_branches():
+    """The oracle's bounce sample with given uniforms: u[0] above the specular
+    probability picks the cosine lobe, whose direction and pdf follow
+    cosine_hemisphere; a GGX sample that reflects below the surface falls back."""
+    q = np.zeros((3, 16), np.float32)
+    q[:, 0:3] = [0.0, 1.0, 0.0]        # V
+    q[:, 3:6] = [0.0, 1.0, 0.0]        # N
+    q[:, 6:9] = 0.5
+    q[:, 9] = 0.5
+    q[:, 10] = 0.0
+    q[0, 11:16] = [0.999, 0.0, 0.25, 0.5, 0.5]   # cosine lobe, u1 = 0: straight up
+    q[1, 11:16] = [0.0, 0.3, 0.7, 0.5, 0.5]      # GGX lobe
+    q[2, 11:16] = [0.0, 0.999999, 0.1, 0.25, 0.5]  # GGX at grazing V? (V = N: reflection stays above)
+    r = orc.brdf_sample(q)
+    lobes = r[:, 5].view(np.int32)
+    assert lobes[0] == 0 and lobes[1] == 1
+    assert r[0, 1] > 0.99 and r[0, 3] > 0.0
+    assert np.all(np.abs(np.linalg.norm(r[:, 0:3], axis=1) - 1) < 1e-5)
+    assert np.all(r[:, 4] >= 0.05) and np.all(r[:, 4] <= 0.95)
