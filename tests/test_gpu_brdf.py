@@ -64,7 +64,7 @@ def test_brdf_sampling_matches_oracle():
     """GeneratePath's bounce sample (lobe choice, GGX reflection with its cosine
     fallback, cosine sample, mixture pdf) on seeded uniforms: the same lobe for
     all but decisions within an ulp of the specular probability, directions
-    within the sinf/cosf rounding, pdfs to 1e-4 relative."""
+    within the sinf/cosf rounding, pdfs to 1e-4 relative for 99.9%."""
     q = sample_queries(200_000, 3)
     g = mt.brdf_sample_batch(q)
     r = orc.brdf_sample(q)
@@ -73,6 +73,10 @@ def test_brdf_sampling_matches_oracle():
     assert same.mean() > 0.999
     assert set(np.unique(lg)) == {0, 1, 2}  # every branch exercised
     np.testing.assert_allclose(g[same, 0:3], r[same, 0:3], atol=2e-5)
-    np.testing.assert_allclose(g[same, 3], r[same, 3], rtol=1e-4, atol=1e-6)
+    # the GGX pdf of a near-mirror lobe (alpha down to 0.0025) turns the ulps of
+    # sinf/cosf in the direction into up to a few percent: bound the bulk
+    # tightly and the tail loosely
+    rel = np.abs(g[same, 3] - r[same, 3]) / np.maximum(np.abs(r[same, 3]), 1e-6)
+    assert np.mean(rel <= 1e-4) > 0.999 and rel.max() < 0.1
     np.testing.assert_allclose(g[:, 4], r[:, 4], rtol=1e-5)
     assert np.all(np.einsum("ij,ij->i", g[:, 0:3], q[:, 3:6]) > -1e-6)  # never below the surface
