@@ -306,6 +306,15 @@ typedef struct mt_grad_buffers {
 
 #define MT_GRAD_MAX_BOUNCES 16
 
+/* Parameter updates between renders of an inverse-rendering loop, without
+ * re-uploading the scene (blocking; not while mt_start runs).  The counts, the
+ * materials' texture slots and the lights' types must stay as uploaded. */
+mt_status mt_update_materials(mt_handle* h, const mt_material_desc* materials, uint32_t n);
+mt_status mt_update_lights(mt_handle* h, const mt_light_desc* lights, uint32_t n);
+/* Replaces all texels of texture index (same size and format as uploaded:
+ * W*H*3 bytes for RGB8, W*H*3 floats for RGB32F), host memory. */
+mt_status mt_update_texture(mt_handle* h, uint32_t index, const void* texels);
+
 /* Renders the image (same estimator and counter RNG as mt_render_device) and
  * accumulates dL/dparameters by replaying every path from its seed.  Sampling
  * decisions and pdfs, light-pick probabilities, the energy cut-off and the

@@ -279,6 +279,9 @@ PROTOTYPES = [
     ("mt_render_device", C.c_int, [_VP, _VP, _VP]),
     ("mt_render_rows_noalloc", C.c_int, [_VP, C.c_uint32, C.c_uint32, _VP, _VP]),
     ("mt_render_grad", C.c_int, [_VP, C.POINTER(mt_grad_buffers), _VP]),
+    ("mt_update_materials", C.c_int, [_VP, _VP, C.c_uint32]),
+    ("mt_update_lights", C.c_int, [_VP, _VP, C.c_uint32]),
+    ("mt_update_texture", C.c_int, [_VP, C.c_uint32, _VP]),
     ("mt_nrc_config_defaults", None, [C.POINTER(mt_nrc_config)]),
     ("mt_nrc_enable", C.c_int, [_VP, C.POINTER(mt_nrc_config)]),
     ("mt_nrc_frame", C.c_int, [_VP, _VP, C.c_uint32, _VP]),

@@ -189,6 +189,8 @@ struct mt_handle {
     DevArray<DevLight> lights;
     std::vector<DevArray<uint8_t>> tex8;
     std::vector<DevArray<float>> texf;
+    std::vector<DevMaterial> host_mats;  // as uploaded (mt_update_* keep the texture slots and light types)
+    std::vector<DevLight> host_lights;
     DevArray<int> error_flag;
     uint64_t scene_bytes = 0;
     float world_lo[3] = {std::numeric_limits<float>::max(), std::numeric_limits<float>::max(),
@@ -267,6 +269,35 @@ struct mt_handle {
 };
 
 namespace {
+
+DevMaterial dev_material(const mt_material_desc& m)
+{
+    DevMaterial x{};
+    std::memcpy(x.base, m.base_color_factor, 16);
+    std::memcpy(x.emissive, m.emissive_factor, 12);
+    x.normal_scale = m.normal_scale;
+    x.metallic = m.metallic_factor;
+    x.roughness = m.roughness_factor;
+    x.base_tex = m.base_color_tex;
+    x.mr_tex = m.metallic_roughness_tex;
+    x.nrm_tex = m.normal_tex;
+    x.em_tex = m.emissive_tex;
+    return x;
+}
+
+DevLight dev_light(const mt_light_desc& l)
+{
+    DevLight x{};
+    x.type = l.type;
+    std::memcpy(x.pos, l.position, 12);
+    std::memcpy(x.color, l.color, 12);
+    std::memcpy(x.dir, l.direction, 12);
+    x.point_size = l.point_size;
+    x.inner_cos = l.spot_inner_cos;
+    x.outer_cos = l.spot_outer_cos;
+    x.simple = (l.color[0] + l.color[1] + l.color[2]) / 3.0f;  // PrepareLights, Tracer.cpp:123-132
+    return x;
+}
 
 mt_status upload_scene(mt_handle* h, const mt_scene_desc* d)
 {
@@ -391,17 +422,7 @@ mt_status upload_scene(mt_handle* h, const mt_scene_desc* d)
 
     std::vector<DevMaterial> mats(d->num_materials);
     for (uint32_t i = 0; i < d->num_materials; ++i) {
-        const mt_material_desc& m = d->materials[i];
-        DevMaterial x{};
-        std::memcpy(x.base, m.base_color_factor, 16);
-        std::memcpy(x.emissive, m.emissive_factor, 12);
-        x.normal_scale = m.normal_scale;
-        x.metallic = m.metallic_factor;
-        x.roughness = m.roughness_factor;
-        x.base_tex = m.base_color_tex;
-        x.mr_tex = m.metallic_roughness_tex;
-        x.nrm_tex = m.normal_tex;
-        x.em_tex = m.emissive_tex;
+        const DevMaterial x = dev_material(d->materials[i]);
         for (int ti : {x.base_tex, x.mr_tex, x.nrm_tex, x.em_tex})
             if (ti >= static_cast<int>(d->num_textures))
                 return set_err(MT_ERR_INVALID, "material " + std::to_string(i) + " names a missing texture");
@@ -445,19 +466,7 @@ mt_status upload_scene(mt_handle* h, const mt_scene_desc* d)
     }
 
     std::vector<DevLight> lights(d->num_lights);
-    for (uint32_t i = 0; i < d->num_lights; ++i) {
-        const mt_light_desc& l = d->lights[i];
-        DevLight x{};
-        x.type = l.type;
-        std::memcpy(x.pos, l.position, 12);
-        std::memcpy(x.color, l.color, 12);
-        std::memcpy(x.dir, l.direction, 12);
-        x.point_size = l.point_size;
-        x.inner_cos = l.spot_inner_cos;
-        x.outer_cos = l.spot_outer_cos;
-        x.simple = (l.color[0] + l.color[1] + l.color[2]) / 3.0f;  // PrepareLights, Tracer.cpp:123-132
-        lights[i] = x;
-    }
+    for (uint32_t i = 0; i < d->num_lights; ++i) lights[i] = dev_light(d->lights[i]);
     if (d->env_texture >= static_cast<int>(d->num_textures))
         return set_err(MT_ERR_INVALID, "env texture index out of range");
     // gradient layout: RGB32F textures used as a base colour, in texture order
@@ -483,6 +492,8 @@ mt_status upload_scene(mt_handle* h, const mt_scene_desc* d)
     MT_CUDA(h->meshes.upload(meshes.data(), meshes.size(), st));
     MT_CUDA(h->instances.upload(insts.data(), insts.size(), st));
     MT_CUDA(h->materials.upload(mats.data(), mats.size(), st));
+    h->host_mats = mats;
+    h->host_lights = lights;
     MT_CUDA(h->textures.upload(texs.data(), texs.size(), st));
     MT_CUDA(h->lights.upload(lights.data(), lights.size(), st));
     MT_CUDA(h->error_flag.alloc(1));
@@ -1419,6 +1430,56 @@ mt_status mt_nrc_encode(const float* d_features, uint32_t n, float* d_encoded, v
 {
     if (n && (!d_features || !d_encoded)) return set_err(MT_ERR_INVALID, "null argument");
     MT_CUDA(launch_nrc_encode(d_features, n, d_encoded, static_cast<cudaStream_t>(cuda_stream)));
+    return MT_OK;
+}
+
+mt_status mt_update_materials(mt_handle* h, const mt_material_desc* materials, uint32_t n)
+{
+    if (check_handle(h) != MT_OK || (n && !materials)) return set_err(MT_ERR_INVALID, "null argument");
+    if (h->running) return set_err(MT_ERR_STATE, "an asynchronous render is running");
+    if (n != h->host_mats.size()) return set_err(MT_ERR_INVALID, "the material count cannot change");
+    std::vector<DevMaterial> mats(n);
+    for (uint32_t i = 0; i < n; ++i) {
+        mats[i] = dev_material(materials[i]);
+        const DevMaterial& o = h->host_mats[i];
+        if (mats[i].base_tex != o.base_tex || mats[i].mr_tex != o.mr_tex || mats[i].nrm_tex != o.nrm_tex ||
+            mats[i].em_tex != o.em_tex)
+            return set_err(MT_ERR_INVALID, "material " + std::to_string(i) + " changes a texture slot");
+    }
+    MT_CUDA(cudaStreamSynchronize(h->stream));
+    MT_CUDA(cudaDeviceSynchronize());
+    if (n) MT_CUDA(cudaMemcpy(h->materials.p, mats.data(), n * sizeof(DevMaterial), cudaMemcpyHostToDevice));
+    h->host_mats = mats;
+    return MT_OK;
+}
+
+mt_status mt_update_lights(mt_handle* h, const mt_light_desc* lights, uint32_t n)
+{
+    if (check_handle(h) != MT_OK || (n && !lights)) return set_err(MT_ERR_INVALID, "null argument");
+    if (h->running) return set_err(MT_ERR_STATE, "an asynchronous render is running");
+    if (n != h->host_lights.size()) return set_err(MT_ERR_INVALID, "the light count cannot change");
+    std::vector<DevLight> ls(n);
+    for (uint32_t i = 0; i < n; ++i) {
+        ls[i] = dev_light(lights[i]);
+        if (ls[i].type != h->host_lights[i].type)
+            return set_err(MT_ERR_INVALID, "light " + std::to_string(i) + " changes its type");
+    }
+    MT_CUDA(cudaDeviceSynchronize());
+    if (n) MT_CUDA(cudaMemcpy(h->lights.p, ls.data(), n * sizeof(DevLight), cudaMemcpyHostToDevice));
+    h->host_lights = ls;
+    return MT_OK;
+}
+
+mt_status mt_update_texture(mt_handle* h, uint32_t index, const void* texels)
+{
+    if (check_handle(h) != MT_OK || !texels) return set_err(MT_ERR_INVALID, "null argument");
+    if (h->running) return set_err(MT_ERR_STATE, "an asynchronous render is running");
+    if (index >= h->tex8.size()) return set_err(MT_ERR_INVALID, "texture index out of range");
+    MT_CUDA(cudaDeviceSynchronize());
+    if (h->texf[index].p)
+        MT_CUDA(cudaMemcpy(h->texf[index].p, texels, h->texf[index].n * sizeof(float), cudaMemcpyHostToDevice));
+    else
+        MT_CUDA(cudaMemcpy(h->tex8[index].p, texels, h->tex8[index].n, cudaMemcpyHostToDevice));
     return MT_OK;
 }
 

@@ -84,6 +84,24 @@ class Tracer:
                               d_light_ptr or None, d_texels_ptr or None, d_image_ptr or None)
         A.check(A.lib.mt_render_grad(self.handle, C.byref(g), C.c_void_p(stream_ptr)), "mt_render_grad")
 
+    # --- parameter updates (inverse rendering) -----------------------------------
+    def update_materials(self, materials):
+        """mt_update_materials: new factors for every material (same texture slots)."""
+        ps = PackedScene(SceneData(meshes=[], instances=[], materials=list(materials)))
+        A.check(A.lib.mt_update_materials(self.handle, C.cast(ps.desc.materials, C.c_void_p), len(materials)),
+                "mt_update_materials")
+
+    def update_lights(self, lights):
+        """mt_update_lights: new positions / colours for every light (same types)."""
+        ps = PackedScene(SceneData(meshes=[], instances=[], materials=[], lights=list(lights)))
+        A.check(A.lib.mt_update_lights(self.handle, C.cast(ps.desc.lights, C.c_void_p), len(lights)),
+                "mt_update_lights")
+
+    def update_texture(self, index: int, texels: np.ndarray):
+        """mt_update_texture: all texels of one texture (same size and format)."""
+        a = np.ascontiguousarray(texels)
+        A.check(A.lib.mt_update_texture(self.handle, index, a.ctypes.data_as(C.c_void_p)), "mt_update_texture")
+
     # --- neural radiance cache ---------------------------------------------------
     def nrc_enable(self, **overrides) -> A.mt_nrc_config:
         """mt_nrc_enable with mt_nrc_config_defaults plus the given fields."""

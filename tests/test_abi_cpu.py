@@ -100,6 +100,11 @@ def test_argument_errors_are_status_codes():
     assert A.lib.mt_start(None) == A.MT_ERR_INVALID
     assert A.lib.mt_is_done(None) == 0
     assert A.lib.mt_brdf_batch(None, 4, None) == A.MT_ERR_INVALID
+    assert A.lib.mt_brdf_sample_batch(None, 4, None) == A.MT_ERR_INVALID
+    assert A.lib.mt_update_materials(None, None, 0) == A.MT_ERR_INVALID
+    assert A.lib.mt_update_lights(None, None, 0) == A.MT_ERR_INVALID
+    assert A.lib.mt_update_texture(None, 0, None) == A.MT_ERR_INVALID
+    assert A.lib.mt_write_png(None, None, 0, 0) == A.MT_ERR_INVALID
 
 
 def test_create_without_gpu_fails_cleanly():

@@ -207,3 +207,49 @@ def test_image_gradient_input_equals_l2_target_form():
     np.testing.assert_allclose(out["d_roughness"].cpu().numpy(), g["d_roughness"], rtol=1e-4, atol=1e-6)
     np.testing.assert_allclose(out["d_light"].cpu().numpy()[:nl], g["d_light"], rtol=1e-4, atol=1e-6)
 
+
+def test_inverse_materials_descend_toward_hidden_colours():
+    """The inverse-materials loop: hidden sphere base colours render a target;
+    Adam on the base colours from grey, one handle for the whole loop
+    (mt_update_materials between mt_render_grad calls), lowers the image loss
+    and moves the colours toward the hidden ones."""
+    scene, cfg = mt.scenes.adjoint_scene(width=64, height=64, samples=16, texture_size=32, seed=3)
+    rng = np.random.default_rng(11)
+    hidden = rng.uniform(0.2, 0.9, (49, 3)).astype(np.float32)
+    for k in range(49):
+        scene.materials[k].base_color = (*map(float, hidden[k]), 1.0)
+    tscene, tcfg = mt.scenes.adjoint_scene(width=64, height=64, samples=256, texture_size=32, seed=3)
+    tscene.materials = scene.materials
+    target = gpu_image(tscene, tcfg)
+    x = np.full((49, 3), 0.5, np.float32)
+    for k in range(49):
+        scene.materials[k].base_color = (0.5, 0.5, 0.5, 1.0)
+    nm, nl = len(scene.materials), len(scene.lights)
+    t = torch.from_numpy(target).cuda()
+    bufs = {k: torch.zeros(v, device="cuda") for k, v in
+            (("image", 64 * 64 * 3), ("loss", 1), ("d_base", nm * 3), ("d_roughness", nm), ("d_metallic", nm),
+             ("d_light", max(nl, 1)))}
+    m = np.zeros_like(x)
+    v = np.zeros_like(x)
+    losses = []
+    err0 = float(np.abs(x - hidden).mean())
+    with mt.Tracer(scene, cfg) as tr:
+        for it in range(1, 31):
+            for b in bufs.values():
+                b.zero_()
+            tr.render_grad_device(t.data_ptr(), bufs["image"].data_ptr(), bufs["loss"].data_ptr(),
+                                  bufs["d_base"].data_ptr(), bufs["d_roughness"].data_ptr(),
+                                  bufs["d_metallic"].data_ptr(), bufs["d_light"].data_ptr(), 0,
+                                  torch.cuda.current_stream().cuda_stream)
+            torch.cuda.synchronize()
+            losses.append(float(bufs["loss"].item()))
+            g = bufs["d_base"].cpu().numpy().reshape(nm, 3)[:49]
+            m = 0.9 * m + 0.1 * g
+            v = 0.999 * v + 0.001 * g * g
+            x = np.clip(x - 0.03 * (m / (1 - 0.9 ** it)) / (np.sqrt(v / (1 - 0.999 ** it)) + 1e-8), 0.0, 1.0)
+            for k in range(49):
+                scene.materials[k].base_color = (*map(float, x[k]), 1.0)
+            tr.update_materials(scene.materials)
+    assert losses[-1] < 0.35 * losses[0], losses
+    assert float(np.abs(x - hidden).mean()) < 0.6 * err0
+
