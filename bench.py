@@ -70,6 +70,7 @@ def parse():
     p.add_argument("--nrc-rows", type=int, default=1920 * 1080 * 4)
     p.add_argument("--nrc-warmup", type=int, default=8, help="training-only frames before the first cached frame")
     p.add_argument("--nrc-frames", type=int, default=48, help="cached frames at most")
+    p.add_argument("--nrc-steps", type=int, default=None, help="Adam steps per frame (default: the library's)")
     return p.parse_args()
 
 
@@ -643,7 +644,7 @@ def nrc_time_to_relmse(a, ref, dev, stream):
     acc = torch.zeros_like(refd)
     out = {"warmup_frames": a.nrc_warmup, "frames": []}
     with mt.Tracer(scene, cfg) as tr:
-        c = tr.nrc_enable()
+        c = tr.nrc_enable(**({"train_steps": a.nrc_steps} if a.nrc_steps else {}))
         out["config"] = {"spp_per_frame": c.spp, "train_paths": c.train_paths, "train_batch": c.train_batch,
                          "train_steps": c.train_steps, "lr": c.learning_rate, "rough_min": c.rough_min}
         ev = []
