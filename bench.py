@@ -71,6 +71,8 @@ def parse():
     p.add_argument("--nrc-warmup", type=int, default=8, help="training-only frames before the first cached frame")
     p.add_argument("--nrc-frames", type=int, default=48, help="cached frames at most")
     p.add_argument("--nrc-steps", type=int, default=None, help="Adam steps per frame (default: the library's)")
+    p.add_argument("--nrc-ema", type=float, default=None, help="moving-average decay of the cache's weights")
+    p.add_argument("--nrc-only", action="store_true", help="time-to-relMSE: skip the plain spp ladder")
     return p.parse_args()
 
 
@@ -585,7 +587,7 @@ def run_time_to_relmse(a):
     ref, ref_s, ref_rays, scene, cfg = render(a.ref_spp, 1)
     ladder = []
     spp = 1
-    while spp <= 1024:
+    while spp <= (0 if a.nrc_only else 1024):
         img, sec, rays, _, _ = render(spp, 0)
         ladder.append({"spp": spp, "seconds": sec, "relmse": relmse(img, ref), "mrays_s": rays / sec / 1e6})
         spp *= 2
@@ -593,9 +595,10 @@ def run_time_to_relmse(a):
     # relMSE ~ c / spp on the rungs above 8 spp
     xs = np.array([r["spp"] for r in ladder if r["spp"] >= 8], dtype=np.float64)
     ys = np.array([r["relmse"] for r in ladder if r["spp"] >= 8], dtype=np.float64)
-    c = float(np.exp(np.mean(np.log(ys * xs))))
+    c = float(np.exp(np.mean(np.log(ys * xs)))) if xs.size else float("nan")
     spp_fit = c / a.relmse_target
-    sec_per_spp = statistics.median(r["seconds"] / r["spp"] for r in ladder if r["spp"] >= 8)
+    sec_per_spp = (statistics.median(r["seconds"] / r["spp"] for r in ladder if r["spp"] >= 8) if xs.size
+                   else float("nan"))
     line = {
         "metric": "time-to-relMSE 0.01 @1080p", "unit": "s", "higher_is_better": False,
         "config": {"workload": workload_name(a), "ref_spp": a.ref_spp, "ref_seed": 1, "seed": 0,
@@ -644,7 +647,12 @@ def nrc_time_to_relmse(a, ref, dev, stream):
     acc = torch.zeros_like(refd)
     out = {"warmup_frames": a.nrc_warmup, "frames": []}
     with mt.Tracer(scene, cfg) as tr:
-        c = tr.nrc_enable(**({"train_steps": a.nrc_steps} if a.nrc_steps else {}))
+        kw = {}
+        if a.nrc_steps:
+            kw["train_steps"] = a.nrc_steps
+        if a.nrc_ema is not None:
+            kw["ema_decay"] = a.nrc_ema
+        c = tr.nrc_enable(**kw)
         out["config"] = {"spp_per_frame": c.spp, "train_paths": c.train_paths, "train_batch": c.train_batch,
                          "train_steps": c.train_steps, "lr": c.learning_rate, "rough_min": c.rough_min}
         ev = []
