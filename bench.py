@@ -73,6 +73,7 @@ def parse():
     p.add_argument("--nrc-steps", type=int, default=None, help="Adam steps per frame (default: the library's)")
     p.add_argument("--nrc-ema", type=float, default=None, help="moving-average decay of the cache's weights")
     p.add_argument("--nrc-only", action="store_true", help="time-to-relMSE: skip the plain spp ladder")
+    p.add_argument("--nrc-spp", type=int, default=None, help="cached samples per pixel per frame")
     return p.parse_args()
 
 
@@ -652,6 +653,8 @@ def nrc_time_to_relmse(a, ref, dev, stream):
             kw["train_steps"] = a.nrc_steps
         if a.nrc_ema is not None:
             kw["ema_decay"] = a.nrc_ema
+        if a.nrc_spp:
+            kw["spp"] = a.nrc_spp
         c = tr.nrc_enable(**kw)
         out["config"] = {"spp_per_frame": c.spp, "train_paths": c.train_paths, "train_batch": c.train_batch,
                          "train_steps": c.train_steps, "lr": c.learning_rate, "rough_min": c.rough_min}
