@@ -68,7 +68,7 @@ def parse():
     p.add_argument("--nrc-kernels-only", action="store_true",
                    help="only time the radiance cache's inference and training kernels")
     p.add_argument("--nrc-rows", type=int, default=1920 * 1080 * 4)
-    p.add_argument("--nrc-warmup", type=int, default=8, help="training-only frames before the first cached frame")
+    p.add_argument("--nrc-warmup", type=int, default=0, help="training-only frames before the first cached frame")
     p.add_argument("--nrc-frames", type=int, default=48, help="cached frames at most")
     p.add_argument("--nrc-steps", type=int, default=None, help="Adam steps per frame (default: the library's)")
     p.add_argument("--nrc-ema", type=float, default=None, help="moving-average decay of the cache's weights")
@@ -634,7 +634,7 @@ def run_time_to_relmse(a):
 def nrc_time_to_relmse(a, ref, dev, stream):
     """The radiance-cache renderer on the same scene: --nrc-warmup training-only
     frames, then cached frames (mt_nrc_config defaults: 4 spp, 65,536 training
-    paths and 4 Adam steps of 16,384 per frame) folded into a running mean.
+    paths and 128 Adam steps of 16,384 per frame) folded into a running mean.
     Every frame is timed with CUDA events on the render stream; relMSE of the
     running mean against the plain reference is evaluated between frames,
     outside the timed spans."""

@@ -353,7 +353,7 @@ mt_status mt_render_grad(mt_handle* h, const mt_grad_buffers* g, void* cuda_stre
 typedef struct mt_nrc_config {
     uint32_t train_paths;  /* full-length training paths traced per frame (65,536) */
     uint32_t train_batch;  /* training samples (path vertices) per Adam step (16,384) */
-    uint32_t train_steps;  /* Adam steps per frame (4) */
+    uint32_t train_steps;  /* Adam steps per frame (128; replayed as one CUDA graph) */
     uint32_t spp;          /* cached-render samples per pixel per frame (4) */
     float learning_rate;   /* Adam step size (1e-2) */
     float beta1, beta2;    /* Adam moment decays (0.9, 0.99) */

@@ -235,6 +235,9 @@ struct mt_handle {
         // [0] cache queries of a batch, [1] training samples, [2] queries of the
         // frame, [3] summed step losses of the frame (float bits)
         DevArray<uint32_t> counters;
+        DevArray<uint32_t> step;  // device Adam step counter
+        cudaGraphExec_t steps_graph = nullptr;  // a frame's training steps, replayed
+        uint32_t graph_steps = 0;
         NrcOptimizer opt{};
         uint64_t frames = 0;          // frames rendered (sample indices continue)
         uint64_t plane_capacity = 0;  // samples the cached render's band planes hold
@@ -262,6 +265,7 @@ struct mt_handle {
     ~mt_handle()
     {
         if (worker.joinable()) worker.join();
+        if (nrc.steps_graph) cudaGraphExecDestroy(nrc.steps_graph);
         if (rays_host) cudaFreeHost(rays_host);
         if (render_done) cudaEventDestroy(render_done);
         if (stream) cudaStreamDestroy(stream);
@@ -805,6 +809,14 @@ mt_status nrc_alloc(mt_handle* h, const mt_nrc_config& c)
     O.beta2 = c.beta2;
     O.eps = c.epsilon;
     O.step = 0;
+    MT_CUDA(N.step.alloc(1));
+    MT_CUDA(cudaMemsetAsync(N.step.p, 0, sizeof(uint32_t), st));
+    O.d_step = N.step.p;
+    if (N.steps_graph) {
+        cudaGraphExecDestroy(N.steps_graph);
+        N.steps_graph = nullptr;
+    }
+    MT_CUDA(nrc_prepare());
     // training paths and their samples
     const uint32_t bounces = std::max<uint32_t>(1, cfg.bounces);
     N.train_chunk = std::min<uint32_t>(c.train_paths, h->batch);
@@ -1219,7 +1231,7 @@ void mt_nrc_config_defaults(mt_nrc_config* c)
     std::memset(c, 0, sizeof(*c));
     c->train_paths = 65536;
     c->train_batch = 16384;
-    c->train_steps = 4;
+    c->train_steps = 128;
     c->spp = 4;
     c->learning_rate = 1e-2f;
     c->beta1 = 0.9f;
@@ -1289,19 +1301,40 @@ mt_status mt_nrc_frame(mt_handle* h, float* d_accum, uint32_t accum_index, void*
         MT_CUDA(launch_batch(St, v.P, v.SQ, v.W, 0, n, static_cast<uint32_t>(npix), 0, st, &launches, nullptr,
                              nullptr, &X));
     }
-    // 2. Adam steps on random vertices of those paths
-    for (uint32_t s = 0; s < nc.train_steps; ++s) {
-        NrcTrainArgs a{};
-        a.feat = N.samples.p;
-        a.fstride = 6;
-        a.targets = reinterpret_cast<const float*>(N.samples.p + 5);
-        a.tstride = 24;
-        a.count = N.counters.p + 1;
-        a.count_cap = N.sample_cap;
-        a.base = static_cast<uint32_t>((N.frames * nc.train_steps + s) * nc.train_batch);
-        a.rows = nc.train_batch;
-        MT_CUDA(launch_nrc_train_step(N.opt, a, reinterpret_cast<float*>(N.counters.p + 3), nullptr, st));
-        launches += 3;
+    // 2. Adam steps on random vertices of those paths, replayed as one CUDA
+    //    graph (the launches are fixed; step numbers live on the device)
+    if (nc.train_steps) {
+        if (!N.steps_graph || N.graph_steps != nc.train_steps) {
+            if (N.steps_graph) cudaGraphExecDestroy(N.steps_graph);
+            N.steps_graph = nullptr;
+            cudaStream_t cs = nullptr;
+            MT_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+            cudaGraph_t graph = nullptr;
+            cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+            const uint64_t host_step = N.opt.step;
+            for (uint32_t s = 0; s < nc.train_steps && e == cudaSuccess; ++s) {
+                NrcTrainArgs a{};
+                a.feat = N.samples.p;
+                a.fstride = 6;
+                a.targets = reinterpret_cast<const float*>(N.samples.p + 5);
+                a.tstride = 24;
+                a.count = N.counters.p + 1;
+                a.count_cap = N.sample_cap;
+                a.rows = nc.train_batch;
+                e = launch_nrc_train_step(N.opt, a, reinterpret_cast<float*>(N.counters.p + 3), nullptr, cs);
+            }
+            N.opt.step = host_step;  // captured, not run
+            const cudaError_t e2 = cudaStreamEndCapture(cs, &graph);
+            if (e == cudaSuccess) e = e2;
+            if (e == cudaSuccess) e = cudaGraphInstantiate(&N.steps_graph, graph, 0);
+            if (graph) cudaGraphDestroy(graph);
+            cudaStreamDestroy(cs);
+            MT_CUDA(e);
+            N.graph_steps = nc.train_steps;
+        }
+        MT_CUDA(cudaGraphLaunch(N.steps_graph, st));
+        N.opt.step += nc.train_steps;
+        launches += 3ull * nc.train_steps;
     }
     // 3. the cached render
     if (d_accum) {
@@ -1386,6 +1419,7 @@ mt_status mt_nrc_set_params(mt_handle* h, const float* params)
     MT_CUDA(cudaMemcpy(N.master.p, params, kNrcParams * sizeof(float), cudaMemcpyHostToDevice));
     MT_CUDA(cudaMemset(N.m.p, 0, kNrcParams * sizeof(float)));
     MT_CUDA(cudaMemset(N.v.p, 0, kNrcParams * sizeof(float)));
+    MT_CUDA(cudaMemset(N.step.p, 0, sizeof(uint32_t)));
     N.opt.step = 0;
     MT_CUDA(launch_nrc_publish(N.opt, h->stream));
     MT_CUDA(cudaStreamSynchronize(h->stream));
@@ -1419,7 +1453,6 @@ mt_status mt_nrc_train_step(mt_handle* h, const float* d_features, const float* 
     a.targets = d_targets;
     a.tstride = 3;
     a.count = nullptr;
-    a.base = 0;
     a.rows = n;
     MT_CUDA(launch_nrc_train_step(h->nrc.opt, a, d_loss, d_grad, st));
     h->launches += 3;

@@ -591,7 +591,8 @@ __device__ __forceinline__ void st32(void* base, uint64_t idx, uint32_t v)
 
 __global__ void __launch_bounds__(kTrainWarps * 32) k_nrc_fwdbwd(const bf16* __restrict__ fwd,
                                                                  const bf16* __restrict__ bwd, NrcTrainArgs a,
-                                                                 uint32_t rows_pad, NrcActs A, float* loss)
+                                                                 uint32_t rows_pad, NrcActs A, float* loss,
+                                                                 const uint32_t* __restrict__ step)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     bf16* WF = reinterpret_cast<bf16*>(smem);
@@ -603,12 +604,13 @@ __global__ void __launch_bounds__(kTrainWarps * 32) k_nrc_fwdbwd(const bf16* __r
     copy_blob(WB, bwd, kNrcBwdElems);
     __syncthreads();
     const uint32_t cnt = a.count ? min(*a.count, a.count_cap) : a.rows;
+    const uint32_t base = *step * a.rows;
     const uint32_t n = cnt ? a.rows : 0;  // valid rows
     const float scale = n ? 1.0f / (3.0f * static_cast<float>(n)) : 0.0f;
     float lsum = 0.0f;
     for (uint32_t tile = blockIdx.x * kTrainWarps + warp; tile < rows_pad / 16; tile += gridDim.x * kTrainWarps) {
         const uint32_t r0 = tile * 16;
-        if (lane < 16) map[lane] = a.count ? (n ? mix32(a.base + r0 + lane) % cnt : 0u) : r0 + lane;
+        if (lane < 16) map[lane] = a.count ? (n ? mix32(base + r0 + lane) % cnt : 0u) : r0 + lane;
         __syncwarp();
         stage_rows(a.feat, a.fstride, r0, n, map, stg);
         __syncwarp();
@@ -701,8 +703,10 @@ __device__ __forceinline__ WgTask wg_task(int id)
 }
 
 __global__ void __launch_bounds__(kWgWarps * 32) k_nrc_wgrad(NrcActs A, uint32_t rows_per_split,
-                                                             float* __restrict__ partial)
+                                                             float* __restrict__ partial, uint32_t* step)
 {
+    // the step this gradient belongs to (read by the Adam kernel that follows)
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(step, 1u);
     extern __shared__ __align__(16) unsigned char smem[];
     bf16* T = reinterpret_cast<bf16*>(smem);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
@@ -794,14 +798,17 @@ __device__ __forceinline__ void publish_param(bf16* fwd, bf16* bwd, bf16* infer,
     infer[fwd_off(l) + o * fwd_stride(l) + i] = __float2bfloat16_rn(wi);
 }
 
-// ema_bc = 1 - decay^step (bias correction of the zero-started average).
+// Bias corrections 1 - beta^t of the moments and of the zero-started weight
+// average, t = the device step counter (already counting this step).
 __global__ void k_nrc_adam(float* __restrict__ master, float* __restrict__ m, float* __restrict__ v,
                            const float* __restrict__ partial, uint32_t splits, float lr, float b1, float b2,
-                           float eps, float bc1, float bc2, bf16* fwd, bf16* bwd, float* grad_out,
-                           bf16* infer, float* __restrict__ ema, float decay, float ema_bc)
+                           float eps, bf16* fwd, bf16* bwd, float* grad_out, bf16* infer, float* __restrict__ ema,
+                           float decay, const uint32_t* __restrict__ step)
 {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= kNrcParams) return;
+    const float t = static_cast<float>(*step);
+    const float bc1 = 1.0f - powf(b1, t), bc2 = 1.0f - powf(b2, t), ema_bc = 1.0f - powf(decay, t);
     float gsum = 0.0f;
     for (uint32_t s = 0; s < splits; ++s) gsum += partial[static_cast<uint64_t>(s) * kNrcParams + q];
     if (grad_out) grad_out[q] = gsum;
@@ -948,11 +955,9 @@ cudaError_t launch_nrc_train_step(NrcOptimizer& O, const NrcTrainArgs& a, float*
                                   cudaStream_t st)
 {
     if (a.rows == 0 || a.rows > O.max_rows) return cudaErrorInvalidValue;
-    static bool ok_t = false, ok_w = false;
-    cudaError_t e = allow_smem(k_nrc_fwdbwd, kTrainSmem, ok_t);
-    if (e != cudaSuccess) return e;
-    e = allow_smem(k_nrc_wgrad, kWgSmem, ok_w);
-    if (e != cudaSuccess) return e;
+    // shared-memory limits were raised by nrc_prepare (no attribute call here:
+    // this function is also recorded into a CUDA graph)
+    cudaError_t e = cudaSuccess;
     // rows padded to whole chunks; split so that every block has whole chunks
     const uint32_t chunks = (a.rows + kChunk - 1) / kChunk;
     const uint32_t per = (chunks + O.max_splits - 1) / O.max_splits;
@@ -964,21 +969,28 @@ cudaError_t launch_nrc_train_step(NrcOptimizer& O, const NrcTrainArgs& a, float*
     const uint64_t cap = static_cast<uint64_t>(sms()) * 2;
     if (blocks > cap) blocks = cap;
     k_nrc_fwdbwd<<<static_cast<unsigned>(blocks), kTrainWarps * 32, kTrainSmem, st>>>(
-        static_cast<const bf16*>(O.fwd), static_cast<const bf16*>(O.bwd), a, rows_pad, O.acts, loss);
+        static_cast<const bf16*>(O.fwd), static_cast<const bf16*>(O.bwd), a, rows_pad, O.acts, loss, O.d_step);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    k_nrc_wgrad<<<splits, kWgWarps * 32, kWgSmem, st>>>(O.acts, per * kChunk, O.partial);
+    k_nrc_wgrad<<<splits, kWgWarps * 32, kWgSmem, st>>>(O.acts, per * kChunk, O.partial, O.d_step);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     O.step += 1;
-    const double bc1 = 1.0 - std::pow(static_cast<double>(O.beta1), static_cast<double>(O.step));
-    const double bc2 = 1.0 - std::pow(static_cast<double>(O.beta2), static_cast<double>(O.step));
-    const double ema_bc = 1.0 - std::pow(static_cast<double>(O.ema_decay), static_cast<double>(O.step));
-    k_nrc_adam<<<(kNrcParams + 255) / 256, 256, 0, st>>>(
-        O.master, O.m, O.v, O.partial, splits, O.lr, O.beta1, O.beta2, O.eps, static_cast<float>(bc1),
-        static_cast<float>(bc2), static_cast<bf16*>(O.fwd), static_cast<bf16*>(O.bwd), grad_out,
-        static_cast<bf16*>(O.infer), O.ema, O.ema_decay, static_cast<float>(ema_bc));
+    k_nrc_adam<<<(kNrcParams + 255) / 256, 256, 0, st>>>(O.master, O.m, O.v, O.partial, splits, O.lr, O.beta1,
+                                                        O.beta2, O.eps, static_cast<bf16*>(O.fwd),
+                                                        static_cast<bf16*>(O.bwd), grad_out,
+                                                        static_cast<bf16*>(O.infer), O.ema, O.ema_decay, O.d_step);
     return cudaGetLastError();
+}
+
+cudaError_t nrc_prepare()
+{
+    static bool ok_t = false, ok_w = false, ok_i0 = false, ok_i1 = false;
+    cudaError_t e = allow_smem(k_nrc_fwdbwd, kTrainSmem, ok_t);
+    if (e == cudaSuccess) e = allow_smem(k_nrc_wgrad, kWgSmem, ok_w);
+    if (e == cudaSuccess) e = allow_smem(k_nrc_infer_tc<false>, kTcSmem, ok_i0);
+    if (e == cudaSuccess) e = allow_smem(k_nrc_infer_tc<true>, kTcSmem, ok_i1);
+    return e;
 }
 
 cudaError_t launch_nrc_publish(const NrcOptimizer& O, cudaStream_t st)

@@ -67,9 +67,11 @@ cudaError_t launch_nrc_infer(const void* net, const float* features, uint32_t n,
                              cudaStream_t st);
 cudaError_t launch_nrc_encode(const float* features, uint32_t n, float* out, cudaStream_t st);
 
-// One training step.  Rows r < rows read sample fmix32(base + r) mod *count of
-// the (features, targets) arrays when count is not null (random draws with
-// replacement; an empty set trains on nothing), else sample r.  feat: the 5 feature float4 of sample
+// One training step.  Rows r < rows read sample fmix32(step * rows + r) mod
+// *count of the (features, targets) arrays when count is not null (random
+// draws with replacement, step = the device step counter; an empty set trains
+// on nothing), else sample r.  The step number lives on the device so that a
+// frame's steps can be replayed as one CUDA graph.  feat: the 5 feature float4 of sample
 // i start at feat[i * fstride]; targets: tstride floats per sample (rgb first).
 struct NrcTrainArgs {
     const float4* feat;
@@ -78,7 +80,6 @@ struct NrcTrainArgs {
     uint32_t tstride;
     const uint32_t* count;
     uint32_t count_cap;  // samples the arrays hold (*count may run past it)
-    uint32_t base;
     uint32_t rows;
 };
 struct NrcOptimizer {
@@ -95,10 +96,13 @@ struct NrcOptimizer {
     uint32_t max_rows;  // multiple of 64
     uint32_t max_splits;
     float lr, beta1, beta2, eps;
-    uint64_t step;      // Adam steps taken
+    uint64_t step;      // Adam steps taken (host copy)
+    uint32_t* d_step;   // Adam steps taken (device; the kernels' bias corrections and sample draws)
 };
 cudaError_t launch_nrc_train_step(NrcOptimizer& O, const NrcTrainArgs& a, float* loss, float* grad_out,
                                   cudaStream_t st);
+// Sets the kernels' shared-memory limits (before any stream capture).
+cudaError_t nrc_prepare();
 // Writes the bf16 blobs from the fp32 master weights (and restarts the average).
 cudaError_t launch_nrc_publish(const NrcOptimizer& O, cudaStream_t st);
 // running mean: accum += (frame - accum) / (index + 1)

@@ -85,7 +85,7 @@ def test_torch_reference_shapes_and_param_count():
 def test_config_defaults():
     c = A.mt_nrc_config()
     A.lib.mt_nrc_config_defaults(C.byref(c))
-    assert (c.train_paths, c.train_batch, c.train_steps, c.spp) == (65536, 16384, 4, 4)
+    assert (c.train_paths, c.train_batch, c.train_steps, c.spp) == (65536, 16384, 128, 4)
     assert c.learning_rate == pytest.approx(1e-2) and c.beta1 == pytest.approx(0.9)
     assert c.beta2 == pytest.approx(0.99) and c.rough_min == pytest.approx(0.3)
     assert c.ema_decay == pytest.approx(0.9)
