@@ -272,6 +272,22 @@ def microbench(a, dev, peak):
     out["roofline_closest"] = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                                "frac": achieved / peak, "alg_bytes": alg_bytes}
     tr.close()
+    # host BVH build of the scene's meshes: the library's builder (independent
+    # subtrees on threads) against the oracle's restatement of the reference's
+    # recursive builder; both give the same nodes and indices
+    from oracle import oracle_py as orc
+
+    builds = []
+    for m in scene.meshes:
+        t0 = time.perf_counter()
+        n1, i1 = mt.bvh_build(m.positions)
+        t1 = time.perf_counter()
+        n2, i2 = orc.bvh_build(m.positions)
+        t2 = time.perf_counter()
+        builds.append({"triangles": int(m.num_triangles), "nodes": int(n1.shape[0]), "library_s": t1 - t0,
+                       "reference_restatement_s": t2 - t1,
+                       "identical": bool(np.array_equal(n1, n2) and np.array_equal(i1, i2))})
+    out["bvh_build"] = builds
     return out
 
 
