@@ -510,6 +510,15 @@ mt_status upload_scene(mt_handle* h, const mt_scene_desc* d)
     DevScene& S = h->S;
     S.nodes = h->nodes.p;
     S.slots = h->slots.p;
+    {
+        int dev = 0, l2 = 0;
+        MT_CUDA(cudaGetDevice(&dev));
+        MT_CUDA(cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev));
+        const double bvh_bytes = (nodes.size() + slots.size()) * 16.0;
+        const bool resident = bvh_bytes <= MT_TRAVERSE_RESIDENT_L2_FRACTION * l2;
+        S.trav_pops = resident ? MT_TRAVERSE_POPS_RESIDENT : 1;
+        S.trav_prefetch = resident ? 0 : 1;
+    }
     S.normals = h->normals.p;
     S.uvs = h->uvs.p;
     S.meshes = h->meshes.p;

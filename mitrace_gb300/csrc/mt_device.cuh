@@ -182,9 +182,31 @@ struct DevScene {
     float firefly_k;
     int* error_flag;
     int32_t debug_mode;  // Config::DebugMode (MT_DEBUG_*), 0 = DebugNone
+    int32_t trav_pops;      // node pops per lane between two leaf passes (>= 1)
+    int32_t trav_prefetch;  // 1: prefetch a reached leaf's slots into L2
 };
 
 #define MT_STACK_SIZE 64
+// Traversal settings chosen per scene at upload (DevScene::trav_pops /
+// trav_prefetch): a scene whose nodes and triangle slots fit in a fraction of
+// L2 pops up to MT_TRAVERSE_POPS_RESIDENT nodes per lane between two leaf
+// passes of the warp and prefetches nothing; a larger scene pops one node per
+// pass and has each leaf's triangle slots (the first 32) brought into L2 the
+// moment a lane reaches the leaf, so that the leaf's warp pass finds them there
+// (measured: +2% Mrays/s on an 11 MB scene, +10% on a 1.5 GB one).
+#ifndef MT_TRAVERSE_POPS_RESIDENT
+#define MT_TRAVERSE_POPS_RESIDENT 4
+#endif
+#ifndef MT_TRAVERSE_RESIDENT_L2_FRACTION
+#define MT_TRAVERSE_RESIDENT_L2_FRACTION 0.5
+#endif
+
+// Bulk prefetch of [p, p + bytes) into L2 (no registers, no completion to wait
+// for); p 16-byte aligned, bytes a multiple of 16.
+__device__ __forceinline__ void prefetch_l2(const void* p, uint32_t bytes)
+{
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
 #define MT_ERRBIT_STACK 1
 #define MT_ERRBIT_TIMEOUT 2  // a bounded wait on the tensor cores ran out
 
@@ -421,44 +443,55 @@ __device__ __forceinline__ void trace_persistent(const DevScene& S, Work& W, uin
             }
         }
 
-        // D. one node pop per lane (IntersectTrianglesBVH's loop body)
-        if (in_inst && !pending && sp > 0) {
-            --sp;
-            const uint32_t ni = stk_node[sp];
-            const float nd = stk_dist[sp];
-            if (COUNT) ++h.bvh_tests;
-            if (!(nd < 0.0f) && !(nd > __fadd_rn(h.t, 0.1f))) {
-                const uint32_t na = f2u(__ldg(&nodes[2 * ni].w));
-                const uint32_t nb = f2u(__ldg(&nodes[2 * ni + 1].w));
-                if (na & MT_BVH_LEAF_BIT) {
-                    pending = true;
-                    pfirst = na & ~MT_BVH_LEAF_BIT;
-                    pcount = nb & ~MT_BVH_LEAF_BIT;
-                    pnode = ni;
-                } else {
-                    if (COUNT) ++h.inner;
-                    const float4 a0 = __ldg(nodes + 2 * na), a1 = __ldg(nodes + 2 * na + 1);
-                    const float4 b0 = __ldg(nodes + 2 * nb), b1 = __ldg(nodes + 2 * nb + 1);
-                    const float da = slab(lo, linv, xyz(a0), xyz(a1));
-                    const float db = slab(lo, linv, xyz(b0), xyz(b1));
-                    const float lim = __fadd_rn(h.t, 0.1f);
-                    const bool pa = da >= 0.0f && da <= lim;
-                    const bool pb = db >= 0.0f && db <= lim;
-                    if (sp + 2 > MT_STACK_SIZE) {
-                        atomicOr(S.error_flag, MT_ERRBIT_STACK);
-                        sp = 0;
-                    } else if (pa && pb) {
-                        if (da < db) {
-                            stk_node[sp] = nb; stk_dist[sp] = db; ++sp;
+        // D. node pops (IntersectTrianglesBVH's loop body): up to
+        // S.trav_pops per pass, a lane stopping at its first leaf, so every
+        // lane still visits its nodes in the reference's order and each leaf is
+        // tested (phase E) before that lane's next pop
+        const int pops = S.trav_pops > 1 ? S.trav_pops : 1;  // at least one pop per pass
+#pragma unroll 1
+        for (int pass = 0; pass < pops; ++pass) {
+            const bool act = in_inst && !pending && sp > 0;
+            if (pass > 0 && !__any_sync(MT_FULL, act)) break;
+            if (act) {
+                --sp;
+                const uint32_t ni = stk_node[sp];
+                const float nd = stk_dist[sp];
+                if (COUNT) ++h.bvh_tests;
+                if (!(nd < 0.0f) && !(nd > __fadd_rn(h.t, 0.1f))) {
+                    const uint32_t na = f2u(__ldg(&nodes[2 * ni].w));
+                    const uint32_t nb = f2u(__ldg(&nodes[2 * ni + 1].w));
+                    if (na & MT_BVH_LEAF_BIT) {
+                        pending = true;
+                        pfirst = na & ~MT_BVH_LEAF_BIT;
+                        pcount = nb & ~MT_BVH_LEAF_BIT;
+                        pnode = ni;
+                        if (S.trav_prefetch && pcount)
+                            prefetch_l2(S.slots + 3ull * (slot_base + pfirst), 48u * (pcount < 32u ? pcount : 32u));
+                    } else {
+                        if (COUNT) ++h.inner;
+                        const float4 a0 = __ldg(nodes + 2 * na), a1 = __ldg(nodes + 2 * na + 1);
+                        const float4 b0 = __ldg(nodes + 2 * nb), b1 = __ldg(nodes + 2 * nb + 1);
+                        const float da = slab(lo, linv, xyz(a0), xyz(a1));
+                        const float db = slab(lo, linv, xyz(b0), xyz(b1));
+                        const float lim = __fadd_rn(h.t, 0.1f);
+                        const bool pa = da >= 0.0f && da <= lim;
+                        const bool pb = db >= 0.0f && db <= lim;
+                        if (sp + 2 > MT_STACK_SIZE) {
+                            atomicOr(S.error_flag, MT_ERRBIT_STACK);
+                            sp = 0;
+                        } else if (pa && pb) {
+                            if (da < db) {
+                                stk_node[sp] = nb; stk_dist[sp] = db; ++sp;
+                                stk_node[sp] = na; stk_dist[sp] = da; ++sp;
+                            } else {
+                                stk_node[sp] = na; stk_dist[sp] = da; ++sp;
+                                stk_node[sp] = nb; stk_dist[sp] = db; ++sp;
+                            }
+                        } else if (pa) {
                             stk_node[sp] = na; stk_dist[sp] = da; ++sp;
-                        } else {
-                            stk_node[sp] = na; stk_dist[sp] = da; ++sp;
+                        } else if (pb) {
                             stk_node[sp] = nb; stk_dist[sp] = db; ++sp;
                         }
-                    } else if (pa) {
-                        stk_node[sp] = na; stk_dist[sp] = da; ++sp;
-                    } else if (pb) {
-                        stk_node[sp] = nb; stk_dist[sp] = db; ++sp;
                     }
                 }
             }
