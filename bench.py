@@ -74,6 +74,8 @@ def parse():
     p.add_argument("--nrc-ema", type=float, default=None, help="moving-average decay of the cache's weights")
     p.add_argument("--nrc-only", action="store_true", help="time-to-relMSE: skip the plain spp ladder")
     p.add_argument("--nrc-spp", type=int, default=None, help="cached samples per pixel per frame")
+    p.add_argument("--nrc-end-at", type=int, default=None,
+                   help="where a cached path ends: 0 after the first diffuse-ish vertex, 1 at it (mt_nrc_config.end_at)")
     return p.parse_args()
 
 
@@ -671,9 +673,12 @@ def nrc_time_to_relmse(a, ref, dev, stream):
             kw["ema_decay"] = a.nrc_ema
         if a.nrc_spp:
             kw["spp"] = a.nrc_spp
+        if a.nrc_end_at is not None:
+            kw["end_at"] = a.nrc_end_at
         c = tr.nrc_enable(**kw)
         out["config"] = {"spp_per_frame": c.spp, "train_paths": c.train_paths, "train_batch": c.train_batch,
-                         "train_steps": c.train_steps, "lr": c.learning_rate, "rough_min": c.rough_min}
+                         "train_steps": c.train_steps, "lr": c.learning_rate, "rough_min": c.rough_min,
+                         "end_at": c.end_at}
         ev = []
         total = 0.0
         for f in range(a.nrc_warmup + a.nrc_frames):

@@ -363,8 +363,20 @@ typedef struct mt_nrc_config {
     float ema_decay;       /* the renderer queries an exponential moving average
                               of the trained weights (bias-corrected) with this
                               decay; 0 queries the trained weights themselves (0.9) */
-    uint32_t reserved[5];
+    uint32_t end_at;       /* where a cached path ends (MT_NRC_END_*) */
+    uint32_t reserved[4];
 } mt_nrc_config;
+
+/* mt_nrc_config::end_at.
+ * AFTER_DIFFUSE: the path ends at the first vertex after a diffuse-ish one
+ *   (bounce >= 1) and the cache stands for that vertex's whole outgoing
+ *   radiance, its next-event estimate included.
+ * AT_DIFFUSE: the path ends at its first diffuse-ish vertex (the primary one
+ *   included) after that vertex's next-event estimate, and the cache stands
+ *   for the radiance the vertex reflects from the rest of its path (the
+ *   estimate excluded).  The cache is trained for the mode it serves. */
+#define MT_NRC_END_AFTER_DIFFUSE 0u
+#define MT_NRC_END_AT_DIFFUSE 1u
 
 /* Counters of the cache (mt_nrc_get_stats synchronizes the device). */
 typedef struct mt_nrc_stats {
@@ -383,12 +395,13 @@ mt_status mt_nrc_enable(mt_handle* h, const mt_nrc_config* c);
 /* One frame of the cached renderer, enqueued on cuda_stream:
  *  1. trace train_paths full-length plain paths from random pixels, record
  *     every vertex's features and the radiance the rest of its path carried
- *     back ((path total - total before the vertex's NEE) / throughput);
+ *     back ((path total - total before the vertex's NEE) / throughput; with
+ *     MT_NRC_END_AT_DIFFUSE the vertex's own NEE is subtracted as well);
  *  2. take train_steps Adam steps on batches of those vertices (relative L2
  *     loss |y - t|^2 / (y^2 + 0.01), y held constant in the denominator);
  *  3. if d_accum is not NULL, render spp samples per pixel in which a path
- *     ends at the first vertex after a diffuse-ish one (bounce >= 1) and adds
- *     throughput * max(cache(vertex), 0) instead of tracing on; resolve them
+ *     ends where end_at says and adds throughput * max(cache(vertex), 0)
+ *     instead of tracing on; resolve them
  *     like mt_render_device (per-sample ACES, firefly clamp over the frame's
  *     spp) and fold the frame into d_accum (W*H*3) as a running mean:
  *     accum += (frame - accum) / (accum_index + 1).

@@ -210,6 +210,8 @@ MT_NRC_INPUTS = 80
 MT_NRC_WIDTH = 64
 MT_NRC_FEATURES = 20
 MT_NRC_PARAMS = 80 * 64 + 3 * 64 * 64 + 64 * 3
+MT_NRC_END_AFTER_DIFFUSE = 0
+MT_NRC_END_AT_DIFFUSE = 1
 
 
 class mt_nrc_config(C.Structure):
@@ -225,7 +227,8 @@ class mt_nrc_config(C.Structure):
         ("rough_min", C.c_float),
         ("seed", C.c_uint32),
         ("ema_decay", C.c_float),
-        ("reserved", C.c_uint32 * 5),
+        ("end_at", C.c_uint32),
+        ("reserved", C.c_uint32 * 4),
     ]
 
 

@@ -829,7 +829,7 @@ mt_status nrc_alloc(mt_handle* h, const mt_nrc_config& c)
     // training paths and their samples
     const uint32_t bounces = std::max<uint32_t>(1, cfg.bounces);
     N.train_chunk = std::min<uint32_t>(c.train_paths, h->batch);
-    MT_CUDA(N.trec.alloc(static_cast<size_t>(N.train_chunk) * bounces * 7));
+    MT_CUDA(N.trec.alloc(static_cast<size_t>(N.train_chunk) * bounces * 8));
     MT_CUDA(cudaMemsetAsync(N.trec.p, 0, N.trec.n * sizeof(float4), st));
     N.sample_cap = c.train_paths * bounces;
     MT_CUDA(N.samples.alloc(static_cast<size_t>(N.sample_cap) * 6));
@@ -1257,7 +1257,8 @@ mt_status mt_nrc_enable(mt_handle* h, const mt_nrc_config* c)
     if (h->running) return set_err(MT_ERR_STATE, "an asynchronous render is running");
     if (c->train_paths == 0 || c->train_batch == 0 || c->train_batch > (1u << 24) || c->spp == 0 ||
         !(c->learning_rate > 0.0f) || !(c->beta1 >= 0.0f && c->beta1 < 1.0f) || !(c->beta2 >= 0.0f && c->beta2 < 1.0f) ||
-        !(c->epsilon >= 0.0f) || !(c->ema_decay >= 0.0f && c->ema_decay < 1.0f))
+        !(c->epsilon >= 0.0f) || !(c->ema_decay >= 0.0f && c->ema_decay < 1.0f) ||
+        c->end_at > MT_NRC_END_AT_DIFFUSE)
         return set_err(MT_ERR_INVALID, "invalid radiance-cache configuration");
     if (static_cast<uint64_t>(c->train_paths) * std::max<uint32_t>(1, h->cfg.bounces) > 0xFFFFFFFFull)
         return set_err(MT_ERR_INVALID, "train_paths * bounces exceeds 2^32");
@@ -1279,6 +1280,7 @@ mt_status mt_nrc_frame(mt_handle* h, float* d_accum, uint32_t accum_index, void*
     const uint64_t npix = static_cast<uint64_t>(c.width) * c.height;
     NrcShade base;
     base.rough_min = nc.rough_min;
+    base.end_at = nc.end_at;
     for (int k = 0; k < 3; ++k) {
         base.lo[k] = h->world_lo[k];
         const float ext = h->world_hi[k] - h->world_lo[k];

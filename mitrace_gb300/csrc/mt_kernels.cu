@@ -393,15 +393,19 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, PathState P, ShadowQu
         const f3 emit_now = ld4(P.emit, p) + (cur_e * S.emission_base) * mp.emission;
         st4(P.emit, p, emit_now);
         float seen_diffuse = 0.0f;
+        bool end_here = false;  // AT_DIFFUSE query: the path ends after this vertex's NEE
         if (HOOKS && NC.mode != MT_NRC_OFF) {
             // Radiance-cache feature record of this vertex (mt_nrc.h)
             seen_diffuse = P.prev[p].w;
-            const bool query = NC.mode == MT_NRC_QUERY && bounce >= 1 && seen_diffuse != 0.0f;
+            const bool query =
+                NC.mode == MT_NRC_QUERY && (NC.end_at == MT_NRC_END_AT_DIFFUSE
+                                                ? mp.roughness >= NC.rough_min
+                                                : bounce >= 1 && seen_diffuse != 0.0f);
             float4* fr = nullptr;
             if (query)
                 fr = NC.rec + 6ull * warp_append(NC.count);
             else if (NC.mode == MT_NRC_TRAIN)
-                fr = NC.rec + (static_cast<uint64_t>(p) * S.bounces + bounce) * 7;
+                fr = NC.rec + (static_cast<uint64_t>(p) * S.bounces + bounce) * 8;
             if (fr) {
                 const f3 pn = {(hit_pos.x - NC.lo[0]) * NC.inv_ext[0], (hit_pos.y - NC.lo[1]) * NC.inv_ext[1],
                                (hit_pos.z - NC.lo[2]) * NC.inv_ext[2]};
@@ -426,9 +430,13 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, PathState P, ShadowQu
                 if (!query) {
                     const f3 pre = ((emit_now + ld4(P.direct, p)) + ld4(P.indirect, p)) + ld4(P.sky, p);
                     fr[6] = make_float4(pre.x, pre.y, pre.z, 1.0f);
+                    fr[7] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);  // NEE, set by the shadow stage
                 }
             }
-            if (query) continue;  // the cache stands in for the rest of the path
+            if (query) {
+                if (NC.end_at != MT_NRC_END_AT_DIFFUSE) continue;  // the cache stands in for the rest
+                end_here = true;
+            }
             if (mp.roughness >= NC.rough_min) seen_diffuse = 1.0f;
         }
         float4* vr = R.vert ? R.vert + (static_cast<uint64_t>(p) * S.bounces + bounce) * 5 : nullptr;
@@ -525,6 +533,8 @@ __global__ void __launch_bounds__(128) k_shade(DevScene S, PathState P, ShadowQu
             }
         }
 
+        if (HOOKS && end_here) continue;  // the cache stands in for the reflected rest
+
         // Bounce sampling (Tracer.cpp:177-208); the last vertex never extends
         // (the debug modes that show the first vertex's sample draw it anyway).
         const bool last = bounce + 1 >= S.bounces;
@@ -611,6 +621,9 @@ struct ShadowWork {
             float4* vr = R.vert + (static_cast<uint64_t>(p) * bounces + static_cast<uint32_t>(c.w)) * 5;
             vr[1].w = __uint_as_float(__float_as_uint(vr[1].w) | MT_VREC_VISIBLE);
         }
+        if (R.nrc)  // radiance-cache training record: this vertex's NEE contribution
+            R.nrc[(static_cast<uint64_t>(p) * bounces + static_cast<uint32_t>(c.w)) * 8 + 7] =
+                make_float4(c.x, c.y, c.z, 0.0f);
         float4* acc = c.w == 0.0f ? P.direct : P.indirect;
         const float4 a = acc[p];
         acc[p] = make_float4(__fadd_rn(a.x, c.x), __fadd_rn(a.y, c.y), __fadd_rn(a.z, c.z), 0.0f);
@@ -892,9 +905,10 @@ cudaError_t launch_batch(const DevScene& S, const PathState& P, const ShadowQueu
                          uint32_t pix_base, cudaStream_t st, uint64_t* launches, Profiler* prof,
                          const RecordBuffers* rec, const BatchExtra* extra)
 {
-    const RecordBuffers R = rec ? *rec : RecordBuffers{};
+    RecordBuffers R = rec ? *rec : RecordBuffers{};
     const BatchExtra X = extra ? *extra : BatchExtra{};
     const NrcShade NC = X.nrc ? *X.nrc : NrcShade{};
+    if (NC.mode == MT_NRC_TRAIN) R.nrc = NC.rec;
     BatchInfo B{g0, n, band_pix, pix_base, X.sample_base, X.scatter_mul, X.scatter_add};
     const unsigned gw = grid_for(n, 128, 16);
     static unsigned g_ext[3] = {0, 0, 0}, g_sh[2] = {0, 0};

@@ -66,6 +66,9 @@ struct WaveBuffers {
 struct RecordBuffers {
     float4* vert = nullptr;
     float4* path = nullptr;
+    // radiance-cache training records (NrcShade::rec, 8 float4 per vertex): the
+    // shadow stage writes an unoccluded NEE contribution into float4 7
+    float4* nrc = nullptr;
 };
 #define MT_VREC_HIT 1u
 #define MT_VREC_CHOSEN 2u

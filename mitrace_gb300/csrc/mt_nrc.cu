@@ -852,12 +852,15 @@ __global__ void k_nrc_targets(PathState P, NrcShade N, uint32_t n, uint32_t boun
         const float4 e = P.emit[p], d = P.direct[p], ind = P.indirect[p], s = P.sky[p];
         const float tot[3] = {((e.x + d.x) + ind.x) + s.x, ((e.y + d.y) + ind.y) + s.y, ((e.z + d.z) + ind.z) + s.z};
         for (uint32_t k = 0; k < bounces; ++k) {
-            float4* r = N.rec + (static_cast<uint64_t>(p) * bounces + k) * 7;
+            float4* r = N.rec + (static_cast<uint64_t>(p) * bounces + k) * 8;
             const float4 pre = r[6];
             if (pre.w != 1.0f) break;  // vertices are recorded in bounce order
             r[6].w = 0.0f;
             const float cur[3] = {r[5].x, r[5].y, r[5].z};
-            const float prv[3] = {pre.x, pre.y, pre.z};
+            // AT_DIFFUSE: the cache stands for what the vertex reflects from the
+            // rest of its path, so its own NEE is part of the prefix
+            const float4 nee = N.end_at == MT_NRC_END_AT_DIFFUSE ? r[7] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            const float prv[3] = {pre.x + nee.x, pre.y + nee.y, pre.z + nee.z};
             float tg[3];
             bool ok = true;
 #pragma unroll

@@ -24,18 +24,20 @@ constexpr int kNrcBwdElems = 3 * 64 * 72 + 64 * 24;           // 15,360
 
 // Render-stage hooks of one wavefront batch.
 #define MT_NRC_OFF 0
-#define MT_NRC_QUERY 1  // end paths at the first vertex after a diffuse-ish one, queue a cache query
+#define MT_NRC_QUERY 1  // end paths where NrcShade::end_at says, queue a cache query
 #define MT_NRC_TRAIN 2  // record every vertex of full-length training paths
 struct NrcShade {
     int mode = MT_NRC_OFF;
+    uint32_t end_at = MT_NRC_END_AFTER_DIFFUSE;  // mt_nrc_config::end_at
     float rough_min = 0.3f;
     float lo[3] = {0, 0, 0};       // world box lower corner
     float inv_ext[3] = {1, 1, 1};  // 1 / world box extent
     // QUERY: query records, 6 float4 each: the 5 feature float4 of the header
     //        and (throughput rgb, path index bits).
-    // TRAIN: vertex records of path p, bounce k at rec[(p * bounces + k) * 7]:
-    //        the 6 float4 of a query record and (radiance collected before the
-    //        vertex's NEE, 1 = recorded).
+    // TRAIN: vertex records of path p, bounce k at rec[(p * bounces + k) * 8]:
+    //        the 6 float4 of a query record, (radiance collected before the
+    //        vertex's NEE, 1 = recorded) and the vertex's NEE contribution when
+    //        its shadow ray was unoccluded (written by the shadow stage, else 0).
     float4* rec = nullptr;
     uint32_t* count = nullptr;  // QUERY: queries appended
     // QUERY: bf16 forward weight blob; queries are also added to *total.

@@ -51,7 +51,7 @@ int main(void) {
   S(mt_light_desc) S(mt_camera_desc) S(mt_scene_desc) S(mt_config) S(mt_stats) S(mt_ray)
   S(mt_hit) S(mt_brdf_query) S(mt_brdf_result) S(mt_stage_profile) S(mt_profile) S(mt_grad_buffers) S(mt_nrc_config) S(mt_nrc_stats) S(mt_brdf_sample_query) S(mt_brdf_sample_result)
   O(mt_scene_desc, camera) O(mt_scene_desc, env_texture) O(mt_config, seed) O(mt_mesh_desc, bvh_indices)
-  O(mt_texture_desc, filter) O(mt_light_desc, direction) O(mt_hit, tri_tests) O(mt_nrc_config, seed) O(mt_nrc_config, ema_decay) O(mt_nrc_stats, train_loss) O(mt_grad_buffers, d_image)
+  O(mt_texture_desc, filter) O(mt_light_desc, direction) O(mt_hit, tri_tests) O(mt_nrc_config, seed) O(mt_nrc_config, ema_decay) O(mt_nrc_config, end_at) O(mt_nrc_stats, train_loss) O(mt_grad_buffers, d_image)
   return 0;
 }
 """

@@ -11,7 +11,8 @@
 5. With no diffuse-ish vertex (rough_min > 1) a cached frame is bit-identical
    to mt_render_device at the same samples: the cache hooks leave the plain
    estimator untouched.
-6. Cached frames on the box room converge near the plain render.
+6. Cached frames on the box room converge near the plain render, for both
+   end points of a cached path (mt_nrc_config.end_at).
 """
 import numpy as np
 import pytest
@@ -121,26 +122,31 @@ def test_training_fits_a_smooth_target():
     assert np.isfinite(last) and last < first / 10, (first, last)
 
 
-def test_cache_hooks_leave_plain_paths_unchanged():
+@pytest.mark.parametrize("end_at", [A.MT_NRC_END_AFTER_DIFFUSE, A.MT_NRC_END_AT_DIFFUSE])
+def test_cache_hooks_leave_plain_paths_unchanged(end_at):
     scene, cfg = small_room()
     img = torch.zeros((cfg.height, cfg.width, 3), device="cuda")
     acc = torch.zeros_like(img)
     st = torch.cuda.current_stream().cuda_stream
     with mt.Tracer(scene, cfg) as tr:
         tr.render_device(img.data_ptr(), st)
-        tr.nrc_enable(train_paths=2048, train_batch=1024, spp=cfg.samples, rough_min=2.0)
+        tr.nrc_enable(train_paths=2048, train_batch=1024, spp=cfg.samples, rough_min=2.0, end_at=end_at)
         tr.nrc_frame(acc.data_ptr(), 0, st)
         torch.cuda.synchronize()
     np.testing.assert_array_equal(acc.cpu().numpy(), img.cpu().numpy())
 
 
-def test_cached_frames_converge_near_plain_render():
+@pytest.mark.parametrize("end_at", [A.MT_NRC_END_AFTER_DIFFUSE, A.MT_NRC_END_AT_DIFFUSE])
+def test_cached_frames_converge_near_plain_render(end_at):
     """Box room at +15 EV, where the per-sample ACES curve is linear (so the
     cache's expectation and the plain estimator's agree; at normal exposure the
     per-sample tonemap of a random suffix and of its mean differ by the Jensen
     gap of the curve).  The cached frames' mean brightness matches the plain
     render within 3% and their relative error is well below that of a render
-    whose cache returns zero (paths cut at the query vertex)."""
+    whose cache returns zero (paths cut at the query vertex).  Both end points:
+    the vertex after the first diffuse-ish one (cache = its outgoing radiance)
+    and the first diffuse-ish vertex itself (every vertex of the room; cache =
+    the indirect light it reflects, its NEE traced)."""
     def room(spp):
         scene, cfg = mt.box_room(width=64, height=64, samples=spp, seed=2)
         cfg.ev_exposure = 15.0
@@ -159,7 +165,7 @@ def test_cached_frames_converge_near_plain_render():
         scene, cfg = room(4)
         acc = torch.zeros_like(plain)
         with mt.Tracer(scene, cfg) as tr:
-            tr.nrc_enable(train_paths=16384, train_batch=4096, spp=4, train_steps=8)
+            tr.nrc_enable(train_paths=16384, train_batch=4096, spp=4, train_steps=8, end_at=end_at)
             if zero:
                 tr.nrc_set_params(np.zeros(A.MT_NRC_PARAMS, np.float32))
             for _ in range(0 if zero else 32):  # training only
