@@ -287,11 +287,20 @@ __device__ __forceinline__ void forward(const bf16* W, const uint32_t (&ax)[5][4
     dense<4, 1>(H.h[3], W + fwd_off(4), fwd_stride(4), y);
 }
 
-__device__ __forceinline__ void copy_blob(bf16* dst, const bf16* __restrict__ src, int elems)
+// 16-byte global -> shared copy that does not hold registers or block the
+// thread (cp.async); cp_async_wait waits for all of this thread's copies.
+__device__ __forceinline__ void cp_async16(void* smem_dst, const void* gsrc)
 {
-    const uint4* s = reinterpret_cast<const uint4*>(src);
-    uint4* d = reinterpret_cast<uint4*>(dst);
-    for (int i = threadIdx.x; i < elems / 8; i += blockDim.x) d[i] = s[i];
+    const uint32_t d = static_cast<uint32_t>(__cvta_generic_to_shared(smem_dst));
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// Starts the copy of a weight blob into shared memory (elems a multiple of 8,
+// both ends 16-byte aligned); the caller waits (cp_async_wait + barrier).
+__device__ __forceinline__ void copy_blob_async(bf16* dst, const bf16* __restrict__ src, int elems)
+{
+    for (int i = threadIdx.x; i < elems / 8; i += blockDim.x) cp_async16(dst + 8 * i, src + 8 * i);
 }
 
 // ---------------------------------------------------------------------------
@@ -600,8 +609,9 @@ __global__ void __launch_bounds__(kTrainWarps * 32) k_nrc_fwdbwd(const bf16* __r
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
     bf16* stg = WB + kNrcBwdElems + warp * 16 * 88;
     uint32_t* map = reinterpret_cast<uint32_t*>(WB + kNrcBwdElems + kTrainWarps * 16 * 88) + warp * 16;
-    copy_blob(WF, fwd, kNrcFwdElems);
-    copy_blob(WB, bwd, kNrcBwdElems);
+    copy_blob_async(WF, fwd, kNrcFwdElems);
+    copy_blob_async(WB, bwd, kNrcBwdElems);
+    cp_async_wait();
     __syncthreads();
     const uint32_t cnt = a.count ? min(*a.count, a.count_cap) : a.rows;
     const uint32_t base = *step * a.rows;
@@ -722,20 +732,21 @@ __global__ void __launch_bounds__(kWgWarps * 32) k_nrc_wgrad(NrcActs A, uint32_t
     for (uint32_t c0 = 0; c0 < rows_per_split; c0 += kChunk) {
         __syncthreads();
         const uint64_t rb = row_begin + c0;
-        // stage the chunk: X (10 x 16 B per row), 8 x (8 x 16 B), DY (1 x 16 B)
+        // stage the chunk: X (10 x 16 B per row), 8 x (8 x 16 B), DY (1 x 16 B),
+        // all copies in flight at once
         for (int i = threadIdx.x; i < kChunk * 10; i += blockDim.x) {
             const int row = i / 10, c = i - row * 10;
-            *reinterpret_cast<uint4*>(T + row * kSX + 8 * c) =
-                reinterpret_cast<const uint4*>(A.x)[((rb + row) * 80 + 8 * c) / 8];
+            cp_async16(T + row * kSX + 8 * c, reinterpret_cast<const uint4*>(A.x) + ((rb + row) * 80 + 8 * c) / 8);
         }
         for (int i = threadIdx.x; i < 8 * kChunk * 8; i += blockDim.x) {
             const int m = i / (kChunk * 8), rem = i - m * kChunk * 8, row = rem >> 3, c = rem & 7;
             const void* src = m < 4 ? A.h[m] : A.d[m - 4];
-            *reinterpret_cast<uint4*>(T + kChunk * kSX + m * kChunk * kSH + row * kSH + 8 * c) =
-                reinterpret_cast<const uint4*>(src)[((rb + row) * 64 + 8 * c) / 8];
+            cp_async16(T + kChunk * kSX + m * kChunk * kSH + row * kSH + 8 * c,
+                       reinterpret_cast<const uint4*>(src) + ((rb + row) * 64 + 8 * c) / 8);
         }
         for (int i = threadIdx.x; i < kChunk; i += blockDim.x)
-            *reinterpret_cast<uint4*>(T + kWgOffY + i * kSY) = reinterpret_cast<const uint4*>(A.dy)[rb + i];
+            cp_async16(T + kWgOffY + i * kSY, reinterpret_cast<const uint4*>(A.dy) + rb + i);
+        cp_async_wait();
         __syncthreads();
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
@@ -800,17 +811,33 @@ __device__ __forceinline__ void publish_param(bf16* fwd, bf16* bwd, bf16* infer,
 
 // Bias corrections 1 - beta^t of the moments and of the zero-started weight
 // average, t = the device step counter (already counting this step).
-__global__ void k_nrc_adam(float* __restrict__ master, float* __restrict__ m, float* __restrict__ v,
-                           const float* __restrict__ partial, uint32_t splits, float lr, float b1, float b2,
-                           float eps, bf16* fwd, bf16* bwd, float* grad_out, bf16* infer, float* __restrict__ ema,
-                           float decay, const uint32_t* __restrict__ step)
+// A block owns 32 consecutive parameters (lane = parameter, so every load of
+// a partial row is one coalesced 128-byte line); warp w sums partials w,
+// w + kAdamWarps, ... and warp 0 adds the warps' sums in order, so the
+// gradient is the same on every run.
+constexpr int kAdamWarps = 8;
+
+__global__ void __launch_bounds__(kAdamWarps * 32) k_nrc_adam(float* __restrict__ master, float* __restrict__ m,
+                                                              float* __restrict__ v, const float* __restrict__ partial,
+                                                              uint32_t splits, float lr, float b1, float b2, float eps,
+                                                              bf16* fwd, bf16* bwd, float* grad_out, bf16* infer,
+                                                              float* __restrict__ ema, float decay,
+                                                              const uint32_t* __restrict__ step)
 {
-    const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= kNrcParams) return;
+    __shared__ float red[kAdamWarps][32];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int q = blockIdx.x * 32 + lane;
+    float part = 0.0f;
+    if (q < kNrcParams)
+        for (uint32_t s = warp; s < splits; s += kAdamWarps) part += partial[static_cast<uint64_t>(s) * kNrcParams + q];
+    red[warp][lane] = part;
+    __syncthreads();
+    if (warp != 0 || q >= kNrcParams) return;
+    float gsum = 0.0f;
+#pragma unroll
+    for (int w = 0; w < kAdamWarps; ++w) gsum += red[w][lane];
     const float t = static_cast<float>(*step);
     const float bc1 = 1.0f - powf(b1, t), bc2 = 1.0f - powf(b2, t), ema_bc = 1.0f - powf(decay, t);
-    float gsum = 0.0f;
-    for (uint32_t s = 0; s < splits; ++s) gsum += partial[static_cast<uint64_t>(s) * kNrcParams + q];
     if (grad_out) grad_out[q] = gsum;
     const float mm = b1 * m[q] + (1.0f - b1) * gsum;
     const float vv = b2 * v[q] + (1.0f - b2) * gsum * gsum;
@@ -979,7 +1006,7 @@ cudaError_t launch_nrc_train_step(NrcOptimizer& O, const NrcTrainArgs& a, float*
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     O.step += 1;
-    k_nrc_adam<<<(kNrcParams + 255) / 256, 256, 0, st>>>(O.master, O.m, O.v, O.partial, splits, O.lr, O.beta1,
+    k_nrc_adam<<<(kNrcParams + 31) / 32, kAdamWarps * 32, 0, st>>>(O.master, O.m, O.v, O.partial, splits, O.lr, O.beta1,
                                                         O.beta2, O.eps, static_cast<bf16*>(O.fwd),
                                                         static_cast<bf16*>(O.bwd), grad_out,
                                                         static_cast<bf16*>(O.infer), O.ema, O.ema_decay, O.d_step);
