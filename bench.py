@@ -587,12 +587,13 @@ def run_time_to_relmse(a):
     stream = torch.cuda.Stream(dev)
     torch.cuda.set_stream(stream)
 
-    def render(spp, seed):
+    def render(spp, seed, warm=True):
         scene, cfg = mt.material_grid(width=a.width, height=a.height, samples=spp, seed=0)
         cfg.seed = seed
         out = torch.empty((a.height, a.width, 3), dtype=torch.float32, device=dev)
         with mt.Tracer(scene, cfg) as tr:
-            tr.render_device(out.data_ptr(), stream.cuda_stream)  # warm-up
+            if warm:
+                tr.render_device(out.data_ptr(), stream.cuda_stream)  # warm-up
             torch.cuda.synchronize()
             s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             s0.record(stream)
@@ -603,7 +604,7 @@ def run_time_to_relmse(a):
         return out.cpu().numpy(), s0.elapsed_time(s1) / 1e3, rays, scene, cfg
 
     t0 = time.perf_counter()
-    ref, ref_s, ref_rays, scene, cfg = render(a.ref_spp, 1)
+    ref, ref_s, ref_rays, scene, cfg = render(a.ref_spp, 1, warm=False)  # seconds-long: no warm-up
     ladder = []
     spp = 1
     while spp <= (0 if a.nrc_only else 1024):

@@ -293,7 +293,32 @@ struct SceneHit {
 // Work must provide, per lane:
 //   bool fetch(uint32_t index, f3& o, f3& d, float& tmax)  (false: index past the end)
 //   void finish(const SceneHit& h)
-template <bool COUNT, bool ANY, class Work>
+// True when the instance's world box starts farther along the ray than lim, by
+// more than a margin for rounding (1e-4 of the distances and coordinates
+// involved): no hit in it can then be accepted, since a closest hit must come
+// in strictly below the best world distance and an occluder at or below the
+// light distance.  The world box bounds the transformed triangles (the xyz of
+// model * p is affine in p, and the box is the hull of the transformed local
+// box corners).  A ray that starts inside the box never skips it.
+__device__ __forceinline__ bool instance_beyond(const DevInstance& I, f3 o, f3 inv, float lim)
+{
+    const f3 wlo = {__ldg(&I.wlo[0]), __ldg(&I.wlo[1]), __ldg(&I.wlo[2])};
+    const f3 whi = {__ldg(&I.whi[0]), __ldg(&I.whi[1]), __ldg(&I.whi[2])};
+    const f3 t1 = (wlo - o) * inv;
+    const f3 t2 = (whi - o) * inv;
+    const f3 tmin = vmin(t1, t2);
+    const float enter = gmax(gmax(tmin.x, tmin.y), tmin.z);
+    const float mag = fmaxf(fmaxf(fmaxf(fabsf(o.x), fabsf(o.y)), fabsf(o.z)),
+                            fmaxf(fmaxf(fmaxf(fabsf(wlo.x), fabsf(wlo.y)), fabsf(wlo.z)),
+                                  fmaxf(fmaxf(fabsf(whi.x), fabsf(whi.y)), fabsf(whi.z))));
+    return enter > lim + 1e-4f * (lim + mag);
+}
+
+// SKIP: instances whose world box lies beyond the current best hit (closest)
+// or the light (any) are not opened.  The result, including the winner's
+// counters, is unchanged; only the work summed over all instances (the totals
+// query, the debug modes' traversal counts) needs every instance visited.
+template <bool COUNT, bool ANY, bool SKIP = true, class Work>
 __device__ __forceinline__ void trace_persistent(const DevScene& S, Work& W, uint32_t* fetch_counter)
 {
     const uint32_t lane = threadIdx.x & 31;
@@ -411,34 +436,45 @@ __device__ __forceinline__ void trace_persistent(const DevScene& S, Work& W, uin
                 W.finish(best);
                 has_ray = false;
             } else {
-                const uint32_t k = __ffs(mask) - 1;
+                uint32_t k = __ffs(mask) - 1;
                 mask &= mask - 1;
-                ii = chunk + k;
-                const DevInstance& I = S.instances[ii];
-                float inv[16];
+                if (SKIP) {
+                    const float lim = ANY ? tmax : best.dist;
+                    while (instance_beyond(S.instances[chunk + k], o, winv, lim)) {
+                        k = 0xffffffffu;
+                        if (!mask) break;
+                        k = __ffs(mask) - 1;
+                        mask &= mask - 1;
+                    }
+                }
+                if (k != 0xffffffffu) {
+                    ii = chunk + k;
+                    const DevInstance& I = S.instances[ii];
+                    float inv[16];
 #pragma unroll
-                for (int q = 0; q < 16; ++q) inv[q] = __ldg(&I.inv[q]);
-                lo = xform_point(inv, o);
-                ld = normalize(xform_dir(inv, d));
-                linv = {__fdiv_rn(1.0f, ld.x), __fdiv_rn(1.0f, ld.y), __fdiv_rn(1.0f, ld.z)};
-                const DevMesh m = S.meshes[__ldg(&I.mesh)];
-                nodes = S.nodes + 2ull * m.node_off;
-                slot_base = m.slot_off;
-                h.t = FLT_MAX;
-                h.u = h.v = 0.0f;
-                h.slot = h.bv = 0;
-                h.bvh_tests = h.tri_tests = h.inner = 0;
-                in_inst = true;
-                if (m.has_bvh) {
-                    const float4 a = __ldg(nodes + 0), b = __ldg(nodes + 1);
-                    stk_node[0] = 0;
-                    stk_dist[0] = slab(lo, linv, xyz(a), xyz(b));
-                    sp = 1;
-                } else {
-                    pending = true;
-                    pfirst = 0;
-                    pcount = m.num_slots;
-                    pnode = 0;
+                    for (int q = 0; q < 16; ++q) inv[q] = __ldg(&I.inv[q]);
+                    lo = xform_point(inv, o);
+                    ld = normalize(xform_dir(inv, d));
+                    linv = {__fdiv_rn(1.0f, ld.x), __fdiv_rn(1.0f, ld.y), __fdiv_rn(1.0f, ld.z)};
+                    const DevMesh m = S.meshes[__ldg(&I.mesh)];
+                    nodes = S.nodes + 2ull * m.node_off;
+                    slot_base = m.slot_off;
+                    h.t = FLT_MAX;
+                    h.u = h.v = 0.0f;
+                    h.slot = h.bv = 0;
+                    h.bvh_tests = h.tri_tests = h.inner = 0;
+                    in_inst = true;
+                    if (m.has_bvh) {
+                        const float4 a = __ldg(nodes + 0), b = __ldg(nodes + 1);
+                        stk_node[0] = 0;
+                        stk_dist[0] = slab(lo, linv, xyz(a), xyz(b));
+                        sp = 1;
+                    } else {
+                        pending = true;
+                        pfirst = 0;
+                        pcount = m.num_slots;
+                        pnode = 0;
+                    }
                 }
             }
         }

@@ -98,7 +98,7 @@ __global__ void __launch_bounds__(128, MT_TRAVERSE_MIN_BLOCKS) k_trace(DevScene 
 {
     QueryWork<QUERY> W{rays, hits, n, 0};
     constexpr bool kCount = QUERY == MT_QUERY_CLOSEST_COUNT || QUERY == MT_QUERY_CLOSEST_TOTALS;
-    trace_persistent<kCount, QUERY == MT_QUERY_ANY>(S, W, fetch);
+    trace_persistent<kCount, QUERY == MT_QUERY_ANY, false>(S, W, fetch);  // IntersectScene as is
 }
 
 __global__ void k_brdf(const mt_brdf_query* __restrict__ q, uint64_t n, mt_brdf_result* __restrict__ out)
@@ -312,7 +312,7 @@ __global__ void __launch_bounds__(128, MT_TRAVERSE_MIN_BLOCKS) k_extend(DevScene
         atomicAdd(rays, static_cast<unsigned long long>(n));
     }
     ExtendWork<COUNT, DBG> W{P, q, n, 0, 0, 0, 0, S.debug_mode};
-    trace_persistent<COUNT, false>(S, W, &counts[3]);
+    trace_persistent<COUNT, false, !DBG>(S, W, &counts[3]);  // debug counts visit every instance
     if (COUNT) flush_counts(cnt, W.pops, W.inner, W.tris);
 }
 
