@@ -364,7 +364,18 @@ typedef struct mt_nrc_config {
                               of the trained weights (bias-corrected) with this
                               decay; 0 queries the trained weights themselves (0.9) */
     uint32_t end_at;       /* where a cached path ends (MT_NRC_END_*) */
-    uint32_t reserved[4];
+    float target_cap;      /* upper bound, per channel, on the radiance times
+                              2^-ev_exposure that the rest of a training path
+                              adds to its vertex's target; <= 0: none (0.5).
+                              The reference tonemaps every sample (ACES, which
+                              saturates: 0.62 at 0.5, 0.92 at 2, 1.03 at
+                              infinity) and its firefly rule drops rare
+                              outliers, so the plain estimate hardly contains
+                              rare very bright suffixes (a sun reached after a
+                              diffuse bounce); uncapped, the cache learns their
+                              mean and the cached image turns brighter the
+                              longer it trains */
+    uint32_t reserved[3];
 } mt_nrc_config;
 
 /* mt_nrc_config::end_at.
@@ -396,7 +407,8 @@ mt_status mt_nrc_enable(mt_handle* h, const mt_nrc_config* c);
  *  1. trace train_paths full-length plain paths from random pixels, record
  *     every vertex's features and the radiance the rest of its path carried
  *     back ((path total - total before the vertex's NEE) / throughput; with
- *     MT_NRC_END_AT_DIFFUSE the vertex's own NEE is subtracted as well);
+ *     MT_NRC_END_AT_DIFFUSE the vertex's own NEE is subtracted as well; the
+ *     numerator capped at target_cap * 2^ev_exposure per channel);
  *  2. take train_steps Adam steps on batches of those vertices (relative L2
  *     loss |y - t|^2 / (y^2 + 0.01), y held constant in the denominator);
  *  3. if d_accum is not NULL, render spp samples per pixel in which a path

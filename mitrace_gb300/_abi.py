@@ -228,7 +228,8 @@ class mt_nrc_config(C.Structure):
         ("seed", C.c_uint32),
         ("ema_decay", C.c_float),
         ("end_at", C.c_uint32),
-        ("reserved", C.c_uint32 * 4),
+        ("target_cap", C.c_float),
+        ("reserved", C.c_uint32 * 3),
     ]
 
 

@@ -518,6 +518,12 @@ mt_status upload_scene(mt_handle* h, const mt_scene_desc* d)
         const bool resident = bvh_bytes <= MT_TRAVERSE_RESIDENT_L2_FRACTION * l2;
         S.trav_pops = resident ? MT_TRAVERSE_POPS_RESIDENT : 1;
         S.trav_prefetch = resident ? 0 : 1;
+        // an L2-resident scene's rays are short (tens of triangle tests), so
+        // instance switches are frequent and worth batching; a large scene's
+        // rays run thousands of tests between switches (measured on the 6.1 M
+        // triangle scene: 8 lanes 45.9 against 45.6 Mrays/s unbatched, 16
+        // lanes 2% slower)
+        S.trav_switch = resident ? MT_TRAVERSE_SWITCH_RESIDENT : 1;
     }
     S.normals = h->normals.p;
     S.uvs = h->uvs.p;
@@ -1249,6 +1255,7 @@ void mt_nrc_config_defaults(mt_nrc_config* c)
     c->rough_min = 0.3f;
     c->seed = 1337;
     c->ema_decay = 0.9f;
+    c->target_cap = 0.5f;
 }
 
 mt_status mt_nrc_enable(mt_handle* h, const mt_nrc_config* c)
@@ -1258,7 +1265,7 @@ mt_status mt_nrc_enable(mt_handle* h, const mt_nrc_config* c)
     if (c->train_paths == 0 || c->train_batch == 0 || c->train_batch > (1u << 24) || c->spp == 0 ||
         !(c->learning_rate > 0.0f) || !(c->beta1 >= 0.0f && c->beta1 < 1.0f) || !(c->beta2 >= 0.0f && c->beta2 < 1.0f) ||
         !(c->epsilon >= 0.0f) || !(c->ema_decay >= 0.0f && c->ema_decay < 1.0f) ||
-        c->end_at > MT_NRC_END_AT_DIFFUSE)
+        c->end_at > MT_NRC_END_AT_DIFFUSE || std::isnan(c->target_cap))
         return set_err(MT_ERR_INVALID, "invalid radiance-cache configuration");
     if (static_cast<uint64_t>(c->train_paths) * std::max<uint32_t>(1, h->cfg.bounces) > 0xFFFFFFFFull)
         return set_err(MT_ERR_INVALID, "train_paths * bounces exceeds 2^32");
@@ -1297,6 +1304,7 @@ mt_status mt_nrc_frame(mt_handle* h, float* d_accum, uint32_t accum_index, void*
     T.samples = N.samples.p;
     T.sample_count = N.counters.p + 1;
     T.sample_cap = N.sample_cap;
+    T.target_cap = nc.target_cap > 0.0f ? nc.target_cap / h->S.exposure : 0.0f;
     uint64_t mul = (0x9E3779B1ull + 2 * N.frames) % npix;
     if (mul == 0) mul = 1;
     while (gcd64(mul, npix) != 1) mul = (mul + 1) % npix ? (mul + 1) % npix : 1;

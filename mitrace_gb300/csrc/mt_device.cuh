@@ -10,6 +10,7 @@
 // only the transcendental calls (sinf, cosf, acosf, atan2f, powf) can differ by
 // an ulp from the host C library.
 #pragma once
+#include <type_traits>
 
 #include <cfloat>
 #include <cstdint>
@@ -184,6 +185,7 @@ struct DevScene {
     int32_t debug_mode;  // Config::DebugMode (MT_DEBUG_*), 0 = DebugNone
     int32_t trav_pops;      // node pops per lane between two leaf passes (>= 1)
     int32_t trav_prefetch;  // 1: prefetch a reached leaf's slots into L2
+    int32_t trav_switch;    // lanes that wait before an instance switch runs (>= 1)
 };
 
 #define MT_STACK_SIZE 64
@@ -199,6 +201,18 @@ struct DevScene {
 #endif
 #ifndef MT_TRAVERSE_RESIDENT_L2_FRACTION
 #define MT_TRAVERSE_RESIDENT_L2_FRACTION 0.5
+#endif
+
+// Instance switches (close an instance, open the next, finish a ray and fetch
+// the next) of a scene whose switches are frequent run once at least
+// DevScene::trav_switch lanes wait for one, or when no lane has a node or a
+// leaf left; each switch is a long stretch of lane-divergent code (two 4x4
+// matrices, exact divisions and square roots), so running it for several
+// lanes at once costs little more than for one (measured on the 50-instance
+// material grid: 1 lane 1035, 8 lanes 1046, 12 lanes 1050, 16 lanes 1050,
+// 24 lanes 1035 Mrays/s).
+#ifndef MT_TRAVERSE_SWITCH_RESIDENT
+#define MT_TRAVERSE_SWITCH_RESIDENT 12
 #endif
 
 // Bulk prefetch of [p, p + bytes) into L2 (no registers, no completion to wait
@@ -224,7 +238,6 @@ __device__ __forceinline__ float slab(f3 o, f3 inv, f3 lo, f3 hi)
     const float exit = gmin(gmin(tmax.x, tmax.y), tmax.z);
     return enter <= exit ? exit : -1.0f;
 }
-
 // Moller-Trumbore (1997), two-sided with |det| > FLT_EPSILON, edge-inclusive.
 // The det<0 branch is folded onto the det>0 one by negating u, v and det, which
 // is exact, so the accept/reject decisions equal the two-branch form.
@@ -314,11 +327,20 @@ __device__ __forceinline__ bool instance_beyond(const DevInstance& I, f3 o, f3 i
     return enter > lim + 1e-4f * (lim + mag);
 }
 
+__device__ __forceinline__ uint32_t lowest_bit(uint32_t m) { return __ffs(static_cast<int>(m)) - 1; }
+__device__ __forceinline__ uint32_t lowest_bit(unsigned long long m)
+{
+    return __ffsll(static_cast<long long>(m)) - 1;
+}
+
 // SKIP: instances whose world box lies beyond the current best hit (closest)
 // or the light (any) are not opened.  The result, including the winner's
 // counters, is unchanged; only the work summed over all instances (the totals
 // query, the debug modes' traversal counts) needs every instance visited.
-template <bool COUNT, bool ANY, bool SKIP = true, class Work>
+// CHUNK (32 or 64) instances are tested per warp pass of the world-box test;
+// with 64 every lane tests two boxes and a ray's mask of met instances is 64
+// bits wide (one pass instead of two per ray on a 33-64 instance scene).
+template <bool COUNT, bool ANY, bool SKIP = true, int CHUNK = 32, class Work>
 __device__ __forceinline__ void trace_persistent(const DevScene& S, Work& W, uint32_t* fetch_counter)
 {
     const uint32_t lane = threadIdx.x & 31;
@@ -328,7 +350,9 @@ __device__ __forceinline__ void trace_persistent(const DevScene& S, Work& W, uin
     float tmax = 0.0f;
     SceneHit best;
     bool stopped = false;
-    uint32_t chunk = 0, mask = 0;
+    typedef typename std::conditional<CHUNK == 64, unsigned long long, uint32_t>::type imask_t;
+    uint32_t chunk = 0;
+    imask_t mask = 0;
     bool need_mask = false;
     bool in_inst = false;
     uint32_t ii = 0;
@@ -384,15 +408,20 @@ __device__ __forceinline__ void trace_persistent(const DevScene& S, Work& W, uin
             const f3 bo = {__shfl_sync(MT_FULL, o.x, L), __shfl_sync(MT_FULL, o.y, L), __shfl_sync(MT_FULL, o.z, L)};
             const f3 bi = {__shfl_sync(MT_FULL, winv.x, L), __shfl_sync(MT_FULL, winv.y, L),
                            __shfl_sync(MT_FULL, winv.z, L)};
-            const uint32_t k = __shfl_sync(MT_FULL, chunk, L) + lane;
-            bool meets = false;
-            if (k < S.num_instances) {
-                const DevInstance& I = S.instances[k];
-                const f3 wlo = {__ldg(&I.wlo[0]), __ldg(&I.wlo[1]), __ldg(&I.wlo[2])};
-                const f3 whi = {__ldg(&I.whi[0]), __ldg(&I.whi[1]), __ldg(&I.whi[2])};
-                meets = slab(bo, bi, wlo, whi) >= 0.0f;
+            const uint32_t c0 = __shfl_sync(MT_FULL, chunk, L);
+            imask_t m = 0;
+#pragma unroll
+            for (int q = 0; q < CHUNK / 32; ++q) {  // lane tests instances c0 + lane (+ 32)
+                const uint32_t k = c0 + 32u * q + lane;
+                bool meets = false;
+                if (k < S.num_instances) {
+                    const DevInstance& I = S.instances[k];
+                    const f3 wlo = {__ldg(&I.wlo[0]), __ldg(&I.wlo[1]), __ldg(&I.wlo[2])};
+                    const f3 whi = {__ldg(&I.whi[0]), __ldg(&I.whi[1]), __ldg(&I.whi[2])};
+                    meets = slab(bo, bi, wlo, whi) >= 0.0f;
+                }
+                m |= static_cast<imask_t>(__ballot_sync(MT_FULL, meets)) << (32 * q);
             }
-            const uint32_t m = __ballot_sync(MT_FULL, meets);
             if (lane == L) {
                 mask = m;
                 need_mask = false;
@@ -400,7 +429,14 @@ __device__ __forceinline__ void trace_persistent(const DevScene& S, Work& W, uin
         }
 
         // C. close the instance whose stack ran dry; open the next; finish the ray
-        if (has_ray && !need_mask && !pending && sp == 0) {
+        const bool want_switch = has_ray && !need_mask && !pending && sp == 0;
+        bool run_switch = true;
+        if (S.trav_switch > 1) {
+            const uint32_t sw = __ballot_sync(MT_FULL, want_switch);
+            if (sw && __popc(sw) < S.trav_switch)
+                run_switch = __ballot_sync(MT_FULL, has_ray && (pending || sp > 0)) == 0;
+        }
+        if (want_switch && run_switch) {
             if (in_inst) {
                 if (COUNT) {
                     best.tot_pops += h.bvh_tests;
@@ -429,21 +465,21 @@ __device__ __forceinline__ void trace_persistent(const DevScene& S, Work& W, uin
                 }
                 in_inst = false;
             }
-            if (mask == 0 && !stopped && chunk + 32 < S.num_instances) {
-                chunk += 32;
+            if (mask == 0 && !stopped && chunk + CHUNK < S.num_instances) {
+                chunk += CHUNK;
                 need_mask = true;
             } else if (mask == 0 || stopped) {
                 W.finish(best);
                 has_ray = false;
             } else {
-                uint32_t k = __ffs(mask) - 1;
+                uint32_t k = lowest_bit(mask);
                 mask &= mask - 1;
                 if (SKIP) {
                     const float lim = ANY ? tmax : best.dist;
                     while (instance_beyond(S.instances[chunk + k], o, winv, lim)) {
                         k = 0xffffffffu;
                         if (!mask) break;
-                        k = __ffs(mask) - 1;
+                        k = lowest_bit(mask);
                         mask &= mask - 1;
                     }
                 }

@@ -297,7 +297,10 @@ struct ExtendWork {
     }
 };
 
-template <bool COUNT, bool DBG>
+// CHUNK: instances per world-box pass (64 for the plain render of a scene with
+// more than 32 instances; the counting and debug forms keep 32, which visits
+// the same nodes in the same order).
+template <bool COUNT, bool DBG, int CHUNK = 32>
 __global__ void __launch_bounds__(128, MT_TRAVERSE_MIN_BLOCKS) k_extend(DevScene S, PathState P,
                                                 const uint32_t* __restrict__ q,
                                                 uint32_t* counts, int cur,
@@ -312,7 +315,7 @@ __global__ void __launch_bounds__(128, MT_TRAVERSE_MIN_BLOCKS) k_extend(DevScene
         atomicAdd(rays, static_cast<unsigned long long>(n));
     }
     ExtendWork<COUNT, DBG> W{P, q, n, 0, 0, 0, 0, S.debug_mode};
-    trace_persistent<COUNT, false, !DBG>(S, W, &counts[3]);  // debug counts visit every instance
+    trace_persistent<COUNT, false, !DBG, CHUNK>(S, W, &counts[3]);  // debug counts visit every instance
     if (COUNT) flush_counts(cnt, W.pops, W.inner, W.tris);
 }
 
@@ -630,7 +633,7 @@ struct ShadowWork {
     }
 };
 
-template <bool COUNT>
+template <bool COUNT, int CHUNK = 32>
 __global__ void __launch_bounds__(128, MT_TRAVERSE_MIN_BLOCKS) k_shadow(DevScene S, PathState P, ShadowQueue SQ,
                                                 uint32_t* counts,
                                                 unsigned long long* rays,
@@ -643,7 +646,7 @@ __global__ void __launch_bounds__(128, MT_TRAVERSE_MIN_BLOCKS) k_shadow(DevScene
         atomicAdd(rays, static_cast<unsigned long long>(n));
     }
     ShadowWork<COUNT> W{P, SQ, R, S.bounces, n, 0, 0, 0, 0};
-    trace_persistent<COUNT, true>(S, W, &counts[4]);
+    trace_persistent<COUNT, true, true, CHUNK>(S, W, &counts[4]);
     if (COUNT) flush_counts(cnt, W.pops, W.inner, W.tris);
 }
 
@@ -911,14 +914,17 @@ cudaError_t launch_batch(const DevScene& S, const PathState& P, const ShadowQueu
     if (NC.mode == MT_NRC_TRAIN) R.nrc = NC.rec;
     BatchInfo B{g0, n, band_pix, pix_base, X.sample_base, X.scatter_mul, X.scatter_add};
     const unsigned gw = grid_for(n, 128, 16);
-    static unsigned g_ext[3] = {0, 0, 0}, g_sh[2] = {0, 0};
+    static unsigned g_ext[4] = {0, 0, 0, 0}, g_sh[3] = {0, 0, 0};
     if (!g_ext[0]) {
         g_ext[0] = persistent_grid(k_extend<false, false>, 128);
         g_ext[1] = persistent_grid(k_extend<true, false>, 128);
         g_ext[2] = persistent_grid(k_extend<true, true>, 128);
+        g_ext[3] = persistent_grid(k_extend<false, false, 64>, 128);
         g_sh[0] = persistent_grid(k_shadow<false>, 128);
         g_sh[1] = persistent_grid(k_shadow<true>, 128);
+        g_sh[2] = persistent_grid(k_shadow<false, 64>, 128);
     }
+    const bool wide = S.num_instances > 32;
     const bool count = prof && prof->counting;
     unsigned long long* cnt = prof ? prof->d_counts : nullptr;
     auto begin = [&](int s) { if (prof) prof->begin(s, st); };
@@ -934,6 +940,8 @@ cudaError_t launch_batch(const DevScene& S, const PathState& P, const ShadowQueu
             k_extend<true, true><<<g_ext[2], 128, 0, st>>>(S, P, W.q[cur], W.counts, cur, W.rays, cnt);
         else if (count)
             k_extend<true, false><<<g_ext[1], 128, 0, st>>>(S, P, W.q[cur], W.counts, cur, W.rays, cnt);
+        else if (wide)
+            k_extend<false, false, 64><<<g_ext[3], 128, 0, st>>>(S, P, W.q[cur], W.counts, cur, W.rays, cnt);
         else
             k_extend<false, false><<<g_ext[0], 128, 0, st>>>(S, P, W.q[cur], W.counts, cur, W.rays, cnt);
         end(MT_STAGE_EXTEND);
@@ -946,6 +954,8 @@ cudaError_t launch_batch(const DevScene& S, const PathState& P, const ShadowQueu
         begin(MT_STAGE_SHADOW);
         if (prof && prof->counting)
             k_shadow<true><<<g_sh[1], 128, 0, st>>>(S, P, SQ, W.counts, W.rays + 1, cnt ? cnt + 3 : nullptr, R);
+        else if (wide)
+            k_shadow<false, 64><<<g_sh[2], 128, 0, st>>>(S, P, SQ, W.counts, W.rays + 1, nullptr, R);
         else
             k_shadow<false><<<g_sh[0], 128, 0, st>>>(S, P, SQ, W.counts, W.rays + 1, nullptr, R);
         end(MT_STAGE_SHADOW);

@@ -893,7 +893,9 @@ __global__ void k_nrc_targets(PathState P, NrcShade N, uint32_t n, uint32_t boun
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
                 ok = ok && cur[c] > 1e-6f;
-                tg[c] = fmaxf(tot[c] - prv[c], 0.0f) / cur[c];
+                float sfx = fmaxf(tot[c] - prv[c], 0.0f);
+                if (N.target_cap > 0.0f) sfx = fminf(sfx, N.target_cap);
+                tg[c] = sfx / cur[c];
                 ok = ok && isfinite(tg[c]);
             }
             if (!ok) continue;

@@ -48,6 +48,9 @@ struct NrcShade {
     float4* samples = nullptr;
     uint32_t* sample_count = nullptr;
     uint32_t sample_cap = 0;
+    // TRAIN: upper bound on the radiance a vertex's suffix adds to its path
+    // (per channel, before the division by throughput); 0 = none.
+    float target_cap = 0.0f;
 };
 
 // Transposable activations of one training batch, row-major BF16 per row.

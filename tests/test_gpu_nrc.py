@@ -13,6 +13,8 @@
    estimator untouched.
 6. Cached frames on the box room converge near the plain render, for both
    end points of a cached path (mt_nrc_config.end_at).
+7. mt_nrc_config.target_cap bounds the training targets: with a cap near zero
+   the trained cache returns about nothing.
 """
 import numpy as np
 import pytest
@@ -185,3 +187,30 @@ def test_cached_frames_converge_near_plain_render(end_at):
     rel0 = float(((z - p) ** 2 / (p * p + eps)).mean())
     assert abs(a.mean() / p.mean() - 1) < 0.03, (a.mean(), p.mean())
     assert rel < 0.5 * rel0, (rel, rel0)
+
+
+def test_target_cap_bounds_training_targets():
+    """Two caches trained on the same box-room paths, one with target_cap near
+    zero (every target is then about 0) and one without a cap: the capped
+    cache's outputs on the same inputs are a small fraction of the uncapped
+    one's, so the cap reaches the target computation."""
+    scene, cfg = small_room()
+    st = torch.cuda.current_stream().cuda_stream
+    f = ref.random_features(4096, seed=11)
+    fd = dev(f)
+
+    def trained_outputs(cap):
+        with mt.Tracer(scene, cfg) as tr:
+            tr.nrc_enable(train_paths=4096, train_batch=2048, spp=4, train_steps=32, target_cap=cap)
+            for _ in range(8):  # training only
+                tr.nrc_frame(0, 0, st)
+            out = torch.zeros((4096, 3), device="cuda")
+            tr.nrc_infer_device(fd.data_ptr(), 4096, out.data_ptr(), st)
+            torch.cuda.synchronize()
+            return out.cpu().numpy().astype(np.float64)
+
+    capped = trained_outputs(1e-7)
+    free = trained_outputs(0.0)
+    assert np.all(np.isfinite(capped)) and np.all(np.isfinite(free))
+    assert np.abs(free).mean() > 1e-2, np.abs(free).mean()
+    assert np.abs(capped).mean() < 0.1 * np.abs(free).mean(), (np.abs(capped).mean(), np.abs(free).mean())
