@@ -490,13 +490,13 @@ def run_ours(a):
             pass
     traffic = None
     if TRAFFIC_FILE.exists():
-        # DRAM bytes per extend launch from the ncu summary (a capture of a
-        # smaller render of the same scene, scaled by rays per launch)
+        # DRAM bytes per extend ray from the ncu summary (a capture of a smaller
+        # render of the same scene), times this run's extend rays per launch
         text = TRAFFIC_FILE.read_text()
         w = re.search(r"^traffic_workload: (\S+)$", text, re.M)
-        b = re.search(r"^traffic_per_launch_bytes: (\d+)$", text, re.M)
+        b = re.search(r"^traffic_bytes_per_extend_ray: ([0-9.]+)$", text, re.M)
         if w and b and w.group(1) == workload_name(a):
-            traffic = int(b.group(1))
+            traffic = round(float(b.group(1)) * counts["extend_rays"] / launches_per_render)
     stage_ms = {n: round(prof.stage[i].milliseconds / a.steps, 3) for i, n in
                 enumerate(["raygen", "extend", "shade", "shadow", "finalize", "resolve"])}
 

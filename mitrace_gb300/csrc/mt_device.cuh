@@ -195,9 +195,11 @@ struct DevScene {
 // passes of the warp and prefetches nothing; a larger scene pops one node per
 // pass and has each leaf's triangle slots (the first 32) brought into L2 the
 // moment a lane reaches the leaf, so that the leaf's warp pass finds them there
-// (measured: +2% Mrays/s on an 11 MB scene, +10% on a 1.5 GB one).
+// (measured: +2% Mrays/s on an 11 MB scene, +10% on a 1.5 GB one).  Pops
+// per pass on the material grid with batched instance switches, Mrays/s:
+// 3 -> 1058, 4 -> 1049, 5 -> 1052.
 #ifndef MT_TRAVERSE_POPS_RESIDENT
-#define MT_TRAVERSE_POPS_RESIDENT 4
+#define MT_TRAVERSE_POPS_RESIDENT 3
 #endif
 #ifndef MT_TRAVERSE_RESIDENT_L2_FRACTION
 #define MT_TRAVERSE_RESIDENT_L2_FRACTION 0.5

@@ -19,10 +19,16 @@
 #include "mt_nrc.h"
 
 // Occupancy hint of the traversal kernels: blocks of 128 threads per SM that
-// the register allocation must allow (6 -> at most 80 registers per thread, no
-// spills; 5, 6 and 8 were measured, 6 and 8 tie and 8 spills).
+// the register allocation must allow (7 -> at most 72 registers per thread).
+// Measured on the material grid render (Mrays/s): 6 blocks 1041, 7 blocks
+// 1049, 8 blocks 1034; on the 6.1 M-triangle incoherent batch the any-hit
+// query gains from 8 blocks (63.6 against 61.6 Mrays/s; closest hit the same),
+// so the any-hit test kernel takes MT_TRACE_ANY_MIN_BLOCKS.
 #ifndef MT_TRAVERSE_MIN_BLOCKS
 #define MT_TRAVERSE_MIN_BLOCKS 7
+#endif
+#ifndef MT_TRACE_ANY_MIN_BLOCKS
+#define MT_TRACE_ANY_MIN_BLOCKS 8
 #endif
 
 namespace mt {
@@ -93,7 +99,7 @@ struct QueryWork {
 };
 
 template <int QUERY>
-__global__ void __launch_bounds__(128, MT_TRAVERSE_MIN_BLOCKS) k_trace(DevScene S, const mt_ray* __restrict__ rays, uint32_t n,
+__global__ void __launch_bounds__(128, QUERY == MT_QUERY_ANY ? MT_TRACE_ANY_MIN_BLOCKS : MT_TRAVERSE_MIN_BLOCKS) k_trace(DevScene S, const mt_ray* __restrict__ rays, uint32_t n,
                                                mt_hit* __restrict__ hits, uint32_t* fetch)
 {
     QueryWork<QUERY> W{rays, hits, n, 0};
@@ -331,8 +337,16 @@ __device__ __forceinline__ void st4(float4* p, uint32_t i, f3 v, float w = 0.0f)
 
 // HOOKS: the radiance-cache and debug-mode code paths; the plain render runs
 // the variant without them.
+// Occupancy hint of the shade kernel (blocks of 128 threads per SM): 8 caps it
+// at 64 registers with a few bytes of spills; the kernel waits on scattered
+// path-state and material loads, so more resident warps pay (measured on the
+// material grid render, shade ms: 80 registers 135, 78 registers 140, 72 registers 145,
+// 64 registers 117, 48 registers 121).
+#ifndef MT_SHADE_MIN_BLOCKS
+#define MT_SHADE_MIN_BLOCKS 8
+#endif
 template <bool HOOKS>
-__global__ void __launch_bounds__(128) k_shade(DevScene S, PathState P, ShadowQueue SQ,
+__global__ void __launch_bounds__(128, MT_SHADE_MIN_BLOCKS) k_shade(DevScene S, PathState P, ShadowQueue SQ,
                                                BatchInfo B, uint32_t bounce,
                                                const uint32_t* __restrict__ q,
                                                uint32_t* __restrict__ nq, uint32_t* counts,

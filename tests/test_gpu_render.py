@@ -101,7 +101,7 @@ def test_small_batches_and_bands_give_same_image(monkeypatch):
 
 
 def test_kill_render_and_state_errors():
-    # long enough (about 1 s, ~250 batches) that the kill lands mid-render
+    # long enough (about 1 s, 16 batches of 2^26 paths) that the kill lands mid-render
     scene, cfg = mt.material_grid(width=1920, height=1080, samples=512)
     with mt.Tracer(scene, cfg) as tr:
         tr.StartRender()
