@@ -205,6 +205,13 @@ struct DevScene {
 #define MT_TRAVERSE_RESIDENT_L2_FRACTION 0.5
 #endif
 
+// Requesting lanes served by one world-box pass on a one-chunk scene (1, 2, 4
+// or 8).  A pass is a short dependent chain (shuffle, slab test, ballot), so
+// two independent chains per pass hide each other's latency; more spill
+// (material grid Mrays/s: 1 -> 1396, 2 -> 1449, 4 -> 1363, 8 -> 1273).
+#ifndef MT_MASK_GROUP
+#define MT_MASK_GROUP 2
+#endif
 // Instance switches (close an instance, open the next, finish a ray and fetch
 // the next) of a scene whose switches are frequent run once at least
 // DevScene::trav_switch lanes wait for one, or when no lane has a node or a
@@ -329,6 +336,43 @@ __device__ __forceinline__ bool instance_beyond(const DevInstance& I, f3 o, f3 i
     return enter > lim + 1e-4f * (lim + mag);
 }
 
+// One world-box pass for G requesting lanes (the G lowest bits of nm) of a
+// scene whose instances fit in one chunk: lane k holds the boxes of instances
+// k and k + 32 (blo, bhi) and tests them against each of the G rays.
+template <int G, int CHUNK, class M>
+__device__ __forceinline__ void mask_group(uint32_t& nm, const DevScene& S, const f3* blo, const f3* bhi, f3 o,
+                                           f3 winv, M& mask, bool& need_mask, uint32_t lane)
+{
+    uint32_t Ls[G];
+    f3 bo[G], bi[G];
+#pragma unroll
+    for (int g = 0; g < G; ++g) {
+        Ls[g] = __ffs(nm) - 1;
+        nm &= nm - 1;
+        bo[g] = {__shfl_sync(MT_FULL, o.x, Ls[g]), __shfl_sync(MT_FULL, o.y, Ls[g]), __shfl_sync(MT_FULL, o.z, Ls[g])};
+        bi[g] = {__shfl_sync(MT_FULL, winv.x, Ls[g]), __shfl_sync(MT_FULL, winv.y, Ls[g]),
+                 __shfl_sync(MT_FULL, winv.z, Ls[g])};
+    }
+    M m[G];
+#pragma unroll
+    for (int g = 0; g < G; ++g) m[g] = 0;
+#pragma unroll
+    for (int q = 0; q < CHUNK / 32; ++q) {
+        const bool in = 32u * q + lane < S.num_instances;
+#pragma unroll
+        for (int g = 0; g < G; ++g) {
+            const bool meets = in && slab(bo[g], bi[g], blo[q], bhi[q]) >= 0.0f;
+            m[g] |= static_cast<M>(__ballot_sync(MT_FULL, meets)) << (32 * q);
+        }
+    }
+#pragma unroll
+    for (int g = 0; g < G; ++g)
+        if (lane == Ls[g]) {
+            mask = m[g];
+            need_mask = false;
+        }
+}
+
 __device__ __forceinline__ uint32_t lowest_bit(uint32_t m) { return __ffs(static_cast<int>(m)) - 1; }
 __device__ __forceinline__ uint32_t lowest_bit(unsigned long long m)
 {
@@ -402,31 +446,61 @@ __device__ __forceinline__ void trace_persistent(const DevScene& S, Work& W, uin
         }
         if (!__any_sync(MT_FULL, has_ray)) break;
 
-        // B. instance boxes of the current chunk, one warp pass per requesting lane
+        // B. instance boxes of the current chunk, one warp pass per requesting
+        // lane.  When every instance fits in one chunk (the chunk is then 0
+        // for every lane) each lane loads its boxes once for all the passes.
         uint32_t nm = __ballot_sync(MT_FULL, need_mask);
-        while (nm) {
-            const uint32_t L = __ffs(nm) - 1;
-            nm &= nm - 1;
-            const f3 bo = {__shfl_sync(MT_FULL, o.x, L), __shfl_sync(MT_FULL, o.y, L), __shfl_sync(MT_FULL, o.z, L)};
-            const f3 bi = {__shfl_sync(MT_FULL, winv.x, L), __shfl_sync(MT_FULL, winv.y, L),
-                           __shfl_sync(MT_FULL, winv.z, L)};
-            const uint32_t c0 = __shfl_sync(MT_FULL, chunk, L);
-            imask_t m = 0;
+        if (nm) {
+            const bool one_chunk = S.num_instances <= CHUNK;  // warp-uniform
+            f3 blo[CHUNK / 32], bhi[CHUNK / 32];
 #pragma unroll
-            for (int q = 0; q < CHUNK / 32; ++q) {  // lane tests instances c0 + lane (+ 32)
-                const uint32_t k = c0 + 32u * q + lane;
-                bool meets = false;
-                if (k < S.num_instances) {
+            for (int q = 0; q < CHUNK / 32; ++q) {
+                blo[q] = bhi[q] = splat(0.0f);
+                const uint32_t k = 32u * q + lane;
+                if (one_chunk && k < S.num_instances) {
                     const DevInstance& I = S.instances[k];
-                    const f3 wlo = {__ldg(&I.wlo[0]), __ldg(&I.wlo[1]), __ldg(&I.wlo[2])};
-                    const f3 whi = {__ldg(&I.whi[0]), __ldg(&I.whi[1]), __ldg(&I.whi[2])};
-                    meets = slab(bo, bi, wlo, whi) >= 0.0f;
+                    blo[q] = {__ldg(&I.wlo[0]), __ldg(&I.wlo[1]), __ldg(&I.wlo[2])};
+                    bhi[q] = {__ldg(&I.whi[0]), __ldg(&I.whi[1]), __ldg(&I.whi[2])};
                 }
-                m |= static_cast<imask_t>(__ballot_sync(MT_FULL, meets)) << (32 * q);
             }
-            if (lane == L) {
-                mask = m;
-                need_mask = false;
+            // groups of requesting lanes share a pass: independent slab chains
+            // overlap their latencies
+            if (one_chunk) {
+                if (MT_MASK_GROUP >= 8)
+                    while (__popc(nm) >= 8) mask_group<8, CHUNK>(nm, S, blo, bhi, o, winv, mask, need_mask, lane);
+                if (MT_MASK_GROUP >= 4)
+                    while (__popc(nm) >= 4) mask_group<4, CHUNK>(nm, S, blo, bhi, o, winv, mask, need_mask, lane);
+                if (MT_MASK_GROUP >= 2)
+                    while (__popc(nm) >= 2) mask_group<2, CHUNK>(nm, S, blo, bhi, o, winv, mask, need_mask, lane);
+            }
+            while (nm) {
+                const uint32_t L = __ffs(nm) - 1;
+                nm &= nm - 1;
+                const f3 bo = {__shfl_sync(MT_FULL, o.x, L), __shfl_sync(MT_FULL, o.y, L),
+                               __shfl_sync(MT_FULL, o.z, L)};
+                const f3 bi = {__shfl_sync(MT_FULL, winv.x, L), __shfl_sync(MT_FULL, winv.y, L),
+                               __shfl_sync(MT_FULL, winv.z, L)};
+                const uint32_t c0 = one_chunk ? 0u : __shfl_sync(MT_FULL, chunk, L);
+                imask_t m = 0;
+#pragma unroll
+                for (int q = 0; q < CHUNK / 32; ++q) {  // lane tests instances c0 + lane (+ 32)
+                    const uint32_t k = c0 + 32u * q + lane;
+                    bool meets = false;
+                    if (k < S.num_instances) {
+                        f3 wlo = blo[q], whi = bhi[q];
+                        if (!one_chunk) {
+                            const DevInstance& I = S.instances[k];
+                            wlo = {__ldg(&I.wlo[0]), __ldg(&I.wlo[1]), __ldg(&I.wlo[2])};
+                            whi = {__ldg(&I.whi[0]), __ldg(&I.whi[1]), __ldg(&I.whi[2])};
+                        }
+                        meets = slab(bo, bi, wlo, whi) >= 0.0f;
+                    }
+                    m |= static_cast<imask_t>(__ballot_sync(MT_FULL, meets)) << (32 * q);
+                }
+                if (lane == L) {
+                    mask = m;
+                    need_mask = false;
+                }
             }
         }
 
