@@ -104,7 +104,9 @@ __global__ void __launch_bounds__(128, QUERY == MT_QUERY_ANY ? MT_TRACE_ANY_MIN_
 {
     QueryWork<QUERY> W{rays, hits, n, 0};
     constexpr bool kCount = QUERY == MT_QUERY_CLOSEST_COUNT || QUERY == MT_QUERY_CLOSEST_TOTALS;
-    trace_persistent<kCount, QUERY == MT_QUERY_ANY, false>(S, W, fetch);  // IntersectScene as is
+    // IntersectScene as is (every met instance opened); leaf pairs for the
+    // closest-hit query
+    trace_persistent<kCount, QUERY == MT_QUERY_ANY, false, 32, QUERY == MT_QUERY_CLOSEST>(S, W, fetch);
 }
 
 __global__ void k_brdf(const mt_brdf_query* __restrict__ q, uint64_t n, mt_brdf_result* __restrict__ out)
