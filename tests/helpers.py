@@ -10,6 +10,22 @@ def small_grid(width=96, height=54, samples=8, seed=3, segments=64, rings=32):
                                    rings=rings)
 
 
+def many_instances(width=64, height=36, samples=4, seed=4, n=12):
+    """The material grid's sphere and ground with n x n sphere instances at
+    staggered depths (n * n + 1 instances: more than one 64-instance chunk of
+    the world-box test, boxes overlapping along most rays)."""
+    scene, cfg = small_grid(width=width, height=height, samples=samples, seed=seed, segments=16, rings=8)
+    inst = []
+    for j in range(n):
+        for i in range(n):
+            z = -0.5 * ((7 * i + 3 * j) % 4)
+            inst.append(mt.scenes.InstanceData(0, (j * n + i) % 49,
+                                               mt.scenes.translate((i - (n - 1) / 2) * 0.8, 0.45 + j * 0.8, z)))
+    inst.append(mt.scenes.InstanceData(1, 49))
+    scene.instances = inst
+    return scene, cfg
+
+
 def small_large_scene(width=64, height=36, samples=4, seed=5):
     return mt.scenes.large_scene(terrain_n=96, num_spheres=400, tex_size=128, width=width, height=height,
                                  samples=samples, seed=seed)

@@ -19,7 +19,7 @@ import mitrace_gb300 as mt
 from mitrace_gb300 import _abi as A
 from oracle import oracle_py as orc
 
-from .helpers import small_grid, small_large_scene
+from .helpers import many_instances, small_grid, small_large_scene
 
 pytestmark = pytest.mark.gpu
 
@@ -27,6 +27,8 @@ CASES = {
     "box_room": lambda: mt.box_room(width=48, height=48, samples=16, seed=1),
     "material_grid": lambda: small_grid(width=96, height=54, samples=8, seed=2),
     "large_scene": lambda: small_large_scene(width=64, height=36, samples=4, seed=3),
+    # 145 instances: the render kernels' 64-wide world-box passes over three chunks
+    "many_instances": lambda: many_instances(width=96, height=54, samples=8, seed=4),
 }
 
 

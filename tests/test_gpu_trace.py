@@ -13,7 +13,7 @@ import mitrace_gb300 as mt
 from mitrace_gb300 import _abi as A
 from oracle import oracle_py as orc
 
-from .helpers import scene_rays, small_grid, small_large_scene
+from .helpers import many_instances, scene_rays, small_grid, small_large_scene
 
 pytestmark = pytest.mark.gpu
 
@@ -21,6 +21,7 @@ SCENES = {
     "box_room": lambda: mt.box_room(width=64, height=64, samples=4),
     "material_grid": lambda: small_grid(),
     "large_scene": lambda: small_large_scene(),
+    "many_instances": lambda: many_instances(),  # 145 instances: five 32-instance chunks
 }
 
 
