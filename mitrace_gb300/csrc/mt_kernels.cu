@@ -323,7 +323,7 @@ __global__ void __launch_bounds__(128, MT_TRAVERSE_MIN_BLOCKS) k_extend(DevScene
         atomicAdd(rays, static_cast<unsigned long long>(n));
     }
     ExtendWork<COUNT, DBG> W{P, q, n, 0, 0, 0, 0, S.debug_mode};
-    trace_persistent<COUNT, false, !DBG, CHUNK>(S, W, &counts[3]);  // debug counts visit every instance
+    trace_persistent<COUNT, false, !DBG, CHUNK, false, true>(S, W, &counts[3]);  // debug counts visit every instance
     if (COUNT) flush_counts(cnt, W.pops, W.inner, W.tris);
 }
 
@@ -662,7 +662,7 @@ __global__ void __launch_bounds__(128, MT_TRAVERSE_MIN_BLOCKS) k_shadow(DevScene
         atomicAdd(rays, static_cast<unsigned long long>(n));
     }
     ShadowWork<COUNT> W{P, SQ, R, S.bounces, n, 0, 0, 0, 0};
-    trace_persistent<COUNT, true, true, CHUNK>(S, W, &counts[4]);
+    trace_persistent<COUNT, true, true, CHUNK, false, true>(S, W, &counts[4]);
     if (COUNT) flush_counts(cnt, W.pops, W.inner, W.tris);
 }
 
