@@ -219,9 +219,10 @@ struct DevScene {
 // matrices, exact divisions and square roots), so running it for several
 // lanes at once costs little more than for one (measured on the 50-instance
 // material grid: 1 lane 1035, 8 lanes 1046, 12 lanes 1050, 16 lanes 1050,
-// 24 lanes 1035 Mrays/s).
+// 24 lanes 1035 Mrays/s; re-measured with the current world-box phase,
+// batches and stack: 8 lanes 1442, 12 lanes 1467, 16 lanes 1480).
 #ifndef MT_TRAVERSE_SWITCH_RESIDENT
-#define MT_TRAVERSE_SWITCH_RESIDENT 12
+#define MT_TRAVERSE_SWITCH_RESIDENT 16
 #endif
 
 // Bulk prefetch of [p, p + bytes) into L2 (no registers, no completion to wait
