@@ -616,7 +616,18 @@ def run_time_to_relmse(a):
         img, sec, rays, _, _ = render(spp, 0)
         ladder.append({"spp": spp, "seconds": sec, "relmse": relmse(img, ref), "mrays_s": rays / sec / 1e6})
         spp *= 2
-    hit = next((r for r in ladder if r["relmse"] <= a.relmse_target), None)
+    rung = next((r for r in ladder if r["relmse"] <= a.relmse_target), None)
+    # the smallest passing spp: every count between the last failing power of
+    # two and the first passing one is rendered (with the same seed)
+    hit, refine = rung, []
+    if rung and rung["spp"] > 1:
+        for spp in range(rung["spp"] // 2 + 1, rung["spp"]):
+            img, sec, rays, _, _ = render(spp, 0)
+            r = {"spp": spp, "seconds": sec, "relmse": relmse(img, ref), "mrays_s": rays / sec / 1e6}
+            refine.append(r)
+            if r["relmse"] <= a.relmse_target:
+                hit = r
+                break
     # relMSE ~ c / spp on the rungs above 8 spp
     xs = np.array([r["spp"] for r in ladder if r["spp"] >= 8], dtype=np.float64)
     ys = np.array([r["relmse"] for r in ladder if r["spp"] >= 8], dtype=np.float64)
@@ -628,7 +639,8 @@ def run_time_to_relmse(a):
         "metric": "time-to-relMSE 0.01 @1080p", "unit": "s", "higher_is_better": False,
         "config": {"workload": workload_name(a), "ref_spp": a.ref_spp, "ref_seed": 1, "seed": 0,
                    "relmse": "mean over pixels/channels of (x-r)^2/(r^2+1e-2) on the tonemapped output"},
-        "gpu_first_rung": hit, "gpu_fit": {"c": c, "spp": spp_fit, "seconds": spp_fit * sec_per_spp},
+        "gpu_first_rung": rung, "gpu_min_spp": hit, "refine": refine,
+        "gpu_fit": {"c": c, "spp": spp_fit, "seconds": spp_fit * sec_per_spp},
         "ladder": ladder, "reference_seconds": ref_s, "reference_rays": ref_rays,
     }
     if not a.no_cpu_baseline and hit:
@@ -645,7 +657,7 @@ def run_time_to_relmse(a):
         cpu_s = time.perf_counter() - t1
         line["cpu"] = {"spp": hit["spp"], "seconds": cpu_s, "relmse": relmse(img_c, ref), "cores": threads,
                        "cpu": cpu_model(), "mrays_s": rays_c / cpu_s / 1e6,
-                       "note": "measured: full image at the GPU's first passing spp, same reference"}
+                       "note": "measured: full image at the GPU's smallest passing spp, same reference"}
         line["speedup_vs_cpu_at_target"] = cpu_s / hit["seconds"]
     if not a.no_nrc:
         line["nrc"] = nrc_time_to_relmse(a, ref, dev, stream)
