@@ -74,10 +74,11 @@ def parse():
     p.add_argument("--nrc-ema", type=float, default=None, help="moving-average decay of the cache's weights")
     p.add_argument("--nrc-only", action="store_true", help="time-to-relMSE: skip the plain spp ladder")
     # the radiance-cache leg's defaults are the configuration measured fastest
-    # to relMSE 0.01 on the 1080p material grid (3 spp per frame, paths ending
-    # at their first diffuse-ish vertex); the library's own defaults (4 spp,
-    # ending after it) converge further but reach 0.01 later
-    p.add_argument("--nrc-spp", type=int, default=3, help="cached samples per pixel per frame (0: the library's)")
+    # to relMSE 0.01 on the 1080p material grid (one frame of 7 spp, paths
+    # ending at their first diffuse-ish vertex; 3 spp per frame needs two
+    # frames); the library's own defaults (4 spp, ending after it) converge
+    # further but reach 0.01 later
+    p.add_argument("--nrc-spp", type=int, default=7, help="cached samples per pixel per frame (0: the library's)")
     p.add_argument("--nrc-end-at", type=int, default=1,
                    help="where a cached path ends: 0 after the first diffuse-ish vertex, 1 at it (mt_nrc_config.end_at); "
                         "-1: the library's")
