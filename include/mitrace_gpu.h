@@ -192,8 +192,11 @@ typedef struct mt_config {
  * (Tracer.cpp:695-716: intensity / maximum intensity, colour ramp or grey).
  * MT_DEBUG_COLOR_PER_MESH hashes the instance index (the reference hashes the
  * low bits of the MeshInstance's address).  PIXEL_STANDARD_DEVIATION and
- * FIREFLY_ELIMINATION render the normal image and then apply the heatmap, as
- * the reference does.  Debug modes work with mt_render_device and
+ * FIREFLY_ELIMINATION render the normal samples; the firefly clamp then
+ * replaces each pixel's samples with the sigma of their intensities or the
+ * number of samples it dropped (Tracer.cpp:516-523, 537-544) before the
+ * heatmap.  With firefly_enable 0 the clamp never runs and they heatmap the
+ * plain image, as the reference does.  Debug modes work with mt_render_device and
  * mt_start/mt_wait; the adjoint, the radiance cache and the allocation-free
  * entry point reject them. */
 #define MT_DEBUG_NONE 0
@@ -276,7 +279,8 @@ mt_status mt_render_device(mt_handle* h, float* d_rgb_out, void* cuda_stream);
  * Calls share that array: work of two calls that overlaps on the GPU races, so
  * serialise them.  The first call on a device looks up the array's address;
  * make it before any stream capture.  Same kernels and results as
- * mt_render_device for those rows. */
+ * mt_render_device for those rows.  mt_get_stats counts the call's samples
+ * but not its rays (their counters stay in the shared array). */
 #define MT_NOALLOC_MAX_PATHS 65536u
 #define MT_NOALLOC_SCRATCH_BYTES (16u << 20)
 mt_status mt_render_rows_noalloc(mt_handle* h, uint32_t row0, uint32_t row1, float* d_rgb_out,
@@ -530,6 +534,15 @@ typedef struct mt_brdf_sample_result {
 } mt_brdf_sample_result;
 
 mt_status mt_brdf_sample_batch(const mt_brdf_sample_query* q, uint64_t n, mt_brdf_sample_result* out);
+
+/* CleanupFireflies + averaging of RenderBlock (Tracer.cpp:490-548, 593-600)
+ * on given samples (test entry point; the render's own resolve kernel):
+ * samples_rgb holds npix pixels x spp samples x RGB, pixel-major, host memory;
+ * rgb_out gets npix RGB means.  debug_mode MT_DEBUG_PIXEL_STANDARD_DEVIATION /
+ * MT_DEBUG_FIREFLY_ELIMINATION give the clamp's sigma / dropped-sample count
+ * per pixel (before WaitForRender's heatmap), as those modes do.  Needs no scene. */
+mt_status mt_resolve_batch(const float* samples_rgb, uint32_t npix, uint32_t spp, int firefly_enable, float k,
+                           int debug_mode, float* rgb_out);
 
 /* ------------------------------------------------------------------------ */
 /* Host BVH builder.                                                        */

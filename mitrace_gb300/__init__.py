@@ -2,11 +2,11 @@
 
 The product is ``libmitrace_gb300.so`` (hand-written CUDA kernels behind the C
 ABI in ``include/mitrace_gpu.h``).  This package is its Python binding plus the
-synthetic scene generators; importing it fails loudly when the library has not
-been built.
+synthetic scene generators.  The scene generators and boundary structs load no
+library; the first use of anything that calls the library (``Tracer``,
+``MTError``, the batch entry points) imports ``_abi``, which raises when the
+library has not been built: there is no fallback.
 """
-from . import _abi
-from ._abi import MTError
 from .scenes import (
     SceneData,
     MeshData,
@@ -23,10 +23,35 @@ from .scenes import (
     incoherent_rays,
     scene_bounds,
 )
-from .tracer import Tracer, Stats, brdf_batch, brdf_sample_batch, bvh_build, image_rgb8_device, nrc_encode_device, write_hdr, write_png
+
+_LIBRARY_NAMES = {
+    "MTError": "_abi",
+    "Tracer": "tracer",
+    "Stats": "tracer",
+    "brdf_batch": "tracer",
+    "brdf_sample_batch": "tracer",
+    "bvh_build": "tracer",
+    "image_rgb8_device": "tracer",
+    "nrc_encode_device": "tracer",
+    "write_hdr": "tracer",
+    "write_png": "tracer",
+}
+
+
+def __getattr__(name):
+    import importlib
+
+    if name in ("_abi", "tracer", "gltf"):
+        return importlib.import_module(f".{name}", __name__)
+    mod = _LIBRARY_NAMES.get(name)
+    if mod is None:
+        raise AttributeError(f"module 'mitrace_gb300' has no attribute {name!r}")
+    value = getattr(importlib.import_module(f".{mod}", __name__), name)
+    globals()[name] = value
+    return value
+
 
 __all__ = [
-    "MTError",
     "SceneData",
     "MeshData",
     "MaterialData",
@@ -41,13 +66,5 @@ __all__ = [
     "large_scene",
     "incoherent_rays",
     "scene_bounds",
-    "Tracer",
-    "Stats",
-    "brdf_batch",
-    "brdf_sample_batch",
-    "bvh_build",
-    "nrc_encode_device",
-    "image_rgb8_device",
-    "write_png",
-    "write_hdr",
+    *_LIBRARY_NAMES,
 ]

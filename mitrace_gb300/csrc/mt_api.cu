@@ -99,6 +99,21 @@ void inverse4(const float* a, float* out)
     for (int i = 0; i < 16; ++i) out[i] = inv[i] * s;
 }
 
+// Every device allocation of a handle goes through here.  Fault injection for
+// tests: when MT_DEVICE_ALLOC_LIMIT holds a byte count, a single allocation
+// larger than that fails with cudaErrorMemoryAllocation, as if the device were
+// out of memory, so the MT_ERR_OOM paths can be exercised without exhausting
+// a shared GPU.
+cudaError_t dev_malloc(void** p, size_t bytes)
+{
+    const char* lim = std::getenv("MT_DEVICE_ALLOC_LIMIT");
+    if (lim && *lim && bytes > std::strtoull(lim, nullptr, 10)) {
+        *p = nullptr;
+        return cudaErrorMemoryAllocation;
+    }
+    return cudaMalloc(p, bytes);
+}
+
 template <class T>
 struct DevArray {
     T* p = nullptr;
@@ -119,7 +134,7 @@ struct DevArray {
         reset();
         n = count;
         if (count == 0) return cudaSuccess;
-        return cudaMalloc(reinterpret_cast<void**>(&p), count * sizeof(T));
+        return dev_malloc(reinterpret_cast<void**>(&p), count * sizeof(T));
     }
     cudaError_t upload(const T* src, size_t count, cudaStream_t st)
     {
@@ -172,6 +187,73 @@ bool bvh_depth(const std::vector<mt_bvh_node>& nodes, const std::vector<uint32_t
     return true;
 }
 
+// Everything mt_create can reject without touching the device: missing
+// arrays, prebuilt BVHs that are malformed or deeper than the traversal stack,
+// empty textures, and indices naming missing meshes, materials, textures or
+// light types.  Runs before the first CUDA call, so a bad scene never reaches
+// an upload.
+mt_status validate_scene(const mt_scene_desc* d, const mt_config& cfg, std::string& why)
+{
+    for (uint32_t mi = 0; mi < d->num_meshes; ++mi) {
+        const mt_mesh_desc& md = d->meshes[mi];
+        const std::string tag = "mesh " + std::to_string(mi) + ": ";
+        if (!md.positions || !md.normals || md.num_triangles == 0) {
+            why = tag + "positions and normals are required (GLTF.cpp:328-329)";
+            return MT_ERR_INVALID;
+        }
+        const bool want_bvh = !cfg.bvh_disable && md.num_triangles > cfg.bvh_max_triangles;  // Mesh.cpp:37-40
+        if (!want_bvh || !(md.bvh_nodes && md.bvh_indices)) continue;
+        if (md.num_bvh_nodes == 0 || md.num_bvh_indices == 0) {
+            why = tag + "prebuilt BVH with no nodes or no indices";
+            return MT_ERR_INVALID;
+        }
+        std::vector<mt_bvh_node> bn(md.bvh_nodes, md.bvh_nodes + md.num_bvh_nodes);
+        std::vector<uint32_t> bi(md.bvh_indices, md.bvh_indices + md.num_bvh_indices);
+        uint32_t depth = 0;
+        std::string w;
+        if (!bvh_depth(bn, bi, md.num_triangles, depth, w)) {
+            why = tag + w;
+            return MT_ERR_INVALID;
+        }
+        if (depth + 2 > MT_STACK_SIZE) {
+            why = tag + "BVH depth " + std::to_string(depth) + " exceeds the traversal stack (" +
+                  std::to_string(MT_STACK_SIZE - 2) + ")";
+            return MT_ERR_INVALID;
+        }
+    }
+    for (uint32_t ti = 0; ti < d->num_textures; ++ti) {
+        const mt_texture_desc& t = d->textures[ti];
+        if (static_cast<uint64_t>(t.width) * t.height == 0 || (!t.rgb8 && !t.rgb32f)) {
+            why = "texture " + std::to_string(ti) + " has no texels";
+            return MT_ERR_INVALID;
+        }
+    }
+    const int nt = static_cast<int>(d->num_textures);
+    for (uint32_t i = 0; i < d->num_materials; ++i) {
+        const mt_material_desc& m = d->materials[i];
+        for (int ti : {m.base_color_tex, m.metallic_roughness_tex, m.normal_tex, m.emissive_tex})
+            if (ti < -1 || ti >= nt) {
+                why = "material " + std::to_string(i) + " names a missing texture";
+                return MT_ERR_INVALID;
+            }
+    }
+    for (uint32_t i = 0; i < d->num_instances; ++i)
+        if (d->instances[i].mesh >= d->num_meshes || d->instances[i].material >= d->num_materials) {
+            why = "instance " + std::to_string(i) + " names a missing mesh or material";
+            return MT_ERR_INVALID;
+        }
+    for (uint32_t i = 0; i < d->num_lights; ++i)
+        if (d->lights[i].type < MT_LIGHT_POINT || d->lights[i].type > MT_LIGHT_AREA) {
+            why = "light " + std::to_string(i) + " has an unknown type";
+            return MT_ERR_INVALID;
+        }
+    if (d->env_texture < -1 || d->env_texture >= nt) {
+        why = "env texture index out of range";
+        return MT_ERR_INVALID;
+    }
+    return MT_OK;
+}
+
 }  // namespace
 
 struct mt_handle {
@@ -210,9 +292,14 @@ struct mt_handle {
     DevArray<float4> dval;       // debug render modes only
     DevArray<uint4> dcnt;
     DevArray<float> image;
-    unsigned long long* rays_host = nullptr;  // pinned, 2 words
-    cudaEvent_t render_done = nullptr;        // end of the last synchronous render
-    bool render_pending = false;
+    // pinned, 4 words: [0] extension rays, [1] shadow rays of the last render,
+    // [2] the device error word after it
+    unsigned long long* rays_host = nullptr;
+    cudaEvent_t render_done = nullptr;        // end of the last enqueued render
+    std::atomic<bool> render_pending{false};
+    // serialises settle_render (the stat thread's mt_get_stats, the render
+    // thread's next render and the profiler calls may all settle a render)
+    std::mutex settle_mu;
     // profiling
     Profiler prof;
     DevArray<unsigned long long> prof_counts;  // 6 words
@@ -353,6 +440,7 @@ mt_status upload_scene(mt_handle* h, const mt_scene_desc* d)
             }
             uint32_t depth = 0;
             std::string why;
+            // prebuilt BVHs passed validate_scene; this checks the library's own build
             if (!bvh_depth(bn, bi, T, depth, why))
                 return set_err(MT_ERR_INVALID, "mesh " + std::to_string(mi) + ": " + why);
             if (depth + 2 > MT_STACK_SIZE)
@@ -500,9 +588,11 @@ mt_status upload_scene(mt_handle* h, const mt_scene_desc* d)
     h->host_lights = lights;
     MT_CUDA(h->textures.upload(texs.data(), texs.size(), st));
     MT_CUDA(h->lights.upload(lights.data(), lights.size(), st));
-    MT_CUDA(h->error_flag.alloc(1));
+    // [0] render and ray-query traversal (MT_ERRBIT_STACK), cleared per render;
+    // [1] the radiance cache's bounded tensor-core waits (MT_ERRBIT_TIMEOUT)
+    MT_CUDA(h->error_flag.alloc(2));
     MT_CUDA(h->qfetch.alloc(1));
-    MT_CUDA(cudaMemsetAsync(h->error_flag.p, 0, sizeof(int), st));
+    MT_CUDA(cudaMemsetAsync(h->error_flag.p, 0, 2 * sizeof(int), st));
     h->scene_bytes += nodes.size() * 16 + slots.size() * 16 + normals.size() * 4 + uvs.size() * 4 +
                       insts.size() * sizeof(DevInstance);
     MT_CUDA(cudaStreamSynchronize(st));
@@ -569,6 +659,31 @@ uint64_t env_u64(const char* name, uint64_t dflt)
     return std::strtoull(v, nullptr, 10);
 }
 
+mt_status alloc_wave(mt_handle* h, uint64_t batch)
+{
+    const mt_config& c = h->cfg;
+    const uint64_t npix = static_cast<uint64_t>(c.width) * c.height;
+    MT_CUDA(h->pstate.alloc(10ull * batch));
+    MT_CUDA(h->phit.alloc(batch));
+    MT_CUDA(h->sq.alloc(3ull * batch));
+    MT_CUDA(h->queues.alloc(2ull * batch));
+    MT_CUDA(h->counts.alloc(8));
+    MT_CUDA(cudaMemset(h->counts.p, 0, 8 * sizeof(uint32_t)));
+    MT_CUDA(h->rays.alloc(2));
+    MT_CUDA(h->samples.alloc(3ull * h->band_capacity));
+    MT_CUDA(h->image.alloc(npix * 3));
+    if (c.debug_mode) {
+        MT_CUDA(h->dval.alloc(batch));
+        MT_CUDA(h->dcnt.alloc(batch));
+    }
+    if (!h->rays_host) {
+        MT_CUDA(cudaMallocHost(reinterpret_cast<void**>(&h->rays_host), 4 * sizeof(unsigned long long)));
+        h->rays_host[0] = h->rays_host[1] = h->rays_host[2] = h->rays_host[3] = 0;
+    }
+    if (!h->render_done) MT_CUDA(cudaEventCreateWithFlags(&h->render_done, cudaEventDisableTiming));
+    return MT_OK;
+}
+
 // Sizes the wavefront: a batch of paths and the per-sample planes of one band
 // of image rows (the firefly clamp needs every sample of a pixel at once).
 mt_status ensure_wave(mt_handle* h)
@@ -595,23 +710,23 @@ mt_status ensure_wave(mt_handle* h)
     uint64_t rows = budget / (static_cast<uint64_t>(c.width) * c.samples * 12ull);
     rows = std::max<uint64_t>(1, std::min<uint64_t>(rows, c.height));
     h->band_capacity = rows * c.width * c.samples;
-    h->batch = static_cast<uint32_t>(batch);
-    MT_CUDA(h->pstate.alloc(10ull * batch));
-    MT_CUDA(h->phit.alloc(batch));
-    MT_CUDA(h->sq.alloc(3ull * batch));
-    MT_CUDA(h->queues.alloc(2ull * batch));
-    MT_CUDA(h->counts.alloc(8));
-    MT_CUDA(cudaMemset(h->counts.p, 0, 8 * sizeof(uint32_t)));
-    MT_CUDA(h->rays.alloc(2));
-    MT_CUDA(h->samples.alloc(3ull * h->band_capacity));
-    MT_CUDA(h->image.alloc(npix * 3));
-    if (c.debug_mode) {
-        MT_CUDA(h->dval.alloc(batch));
-        MT_CUDA(h->dcnt.alloc(batch));
+    // h->batch stays 0 (wave not ready) until every buffer exists: a failed
+    // allocation releases what was taken and a later call tries again
+    const mt_status rc = alloc_wave(h, batch);
+    if (rc != MT_OK) {
+        h->pstate.reset();
+        h->phit.reset();
+        h->sq.reset();
+        h->queues.reset();
+        h->counts.reset();
+        h->rays.reset();
+        h->samples.reset();
+        h->image.reset();
+        h->dval.reset();
+        h->dcnt.reset();
+        return rc;
     }
-    MT_CUDA(cudaMallocHost(reinterpret_cast<void**>(&h->rays_host), 2 * sizeof(unsigned long long)));
-    h->rays_host[0] = h->rays_host[1] = 0;
-    MT_CUDA(cudaEventCreateWithFlags(&h->render_done, cudaEventDisableTiming));
+    h->batch = static_cast<uint32_t>(batch);
     return MT_OK;
 }
 
@@ -652,15 +767,22 @@ WaveViews views(mt_handle* h)
     return v;
 }
 
+mt_status settle_render(mt_handle* h);
+
 // Enqueues a whole render into `out` on `st`.  With sync_each_batch the host
 // waits for every batch (progress/kill granularity for the async API).
 mt_status render_into(mt_handle* h, float* out, cudaStream_t st, bool sync_each_batch)
 {
     mt_status rc = ensure_wave(h);
     if (rc != MT_OK) return rc;
+    // the previous render's counters and error word share the pinned words
+    // this render copies back into: fold them in first
+    rc = settle_render(h);
+    if (rc != MT_OK) return rc;
     const mt_config& c = h->cfg;
     const WaveViews v = views(h);
     MT_CUDA(cudaMemsetAsync(h->rays.p, 0, 2 * sizeof(unsigned long long), st));
+    MT_CUDA(cudaMemsetAsync(h->error_flag.p, 0, sizeof(int), st));
     Profiler* prof = (h->prof.timing || h->prof.counting) ? &h->prof : nullptr;
     const uint64_t rows_per_band = h->band_capacity / (static_cast<uint64_t>(c.width) * c.samples);
     uint64_t total_batches = 0;
@@ -701,15 +823,22 @@ mt_status render_into(mt_handle* h, float* out, cudaStream_t st, bool sync_each_
         launches += 2;
     }
     MT_CUDA(cudaMemcpyAsync(h->rays_host, h->rays.p, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
-    MT_CUDA(cudaEventRecord(h->render_done, st));
-    h->render_pending = true;
+    MT_CUDA(cudaMemcpyAsync(h->rays_host + 2, h->error_flag.p, sizeof(int), cudaMemcpyDeviceToHost, st));
+    {
+        std::lock_guard<std::mutex> lk(h->settle_mu);
+        MT_CUDA(cudaEventRecord(h->render_done, st));
+        h->render_pending = true;
+    }
     h->launches += launches;
     return MT_OK;
 }
 
-// Folds the finished render's ray counters (and profile) into the handle.
+// Folds the finished render's ray counters (and profile) into the handle and
+// reports a device error word the render left set (a traversal stack overflow:
+// MT_ERR_INVALID).  Thread-safe; blocks until that render has finished.
 mt_status settle_render(mt_handle* h)
 {
+    std::lock_guard<std::mutex> lk(h->settle_mu);
     if (!h->render_pending) return MT_OK;
     MT_CUDA(cudaEventSynchronize(h->render_done));
     h->render_pending = false;
@@ -717,6 +846,10 @@ mt_status settle_render(mt_handle* h)
     h->prof_rays[0] += h->rays_host[0];
     h->prof_rays[1] += h->rays_host[1];
     if (h->prof.timing) MT_CUDA(h->prof.collect(h->prof_ms, h->prof_launches));
+    const unsigned long long flag = h->rays_host[2];
+    h->rays_host[2] = 0;
+    if (flag & MT_ERRBIT_STACK)
+        return set_err(MT_ERR_INVALID, "device error flag set (traversal stack overflow)");
     return MT_OK;
 }
 
@@ -752,6 +885,10 @@ namespace mt {
 
 const DevScene* internal_scene(const mt_handle* h) { return h ? &h->S : nullptr; }
 bool internal_busy(const mt_handle* h) { return h && h->running.load() != 0; }
+void internal_count_samples(mt_handle* h, uint64_t n)
+{
+    if (h) h->stat_samples += n;
+}
 mt_status internal_error(mt_status code, const std::string& msg) { return set_err(code, msg); }
 
 }  // namespace mt
@@ -928,6 +1065,11 @@ mt_status mt_create(const mt_scene_desc* scene, const mt_config* cfg, mt_handle*
     if (scene->num_materials && !scene->materials) return set_err(MT_ERR_INVALID, "materials is null");
     if (scene->num_textures && !scene->textures) return set_err(MT_ERR_INVALID, "textures is null");
     if (scene->num_lights && !scene->lights) return set_err(MT_ERR_INVALID, "lights is null");
+    {
+        std::string why;
+        const mt_status v = validate_scene(scene, *cfg, why);
+        if (v != MT_OK) return set_err(v, why);
+    }
     mt_handle* h = new (std::nothrow) mt_handle();
     if (!h) return set_err(MT_ERR_OOM, "host allocation failed");
     h->cfg = *cfg;
@@ -1001,8 +1143,11 @@ mt_status mt_kill(mt_handle* h)
 mt_status mt_get_stats(const mt_handle* h, mt_stats* out)
 {
     if (check_handle(h) != MT_OK || !out) return set_err(MT_ERR_INVALID, "null argument");
+    // a finished render's counters are folded in here (under the handle's
+    // settle lock); a render still on the GPU is left alone, never waited for
+    mt_status settled = MT_OK;
     if (!h->running && h->render_pending && cudaEventQuery(h->render_done) == cudaSuccess)
-        settle_render(const_cast<mt_handle*>(h));
+        settled = settle_render(const_cast<mt_handle*>(h));
     mt_stats s{};
     const double el = h->started ? std::chrono::duration<double>(std::chrono::steady_clock::now() - h->t0).count() : 0.0;
     s.progress = static_cast<float>(static_cast<double>(h->work_done.load()) / static_cast<double>(h->work_total.load()));
@@ -1012,7 +1157,7 @@ mt_status mt_get_stats(const mt_handle* h, mt_stats* out)
     s.rays = h->stat_rays.load();
     s.samples = h->stat_samples.load();
     *out = s;
-    return MT_OK;
+    return settled;
 }
 
 int mt_is_done(const mt_handle* h) { return h && h->started && h->done ? 1 : 0; }
@@ -1039,6 +1184,7 @@ mt_status mt_profile_reset(mt_handle* h)
     if (h->running) return set_err(MT_ERR_STATE, "a render is running");
     mt_status rc = settle_render(h);
     if (rc != MT_OK) return rc;
+    std::lock_guard<std::mutex> lk(h->settle_mu);
     for (int i = 0; i < MT_NUM_STAGES; ++i) {
         h->prof_ms[i] = 0.0;
         h->prof_launches[i] = 0;
@@ -1054,6 +1200,7 @@ mt_status mt_profile_read(mt_handle* h, mt_profile* out)
     if (h->running) return set_err(MT_ERR_STATE, "a render is running");
     mt_status rc = settle_render(h);
     if (rc != MT_OK) return rc;
+    std::lock_guard<std::mutex> lk(h->settle_mu);
     std::memset(out, 0, sizeof(*out));
     for (int i = 0; i < MT_NUM_STAGES; ++i) {
         out->stage[i].launches = h->prof_launches[i];
@@ -1102,10 +1249,10 @@ mt_status mt_render_grad(mt_handle* h, const mt_grad_buffers* g, void* cuda_stre
     const uint64_t rows_per_band = h->band_capacity / (static_cast<uint64_t>(c.width) * c.samples);
     if (!h->grad_batch) {
         const uint64_t gb = std::min<uint64_t>(h->batch, env_u64("MT_GRAD_BATCH_PATHS", 1ull << 20));
-        h->grad_batch = static_cast<uint32_t>(gb);
         MT_CUDA(h->rec_vert.alloc(gb * std::max<uint32_t>(1, c.bounces) * 5));
         MT_CUDA(h->rec_path.alloc(gb * 2));
         MT_CUDA(h->grad_pix.alloc(2 * rows_per_band * c.width));
+        h->grad_batch = static_cast<uint32_t>(gb);  // set once every record buffer exists
     }
     cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
     const WaveViews v = views(h);
@@ -1218,6 +1365,40 @@ mt_status mt_brdf_batch(const mt_brdf_query* q, uint64_t n, mt_brdf_result* out)
     if (dq) cudaFree(dq);
     if (dr) cudaFree(dr);
     if (e != cudaSuccess) return set_err(MT_ERR_CUDA, cudaGetErrorString(e));
+    return MT_OK;
+}
+
+mt_status mt_resolve_batch(const float* samples_rgb, uint32_t npix, uint32_t spp, int firefly_enable, float k,
+                           int debug_mode, float* rgb_out)
+{
+    if (npix == 0) return MT_OK;
+    if (!samples_rgb || !rgb_out) return set_err(MT_ERR_INVALID, "null argument");
+    if (spp == 0) return set_err(MT_ERR_INVALID, "spp must be positive");
+    if (debug_mode < 0 || debug_mode >= MT_DEBUG_COUNT)
+        return set_err(MT_ERR_INVALID, "debug_mode is not a Config::DebugMode value");
+    const uint64_t n = static_cast<uint64_t>(npix) * spp;
+    // pixel-major host samples -> the render's sample-major R, G, B planes
+    std::vector<float> planes;
+    try {
+        planes.resize(3 * n);
+    } catch (const std::bad_alloc&) {
+        return set_err(MT_ERR_OOM, "host allocation failed");
+    }
+    for (uint64_t p = 0; p < npix; ++p)
+        for (uint64_t s = 0; s < spp; ++s)
+            for (int c = 0; c < 3; ++c) planes[c * n + s * npix + p] = samples_rgb[(p * spp + s) * 3 + c];
+    float* dp = nullptr;
+    float* dout = nullptr;
+    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(&dp), 3 * n * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&dout), 3ull * npix * sizeof(float));
+    if (e == cudaSuccess) e = cudaMemcpy(dp, planes.data(), 3 * n * sizeof(float), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = launch_resolve_planes(dp, dp + n, dp + 2 * n, npix, spp, firefly_enable, k, debug_mode, dout, 0);
+    if (e == cudaSuccess) e = cudaMemcpy(rgb_out, dout, 3ull * npix * sizeof(float), cudaMemcpyDeviceToHost);
+    if (dp) cudaFree(dp);
+    if (dout) cudaFree(dout);
+    if (e != cudaSuccess)
+        return set_err(e == cudaErrorMemoryAllocation ? MT_ERR_OOM : MT_ERR_CUDA, cudaGetErrorString(e));
     return MT_OK;
 }
 
@@ -1381,7 +1562,7 @@ mt_status mt_nrc_frame(mt_handle* h, float* d_accum, uint32_t accum_index, void*
         Q.count = N.counters.p;
         Q.net = N.infer.p;
         Q.total = N.counters.p + 2;
-        Q.err = h->error_flag.p;
+        Q.err = h->error_flag.p + 1;
         const uint64_t rows_per_band = N.plane_capacity / (static_cast<uint64_t>(c.width) * nc.spp);
         for (uint64_t r0 = 0; r0 < c.height; r0 += rows_per_band) {
             const uint64_t rows = std::min<uint64_t>(rows_per_band, c.height - r0);
@@ -1417,8 +1598,12 @@ mt_status mt_nrc_get_stats(mt_handle* h, mt_nrc_stats* out)
     int flag = 0;
     MT_CUDA(cudaDeviceSynchronize());
     MT_CUDA(cudaMemcpy(c, h->nrc.counters.p, sizeof(c), cudaMemcpyDeviceToHost));
-    MT_CUDA(cudaMemcpy(&flag, h->error_flag.p, sizeof(int), cudaMemcpyDeviceToHost));
-    if (flag & MT_ERRBIT_TIMEOUT) return set_err(MT_ERR_TIMEOUT, "a bounded wait on the tensor cores ran out");
+    MT_CUDA(cudaMemcpy(&flag, h->error_flag.p + 1, sizeof(int), cudaMemcpyDeviceToHost));
+    if (flag & MT_ERRBIT_TIMEOUT) {
+        // reported once: the word is cleared so the handle's later work is judged afresh
+        MT_CUDA(cudaMemset(h->error_flag.p + 1, 0, sizeof(int)));
+        return set_err(MT_ERR_TIMEOUT, "a bounded wait on the tensor cores ran out");
+    }
     std::memset(out, 0, sizeof(*out));
     out->frames = h->nrc.frames;
     out->adam_steps = h->nrc.opt.step;
@@ -1462,7 +1647,7 @@ mt_status mt_nrc_infer(mt_handle* h, const float* d_features, uint32_t n, float*
     mt_status rc = nrc_ready(h);
     if (rc != MT_OK) return rc;
     if (n && (!d_features || !d_rgb)) return set_err(MT_ERR_INVALID, "null argument");
-    MT_CUDA(launch_nrc_infer(h->nrc.infer.p, d_features, n, d_rgb, h->error_flag.p,
+    MT_CUDA(launch_nrc_infer(h->nrc.infer.p, d_features, n, d_rgb, h->error_flag.p + 1,
                              static_cast<cudaStream_t>(cuda_stream)));
     h->launches += n ? 1 : 0;
     return MT_OK;

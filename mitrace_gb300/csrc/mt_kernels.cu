@@ -14,6 +14,8 @@
 //   resolve  per-pixel firefly clamp + mean     (Tracer.cpp:490-548, 593-601)
 #include <cuda_runtime.h>
 
+#include <mutex>
+
 #include "mt_device.cuh"
 #include "mt_kernels.h"
 #include "mt_nrc.h"
@@ -719,12 +721,17 @@ __global__ void __launch_bounds__(256) k_finalize(DevScene S, PathState P, Batch
     }
 }
 
-// CleanupFireflies + average: population mean/variance of the sample
-// intensities in sample order, reject |I - mean| > k*sigma, mean of the rest.
+// CleanupFireflies + average (Tracer.cpp:490-548, 593-600): population
+// mean/variance of the sample intensities in sample order, reject
+// |I - mean| > k*sigma, mean of the rest.  DebugPixelStandardDeviation turns
+// every sample into sigma (taken before any sample is dropped) and
+// DebugFireflyElimination into the number of dropped samples; both then
+// divide the sum by spp, as CleanupFireflies returns buffer.size() for them.
+// Without the clamp neither mode touches the samples.
 __global__ void __launch_bounds__(256) k_resolve(const float* __restrict__ sr, const float* __restrict__ sg,
                                                  const float* __restrict__ sb, uint32_t band_pix,
                                                  uint32_t spp, uint32_t pix_base, int enable, float k,
-                                                 float* __restrict__ out)
+                                                 int debug_mode, float* __restrict__ out)
 {
     for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < band_pix; j += gridDim.x * blockDim.x) {
         f3 acc = splat(0.0f);
@@ -743,15 +750,26 @@ __global__ void __launch_bounds__(256) k_resolve(const float* __restrict__ sr, c
                 var = __fadd_rn(var, __fmul_rn(df, df));
             }
             var = __fdiv_rn(var, static_cast<float>(spp));
-            const float thr = __fmul_rn(k, __fsqrt_rn(var));
-            for (uint32_t s = 0; s < spp; ++s) {
-                const uint64_t g = static_cast<uint64_t>(s) * band_pix + j;
-                const f3 c = {sr[g], sg[g], sb[g]};
-                const float in = __fdiv_rn(__fadd_rn(__fadd_rn(c.x, c.y), c.z), 3.0f);
-                if (fabsf(__fsub_rn(in, mean)) > thr)
-                    --kept;
-                else
-                    acc = acc + c;
+            const float sigma = __fsqrt_rn(var);
+            if (debug_mode == MT_DEBUG_PIXEL_STANDARD_DEVIATION) {
+                for (uint32_t s = 0; s < spp; ++s) acc = acc + splat(sigma);
+            } else {
+                const float thr = __fmul_rn(k, sigma);
+                for (uint32_t s = 0; s < spp; ++s) {
+                    const uint64_t g = static_cast<uint64_t>(s) * band_pix + j;
+                    const f3 c = {sr[g], sg[g], sb[g]};
+                    const float in = __fdiv_rn(__fadd_rn(__fadd_rn(c.x, c.y), c.z), 3.0f);
+                    if (fabsf(__fsub_rn(in, mean)) > thr)
+                        --kept;
+                    else
+                        acc = acc + c;
+                }
+                if (debug_mode == MT_DEBUG_FIREFLY_ELIMINATION) {
+                    const float dropped = static_cast<float>(spp - kept);
+                    acc = splat(0.0f);
+                    for (uint32_t s = 0; s < spp; ++s) acc = acc + splat(dropped);
+                    kept = spp;
+                }
             }
             if (kept == 0) kept = 1;
         } else {
@@ -802,41 +820,68 @@ __global__ void k_debug_heatmap(float* __restrict__ img, uint64_t npix, const ui
 // ---------------------------------------------------------------------------
 // Host-side launchers
 // ---------------------------------------------------------------------------
-static int g_sms = 0;
-static int sm_count()
-{
-    if (g_sms == 0) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
-        if (g_sms <= 0) g_sms = 1;
-    }
-    return g_sms;
-}
+// Launch geometry per device: the SM count and the resident-wave grid of every
+// persistent kernel, computed once per device under a lock (devices may differ
+// in SM count, and several host threads may launch at once).
+struct DeviceGrids {
+    int sms = 1;
+    unsigned ext[4] = {}, sh[3] = {}, trace[4] = {};
+};
 
-static unsigned grid_for(uint64_t n, unsigned block, unsigned per_sm)
-{
-    const uint64_t need = (n + block - 1) / block;
-    const uint64_t cap = static_cast<uint64_t>(sm_count()) * per_sm;
-    return static_cast<unsigned>(need < cap ? (need ? need : 1) : cap);
-}
-
-// One resident wave of blocks for a persistent kernel.
 template <class K>
-static unsigned persistent_grid(K kernel, int block)
+static unsigned persistent_grid(K kernel, int block, int sms)
 {
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, 0) != cudaSuccess || per_sm < 1)
         per_sm = 1;
-    return static_cast<unsigned>(per_sm * sm_count());
+    return static_cast<unsigned>(per_sm * sms);
+}
+
+static const DeviceGrids& device_grids()
+{
+    constexpr int kMaxDevices = 64;
+    static std::mutex mu;
+    static DeviceGrids grids[kMaxDevices];
+    static bool ready[kMaxDevices] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= kMaxDevices) dev = 0;
+    std::lock_guard<std::mutex> lk(mu);
+    DeviceGrids& g = grids[dev];
+    if (!ready[dev]) {
+        int sms = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        g.sms = sms > 0 ? sms : 1;
+        g.ext[0] = persistent_grid(k_extend<false, false>, 128, g.sms);
+        g.ext[1] = persistent_grid(k_extend<true, false>, 128, g.sms);
+        g.ext[2] = persistent_grid(k_extend<true, true>, 128, g.sms);
+        g.ext[3] = persistent_grid(k_extend<false, false, 64>, 128, g.sms);
+        g.sh[0] = persistent_grid(k_shadow<false>, 128, g.sms);
+        g.sh[1] = persistent_grid(k_shadow<true>, 128, g.sms);
+        g.sh[2] = persistent_grid(k_shadow<false, 64>, 128, g.sms);
+        g.trace[MT_QUERY_CLOSEST] = persistent_grid(k_trace<MT_QUERY_CLOSEST>, 128, g.sms);
+        g.trace[MT_QUERY_ANY] = persistent_grid(k_trace<MT_QUERY_ANY>, 128, g.sms);
+        g.trace[MT_QUERY_CLOSEST_COUNT] = persistent_grid(k_trace<MT_QUERY_CLOSEST_COUNT>, 128, g.sms);
+        g.trace[MT_QUERY_CLOSEST_TOTALS] = persistent_grid(k_trace<MT_QUERY_CLOSEST_TOTALS>, 128, g.sms);
+        ready[dev] = true;
+    }
+    return g;
+}
+
+int device_sm_count() { return device_grids().sms; }
+
+static unsigned grid_for(uint64_t n, unsigned block, unsigned per_sm)
+{
+    const uint64_t need = (n + block - 1) / block;
+    const uint64_t cap = static_cast<uint64_t>(device_sm_count()) * per_sm;
+    return static_cast<unsigned>(need < cap ? (need ? need : 1) : cap);
 }
 
 template <int Q>
 static cudaError_t trace_chunks(const DevScene& S, const mt_ray* rays, uint64_t n, mt_hit* hits,
                                 uint32_t* fetch, cudaStream_t st)
 {
-    static unsigned grid = 0;
-    if (!grid) grid = persistent_grid(k_trace<Q>, 128);
+    const unsigned grid = device_grids().trace[Q];
     const uint64_t chunk = 1ull << 30;
     for (uint64_t b = 0; b < n; b += chunk) {
         const uint32_t m = static_cast<uint32_t>(n - b < chunk ? n - b : chunk);
@@ -930,16 +975,9 @@ cudaError_t launch_batch(const DevScene& S, const PathState& P, const ShadowQueu
     if (NC.mode == MT_NRC_TRAIN) R.nrc = NC.rec;
     BatchInfo B{g0, n, band_pix, pix_base, X.sample_base, X.scatter_mul, X.scatter_add};
     const unsigned gw = grid_for(n, 128, 16);
-    static unsigned g_ext[4] = {0, 0, 0, 0}, g_sh[3] = {0, 0, 0};
-    if (!g_ext[0]) {
-        g_ext[0] = persistent_grid(k_extend<false, false>, 128);
-        g_ext[1] = persistent_grid(k_extend<true, false>, 128);
-        g_ext[2] = persistent_grid(k_extend<true, true>, 128);
-        g_ext[3] = persistent_grid(k_extend<false, false, 64>, 128);
-        g_sh[0] = persistent_grid(k_shadow<false>, 128);
-        g_sh[1] = persistent_grid(k_shadow<true>, 128);
-        g_sh[2] = persistent_grid(k_shadow<false, 64>, 128);
-    }
+    const DeviceGrids& G = device_grids();
+    const unsigned* g_ext = G.ext;
+    const unsigned* g_sh = G.sh;
     const bool wide = S.num_instances > 32;
     const bool count = prof && prof->counting;
     unsigned long long* cnt = prof ? prof->d_counts : nullptr;
@@ -1026,8 +1064,16 @@ cudaError_t launch_resolve(const DevScene& S, const WaveBuffers& W, uint32_t ban
 {
     if (prof) prof->begin(MT_STAGE_RESOLVE, st);
     k_resolve<<<grid_for(band_pix, 256, 8), 256, 0, st>>>(W.sr, W.sg, W.sb, band_pix, S.spp, pix_base,
-                                                          S.firefly_enable, S.firefly_k, out);
+                                                          S.firefly_enable, S.firefly_k, S.debug_mode, out);
     if (prof) prof->end(MT_STAGE_RESOLVE, st);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_resolve_planes(const float* sr, const float* sg, const float* sb, uint32_t npix, uint32_t spp,
+                                  int enable, float k, int debug_mode, float* out, cudaStream_t st)
+{
+    if (npix == 0) return cudaSuccess;
+    k_resolve<<<grid_for(npix, 256, 8), 256, 0, st>>>(sr, sg, sb, npix, spp, 0, enable, k, debug_mode, out);
     return cudaGetLastError();
 }
 

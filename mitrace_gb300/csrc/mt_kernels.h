@@ -109,6 +109,13 @@ cudaError_t launch_batch(const DevScene& S, const PathState& P, const ShadowQueu
                          const RecordBuffers* rec = nullptr, const BatchExtra* extra = nullptr);
 cudaError_t launch_resolve(const DevScene& S, const WaveBuffers& W, uint32_t band_pix,
                            uint32_t pix_base, float* out, cudaStream_t st, Profiler* prof);
+// k_resolve on caller planes (sample-major: plane[s * npix + j]) for the
+// mt_resolve_batch test entry; writes npix RGB triples to out.
+cudaError_t launch_resolve_planes(const float* sr, const float* sg, const float* sb, uint32_t npix, uint32_t spp,
+                                  int enable, float k, int debug_mode, float* out, cudaStream_t st);
+// SM count of the current device (cached per device).
+int device_sm_count();
+
 // True when S.debug_mode ends with WaitForRender's heatmap post-processing.
 bool debug_needs_post(int mode);
 // Heatmap post-processing of a whole W*H image (scratch: one device word).

@@ -20,6 +20,7 @@
 //     contents; the counters that must start at zero are cleared on the stream
 //     at the start of each call.  Calls whose work overlaps on the GPU (two
 //     streams, two host threads, two handles) race on the array: serialise them;
+//   * mt_get_stats counts the samples of these calls but not their rays;
 //   * the first call on a device looks up the array's device address with
 //     cudaGetSymbolAddress (once per device, that device current).  Make that
 //     first call before any stream capture begins.
@@ -133,5 +134,9 @@ extern "C" mt_status mt_render_rows_noalloc(mt_handle* h, uint32_t row0, uint32_
     if (e == cudaSuccess)
         e = launch_resolve(*S, w, static_cast<uint32_t>(band_pix), row0 * S->width, d_rgb_out, st, nullptr);
     if (e != cudaSuccess) return internal_error(MT_ERR_CUDA, cudaGetErrorString(e));
+    // mt_get_stats counts the call's camera samples; its ray counters stay in
+    // the shared scratch array (reading them back would need a host copy that
+    // waits for the GPU), so the rays of allocation-free calls are not counted
+    internal_count_samples(h, paths);
     return MT_OK;
 }

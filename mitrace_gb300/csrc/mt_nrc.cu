@@ -24,6 +24,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <cstdlib>
 
 #include "mt_device.cuh"
 #include "mt_nrc.h"
@@ -367,10 +368,11 @@ __device__ __forceinline__ void tc_commit(uint32_t bar)
                  : "memory");
 }
 
-// Waits for phase `parity` of the mbarrier; false when the bound ran out.
-__device__ __forceinline__ bool tc_wait(uint32_t bar, uint32_t parity)
+// Waits for phase `parity` of the mbarrier, polling at most `limit` times;
+// false when the bound ran out.
+__device__ __forceinline__ bool tc_wait(uint32_t bar, uint32_t parity, uint32_t limit)
 {
-    for (uint32_t i = 0; i < kTcWaitLimit; ++i) {
+    for (uint32_t i = 0; i < limit; ++i) {
         uint32_t done;
         asm volatile(
             "{\n.reg .pred q;\nmbarrier.try_wait.parity.shared::cta.b64 q, [%1], %2;\nselp.b32 %0, 1, 0, q;\n}\n"
@@ -423,7 +425,8 @@ __global__ void __launch_bounds__(kTcRows * kTcGroups) k_nrc_infer_tc(const bf16
                                                                       const float4* __restrict__ feat, uint32_t n_host,
                                                                       const uint32_t* __restrict__ count,
                                                                       float* __restrict__ out, PathState P,
-                                                                      uint32_t* total, int* err)
+                                                                      uint32_t* total, int* err,
+                                                                      uint32_t wait_limit)
 {
     extern __shared__ __align__(1024) unsigned char tc_smem[];
     unsigned char* smem = tc_smem;
@@ -507,7 +510,7 @@ __global__ void __launch_bounds__(kTcRows * kTcGroups) k_nrc_infer_tc(const bf16
                 const uint32_t w = l == 0 ? kTcW0 : (l == 4 ? kTcW4 : kTcW1 + (l - 1) * 64 * 64 * 2);
                 tc_layer(tmem, a_s, s0 + w, l == 0 ? 10 : 8, l == 4 ? 16 : 64, bar);
             }
-            if (!tc_wait(bar, phase)) *flag = 1;
+            if (!tc_wait(bar, phase, wait_limit)) *flag = 1;
             phase ^= 1;
             group_sync(group);
             if (*flag) {
@@ -556,7 +559,7 @@ __global__ void __launch_bounds__(kTcRows * kTcGroups) k_nrc_infer_tc(const bf16
     }
     // release TMEM only when no MMA of this CTA can still be in flight: after a
     // timeout, wait (bounded) for the warpgroup's last commit first
-    if (*flag && row == 0) (void)tc_wait(bar, phase ^ 1);
+    if (*flag && row == 0) (void)tc_wait(bar, phase ^ 1, kTcWaitLimit);
     tc_fence_before();
     __syncthreads();
     if (warp == 0) {
@@ -909,37 +912,43 @@ __global__ void k_nrc_targets(PathState P, NrcShade N, uint32_t n, uint32_t boun
     }
 }
 
-int g_sms_nrc = 0;
-int sms()
-{
-    if (!g_sms_nrc) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&g_sms_nrc, cudaDevAttrMultiProcessorCount, dev);
-        if (g_sms_nrc <= 0) g_sms_nrc = 1;
-    }
-    return g_sms_nrc;
-}
+int sms() { return device_sm_count(); }
 
 constexpr size_t kTrainSmem =
     (kNrcFwdElems + kNrcBwdElems + kTrainWarps * 16 * 88) * sizeof(bf16) + kTrainWarps * 16 * sizeof(uint32_t);
 constexpr size_t kWgSmem = kWgElems * sizeof(bf16);
 
+// The shared-memory limit of a kernel is an attribute per device: raised once
+// per device (the flags are indexed by the current device).
+constexpr int kMaxDevices = 64;
 template <class K>
-cudaError_t allow_smem(K kernel, size_t bytes, bool& done)
+cudaError_t allow_smem(K kernel, size_t bytes, bool (&done)[kMaxDevices])
 {
-    if (done) return cudaSuccess;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= kMaxDevices) dev = 0;
+    if (done[dev]) return cudaSuccess;
     const cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                static_cast<int>(bytes));
-    if (e == cudaSuccess) done = true;
+    if (e == cudaSuccess) done[dev] = true;
     return e;
+}
+
+// Polls of the inference kernel's in-loop mbarrier waits.  MT_NRC_WAIT_LIMIT
+// lowers it for tests (0: every wait gives up at once, as if the tensor cores
+// never answered); the wait before TMEM is released always keeps the full bound.
+uint32_t infer_wait_limit()
+{
+    const char* v = std::getenv("MT_NRC_WAIT_LIMIT");
+    if (!v || !*v) return kTcWaitLimit;
+    return static_cast<uint32_t>(std::strtoul(v, nullptr, 10));
 }
 
 template <bool PATHS>
 cudaError_t infer(const void* net, const float4* feat, uint32_t n_host, const uint32_t* count, uint32_t capacity,
                   float* out, const PathState& P, uint32_t* total, int* err, cudaStream_t st)
 {
-    static bool ok = false;
+    static bool ok[kMaxDevices] = {};
     cudaError_t e = allow_smem(k_nrc_infer_tc<PATHS>, kTcSmem, ok);
     if (e != cudaSuccess) return e;
     uint64_t blocks = (static_cast<uint64_t>(capacity) + kTcRows * kTcGroups - 1) / (kTcRows * kTcGroups);
@@ -947,7 +956,7 @@ cudaError_t infer(const void* net, const float4* feat, uint32_t n_host, const ui
     if (blocks > cap) blocks = cap;
     if (blocks == 0) blocks = 1;
     k_nrc_infer_tc<PATHS><<<static_cast<unsigned>(blocks), kTcRows * kTcGroups, kTcSmem, st>>>(
-        static_cast<const bf16*>(net), feat, n_host, count, out, P, total, err);
+        static_cast<const bf16*>(net), feat, n_host, count, out, P, total, err, infer_wait_limit());
     return cudaGetLastError();
 }
 
@@ -1017,7 +1026,7 @@ cudaError_t launch_nrc_train_step(NrcOptimizer& O, const NrcTrainArgs& a, float*
 
 cudaError_t nrc_prepare()
 {
-    static bool ok_t = false, ok_w = false, ok_i0 = false, ok_i1 = false;
+    static bool ok_t[kMaxDevices] = {}, ok_w[kMaxDevices] = {}, ok_i0[kMaxDevices] = {}, ok_i1[kMaxDevices] = {};
     cudaError_t e = allow_smem(k_nrc_fwdbwd, kTrainSmem, ok_t);
     if (e == cudaSuccess) e = allow_smem(k_nrc_wgrad, kWgSmem, ok_w);
     if (e == cudaSuccess) e = allow_smem(k_nrc_infer_tc<false>, kTcSmem, ok_i0);

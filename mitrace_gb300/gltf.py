@@ -38,7 +38,7 @@ from typing import Dict, List, Optional, Tuple
 
 import numpy as np
 
-from . import _abi as A
+from . import _types as A
 from .scenes import CameraData, InstanceData, LightData, MaterialData, MeshData, SceneData, TextureData, make_config
 
 _F = np.float32

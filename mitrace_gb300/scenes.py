@@ -21,7 +21,7 @@ from typing import List, Optional, Tuple
 
 import numpy as np
 
-from . import _abi as A
+from . import _types as A
 
 # ----------------------------------------------------------------------------
 # Data classes
@@ -127,8 +127,7 @@ class SceneData:
 
 def make_config(**kw) -> A.mt_config:
     """mt_config with the reference defaults (Config.hpp:50-70), then overrides."""
-    c = A.mt_config()
-    A.lib.mt_config_defaults(C.byref(c))
+    c = A.config_defaults(A.mt_config())
     for k, v in kw.items():
         if not hasattr(c, k):
             raise KeyError(f"unknown config field {k}")

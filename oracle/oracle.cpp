@@ -1242,8 +1242,15 @@ void debug_postprocess(float* rgb, uint32_t W, uint32_t H, int mode)
     }
 }
 
-// CleanupFireflies (Tracer.cpp:490-548) + average (Tracer.cpp:598-600)
-V3 resolve_pixel(std::vector<V3>& buf, bool enable, float k)
+// CleanupFireflies (Tracer.cpp:490-548) + average (Tracer.cpp:593-600).
+// The two debug modes that read the clamp's own statistics replace every
+// sample and divide by the sample count (CleanupFireflies returns
+// buffer.size() for them): DebugPixelStandardDeviation writes sqrt of the
+// population variance of the intensities (Tracer.cpp:516-523), computed before
+// any sample is dropped; DebugFireflyElimination writes the number of samples
+// the threshold dropped (Tracer.cpp:537-544).  Without the clamp the reference
+// never calls CleanupFireflies, so both modes then average the plain samples.
+V3 resolve_pixel(std::vector<V3>& buf, bool enable, float k, int debug_mode)
 {
     size_t n = buf.size();
     if (enable) {
@@ -1257,11 +1264,21 @@ V3 resolve_pixel(std::vector<V3>& buf, bool enable, float k)
             var = var + df * df;
         }
         var = var / static_cast<float>(buf.size());
-        const float thr = k * std::sqrt(var);
-        for (V3& c : buf) {
-            if (std::fabs(inten(c) - mean) > thr) {
-                c = v3(0.0f);
-                --n;
+        const float sigma = std::sqrt(var);
+        if (debug_mode == MT_DEBUG_PIXEL_STANDARD_DEVIATION) {
+            for (V3& c : buf) c = v3(sigma);
+        } else {
+            const float thr = k * sigma;
+            for (V3& c : buf) {
+                if (std::fabs(inten(c) - mean) > thr) {
+                    c = v3(0.0f);
+                    --n;
+                }
+            }
+            if (debug_mode == MT_DEBUG_FIREFLY_ELIMINATION) {
+                const float dropped = static_cast<float>(buf.size() - n);
+                for (V3& c : buf) c = v3(dropped);
+                n = buf.size();
             }
         }
         if (n == 0) n = 1;
@@ -1843,11 +1860,12 @@ void orc_aces(const float in_rgb[3], float expo, float out_rgb[3])
 }
 
 int orc_resolve_pixel(const float* samples_rgb, uint32_t n, int firefly_enable, float k,
-                      float out_rgb[3])
+                      int debug_mode, float out_rgb[3])
 {
+    if (n == 0) return fail("no samples");
     std::vector<V3> buf(n);
     std::memcpy(buf.data(), samples_rgb, static_cast<size_t>(n) * 12);
-    const V3 r = resolve_pixel(buf, firefly_enable != 0, k);
+    const V3 r = resolve_pixel(buf, firefly_enable != 0, k, debug_mode);
     out_rgb[0] = r.x;
     out_rgb[1] = r.y;
     out_rgb[2] = r.z;
@@ -1913,7 +1931,7 @@ int orc_render(const orc_scene* s, int rng_mode, int threads, uint32_t row0, uin
                         ++localSamples;
                     }
                     const V3 c = resolve_pixel(sampleBuf, cfg.firefly_enable != 0,
-                                               cfg.firefly_threshold);
+                                               cfg.firefly_threshold, cfg.debug_mode);
                     float* px = rgb_out + (static_cast<size_t>(y) * W + x) * 3;
                     px[0] = c.x;
                     px[1] = c.y;
@@ -2016,7 +2034,7 @@ int orc_render_grad(const orc_scene* s, const float* target, float* image, float
             paths[sm] = w.path;
         }
         std::vector<V3> buf = vals;
-        const V3 img = resolve_pixel(buf, cfg.firefly_enable != 0, cfg.firefly_threshold);
+        const V3 img = resolve_pixel(buf, cfg.firefly_enable != 0, cfg.firefly_threshold, MT_DEBUG_NONE);
         float* ip = image + 3 * p;
         ip[0] = img.x, ip[1] = img.y, ip[2] = img.z;
         const V3 r{img.x - target[3 * p], img.y - target[3 * p + 1], img.z - target[3 * p + 2]};

@@ -82,9 +82,11 @@ int orc_render(const orc_scene* s, int rng_mode, int threads, uint32_t row0, uin
 int orc_render_samples(const orc_scene* s, int threads, uint32_t row0, uint32_t row1,
                        float* out);
 
-/* Firefly clamp + average of one pixel's samples (Tracer.cpp:490-548, 593-601). */
+/* Firefly clamp + average of one pixel's samples (Tracer.cpp:490-548, 593-601).
+ * debug_mode MT_DEBUG_PIXEL_STANDARD_DEVIATION / MT_DEBUG_FIREFLY_ELIMINATION
+ * return the clamp's sigma / dropped-sample count (before the heatmap). */
 int orc_resolve_pixel(const float* samples_rgb, uint32_t n, int firefly_enable, float k,
-                      float out_rgb[3]);
+                      int debug_mode, float out_rgb[3]);
 
 /* Adjoint check: renders with the counter RNG, and adds dL/dparameters for
  * L = sum over pixels/channels of (image - target)^2, replaying each kept

@@ -48,7 +48,7 @@ def load(fast: bool = False):
         "orc_render": (C.c_int, [vp, C.c_int, C.c_int, C.c_uint32, C.c_uint32, vp, C.POINTER(C.c_uint64),
                                  C.POINTER(C.c_uint64)]),
         "orc_render_samples": (C.c_int, [vp, C.c_int, C.c_uint32, C.c_uint32, vp]),
-        "orc_resolve_pixel": (C.c_int, [vp, C.c_uint32, C.c_int, C.c_float, vp]),
+        "orc_resolve_pixel": (C.c_int, [vp, C.c_uint32, C.c_int, C.c_float, C.c_int, vp]),
         "orc_aces": (None, [vp, C.c_float, vp]),
         "orc_render_grad": (C.c_int, [vp, vp, vp, vp, vp, vp, vp, vp, vp, C.c_int]),
         "orc_last_error": (C.c_char_p, []),
@@ -129,11 +129,12 @@ def aces(rgb, exposure):
     return o
 
 
-def resolve_pixel(samples: np.ndarray, enable=True, k=6.0):
+def resolve_pixel(samples: np.ndarray, enable=True, k=6.0, debug_mode=0):
     L = lib()
     s = np.ascontiguousarray(samples, dtype=np.float32)
     o = np.zeros(3, dtype=np.float32)
-    _check(L.orc_resolve_pixel(_p(s), s.shape[0], int(enable), float(k), _p(o)), L, "orc_resolve_pixel")
+    _check(L.orc_resolve_pixel(_p(s), s.shape[0], int(enable), float(k), int(debug_mode), _p(o)), L,
+           "orc_resolve_pixel")
     return o
 
 

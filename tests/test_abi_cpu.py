@@ -4,6 +4,7 @@ reference's Config.hpp, and argument errors come back as status codes."""
 import ctypes as C
 import re
 import subprocess
+import sys
 from pathlib import Path
 
 import numpy as np
@@ -100,6 +101,10 @@ def test_argument_errors_are_status_codes():
     assert A.lib.mt_start(None) == A.MT_ERR_INVALID
     assert A.lib.mt_is_done(None) == 0
     assert A.lib.mt_brdf_batch(None, 4, None) == A.MT_ERR_INVALID
+    assert A.lib.mt_resolve_batch(None, 4, 4, 1, 4.0, 0, None) == A.MT_ERR_INVALID
+    one = np.zeros(3, np.float32)
+    assert A.lib.mt_resolve_batch(one.ctypes.data, 1, 0, 1, 4.0, 0, one.ctypes.data) == A.MT_ERR_INVALID
+    assert A.lib.mt_resolve_batch(one.ctypes.data, 1, 1, 1, 4.0, 99, one.ctypes.data) == A.MT_ERR_INVALID
     assert A.lib.mt_brdf_sample_batch(None, 4, None) == A.MT_ERR_INVALID
     assert A.lib.mt_update_materials(None, None, 0) == A.MT_ERR_INVALID
     assert A.lib.mt_update_lights(None, None, 0) == A.MT_ERR_INVALID
@@ -127,3 +132,27 @@ def test_packed_scene_round_trip():
     t = np.array(d.instances[8].transform[:])
     np.testing.assert_allclose(t[12:15], scene.instances[8].transform[:3, 3])
     assert d.textures[0].width == 512 and d.textures[0].height == 256
+
+
+def test_python_config_defaults_equal_the_library_defaults():
+    from mitrace_gb300 import _types
+
+    a, b = A.mt_config(), _types.config_defaults(_types.mt_config())
+    A.lib.mt_config_defaults(C.byref(a))
+    assert bytes(a) == bytes(b)
+
+
+def test_scene_generators_load_no_product_library():
+    """The benchmark's CPU reference arm builds its scenes with
+    mitrace_gb300.scenes; that import must not map libmitrace_gb300.so."""
+    code = (
+        "import sys; sys.path.insert(0, %r)\n"
+        "import mitrace_gb300.scenes as S\n"
+        "scene, cfg = S.material_grid(width=16, height=8, samples=1, segments=8, rings=4)\n"
+        "S.PackedScene(scene)\n"
+        "maps = open('/proc/self/maps').read()\n"
+        "assert 'libmitrace_gb300' not in maps, 'product library mapped'\n"
+        "print('ok')\n" % str(ROOT)
+    )
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0 and r.stdout.strip() == "ok", r.stderr

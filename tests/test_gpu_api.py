@@ -1,0 +1,107 @@
+"""Robustness of the C ABI on the GPU: allocation failures come back as
+MT_ERR_OOM and leave the handle usable, and the statistics a stat thread polls
+(Tracer::GetStats, src/Tracer/Tracer.cpp:806-821, polled by StatThread in
+src/main.cpp:52-57) stay consistent while another thread renders.
+
+Allocation failures are injected on the host: MT_DEVICE_ALLOC_LIMIT makes any
+single device allocation above the given byte count fail as cudaMalloc does
+when the device is out of memory, so no test exhausts a shared GPU."""
+import ctypes as C
+import os
+import threading
+
+import numpy as np
+import pytest
+
+import mitrace_gb300 as mt
+from mitrace_gb300 import _abi as A
+
+pytestmark = pytest.mark.gpu
+
+
+class alloc_limit:
+    def __init__(self, nbytes):
+        self.nbytes = nbytes
+
+    def __enter__(self):
+        os.environ["MT_DEVICE_ALLOC_LIMIT"] = str(self.nbytes)
+
+    def __exit__(self, *exc):
+        os.environ.pop("MT_DEVICE_ALLOC_LIMIT", None)
+
+
+def test_oom_on_create_is_reported():
+    scene, cfg = mt.material_grid(width=32, height=18, samples=1)
+    h = C.c_void_p()
+    with alloc_limit(64 << 10):  # the sphere's 4096 triangle slots alone are 200 KB
+        rc = A.lib.mt_create(mt.PackedScene(scene).ptr(), C.byref(cfg), C.byref(h))
+    assert rc == A.MT_ERR_OOM, A.lib.mt_last_error().decode()
+    assert not h.value
+
+
+def test_oom_on_first_render_leaves_a_usable_handle():
+    torch = pytest.importorskip("torch")
+    scene, cfg = mt.box_room(width=48, height=48, samples=4, seed=3)
+    with mt.Tracer(scene, cfg) as tr:  # the box room's scene buffers are a few KB
+        out = torch.zeros((48, 48, 3), device="cuda")
+        with alloc_limit(1 << 20):  # the wavefront state is far larger
+            rc = A.lib.mt_render_device(tr.handle, C.c_void_p(out.data_ptr()), None)
+        assert rc == A.MT_ERR_OOM
+        assert "out of memory" in A.lib.mt_last_error().decode() or "Allocation" in A.lib.mt_last_error().decode()
+        with alloc_limit(1 << 20):
+            assert A.lib.mt_start(tr.handle) == A.MT_ERR_OOM
+        # without the limit the same handle renders, and matches a fresh handle
+        tr.render_device(out.data_ptr(), 0)
+        torch.cuda.synchronize()
+        with mt.Tracer(scene, cfg) as fresh:
+            ref = torch.zeros_like(out)
+            fresh.render_device(ref.data_ptr(), 0)
+            torch.cuda.synchronize()
+        np.testing.assert_array_equal(out.cpu().numpy(), ref.cpu().numpy())
+        assert tr.GetStats().rays > 0
+
+
+def test_stats_polled_while_rendering():
+    """A stat thread polls mt_get_stats / mt_is_done while the render thread
+    runs device renders and an asynchronous render: every poll succeeds, the
+    counters never go backwards within a render, and the final counts are
+    exact."""
+    torch = pytest.importorskip("torch")
+    scene, cfg = mt.box_room(width=96, height=96, samples=16, seed=5)
+    with mt.Tracer(scene, cfg) as tr:
+        out = torch.zeros((96, 96, 3), device="cuda")
+        tr.render_device(out.data_ptr(), 0)
+        torch.cuda.synchronize()
+        rays_one = tr.GetStats().rays
+        assert rays_one > 0
+        stop = threading.Event()
+        errors, polls = [], [0]
+
+        def poll():
+            s = A.mt_stats()
+            while not stop.is_set():
+                rc = A.lib.mt_get_stats(tr.handle, C.byref(s))
+                if rc != A.MT_OK:
+                    errors.append(rc)
+                if not 0.0 <= s.progress <= 1.0:
+                    errors.append(("progress", s.progress))
+                A.lib.mt_is_done(tr.handle)
+                polls[0] += 1
+
+        t = threading.Thread(target=poll)
+        t.start()
+        try:
+            for _ in range(6):
+                tr.render_device(out.data_ptr(), 0)
+            torch.cuda.synchronize()
+            tr.StartRender()
+            img = tr.WaitForRender()
+        finally:
+            stop.set()
+            t.join()
+        assert not errors, errors[:5]
+        assert polls[0] > 0
+        s = tr.GetStats()
+        assert s.rays == rays_one  # the last render's rays, as GetStats reports them
+        assert s.samples == 96 * 96 * 16
+        np.testing.assert_array_equal(img, out.cpu().numpy())

@@ -214,3 +214,44 @@ def test_target_cap_bounds_training_targets():
     assert np.all(np.isfinite(capped)) and np.all(np.isfinite(free))
     assert np.abs(free).mean() > 1e-2, np.abs(free).mean()
     assert np.abs(capped).mean() < 0.1 * np.abs(free).mean(), (np.abs(capped).mean(), np.abs(free).mean())
+
+
+def test_bounded_tensor_core_wait_reports_timeout_and_handle_recovers():
+    """MT_NRC_WAIT_LIMIT=0 makes every in-loop mbarrier wait of the inference
+    kernel give up at once, as if the tensor cores never answered: the kernel
+    skips its remaining tiles, waits (with the full bound) for its last MMA,
+    frees its TMEM and returns; mt_nrc_get_stats reports MT_ERR_TIMEOUT once,
+    and the same handle then infers and renders normally."""
+    import ctypes as C
+    import os
+
+    scene, cfg = mt.box_room(width=32, height=32, samples=2, seed=3)
+    with mt.Tracer(scene, cfg) as tr:
+        tr.nrc_enable(train_paths=2048, train_batch=2048, spp=2)
+        n = 1000
+        fd = dev(ref.random_features(n, seed=9))
+        out = torch.zeros((n, 3), device="cuda")
+        stream = torch.cuda.current_stream().cuda_stream
+        tr.nrc_infer_device(fd.data_ptr(), n, out.data_ptr(), stream)
+        torch.cuda.synchronize()
+        good = out.cpu().numpy().copy()
+        os.environ["MT_NRC_WAIT_LIMIT"] = "0"
+        try:
+            out.zero_()
+            tr.nrc_infer_device(fd.data_ptr(), n, out.data_ptr(), stream)
+            torch.cuda.synchronize()
+        finally:
+            os.environ.pop("MT_NRC_WAIT_LIMIT", None)
+        st = A.mt_nrc_stats()
+        assert A.lib.mt_nrc_get_stats(tr.handle, C.byref(st)) == A.MT_ERR_TIMEOUT
+        assert "bounded wait" in A.lib.mt_last_error().decode()
+        assert np.all(out.cpu().numpy() == 0.0)  # no tile was written
+        # reported once; the handle works again
+        assert A.lib.mt_nrc_get_stats(tr.handle, C.byref(st)) == A.MT_OK
+        tr.nrc_infer_device(fd.data_ptr(), n, out.data_ptr(), stream)
+        img = torch.zeros((32, 32, 3), device="cuda")
+        tr.render_device(img.data_ptr(), stream)
+        torch.cuda.synchronize()
+        np.testing.assert_array_equal(out.cpu().numpy(), good)
+        assert img.max().item() > 0
+        assert A.lib.mt_nrc_get_stats(tr.handle, C.byref(st)) == A.MT_OK

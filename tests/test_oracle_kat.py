@@ -191,6 +191,44 @@ def test_firefly_clamp_rejects_outlier_and_keeps_count():
     np.testing.assert_allclose(orc.resolve_pixel(s, False, 4.0), [mean] * 3, rtol=1e-6)
 
 
+def _intensity_samples(intensities):
+    """Samples whose channels differ but whose (r+g+b)/3 is the given value."""
+    i = np.asarray(intensities, np.float32)
+    return np.stack([i * np.float32(0.5), i, i * np.float32(1.5)], axis=1).astype(np.float32)
+
+
+def test_debug_pixel_standard_deviation_known_answer():
+    # intensities {0, 0, 0, 3}: mean 0.75, population variance
+    # (3 * 0.75^2 + 2.25^2) / 4 = 1.6875, sigma = sqrt(1.6875) = 1.2990381
+    s = _intensity_samples([0, 0, 0, 3])
+    got = orc.resolve_pixel(s, True, 1.0, debug_mode=21)
+    np.testing.assert_allclose(got, [1.2990381] * 3, rtol=1e-6)
+    # sigma is taken before any sample is dropped, whatever k is
+    np.testing.assert_allclose(orc.resolve_pixel(s, True, 0.0, debug_mode=21), [1.2990381] * 3, rtol=1e-6)
+    # constant samples: sigma 0
+    np.testing.assert_array_equal(orc.resolve_pixel(_intensity_samples([2, 2, 2]), True, 4.0, debug_mode=21),
+                                  np.zeros(3, np.float32))
+
+
+def test_debug_firefly_elimination_known_answer():
+    # k = 1: threshold 1.299; |0 - 0.75| = 0.75 kept, |3 - 0.75| = 2.25 dropped
+    s = _intensity_samples([0, 0, 0, 3])
+    np.testing.assert_array_equal(orc.resolve_pixel(s, True, 1.0, debug_mode=22), np.float32([1, 1, 1]))
+    # k = 2 keeps all four samples
+    np.testing.assert_array_equal(orc.resolve_pixel(s, True, 2.0, debug_mode=22), np.zeros(3, np.float32))
+    # ten samples, two far outliers: intensities 8 x 1, 2 x 21 -> mean 5, sigma 8, k = 1 drops both
+    s = _intensity_samples([1] * 8 + [21, 21])
+    np.testing.assert_array_equal(orc.resolve_pixel(s, True, 1.0, debug_mode=22), np.float32([2, 2, 2]))
+
+
+def test_debug_clamp_modes_without_the_clamp_average_the_samples():
+    # with the clamp off CleanupFireflies is never called (Tracer.cpp:595-596)
+    s = _intensity_samples([0, 0, 0, 3])
+    mean = s.astype(np.float64).mean(axis=0)
+    for mode in (21, 22):
+        np.testing.assert_allclose(orc.resolve_pixel(s, False, 1.0, debug_mode=mode), mean, rtol=1e-6)
+
+
 def test_firefly_clamp_all_rejected_divides_by_one():
     # zero variance: |I - mean| > 0 is false for all, nothing rejected
     s = np.full((8, 3), 0.25, dtype=np.float32)

@@ -45,6 +45,8 @@ def test_noalloc_rows_match_render_device():
         torch.cuda.synchronize()
         got = out2.cpu().numpy()
         np.testing.assert_array_equal(got[16:48], ref_np[16:48])
+        # samples of the two calls are counted, as for mt_render_device
+        assert tr.GetStats().samples == (64 * 64 + 32 * 64) * 16 + 64 * 64 * 16
         assert (got[:16] == -1.0).all() and (got[48:] == -1.0).all()  # rows outside the band untouched
 
 
