@@ -261,10 +261,27 @@ mt_status mt_get_stats(const mt_handle* h, mt_stats* out);
 /* 1 when a render was started and has finished, else 0. */
 int mt_is_done(const mt_handle* h);
 
+/* Seed of the counter-based RNG for the handle's later renders (the value
+ * mt_config.seed gave at mt_create).  The reference reseeds every tile of every
+ * render from std::random_device (Tracer.cpp:564); here a render's random
+ * numbers are a function of (seed, pixel, sample, bounce), so a caller that
+ * wants independent images changes the seed between them.  Not while an
+ * asynchronous render runs. */
+mt_status mt_set_seed(mt_handle* h, uint64_t seed);
+
 /* Render into a caller-owned DEVICE buffer (W*H*3 floats) enqueued on the
  * given CUDA stream (0 = the legacy default stream).  Returns when the work is
  * enqueued; mt_get_stats reports its rays once the stream has finished it. */
 mt_status mt_render_device(mt_handle* h, float* d_rgb_out, void* cuda_stream);
+
+/* Render of image rows [row0, row1) into a caller-owned DEVICE buffer holding
+ * the whole W*H*3 image (only those rows are written), enqueued on
+ * cuda_stream: Tracer::RenderBlock (Tracer.cpp:550-616) over the blocks of
+ * those rows.  A pixel's samples and random numbers do not depend on the band,
+ * so bands of one image rendered on several GPUs (one handle each) assemble
+ * the image mt_render_device renders.  Heatmap debug modes, which normalise
+ * over the whole image, need row0 = 0 and row1 = height. */
+mt_status mt_render_rows_device(mt_handle* h, uint32_t row0, uint32_t row1, float* d_rgb_out, void* cuda_stream);
 
 /* Allocation-free render of rows [row0, row1) into a caller-owned DEVICE
  * buffer holding the whole W*H*3 image (only those rows are written), enqueued

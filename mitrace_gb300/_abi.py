@@ -27,7 +27,9 @@ PROTOTYPES = [
     ("mt_kill", C.c_int, [_VP]),
     ("mt_get_stats", C.c_int, [_VP, C.POINTER(mt_stats)]),
     ("mt_is_done", C.c_int, [_VP]),
+    ("mt_set_seed", C.c_int, [_VP, C.c_uint64]),
     ("mt_render_device", C.c_int, [_VP, _VP, _VP]),
+    ("mt_render_rows_device", C.c_int, [_VP, C.c_uint32, C.c_uint32, _VP, _VP]),
     ("mt_render_rows_noalloc", C.c_int, [_VP, C.c_uint32, C.c_uint32, _VP, _VP]),
     ("mt_render_grad", C.c_int, [_VP, C.POINTER(mt_grad_buffers), _VP]),
     ("mt_update_materials", C.c_int, [_VP, _VP, C.c_uint32]),

@@ -769,9 +769,11 @@ WaveViews views(mt_handle* h)
 
 mt_status settle_render(mt_handle* h);
 
-// Enqueues a whole render into `out` on `st`.  With sync_each_batch the host
-// waits for every batch (progress/kill granularity for the async API).
-mt_status render_into(mt_handle* h, float* out, cudaStream_t st, bool sync_each_batch)
+// Enqueues a render of rows [row0, row1) (the whole image by default) into
+// `out` on `st`.  With sync_each_batch the host waits for every batch
+// (progress/kill granularity for the async API).
+mt_status render_into(mt_handle* h, float* out, cudaStream_t st, bool sync_each_batch, uint32_t row0 = 0,
+                      uint32_t row1 = 0xFFFFFFFFu)
 {
     mt_status rc = ensure_wave(h);
     if (rc != MT_OK) return rc;
@@ -780,21 +782,23 @@ mt_status render_into(mt_handle* h, float* out, cudaStream_t st, bool sync_each_
     rc = settle_render(h);
     if (rc != MT_OK) return rc;
     const mt_config& c = h->cfg;
+    row1 = std::min<uint32_t>(row1, c.height);
+    const bool whole = row0 == 0 && row1 == c.height;
     const WaveViews v = views(h);
     MT_CUDA(cudaMemsetAsync(h->rays.p, 0, 2 * sizeof(unsigned long long), st));
     MT_CUDA(cudaMemsetAsync(h->error_flag.p, 0, sizeof(int), st));
     Profiler* prof = (h->prof.timing || h->prof.counting) ? &h->prof : nullptr;
     const uint64_t rows_per_band = h->band_capacity / (static_cast<uint64_t>(c.width) * c.samples);
     uint64_t total_batches = 0;
-    for (uint64_t r0 = 0; r0 < c.height; r0 += rows_per_band) {
-        const uint64_t rows = std::min<uint64_t>(rows_per_band, c.height - r0);
+    for (uint64_t r0 = row0; r0 < row1; r0 += rows_per_band) {
+        const uint64_t rows = std::min<uint64_t>(rows_per_band, row1 - r0);
         total_batches += (rows * c.width * c.samples + h->batch - 1) / h->batch;
     }
     h->work_total = std::max<uint64_t>(1, total_batches);
     h->work_done = 0;
     uint64_t launches = 0;
-    for (uint64_t r0 = 0; r0 < c.height; r0 += rows_per_band) {
-        const uint64_t rows = std::min<uint64_t>(rows_per_band, c.height - r0);
+    for (uint64_t r0 = row0; r0 < row1; r0 += rows_per_band) {
+        const uint64_t rows = std::min<uint64_t>(rows_per_band, row1 - r0);
         const uint32_t band_pix = static_cast<uint32_t>(rows * c.width);
         const uint32_t pix_base = static_cast<uint32_t>(r0 * c.width);
         const uint64_t paths = static_cast<uint64_t>(band_pix) * c.samples;
@@ -817,7 +821,7 @@ mt_status render_into(mt_handle* h, float* out, cudaStream_t st, bool sync_each_
         MT_CUDA(launch_resolve(h->S, v.W, band_pix, pix_base, out, st, prof));
         ++launches;
     }
-    if (debug_needs_post(c.debug_mode)) {
+    if (whole && debug_needs_post(c.debug_mode)) {
         // WaitForRender's post-processing (Tracer.cpp:781-799) over the whole image
         MT_CUDA(launch_debug_post(out, static_cast<uint64_t>(c.width) * c.height, c.debug_mode, h->counts.p + 7, st));
         launches += 2;
@@ -1229,6 +1233,29 @@ mt_status mt_render_device(mt_handle* h, float* d_rgb_out, void* cuda_stream)
     h->kill = 0;
     const mt_status rc = render_into(h, d_rgb_out, st, false);
     if (rc == MT_OK) h->stat_samples += static_cast<uint64_t>(h->cfg.width) * h->cfg.height * h->cfg.samples;
+    return rc;
+}
+
+mt_status mt_set_seed(mt_handle* h, uint64_t seed)
+{
+    if (check_handle(h) != MT_OK) return MT_ERR_INVALID;
+    if (h->running) return set_err(MT_ERR_STATE, "an asynchronous render is running");
+    h->cfg.seed = seed;
+    h->S.key0 = static_cast<uint32_t>(seed);
+    h->S.key1 = static_cast<uint32_t>(seed >> 32);
+    return MT_OK;
+}
+
+mt_status mt_render_rows_device(mt_handle* h, uint32_t row0, uint32_t row1, float* d_rgb_out, void* cuda_stream)
+{
+    if (check_handle(h) != MT_OK || !d_rgb_out) return set_err(MT_ERR_INVALID, "null argument");
+    if (h->running) return set_err(MT_ERR_STATE, "an asynchronous render is running");
+    if (row0 >= row1 || row1 > h->cfg.height) return set_err(MT_ERR_INVALID, "rows must satisfy row0 < row1 <= height");
+    if ((row0 != 0 || row1 != h->cfg.height) && debug_needs_post(h->cfg.debug_mode))
+        return set_err(MT_ERR_INVALID, "heatmap debug modes normalise over the whole image: render every row");
+    h->kill = 0;
+    const mt_status rc = render_into(h, d_rgb_out, static_cast<cudaStream_t>(cuda_stream), false, row0, row1);
+    if (rc == MT_OK) h->stat_samples += static_cast<uint64_t>(row1 - row0) * h->cfg.width * h->cfg.samples;
     return rc;
 }
 

@@ -61,6 +61,13 @@ class Tracer:
     def render_device(self, out_ptr: int, stream_ptr: int = 0):
         A.check(A.lib.mt_render_device(self.handle, C.c_void_p(out_ptr), C.c_void_p(stream_ptr)), "mt_render_device")
 
+    def set_seed(self, seed: int):
+        A.check(A.lib.mt_set_seed(self.handle, seed), "mt_set_seed")
+
+    def render_rows_device(self, row0: int, row1: int, out_ptr: int, stream_ptr: int = 0):
+        A.check(A.lib.mt_render_rows_device(self.handle, row0, row1, C.c_void_p(out_ptr), C.c_void_p(stream_ptr)),
+                "mt_render_rows_device")
+
     def trace_device(self, rays_ptr: int, n: int, hits_ptr: int, query: int = A.MT_QUERY_CLOSEST, stream_ptr: int = 0):
         A.check(A.lib.mt_trace_rays_device(self.handle, C.c_void_p(rays_ptr), n, C.c_void_p(hits_ptr), query,
                                            C.c_void_p(stream_ptr)), "mt_trace_rays_device")

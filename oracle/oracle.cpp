@@ -38,6 +38,10 @@
 #include <random>
 #include <string>
 #include <thread>
+#ifdef __linux__
+#include <pthread.h>
+#include <sched.h>
+#endif
 #include <vector>
 
 namespace {
@@ -1306,6 +1310,22 @@ void camera_ray(const Camera& c, float u, float v, float aspect, V3& o, V3& d)
     }
 }
 
+// Platform::SetThreadAffinity (src/Platform/Platform.cpp:7-18): core
+// coreId modulo the hardware threads; a failure only costs speed.
+void pin_thread(std::thread& th, unsigned core)
+{
+#ifdef __linux__
+    const unsigned n = std::max(1u, std::thread::hardware_concurrency());
+    cpu_set_t set;
+    CPU_ZERO(&set);
+    CPU_SET(core % n, &set);
+    (void)pthread_setaffinity_np(th.native_handle(), sizeof(cpu_set_t), &set);
+#else
+    (void)th;
+    (void)core;
+#endif
+}
+
 unsigned hw_threads(int threads)
 {
     if (threads > 0) return static_cast<unsigned>(threads);
@@ -1944,7 +1964,13 @@ int orc_render(const orc_scene* s, int rng_mode, int threads, uint32_t row0, uin
     };
     const unsigned T = hw_threads(threads);
     std::vector<std::thread> pool;
-    for (unsigned t = 0; t < T; ++t) pool.emplace_back(work);
+    // Tracer::StartRender pins worker i to core i * (cores / workers) when the
+    // workers fit the cores (Tracer.cpp:755-775)
+    const unsigned cores = std::max(1u, std::thread::hardware_concurrency());
+    for (unsigned t = 0; t < T; ++t) {
+        pool.emplace_back(work);
+        if (T <= cores) pin_thread(pool.back(), t * (cores / T));
+    }
     for (auto& th : pool) th.join();
     if (rays_out) *rays_out = rays.load();
     if (samples_out) *samples_out = samples.load();

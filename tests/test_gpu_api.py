@@ -105,3 +105,49 @@ def test_stats_polled_while_rendering():
         assert s.rays == rays_one  # the last render's rays, as GetStats reports them
         assert s.samples == 96 * 96 * 16
         np.testing.assert_array_equal(img, out.cpu().numpy())
+
+
+@pytest.mark.parametrize("world", [2, 3])
+def test_row_bands_assemble_the_single_gpu_render(world):
+    """mt_render_rows_device on one handle per 'rank' (as on separate GPUs):
+    the bands of mitrace_gb300.bands.row_bands assemble mt_render_device's
+    image bit for bit, and rows outside a band stay untouched."""
+    torch = pytest.importorskip("torch")
+    from mitrace_gb300.bands import row_bands
+
+    from .helpers import small_grid
+
+    scene, cfg = small_grid(width=96, height=54, samples=4, seed=6)
+    with mt.Tracer(scene, cfg) as tr:
+        ref = torch.zeros((54, 96, 3), device="cuda")
+        tr.render_device(ref.data_ptr(), 0)
+        torch.cuda.synchronize()
+    img = torch.full((54, 96, 3), -1.0, device="cuda")
+    for r0, r1 in row_bands(54, world):
+        with mt.Tracer(scene, cfg) as rank_tr:
+            band = torch.full((54, 96, 3), -2.0, device="cuda")
+            rank_tr.render_rows_device(r0, r1, band.data_ptr(), 0)
+            torch.cuda.synchronize()
+            assert (band[:r0] == -2.0).all() and (band[r1:] == -2.0).all()
+            assert rank_tr.GetStats().samples == (r1 - r0) * 96 * 4
+            img[r0:r1] = band[r0:r1]
+    np.testing.assert_array_equal(img.cpu().numpy(), ref.cpu().numpy())
+
+
+def test_set_seed_equals_a_handle_created_with_that_seed():
+    torch = pytest.importorskip("torch")
+    scene, cfg = mt.box_room(width=40, height=40, samples=4, seed=1)
+    with mt.Tracer(scene, cfg) as tr:
+        a = torch.zeros((40, 40, 3), device="cuda")
+        tr.render_device(a.data_ptr(), 0)
+        tr.set_seed(77)
+        b = torch.zeros_like(a)
+        tr.render_device(b.data_ptr(), 0)
+        torch.cuda.synchronize()
+    cfg.seed = 77
+    with mt.Tracer(scene, cfg) as t2:
+        c = torch.zeros_like(a)
+        t2.render_device(c.data_ptr(), 0)
+        torch.cuda.synchronize()
+    assert not torch.equal(a, b)
+    np.testing.assert_array_equal(b.cpu().numpy(), c.cpu().numpy())
