@@ -1,9 +1,9 @@
 """Writes tests/golden/<name>.npz from the reference's glTF test scenes
 (assets/tests/*/ of the MiTrace project) with mitrace_gb300.gltf, plus the
 render settings of each scene's render_params.txt.  Run from the repository
-root where the reference checkout is at /root/reference:
+root with the path of a MiTrace checkout (or set MITRACE_REFERENCE to it):
 
-    python tests/golden/make_gltf_fixtures.py /root/reference
+    python tests/golden/make_gltf_fixtures.py <path to the MiTrace checkout>
 
 Scenes whose textures are JPEG (light_type_test, offset_scale_test,
 normal_mapping_test) are skipped: no JPEG decoder is available here.
@@ -35,4 +35,9 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    import os
+
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("MITRACE_REFERENCE")
+    if not root:
+        sys.exit("usage: make_gltf_fixtures.py <MiTrace checkout>  (or set MITRACE_REFERENCE)")
+    main(root)

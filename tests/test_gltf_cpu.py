@@ -1,6 +1,7 @@
 """The glTF loader (mitrace_gb300/gltf.py) and the committed fixtures made from
 the reference's own test scenes (tests/golden/make_gltf_fixtures.py)."""
 import math
+import os
 from pathlib import Path
 
 import numpy as np
@@ -12,7 +13,8 @@ from oracle import oracle_py as orc
 from tests.golden.scene_npz import load_scene
 
 GOLDEN = Path(__file__).resolve().parent / "golden"
-REF = Path("/root/reference")
+# a MiTrace checkout, when one is at hand: the fixtures are re-derived from it
+REF = Path(os.environ["MITRACE_REFERENCE"]) if os.environ.get("MITRACE_REFERENCE") else None
 NAMES = ["cornell_box", "material_spheres", "light_creep"]
 
 
@@ -83,7 +85,7 @@ def test_node_transform_is_translate_rotate_scale():
     np.testing.assert_array_equal(gltf.node_transform({"matrix": m.tolist()}), m.reshape(4, 4).T)
 
 
-@pytest.mark.skipif(not REF.exists(), reason="the reference checkout is not on this machine")
+@pytest.mark.skipif(REF is None or not REF.exists(), reason="MITRACE_REFERENCE does not name a MiTrace checkout")
 @pytest.mark.parametrize("name", NAMES)
 def test_loader_reproduces_the_committed_fixture(name, tmp_path):
     from tests.golden.make_gltf_fixtures import FIXTURES

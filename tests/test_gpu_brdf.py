@@ -64,7 +64,16 @@ def test_brdf_sampling_matches_oracle():
     """GeneratePath's bounce sample (lobe choice, GGX reflection with its cosine
     fallback, cosine sample, mixture pdf) on seeded uniforms: the same lobe for
     all but decisions within an ulp of the specular probability, directions
-    within the sinf/cosf rounding, pdfs to 1e-4 relative for 99.9%."""
+    within the sinf/cosf rounding, the specular probability to 1e-5, and the
+    mixture pdf to 1e-5 relative of the reference functions evaluated at the
+    sampled direction.
+
+    The direction goes through sinf/cosf/sqrtf, whose last-ulp rounding differs
+    between the GPU and the host C library, and a near-mirror GGX lobe (alpha
+    down to 0.0025) turns a 1e-7 change of direction into percents of pdf, in
+    exact arithmetic as in float.  So the pdf is checked where it is defined:
+    the oracle's DiffusePdf / SpecularPdf (BRDF.hpp:80-97) and mixture
+    (Tracer.cpp:190-194) are evaluated at the GPU's sampled direction."""
     q = sample_queries(200_000, 3)
     g = mt.brdf_sample_batch(q)
     r = orc.brdf_sample(q)
@@ -73,10 +82,14 @@ def test_brdf_sampling_matches_oracle():
     assert same.mean() > 0.999
     assert set(np.unique(lg)) == {0, 1, 2}  # every branch exercised
     np.testing.assert_allclose(g[same, 0:3], r[same, 0:3], atol=2e-5)
-    # the GGX pdf of a near-mirror lobe (alpha down to 0.0025) turns the ulps of
-    # sinf/cosf in the direction into up to a few percent: bound the bulk
-    # tightly and the tail loosely
-    rel = np.abs(g[same, 3] - r[same, 3]) / np.maximum(np.abs(r[same, 3]), 1e-6)
-    assert np.mean(rel <= 1e-4) > 0.999 and rel.max() < 0.1
     np.testing.assert_allclose(g[:, 4], r[:, 4], rtol=1e-5)
+    # reference pdfs at the GPU's directions: mt_brdf_query = L, V, N, base, roughness, metallic
+    bq = np.zeros((q.shape[0], 14), np.float32)
+    bq[:, 0:3], bq[:, 3:6], bq[:, 6:9] = g[:, 0:3], q[:, 0:3], q[:, 3:6]
+    bq[:, 9:12], bq[:, 12], bq[:, 13] = q[:, 6:9], q[:, 9], q[:, 10]
+    e = orc.brdf_batch(bq)
+    ps = r[:, 4]
+    one = np.float32(1.0)
+    mix = ((one - ps) * e[:, 3]).astype(np.float32) + (ps * e[:, 4]).astype(np.float32)
+    np.testing.assert_allclose(g[:, 3], mix, rtol=1e-5, atol=1e-12)
     assert np.all(np.einsum("ij,ij->i", g[:, 0:3], q[:, 3:6]) > -1e-6)  # never below the surface
