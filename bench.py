@@ -91,6 +91,8 @@ def parse():
     p.add_argument("--nrc-end-at", type=int, default=1)
     p.add_argument("--nrc-steps", type=int, default=None)
     p.add_argument("--nrc-rows", type=int, default=1920 * 1080 * 4)
+    p.add_argument("--case", choices=["render", "adjoint", "nrc_train", "nrc_frame", "microbench"], default=None,
+                   help="run one small workload of a kernel family and print its timings (profiling runs)")
     return p.parse_args()
 
 
@@ -454,27 +456,35 @@ def e2e_leg(a, ctx):
 
     torch = ctx.torch
     scene, cfg = scene_and_config(a, a.spp, 300)
-    img = np.empty((a.height, a.width, 3), dtype=np.float32)
-    times = []
+    # the result lands in pinned host memory (mt_wait copies into it)
+    img_t = torch.empty((a.height, a.width, 3), dtype=torch.float32).pin_memory()
+    img = img_t.numpy()
+    times, phases = [], []
     for i in range(a.e2e_steps + 1):
         torch.cuda.synchronize()
         ctx.barrier()
         t0 = time.perf_counter()
-        with mt.Tracer(scene, cfg) as tr:
-            if ctx.world == 1:
-                tr.StartRender()
-                img[...] = tr.WaitForRender()
-            else:
-                band = torch.empty((a.height, a.width, 3), device=ctx.dev)
-                render_band(ctx, tr, band)
-                img[ctx.r0:ctx.r1] = band[ctx.r0:ctx.r1].cpu().numpy()
-        dt = time.perf_counter() - t0
+        tr = mt.Tracer(scene, cfg)
+        t1 = time.perf_counter()
+        if ctx.world == 1:
+            tr.StartRender()
+            tr.WaitForRender(out=img)
+        else:
+            band = torch.empty((a.height, a.width, 3), device=ctx.dev)
+            render_band(ctx, tr, band)
+            img_t[ctx.r0:ctx.r1].copy_(band[ctx.r0:ctx.r1])
+        t2 = time.perf_counter()
+        tr.close()
+        t3 = time.perf_counter()
         if i > 0:  # the first one is a warm-up
-            times.append(dt)
+            times.append(t3 - t0)
+            phases.append((t1 - t0, t2 - t1, t3 - t2))
     sec = ctx.max_over_ranks(statistics.mean(times))
     d2h = (ctx.r1 - ctx.r0) * a.width * 3 * 4
+    ph = [statistics.mean(p[k] for p in phases) * 1e3 for k in range(3)]
     return {"value": sec, "unit": "s", "h2d_bytes_per_step": int(scene.nbytes()), "d2h_bytes_per_step": int(d2h),
-            "steps": len(times)}
+            "steps": len(times),
+            "phases_ms": {"create_upload_bvh": ph[0], "render_and_copy_out": ph[1], "destroy": ph[2]}}
 
 
 # --------------------------------------------------------------------------- extras (rank 0, one GPU)
@@ -532,7 +542,7 @@ def throughput_leg(a, ctx, hbm_peak):
     }
 
 
-def microbench(a, ctx, hbm_peak):
+def microbench(a, ctx, hbm_peak, builds=True):
     """Incoherent rays (origins uniform in the scene box, directions uniform on
     the sphere, seed 0) against the large scene: fBm terrain of 2 * 1023^2
     triangles plus 50k icospheres of 80 triangles, each set one mesh.  Closest
@@ -582,6 +592,8 @@ def microbench(a, ctx, hbm_peak):
     out["roofline_closest"] = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                                "frac": achieved / hbm_peak, "alg_bytes": alg_bytes}
     tr.close()
+    if not builds:
+        return out
     builds = []
     for m in scene.meshes:
         t0 = time.perf_counter()
@@ -816,8 +828,60 @@ def run_ours(a):
         torch.distributed.destroy_process_group()
 
 
+def run_case(a):
+    """One workload per kernel family, for profiler runs: `render` renders
+    --warmup + --steps images of the headline configuration (--width, --height,
+    --spp); `adjoint` is the adjoint leg; `nrc_train` the cache's kernels;
+    `nrc_frame` two cached frames; `microbench` --microbench-rays incoherent rays
+    on the large scene."""
+    import mitrace_gb300 as mt
+
+    ctx = GpuCtx(a)
+    torch = ctx.torch
+    hbm_peak, bf16_peak, _ = peaks()
+    out = {"case": a.case}
+    if a.case == "render":
+        scene, cfg = scene_and_config(a, a.spp, 100)
+        img = torch.zeros((a.height, a.width, 3), device=ctx.dev)
+        with mt.Tracer(scene, cfg) as tr:
+            ms = []
+            for i in range(a.warmup + a.steps):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(ctx.stream)
+                tr.render_device(img.data_ptr(), ctx.sptr)
+                e1.record(ctx.stream)
+                torch.cuda.synchronize()
+                if i >= a.warmup:
+                    ms.append(e0.elapsed_time(e1))
+            out.update(ms=ms, rays=tr.GetStats().rays, launches=tr.kernel_launches())
+    elif a.case == "adjoint":
+        out["adjoint"] = adjoint_bench(ctx)
+    elif a.case == "nrc_train":
+        out["nrc_kernels"] = nrc_microbench(ctx, bf16_peak, a.nrc_rows)
+    elif a.case == "nrc_frame":
+        scene, cfg = scene_and_config(a, 4, 400)
+        acc = torch.zeros((a.height, a.width, 3), device=ctx.dev)
+        with mt.Tracer(scene, cfg) as tr:
+            tr.nrc_enable(spp=a.nrc_spp, end_at=a.nrc_end_at)
+            ms = []
+            for f in range(2):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(ctx.stream)
+                tr.nrc_frame(acc.data_ptr(), f, ctx.sptr)
+                e1.record(ctx.stream)
+                torch.cuda.synchronize()
+                ms.append(e0.elapsed_time(e1))
+            out["ms"] = ms
+    elif a.case == "microbench":
+        out["incoherent"] = microbench(a, ctx, hbm_peak, builds=False)
+    print(json.dumps(out), flush=True)
+
+
 def main():
     a = parse()
+    if a.case:
+        run_case(a)
+        return
     if a.impl == "reference":
         run_reference(a)
     else:

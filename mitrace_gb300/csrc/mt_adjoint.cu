@@ -11,6 +11,8 @@
 // pdfs, the light-pick probabilities, the energy cut-off and the firefly mask
 // are held constant (the path-replay convention), so each sample's gradient is
 // that of its BRDF, light and sky factors along the fixed path.
+#include <cooperative_groups.h>
+#include <cooperative_groups/reduce.h>
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -192,6 +194,28 @@ __device__ int texel_taps(const DevTexture& t, float uvx, float uvy, long long* 
     idx[0] = at(ix, iy);
     w[0] = 1.0f;
     return 1;
+}
+
+// Adds (x, y, z) to the RGB texel gradient at p, aggregated over the warp: the
+// lanes that reach this call with the same texel (adjacent pixels of a sample
+// often land on one texel) sum their values first and one of them issues the
+// three atomics.
+__device__ __forceinline__ void texel_add(float* p, float x, float y, float z)
+{
+    namespace cg = cooperative_groups;
+    const cg::coalesced_group active = cg::coalesced_threads();
+    const cg::coalesced_group same =
+        cg::labeled_partition(active, static_cast<unsigned long long>(reinterpret_cast<uintptr_t>(p)));
+    if (same.size() > 1) {
+        x = cg::reduce(same, x, cg::plus<float>());
+        y = cg::reduce(same, y, cg::plus<float>());
+        z = cg::reduce(same, z, cg::plus<float>());
+    }
+    if (same.thread_rank() == 0) {
+        atomicAdd(p, x);
+        atomicAdd(p + 1, y);
+        atomicAdd(p + 2, z);
+    }
 }
 
 struct VertexMat {
@@ -393,9 +417,8 @@ __global__ void __launch_bounds__(128) k_adjoint(DevScene S, GradParams G, Recor
                 float* dt = G.d_texels + G.texel_off[M.base_tex];
                 for (int q = 0; q < nt; ++q) {
                     if (w[q] == 0.0f) continue;
-                    atomicAdd(dt + 3 * idx[q], db.x * M.base[0] * w[q]);
-                    atomicAdd(dt + 3 * idx[q] + 1, db.y * M.base[1] * w[q]);
-                    atomicAdd(dt + 3 * idx[q] + 2, db.z * M.base[2] * w[q]);
+                    texel_add(dt + 3 * idx[q], db.x * M.base[0] * w[q], db.y * M.base[1] * w[q],
+                              db.z * M.base[2] * w[q]);
                 }
             }
         }

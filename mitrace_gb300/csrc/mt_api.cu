@@ -282,6 +282,7 @@ struct mt_handle {
     // wavefront storage (allocated on first render)
     uint32_t batch = 0;
     uint64_t band_capacity = 0;  // samples the band planes hold
+    uint32_t wave_spp = 0;       // paths per pixel the batch is sized for (0: cfg.samples)
     DevArray<float4> pstate;     // 10 float4 planes
     DevArray<uint4> phit;
     DevArray<float4> sq;         // 3 float4 planes
@@ -691,7 +692,7 @@ mt_status ensure_wave(mt_handle* h)
     if (h->batch) return MT_OK;
     const mt_config& c = h->cfg;
     const uint64_t npix = static_cast<uint64_t>(c.width) * c.height;
-    const uint64_t total = npix * c.samples;
+    const uint64_t total = npix * std::max<uint32_t>(c.samples, h->wave_spp);
     // Paths in flight per batch.  Every bounce launches the persistent
     // traversal kernels once per batch, and each launch ends with a tail in
     // which a few long rays keep their warps busy while the rest of the GPU
@@ -728,6 +729,31 @@ mt_status ensure_wave(mt_handle* h)
     }
     h->batch = static_cast<uint32_t>(batch);
     return MT_OK;
+}
+
+mt_status settle_render(mt_handle* h);
+
+// Drops the wavefront state so that the next ensure_wave sizes it afresh
+// (the last render's counters are folded in first; the NRC and adjoint
+// buffers sized from the old batch are released too).
+void rc_settle_and_release_wave(mt_handle* h)
+{
+    (void)settle_render(h);
+    h->batch = 0;
+    h->pstate.reset();
+    h->phit.reset();
+    h->sq.reset();
+    h->queues.reset();
+    h->counts.reset();
+    h->rays.reset();
+    h->samples.reset();
+    h->image.reset();
+    h->dval.reset();
+    h->dcnt.reset();
+    h->grad_batch = 0;
+    h->rec_vert.reset();
+    h->rec_path.reset();
+    h->grad_pix.reset();
 }
 
 struct WaveViews {
@@ -1275,7 +1301,18 @@ mt_status mt_render_grad(mt_handle* h, const mt_grad_buffers* g, void* cuda_stre
     const mt_config& c = h->cfg;
     const uint64_t rows_per_band = h->band_capacity / (static_cast<uint64_t>(c.width) * c.samples);
     if (!h->grad_batch) {
-        const uint64_t gb = std::min<uint64_t>(h->batch, env_u64("MT_GRAD_BATCH_PATHS", 1ull << 20));
+        // Paths replayed per batch: their vertex records (5 float4 per bounce
+        // plus 2 per path) are the adjoint's only storage, O(batch).  Sixteen
+        // samples per pixel of a band (at least 2^20 paths) keep the memory
+        // proportional to the pixels, not to the samples, while batches stay
+        // large enough that the replay's traversal launches are not dominated
+        // by their tails; capped at an eighth of the free device memory.
+        const uint64_t rec_bytes = (static_cast<uint64_t>(std::max<uint32_t>(1, c.bounces)) * 5 + 2) * 16;
+        uint64_t want = std::max<uint64_t>(1ull << 20, 16ull * rows_per_band * c.width);
+        size_t free_b = 0, total_b = 0;
+        if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess && free_b > 0)
+            want = std::min<uint64_t>(want, std::max<uint64_t>(1024, free_b / 8 / rec_bytes));
+        const uint64_t gb = std::min<uint64_t>(h->batch, env_u64("MT_GRAD_BATCH_PATHS", want));
         MT_CUDA(h->rec_vert.alloc(gb * std::max<uint32_t>(1, c.bounces) * 5));
         MT_CUDA(h->rec_path.alloc(gb * 2));
         MT_CUDA(h->grad_pix.alloc(2 * rows_per_band * c.width));
@@ -1489,9 +1526,21 @@ mt_status mt_nrc_enable(mt_handle* h, const mt_nrc_config* c)
         return set_err(MT_ERR_INVALID, "invalid radiance-cache configuration");
     if (static_cast<uint64_t>(c->train_paths) * std::max<uint32_t>(1, h->cfg.bounces) > 0xFFFFFFFFull)
         return set_err(MT_ERR_INVALID, "train_paths * bounces exceeds 2^32");
+    if (h->cfg.debug_mode) return set_err(MT_ERR_INVALID, "the radiance cache needs debug_mode 0");
+    // a cached frame renders c->spp samples per pixel: size the wavefront so
+    // that a frame is one batch when the device allows it (a batch holds at
+    // most 2^26 paths), rather than the mt_config samples it was sized for
+    if (c->spp > std::max<uint32_t>(h->cfg.samples, h->wave_spp)) {
+        const uint64_t npix = static_cast<uint64_t>(h->cfg.width) * h->cfg.height;
+        const bool grow = h->batch && h->batch < std::min<uint64_t>(1ull << 26, npix * c->spp);
+        h->wave_spp = c->spp;
+        if (grow) {
+            MT_CUDA(cudaStreamSynchronize(h->stream));
+            rc_settle_and_release_wave(h);
+        }
+    }
     mt_status rc = ensure_wave(h);
     if (rc != MT_OK) return rc;
-    if (h->cfg.debug_mode) return set_err(MT_ERR_INVALID, "the radiance cache needs debug_mode 0");
     return nrc_alloc(h, *c);
 }
 

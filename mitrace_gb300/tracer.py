@@ -42,9 +42,14 @@ class Tracer:
     def StartRender(self):
         A.check(A.lib.mt_start(self.handle), "mt_start")
 
-    def WaitForRender(self) -> np.ndarray:
-        A.check(A.lib.mt_wait(self.handle, self.image.ctypes.data_as(C.c_void_p)), "mt_wait")
-        return self.image
+    def WaitForRender(self, out: np.ndarray = None) -> np.ndarray:
+        """mt_wait; the image lands in `out` (a C-contiguous float32 H x W x 3
+        host array, e.g. pinned memory) or in the tracer's own buffer."""
+        dst = self.image if out is None else out
+        if out is not None:
+            assert out.dtype == np.float32 and out.flags.c_contiguous and out.size == self.image.size
+        A.check(A.lib.mt_wait(self.handle, dst.ctypes.data_as(C.c_void_p)), "mt_wait")
+        return dst
 
     def KillRender(self):
         A.check(A.lib.mt_kill(self.handle), "mt_kill")

@@ -7,7 +7,8 @@
 2. Against central finite differences (h = 1e-3) of the GPU forward render on
    32 parameters (base colours, light intensities, albedo texels), with the
    energy cut-off and firefly clamp off so the estimator is smooth in them:
-   <= 1e-2 relative.
+   <= 1e-2 relative; and on 16 roughness and metallic factors with one bounce,
+   where they enter a sample only through the BRDF evaluation.
 3. The loss it reports equals sum (image - target)^2 of the image it renders,
    and that image equals mt_render_device's.
 4. A torch.autograd.Function (this harness only) backpropagates through it.
@@ -154,6 +155,53 @@ def test_gpu_adjoint_matches_finite_differences():
         worst = max(worst, rel)
         assert rel <= 1e-2, (kind, idx, fd, ad)
     assert len(picks) == 32
+
+
+def fd_scene_one_bounce():
+    """bounces = 1: a sample is the primary vertex's emission plus its
+    next-event estimate (or the sky on a miss); the bounce direction it samples
+    is never traced.  Roughness and metallic then enter the sample only through
+    EvaluateBRDF of the light direction, so holding the sampling decisions
+    fixed (the path-replay convention) and moving the parameters in the forward
+    render change the sample in the same way, and central differences pin
+    their gradients.  With more bounces the GGX-sampled direction moves with
+    roughness (and the lobe choice with metallic): the two then agree only in
+    expectation."""
+    scene, cfg = fd_scene()
+    cfg.bounces = 1
+    for j in range(7):  # metallic inside (0, 1): away from clamp(metallic, 0, 1)'s kinks
+        for i in range(7):
+            scene.materials[j * 7 + i].metallic = 0.1 + 0.8 * j / 6.0
+    return scene, cfg
+
+
+def test_gpu_adjoint_roughness_and_metallic_match_finite_differences():
+    h = 1e-3
+    scene, cfg = fd_scene_one_bounce()
+    target = np.full((cfg.height, cfg.width, 3), 0.2, np.float32)
+    g = gpu_grad(scene, cfg, target)
+    rng = np.random.default_rng(9)
+    # spheres of columns 1..6 (roughness 0.21 .. 1, above the 0.05 floor of BRDF.hpp)
+    cand = [m for m in range(49) if m % 7 > 0]
+    picks = []
+    for kind, key in (("rough", "d_roughness"), ("metal", "d_metallic")):
+        nz = [m for m in cand if abs(g[key][m]) > 1e-2 * np.abs(g[key]).max()]
+        picks += [(kind, int(m)) for m in rng.choice(nz, size=min(8, len(nz)), replace=False)]
+
+    def loss_with(kind, m, s):
+        sc, cf = fd_scene_one_bounce()
+        if kind == "rough":
+            sc.materials[m].roughness += s * h
+        else:
+            sc.materials[m].metallic += s * h
+        img = gpu_image(sc, cf).astype(np.float64)
+        return float(((img - target) ** 2).sum())
+
+    for kind, m in picks:
+        fd = (loss_with(kind, m, 1) - loss_with(kind, m, -1)) / (2 * h)
+        ad = float(g["d_roughness" if kind == "rough" else "d_metallic"][m])
+        assert abs(fd - ad) <= 1e-2 * max(abs(fd), 1e-6), (kind, m, fd, ad)
+    assert len(picks) == 16
 
 
 class RenderLoss(torch.autograd.Function):

@@ -255,3 +255,28 @@ def test_bounded_tensor_core_wait_reports_timeout_and_handle_recovers():
         np.testing.assert_array_equal(out.cpu().numpy(), good)
         assert img.max().item() > 0
         assert A.lib.mt_nrc_get_stats(tr.handle, C.byref(st)) == A.MT_OK
+
+
+def test_cache_spp_above_the_handle_samples_regrows_the_wavefront():
+    """mt_nrc_enable with more samples per frame than the handle was created
+    for resizes the wavefront to one batch per frame; the cached frame (no
+    diffuse-ish vertex) still equals the plain render at that spp, and the
+    handle's own renders are unchanged."""
+    scene, cfg = mt.box_room(width=48, height=48, samples=2, seed=2)
+    st = torch.cuda.current_stream().cuda_stream
+    before = torch.zeros((48, 48, 3), device="cuda")
+    after = torch.zeros_like(before)
+    acc = torch.zeros_like(before)
+    with mt.Tracer(scene, cfg) as tr:
+        tr.render_device(before.data_ptr(), st)
+        tr.nrc_enable(train_paths=2048, train_batch=1024, spp=6, rough_min=2.0)
+        tr.nrc_frame(acc.data_ptr(), 0, st)
+        tr.render_device(after.data_ptr(), st)
+        torch.cuda.synchronize()
+    cfg6 = mt.box_room(width=48, height=48, samples=6, seed=2)[1]
+    ref6 = torch.zeros_like(before)
+    with mt.Tracer(scene, cfg6) as tr6:
+        tr6.render_device(ref6.data_ptr(), st)
+        torch.cuda.synchronize()
+    np.testing.assert_array_equal(acc.cpu().numpy(), ref6.cpu().numpy())
+    np.testing.assert_array_equal(after.cpu().numpy(), before.cpu().numpy())
