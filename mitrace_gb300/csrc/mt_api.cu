@@ -317,7 +317,7 @@ struct mt_handle {
         bool on = false;
         mt_nrc_config cfg{};
         DevArray<float> master, m, v, partial, planes, frame;
-        DevArray<uint16_t> fwd, bwd, infer, acts;
+        DevArray<uint16_t> fwd, infer;
         DevArray<float> ema;
         DevArray<float4> qrec, trec, samples;
         // [0] cache queries of a batch, [1] training samples, [2] queries of the
@@ -969,32 +969,21 @@ mt_status nrc_alloc(mt_handle* h, const mt_nrc_config& c)
     const cudaStream_t st = h->stream;
     NrcOptimizer& O = N.opt;
     O.max_splits = 128;
-    O.max_rows = static_cast<uint32_t>(((4ull * c.train_batch + 63) / 64) * 64 + 64ull * O.max_splits);
+    O.max_rows = 4u * c.train_batch;
     MT_CUDA(N.master.alloc(kNrcParams));
     MT_CUDA(N.m.alloc(kNrcParams));
     MT_CUDA(N.v.alloc(kNrcParams));
     MT_CUDA(N.partial.alloc(static_cast<size_t>(O.max_splits) * kNrcParams));
     MT_CUDA(N.fwd.alloc(kNrcFwdElems));
-    MT_CUDA(N.bwd.alloc(kNrcBwdElems));
     MT_CUDA(N.infer.alloc(kNrcFwdElems));
     MT_CUDA(N.ema.alloc(kNrcParams));
     MT_CUDA(cudaMemsetAsync(N.fwd.p, 0, kNrcFwdElems * 2, st));
-    MT_CUDA(cudaMemsetAsync(N.bwd.p, 0, kNrcBwdElems * 2, st));
     MT_CUDA(cudaMemsetAsync(N.infer.p, 0, kNrcFwdElems * 2, st));
-    const uint64_t R = O.max_rows;
-    MT_CUDA(N.acts.alloc(R * (80 + 8 * 64 + 8)));
-    O.acts.x = N.acts.p;
-    for (int l = 0; l < 4; ++l) {
-        O.acts.h[l] = N.acts.p + R * (80 + 64 * l);
-        O.acts.d[l] = N.acts.p + R * (80 + 256 + 64 * l);
-    }
-    O.acts.dy = N.acts.p + R * (80 + 512);
     O.master = N.master.p;
     O.m = N.m.p;
     O.v = N.v.p;
     O.partial = N.partial.p;
     O.fwd = N.fwd.p;
-    O.bwd = N.bwd.p;
     O.infer = N.infer.p;
     O.ema = N.ema.p;
     O.ema_decay = c.ema_decay;
@@ -1003,9 +992,12 @@ mt_status nrc_alloc(mt_handle* h, const mt_nrc_config& c)
     O.beta2 = c.beta2;
     O.eps = c.epsilon;
     O.step = 0;
-    MT_CUDA(N.step.alloc(1));
-    MT_CUDA(cudaMemsetAsync(N.step.p, 0, sizeof(uint32_t), st));
+    // [0] Adam steps taken, [1] Adam blocks done with the current step
+    MT_CUDA(N.step.alloc(2));
+    MT_CUDA(cudaMemsetAsync(N.step.p, 0, 2 * sizeof(uint32_t), st));
     O.d_step = N.step.p;
+    O.d_done = N.step.p + 1;
+    O.err = h->error_flag.p + 1;
     if (N.steps_graph) {
         cudaGraphExecDestroy(N.steps_graph);
         N.steps_graph = nullptr;
@@ -1711,7 +1703,7 @@ mt_status mt_nrc_set_params(mt_handle* h, const float* params)
     MT_CUDA(cudaMemcpy(N.master.p, params, kNrcParams * sizeof(float), cudaMemcpyHostToDevice));
     MT_CUDA(cudaMemset(N.m.p, 0, kNrcParams * sizeof(float)));
     MT_CUDA(cudaMemset(N.v.p, 0, kNrcParams * sizeof(float)));
-    MT_CUDA(cudaMemset(N.step.p, 0, sizeof(uint32_t)));
+    MT_CUDA(cudaMemset(N.step.p, 0, 2 * sizeof(uint32_t)));
     N.opt.step = 0;
     MT_CUDA(launch_nrc_publish(N.opt, h->stream));
     MT_CUDA(cudaStreamSynchronize(h->stream));

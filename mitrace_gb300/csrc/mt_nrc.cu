@@ -7,15 +7,12 @@
 //
 //   k_nrc_infer_tc fused encoding + 5 layers on tcgen05 (TMEM accumulators,
 //                  operands in shared memory), 128-row tiles per warpgroup.
-//   k_nrc_fwdbwd   forward pass on mma.sync m16n8k16 (a warp owns 16 rows,
-//                  the accumulator layout of one layer is the A-operand layout
-//                  of the next, so activations stay in registers), the
-//                  relative-L2 loss gradient and the backward pass through the
-//                  activations; writes the layer inputs and pre-activation
-//                  gradients row-major (BF16).
-//   k_nrc_wgrad    dW_l = sum over rows of delta_l^T x input_l: 64-row chunks
-//                  staged in shared memory, transposed operands fetched with
-//                  ldmatrix.trans, one partial sum per block (fixed order).
+//   k_nrc_train_tc one training step's forward pass, relative-L2 loss
+//                  gradient, backward pass and weight gradient on tcgen05:
+//                  a CTA per 128-row tile, every product an M = 128 MMA into
+//                  TMEM, the backward and weight-gradient operands read as
+//                  transposed (MN-major) views of the forward ones; one
+//                  gradient partial per CTA.
 //   k_nrc_adam     sums the partials in block order, Adam, and rewrites the BF16
 //                  weight blobs.
 #include <cuda_bf16.h>
@@ -39,13 +36,10 @@ using bf16 = __nv_bfloat16;
 // ---------------------------------------------------------------------------
 __host__ __device__ constexpr int fwd_off(int l) { return l == 0 ? 0 : 64 * 88 + (l - 1) * 64 * 72; }
 __host__ __device__ constexpr int fwd_stride(int l) { return l == 0 ? 88 : 72; }
-__host__ __device__ constexpr int bwd_off(int l) { return (l - 1) * 64 * 72; }  // l = 1..4
-__host__ __device__ constexpr int bwd_stride(int l) { return l == 4 ? 24 : 72; }
 __host__ __device__ constexpr int master_off(int l) { return l == 0 ? 0 : 5120 + (l - 1) * 4096; }
 __host__ __device__ constexpr int layer_in(int l) { return l == 0 ? 80 : 64; }
 __host__ __device__ constexpr int layer_out(int l) { return l == 4 ? 3 : 64; }
 static_assert(fwd_off(4) + 8 * 72 == kNrcFwdElems, "forward blob size");
-static_assert(bwd_off(4) + 64 * 24 == kNrcBwdElems, "backward blob size");
 static_assert(master_off(4) + 3 * 64 == kNrcParams, "parameter count");
 
 __device__ __forceinline__ void param_coords(int q, int& l, int& o, int& i)
@@ -139,169 +133,11 @@ __device__ __forceinline__ void encode_part1(float4 f1, float4 f2, Out out)
     out(76, f2.w);
 }
 
-// Encodes the 16 rows [r0, r0+16) of a feature array into a warp's staging
-// tile stg[16][88] (BF16); rows >= n become zeros (constant lanes included, so
-// their outputs and gradients are exactly zero).  Lanes 0-15 do part 0 of row
-// lane, lanes 16-31 part 1.
-__device__ __forceinline__ void stage_rows(const float4* __restrict__ feat, uint32_t fstride, uint32_t r0,
-                                           uint32_t n, const uint32_t* map, bf16* stg)
-{
-    const int lane = threadIdx.x & 31;
-    const int row = lane & 15;
-    const uint32_t r = r0 + row;
-    bf16* dst = stg + row * 88;
-    auto put = [&](int k, float v) { dst[k] = __float2bfloat16_rn(v); };
-    if (r < n) {
-        const float4* f = feat + static_cast<uint64_t>(map ? map[row] : r) * fstride;
-        if (lane < 16)
-            encode_part0(f[0], f[3], f[4], put);
-        else
-            encode_part1(f[1], f[2], put);
-    } else {
-        const bf16 z = __float2bfloat16_rn(0.0f);
-        if (lane < 16) {
-            for (int k = 0; k < 36; ++k) dst[k] = z;
-            for (int k = 68; k < 75; ++k) dst[k] = z;
-            for (int k = 77; k < 80; ++k) dst[k] = z;
-        } else {
-            for (int k = 36; k < 68; ++k) dst[k] = z;
-            dst[75] = z;
-            dst[76] = z;
-        }
-    }
-}
-
-// ---------------------------------------------------------------------------
-// Tensor-core helpers (mma.sync m16n8k16, BF16 in, FP32 accumulate)
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ uint32_t lds32(const bf16* p) { return *reinterpret_cast<const uint32_t*>(p); }
-
-__device__ __forceinline__ void mma16816(float* d, const uint32_t* a, uint32_t b0, uint32_t b1)
-{
-    asm volatile(
-        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
-        "{%0,%1,%2,%3};\n"
-        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
-}
-
+// BF16 pair packing (round to nearest even), low half first.
 __device__ __forceinline__ uint32_t pack2(float lo, float hi)
 {
     const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
     return *reinterpret_cast<const uint32_t*>(&v);
-}
-
-__device__ __forceinline__ void ldsm_x4_trans(uint32_t* r, const bf16* p)
-{
-    const uint32_t a = static_cast<uint32_t>(__cvta_generic_to_shared(p));
-    asm volatile("ldmatrix.sync.aligned.m8n8.x4.trans.shared.b16 {%0,%1,%2,%3}, [%4];\n"
-                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
-                 : "r"(a));
-}
-__device__ __forceinline__ void ldsm_x2_trans(uint32_t* r, const bf16* p)
-{
-    const uint32_t a = static_cast<uint32_t>(__cvta_generic_to_shared(p));
-    asm volatile("ldmatrix.sync.aligned.m8n8.x2.trans.shared.b16 {%0,%1}, [%2];\n"
-                 : "=r"(r[0]), "=r"(r[1])
-                 : "r"(a));
-}
-
-// acc[16 x 8*NT] = A[16 x 16*KT] * W^T, W given as rows [n][k] with stride.
-template <int KT, int NT>
-__device__ __forceinline__ void dense(const uint32_t (&a)[KT][4], const bf16* w, int stride, float (&acc)[NT][4])
-{
-    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-#pragma unroll
-    for (int j = 0; j < NT; ++j) {
-        acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.0f;
-        const bf16* row = w + (8 * j + g) * stride + 2 * t;
-#pragma unroll
-        for (int kt = 0; kt < KT; ++kt) mma16816(acc[j], a[kt], lds32(row + 16 * kt), lds32(row + 16 * kt + 8));
-    }
-}
-
-// Accumulator tiles -> A-operand fragments of the next layer (with ReLU).
-template <int NT>
-__device__ __forceinline__ void relu_pack(const float (&acc)[NT][4], uint32_t (&a)[NT / 2][4])
-{
-#pragma unroll
-    for (int kt = 0; kt < NT / 2; ++kt) {
-        a[kt][0] = pack2(fmaxf(acc[2 * kt][0], 0.0f), fmaxf(acc[2 * kt][1], 0.0f));
-        a[kt][1] = pack2(fmaxf(acc[2 * kt][2], 0.0f), fmaxf(acc[2 * kt][3], 0.0f));
-        a[kt][2] = pack2(fmaxf(acc[2 * kt + 1][0], 0.0f), fmaxf(acc[2 * kt + 1][1], 0.0f));
-        a[kt][3] = pack2(fmaxf(acc[2 * kt + 1][2], 0.0f), fmaxf(acc[2 * kt + 1][3], 0.0f));
-    }
-}
-
-// Zeroes gradient entries whose ReLU output was zero, then packs them as
-// A-operand fragments.
-template <int NT>
-__device__ __forceinline__ void mask_pack(float (&acc)[NT][4], const uint32_t (&h)[NT / 2][4],
-                                          uint32_t (&a)[NT / 2][4])
-{
-#pragma unroll
-    for (int j = 0; j < NT; ++j) {
-#pragma unroll
-        for (int c = 0; c < 4; ++c) {
-            const uint32_t hw = h[j >> 1][(j & 1) * 2 + (c >> 1)];
-            const uint32_t bits = (c & 1) ? (hw >> 16) : (hw & 0xffffu);
-            if ((bits & 0x7fffu) == 0) acc[j][c] = 0.0f;
-        }
-    }
-#pragma unroll
-    for (int kt = 0; kt < NT / 2; ++kt) {
-        a[kt][0] = pack2(acc[2 * kt][0], acc[2 * kt][1]);
-        a[kt][1] = pack2(acc[2 * kt][2], acc[2 * kt][3]);
-        a[kt][2] = pack2(acc[2 * kt + 1][0], acc[2 * kt + 1][1]);
-        a[kt][3] = pack2(acc[2 * kt + 1][2], acc[2 * kt + 1][3]);
-    }
-}
-
-__device__ __forceinline__ void load_x_frags(const bf16* stg, uint32_t (&ax)[5][4])
-{
-    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-#pragma unroll
-    for (int kt = 0; kt < 5; ++kt) {
-        ax[kt][0] = lds32(stg + g * 88 + 16 * kt + 2 * t);
-        ax[kt][1] = lds32(stg + (g + 8) * 88 + 16 * kt + 2 * t);
-        ax[kt][2] = lds32(stg + g * 88 + 16 * kt + 8 + 2 * t);
-        ax[kt][3] = lds32(stg + (g + 8) * 88 + 16 * kt + 8 + 2 * t);
-    }
-}
-
-struct Hidden {
-    uint32_t h[4][4][4];  // layer, k-tile, register
-};
-
-// Forward pass of one 16-row tile; returns the output accumulator y.
-__device__ __forceinline__ void forward(const bf16* W, const uint32_t (&ax)[5][4], Hidden& H, float (&y)[1][4])
-{
-    float acc[8][4];
-    dense<5, 8>(ax, W + fwd_off(0), fwd_stride(0), acc);
-    relu_pack<8>(acc, H.h[0]);
-    dense<4, 8>(H.h[0], W + fwd_off(1), fwd_stride(1), acc);
-    relu_pack<8>(acc, H.h[1]);
-    dense<4, 8>(H.h[1], W + fwd_off(2), fwd_stride(2), acc);
-    relu_pack<8>(acc, H.h[2]);
-    dense<4, 8>(H.h[2], W + fwd_off(3), fwd_stride(3), acc);
-    relu_pack<8>(acc, H.h[3]);
-    dense<4, 1>(H.h[3], W + fwd_off(4), fwd_stride(4), y);
-}
-
-// 16-byte global -> shared copy that does not hold registers or block the
-// thread (cp.async); cp_async_wait waits for all of this thread's copies.
-__device__ __forceinline__ void cp_async16(void* smem_dst, const void* gsrc)
-{
-    const uint32_t d = static_cast<uint32_t>(__cvta_generic_to_shared(smem_dst));
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(gsrc) : "memory");
-}
-__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_all;" ::: "memory"); }
-
-// Starts the copy of a weight blob into shared memory (elems a multiple of 8,
-// both ends 16-byte aligned); the caller waits (cp_async_wait + barrier).
-__device__ __forceinline__ void copy_blob_async(bf16* dst, const bf16* __restrict__ src, int elems)
-{
-    for (int i = threadIdx.x; i < elems / 8; i += blockDim.x) cp_async16(dst + 8 * i, src + 8 * i);
 }
 
 // ---------------------------------------------------------------------------
@@ -580,11 +416,6 @@ __global__ void k_nrc_encode(const float4* __restrict__ feat, uint32_t n, float*
     }
 }
 
-// ---------------------------------------------------------------------------
-// Training: forward + backward through the activations
-// ---------------------------------------------------------------------------
-constexpr int kTrainWarps = 4;
-
 // 32-bit integer finaliser (MurmurHash3 fmix32): row -> pseudo-random sample.
 __device__ __forceinline__ uint32_t mix32(uint32_t h)
 {
@@ -596,224 +427,318 @@ __device__ __forceinline__ uint32_t mix32(uint32_t h)
     return h;
 }
 
-__device__ __forceinline__ void st32(void* base, uint64_t idx, uint32_t v)
+// ---------------------------------------------------------------------------
+// Training on the 5th-generation tensor cores (tcgen05): forward, loss,
+// backward and weight gradient of a training step in one kernel
+// ---------------------------------------------------------------------------
+// One warpgroup per CTA, one 128-row tile at a time (thread r <-> row r <->
+// TMEM lane r).  Every activation is written once, by the thread that owns
+// its row, in the canonical K-major no-swizzle layout (8-row x 16-byte core
+// matrices) that the next forward MMA reads as its A operand: the input X
+// (128 x 80), the hidden outputs H0..H3 (128 x 64) and the loss gradient of
+// the layer being differentiated, dY (128 x 64, or 128 x 16 at the output).
+// The backward and weight-gradient products read the same bytes transposed:
+//   backward   dX_l = dY_l W_l        A = dY_l (K-major, K = out_l),
+//                                     B = W_l read MN-major (N = in_l, K = out_l)
+//   gradient   dW_l^T = X_l^T dY_l    A = X_l read MN-major (M = in_l, padded to
+//                                     128; lanes >= in_l are not read back),
+//                                     B = dY_l read MN-major (N = out_l, K = rows)
+// so no transposed copy is ever written.  In every descriptor the leading
+// byte offset (LBO) is the stride between core matrices along K and the stride
+// byte offset (SBO) the stride along M/N: for a K-major operand LBO = 128 B
+// (the next 8 K elements) and SBO = one 8-row group; for an MN-major view of
+// the same bytes LBO = one 8-row group (now 8 K values) and SBO = 128 B.  TMEM columns: [0,64) forward accumulator, [64,128) backward
+// accumulator, 128 + 64 l the gradient of layer l (accumulated over the CTA's
+// tiles).  The CTA's weight-gradient sums are written to its partial row, which
+// k_nrc_adam adds up in CTA order.  Waits on the mbarrier are bounded as in
+// the inference kernel.
+constexpr int kTrRows = 128;
+constexpr int kTrX = kTcW4 + 16 * 64 * 2;        // X: 128 x 80
+constexpr int kTrH = kTrX + kTrRows * 80 * 2;    // H0..H3: 128 x 64 each
+constexpr int kTrDY = kTrH + 4 * kTrRows * 64 * 2;  // dY: 128 x 64 (128 x 16 at the output layer)
+// 8 KB after dY: whichever way a descriptor's two strides are read, no
+// operand read reaches past the allocation (checked below)
+constexpr int kTrPad = kTrDY + kTrRows * 64 * 2;
+constexpr int kTrBar = kTrPad + 8192;
+constexpr int kTrTmem = kTrBar + 8;
+constexpr int kTrFlag = kTrTmem + 4;
+constexpr int kTrSmem = kTrFlag + 12;
+constexpr uint32_t kTrCols = 512;
+static_assert(kTrX % 1024 == 0 && kTrH % 1024 == 0 && kTrDY % 1024 == 0, "operand alignment");
+// The transposed reads of X and H3 as 128-row A operands run up to 1 KB past
+// their buffers (into H0 and dY).  Bounds that hold for either reading of the
+// two strides (all groups at the larger stride): X, H3 and dY as MN-major
+// operands, W4 as the backward B operand.
+static_assert(kTrX + 30 * 1280 + 128 <= kTrSmem, "X read bound");
+static_assert(kTrH + 3 * kTrRows * 128 + 30 * 1024 + 128 <= kTrSmem, "H3 read bound");
+static_assert(kTrDY + 22 * 1024 + 128 <= kTrBar, "dY read bound");
+static_assert(kTcW4 + 8 * 1024 + 128 <= kTrSmem, "W4 read bound");
+
+__device__ __forceinline__ uint32_t tr_act(int l) { return l == 0 ? kTrX : kTrH + (l - 1) * kTrRows * 128; }
+__device__ __forceinline__ uint32_t tr_w(int l) { return l == 0 ? kTcW0 : (l == 4 ? kTcW4 : kTcW1 + (l - 1) * 64 * 64 * 2); }
+
+// D (+)= A B over ksteps K-steps of 16, descriptor starts advancing by a_step /
+// b_step bytes per step.
+__device__ __forceinline__ void tc_gemm(uint32_t d, uint32_t a, uint32_t a_lbo, uint32_t a_sbo, uint32_t a_step,
+                                        uint32_t b, uint32_t b_lbo, uint32_t b_sbo, uint32_t b_step, uint32_t ksteps,
+                                        uint32_t idesc, bool accumulate)
 {
-    reinterpret_cast<uint32_t*>(base)[idx] = v;
+    for (uint32_t j = 0; j < ksteps; ++j)
+        tc_mma(d, smem_desc(a + j * a_step, a_lbo, a_sbo), smem_desc(b + j * b_step, b_lbo, b_sbo), idesc,
+               (accumulate || j > 0) ? 1u : 0u);
 }
 
-__global__ void __launch_bounds__(kTrainWarps * 32) k_nrc_fwdbwd(const bf16* __restrict__ fwd,
-                                                                 const bf16* __restrict__ bwd, NrcTrainArgs a,
-                                                                 uint32_t rows_pad, NrcActs A, float* loss,
-                                                                 const uint32_t* __restrict__ step)
+__global__ void __launch_bounds__(kTrRows) k_nrc_train_tc(const bf16* __restrict__ fwd, NrcTrainArgs a,
+                                                         uint32_t tiles, float* __restrict__ partial, float* loss,
+                                                         const uint32_t* __restrict__ step, int* err,
+                                                         uint32_t wait_limit)
 {
-    extern __shared__ __align__(16) unsigned char smem[];
-    bf16* WF = reinterpret_cast<bf16*>(smem);
-    bf16* WB = WF + kNrcFwdElems;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    bf16* stg = WB + kNrcBwdElems + warp * 16 * 88;
-    uint32_t* map = reinterpret_cast<uint32_t*>(WB + kNrcBwdElems + kTrainWarps * 16 * 88) + warp * 16;
-    copy_blob_async(WF, fwd, kNrcFwdElems);
-    copy_blob_async(WB, bwd, kNrcBwdElems);
-    cp_async_wait();
+    extern __shared__ __align__(1024) unsigned char tc_smem[];
+    unsigned char* smem = tc_smem;
+    const uint32_t s0 = static_cast<uint32_t>(__cvta_generic_to_shared(smem));
+    const uint32_t tid = threadIdx.x, warp = tid >> 5, row = tid;
+    // forward weights, canonical K-major (N = out rows, K = in)
+    for (uint32_t i = tid; i < 64 * 10 + 3 * 64 * 8 + 16 * 8; i += blockDim.x) {
+        uint32_t l, r, c;
+        if (i < 640) {
+            l = 0; r = i / 10; c = i % 10;
+        } else if (i < 640 + 1536) {
+            const uint32_t j = i - 640;
+            l = 1 + j / 512; r = (j % 512) / 8; c = j % 8;
+        } else {
+            const uint32_t j = i - 2176;
+            l = 4; r = j / 8; c = j % 8;
+        }
+        const uint32_t kc = l == 0 ? 10 : 8;
+        uint4 v = make_uint4(0u, 0u, 0u, 0u);
+        if (l < 4 || r < 8)
+            v = *reinterpret_cast<const uint4*>(fwd + fwd_off(l) + r * fwd_stride(l) + 8 * c);
+        *reinterpret_cast<uint4*>(smem + tr_w(l) + canon_off(r, 8 * c, kc)) = v;
+    }
+    const uint32_t bar = s0 + kTrBar;
+    volatile int* flag = reinterpret_cast<volatile int*>(smem + kTrFlag);
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar));
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        *flag = 0;
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(s0 + kTrTmem),
+                     "r"(kTrCols));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+    }
+    fence_async_smem();
+    tc_fence_before();
     __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *reinterpret_cast<const uint32_t*>(smem + kTrTmem);
+    const uint32_t lane_addr = tmem + ((warp * 32u) << 16);
+
     const uint32_t cnt = a.count ? min(*a.count, a.count_cap) : a.rows;
     const uint32_t base = *step * a.rows;
-    const uint32_t n = cnt ? a.rows : 0;  // valid rows
+    const uint32_t n = cnt ? a.rows : 0;  // valid rows (none when there is nothing to train on)
     const float scale = n ? 1.0f / (3.0f * static_cast<float>(n)) : 0.0f;
     float lsum = 0.0f;
-    for (uint32_t tile = blockIdx.x * kTrainWarps + warp; tile < rows_pad / 16; tile += gridDim.x * kTrainWarps) {
-        const uint32_t r0 = tile * 16;
-        if (lane < 16) map[lane] = a.count ? (n ? mix32(base + r0 + lane) % cnt : 0u) : r0 + lane;
-        __syncwarp();
-        stage_rows(a.feat, a.fstride, r0, n, map, stg);
-        __syncwarp();
-        uint32_t ax[5][4];
-        load_x_frags(stg, ax);
-        // layer input x: 16 rows x 160 B, copied as 16-byte pieces
-        for (int i = lane; i < 160; i += 32) {
-            const int row = i / 10, c = i - row * 10;
-            reinterpret_cast<uint4*>(A.x)[(static_cast<uint64_t>(r0 + row) * 80 + 8 * c) / 8] =
-                *reinterpret_cast<const uint4*>(stg + row * 88 + 8 * c);
+    uint32_t phase = 0;
+    bool first = true, timed_out = false;
+
+    // every thread of the warpgroup waits for the last commit; false on timeout
+    auto wait_mma = [&]() -> bool {
+        if (!tc_wait(bar, phase, wait_limit)) *flag = 1;
+        phase ^= 1;
+        __syncthreads();
+        if (*flag) return false;
+        tc_fence_after();
+        return true;
+    };
+    // generic-proxy shared-memory writes -> visible to the next MMA
+    auto publish = [&]() {
+        fence_async_smem();
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+    };
+
+    for (uint32_t tile = blockIdx.x; tile < tiles && !timed_out; tile += gridDim.x) {
+        const uint32_t r = tile * kTrRows + row;
+        const bool valid = r < n;
+        const uint32_t sample = a.count ? (n ? mix32(base + r) % cnt : 0u) : r;
+        {  // encoded input row
+            float e[80];
+            if (valid) {
+                const float4* f = a.feat + static_cast<uint64_t>(sample) * a.fstride;
+                auto put = [&](int k, float v) { e[k] = v; };
+                encode_part0(f[0], f[3], f[4], put);
+                encode_part1(f[1], f[2], put);
+            } else {
+#pragma unroll
+                for (int k = 0; k < 80; ++k) e[k] = 0.0f;
+            }
+#pragma unroll
+            for (int c = 0; c < 10; ++c)
+                *reinterpret_cast<uint4*>(smem + kTrX + canon_off(row, 8 * c, 10)) =
+                    make_uint4(pack2(e[8 * c], e[8 * c + 1]), pack2(e[8 * c + 2], e[8 * c + 3]),
+                               pack2(e[8 * c + 4], e[8 * c + 5]), pack2(e[8 * c + 6], e[8 * c + 7]));
         }
-        __syncwarp();
-        Hidden H;
-        float y[1][4];
-        forward(WF, ax, H, y);
-        // hidden outputs
+        publish();
+        // forward
+        uint32_t mask[4][2];
+#pragma unroll 1
+        for (int l = 0; l < 5 && !timed_out; ++l) {
+            const uint32_t kc = l == 0 ? 10 : 8;
+            if (tid == 0) {
+                tc_gemm(tmem, s0 + tr_act(l), 128, kc * 128, 256, s0 + tr_w(l), 128, kc * 128, 256, kc / 2,
+                        tc_idesc(l == 4 ? 16 : 64), false);
+                tc_commit(bar);
+            }
+            if (!wait_mma()) {
+                timed_out = true;
+                break;
+            }
+            if (l < 4) {
+                uint32_t m0 = 0, m1 = 0;
+                unsigned char* H = smem + tr_act(l + 1);
 #pragma unroll
-        for (int l = 0; l < 4; ++l)
+                for (int q = 0; q < 4; ++q) {
+                    float v[16];
+                    tc_ld16(lane_addr + 16 * q, v);
+                    tc_wait_ld();
+                    uint32_t bits = 0;
 #pragma unroll
-            for (int kt = 0; kt < 4; ++kt)
+                    for (int j = 0; j < 16; ++j) {
+                        if (v[j] > 0.0f) bits |= 1u << j;
+                        v[j] = fmaxf(v[j], 0.0f);
+                    }
+                    if (q < 2) m0 |= bits << (16 * q); else m1 |= bits << (16 * (q - 2));
 #pragma unroll
-                for (int q = 0; q < 4; ++q)
-                    st32(A.h[l], ((static_cast<uint64_t>(r0 + g + 8 * (q & 1)) * 64) + 16 * kt + 8 * (q >> 1) + 2 * t) / 2,
-                         H.h[l][kt][q]);
-        // relative L2 loss and its gradient (columns 2t, 2t+1 of rows g, g+8)
-        float dy[4];
+                    for (int c = 0; c < 2; ++c) {
+                        const float* x = v + 8 * c;
+                        *reinterpret_cast<uint4*>(H + canon_off(row, 16 * q + 8 * c, 8)) =
+                            make_uint4(pack2(x[0], x[1]), pack2(x[2], x[3]), pack2(x[4], x[5]), pack2(x[6], x[7]));
+                    }
+                }
+                mask[l][0] = m0;
+                mask[l][1] = m1;
+            } else {
+                float y[16];
+                tc_ld16(lane_addr, y);
+                tc_wait_ld();
+                // relative L2 loss |y - t|^2 / (y^2 + 0.01), y constant in the denominator
+                float dy[3] = {0.0f, 0.0f, 0.0f};
+                if (valid) {
 #pragma unroll
-        for (int c = 0; c < 4; ++c) {
-            const uint32_t r = r0 + g + 8 * (c >> 1);
-            const int col = 2 * t + (c & 1);
-            dy[c] = 0.0f;
-            if (r < n && col < 3) {
-                const float target = a.targets[static_cast<uint64_t>(map[g + 8 * (c >> 1)]) * a.tstride + col];
-                const float diff = y[0][c] - target;
-                const float den = y[0][c] * y[0][c] + 0.01f;
-                lsum += diff * diff / den;
-                dy[c] = 2.0f * diff / den * scale;
+                    for (int c = 0; c < 3; ++c) {
+                        const float target = a.targets[static_cast<uint64_t>(sample) * a.tstride + c];
+                        const float diff = y[c] - target;
+                        const float den = y[c] * y[c] + 0.01f;
+                        lsum += diff * diff / den;
+                        dy[c] = 2.0f * diff / den * scale;
+                    }
+                }
+                *reinterpret_cast<uint4*>(smem + kTrDY + canon_off(row, 0, 2)) =
+                    make_uint4(pack2(dy[0], dy[1]), pack2(dy[2], 0.0f), 0u, 0u);
+                *reinterpret_cast<uint4*>(smem + kTrDY + canon_off(row, 8, 2)) = make_uint4(0u, 0u, 0u, 0u);
+            }
+            publish();
+        }
+        // backward: layers 4..1 (input gradient and weight gradient), then the
+        // first layer's weight gradient
+#pragma unroll 1
+        for (int l = 4; l >= 0 && !timed_out; --l) {
+            const uint32_t kcy = l == 4 ? 2 : 8;            // k-chunks of dY_l (out_l / 8)
+            const uint32_t kin = l == 0 ? 10 : 8;           // k-chunks of the layer input (in_l / 8)
+            if (tid == 0) {
+                if (l > 0)  // dH = dY_l W_l -> TMEM [64, 128); W_l read MN-major
+                    tc_gemm(tmem + 64, s0 + kTrDY, 128, kcy * 128, 256, s0 + tr_w(l), kin * 128, 128,
+                            2 * kin * 128, kcy / 2, tc_idesc(64) | (1u << 16), false);
+                // dW_l^T += X_l^T dY_l -> TMEM [128 + 64 l, ...); both operands MN-major
+                tc_gemm(tmem + 128 + 64 * l, s0 + tr_act(l), kin * 128, 128, 2 * kin * 128, s0 + kTrDY, kcy * 128,
+                        128, 2 * kcy * 128, kTrRows / 16, tc_idesc(l == 4 ? 16 : 64) | (1u << 15) | (1u << 16),
+                        !first);
+                tc_commit(bar);
+            }
+            if (!wait_mma()) {
+                timed_out = true;
+                break;
+            }
+            if (l == 0) break;
+            // dY_{l-1} = dH masked by the ReLU of H_{l-1}
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                float v[16];
+                tc_ld16(lane_addr + 64 + 16 * q, v);
+                tc_wait_ld();
+                const uint32_t bits = (q < 2 ? mask[l - 1][0] >> (16 * q) : mask[l - 1][1] >> (16 * (q - 2)));
+#pragma unroll
+                for (int j = 0; j < 16; ++j)
+                    if (!((bits >> j) & 1u)) v[j] = 0.0f;
+#pragma unroll
+                for (int c = 0; c < 2; ++c) {
+                    const float* x = v + 8 * c;
+                    *reinterpret_cast<uint4*>(smem + kTrDY + canon_off(row, 16 * q + 8 * c, 8)) =
+                        make_uint4(pack2(x[0], x[1]), pack2(x[2], x[3]), pack2(x[4], x[5]), pack2(x[6], x[7]));
+                }
+            }
+            publish();
+        }
+        first = false;
+    }
+    // this CTA's weight-gradient sums (TMEM lane i = input i of the layer)
+    float* out = partial + static_cast<uint64_t>(blockIdx.x) * kNrcParams;
+    if (!timed_out) {
+#pragma unroll 1
+        for (int l = 0; l < 5; ++l) {
+            const int in = layer_in(l), outs = layer_out(l);
+            const int nq = l == 4 ? 1 : 4;
+            for (int q = 0; q < nq; ++q) {
+                float v[16];
+                tc_ld16(lane_addr + 128 + 64 * l + 16 * q, v);
+                tc_wait_ld();
+                if (static_cast<int>(row) < in) {
+#pragma unroll
+                    for (int j = 0; j < 16; ++j) {
+                        const int o = 16 * q + j;
+                        if (o < outs) out[master_off(l) + o * in + row] = v[j];
+                    }
+                }
             }
         }
-        st32(A.dy, (static_cast<uint64_t>(r0 + g) * 8 + 2 * t) / 2, pack2(dy[0], dy[1]));
-        st32(A.dy, (static_cast<uint64_t>(r0 + g + 8) * 8 + 2 * t) / 2, pack2(dy[2], dy[3]));
-        uint32_t ady[1][4] = {{pack2(dy[0], dy[1]), pack2(dy[2], dy[3]), 0u, 0u}};
-        float acc[8][4];
-        uint32_t ad[4][4];
-        dense<1, 8>(ady, WB + bwd_off(4), bwd_stride(4), acc);
-#pragma unroll
-        for (int l = 3; l >= 0; --l) {
-            mask_pack<8>(acc, H.h[l], ad);
-#pragma unroll
-            for (int kt = 0; kt < 4; ++kt)
-#pragma unroll
-                for (int q = 0; q < 4; ++q)
-                    st32(A.d[l], ((static_cast<uint64_t>(r0 + g + 8 * (q & 1)) * 64) + 16 * kt + 8 * (q >> 1) + 2 * t) / 2,
-                         ad[kt][q]);
-            if (l > 0) dense<4, 8>(ad, WB + bwd_off(l), bwd_stride(l), acc);
-        }
-        __syncwarp();
+    } else {
+        // a timed-out CTA contributes nothing to this step's gradient
+        for (int q = tid; q < kNrcParams; q += blockDim.x) out[q] = 0.0f;
+        if (tid == 0) atomicOr(err, MT_ERRBIT_TIMEOUT);
     }
     if (loss) {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) lsum += __shfl_down_sync(0xffffffffu, lsum, o);
-        if (lane == 0) atomicAdd(loss, lsum * scale);
+        if ((tid & 31) == 0) atomicAdd(loss, lsum * scale);
     }
-}
-
-// ---------------------------------------------------------------------------
-// Training: weight gradients
-// ---------------------------------------------------------------------------
-constexpr int kWgWarps = 16;
-constexpr int kChunk = 64;
-// Shared tile strides (elements) and offsets: X, H1..H4, D1..D4, DY.
-constexpr int kSX = 88, kSH = 72, kSY = 24;
-__host__ __device__ constexpr int wg_off_h(int l) { return kChunk * kSX + l * kChunk * kSH; }
-__host__ __device__ constexpr int wg_off_d(int l) { return kChunk * kSX + (4 + l) * kChunk * kSH; }
-constexpr int kWgOffY = kChunk * kSX + 8 * kChunk * kSH;
-constexpr int kWgElems = kWgOffY + kChunk * kSY;
-constexpr int kWgTasks = 34;
-
-struct WgTask {
-    int l, m0, n0, nt;
-};
-__device__ __forceinline__ WgTask wg_task(int id)
-{
-    if (id < 8) return {0, (id >> 1) * 16, (id & 1) * 40, 5};
-    if (id < 32) {
-        const int r = (id - 8) & 7;
-        return {1 + (id - 8) / 8, (r >> 1) * 16, (r & 1) * 32, 4};
-    }
-    return {4, 0, (id - 32) * 32, 4};
-}
-
-__global__ void __launch_bounds__(kWgWarps * 32) k_nrc_wgrad(NrcActs A, uint32_t rows_per_split,
-                                                             float* __restrict__ partial, uint32_t* step)
-{
-    // the step this gradient belongs to (read by the Adam kernel that follows)
-    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(step, 1u);
-    extern __shared__ __align__(16) unsigned char smem[];
-    bf16* T = reinterpret_cast<bf16*>(smem);
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
-    // DY columns 8..23 stay zero (the output layer's padded rows)
-    for (int i = threadIdx.x; i < kChunk * kSY; i += blockDim.x) T[kWgOffY + i] = __float2bfloat16_rn(0.0f);
-    const int ntask = warp + 32 < kWgTasks ? 3 : 2;
-    float acc[3][5][4];
-#pragma unroll
-    for (int a = 0; a < 3; ++a)
-#pragma unroll
-        for (int j = 0; j < 5; ++j) acc[a][j][0] = acc[a][j][1] = acc[a][j][2] = acc[a][j][3] = 0.0f;
-    const uint64_t row_begin = static_cast<uint64_t>(blockIdx.x) * rows_per_split;
-    for (uint32_t c0 = 0; c0 < rows_per_split; c0 += kChunk) {
-        __syncthreads();
-        const uint64_t rb = row_begin + c0;
-        // stage the chunk: X (10 x 16 B per row), 8 x (8 x 16 B), DY (1 x 16 B),
-        // all copies in flight at once
-        for (int i = threadIdx.x; i < kChunk * 10; i += blockDim.x) {
-            const int row = i / 10, c = i - row * 10;
-            cp_async16(T + row * kSX + 8 * c, reinterpret_cast<const uint4*>(A.x) + ((rb + row) * 80 + 8 * c) / 8);
-        }
-        for (int i = threadIdx.x; i < 8 * kChunk * 8; i += blockDim.x) {
-            const int m = i / (kChunk * 8), rem = i - m * kChunk * 8, row = rem >> 3, c = rem & 7;
-            const void* src = m < 4 ? A.h[m] : A.d[m - 4];
-            cp_async16(T + kChunk * kSX + m * kChunk * kSH + row * kSH + 8 * c,
-                       reinterpret_cast<const uint4*>(src) + ((rb + row) * 64 + 8 * c) / 8);
-        }
-        for (int i = threadIdx.x; i < kChunk; i += blockDim.x)
-            cp_async16(T + kWgOffY + i * kSY, reinterpret_cast<const uint4*>(A.dy) + rb + i);
-        cp_async_wait();
-        __syncthreads();
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-            if (a >= ntask) break;
-            const WgTask k = wg_task(warp + 16 * a);
-            // A = delta^T (rows: outputs of layer l), B = the layer input
-            const bf16* Dt = k.l == 4 ? T + kWgOffY : T + wg_off_d(k.l);
-            const int ds = k.l == 4 ? kSY : kSH;
-            const bf16* Bt = k.l == 0 ? T : T + wg_off_h(k.l - 1);
-            const int bs = k.l == 0 ? kSX : kSH;
-#pragma unroll
-            for (int ks = 0; ks < kChunk / 16; ++ks) {
-                uint32_t af[4];
-                ldsm_x4_trans(af, Dt + (ks * 16 + (lane & 7) + ((lane >> 4) << 3)) * ds + k.m0 + (((lane >> 3) & 1) << 3));
-                const int brow = ks * 16 + (lane & 7) + (((lane >> 3) & 1) << 3);
-#pragma unroll
-                for (int p = 0; p < 2; ++p) {
-                    uint32_t bf[4];
-                    ldsm_x4_trans(bf, Bt + brow * bs + k.n0 + 16 * p + ((lane >> 4) << 3));
-                    mma16816(acc[a][2 * p], af, bf[0], bf[1]);
-                    mma16816(acc[a][2 * p + 1], af, bf[2], bf[3]);
-                }
-                if (k.nt == 5) {
-                    uint32_t bf[2];
-                    ldsm_x2_trans(bf, Bt + brow * bs + k.n0 + 32);
-                    mma16816(acc[a][4], af, bf[0], bf[1]);
-                }
-            }
-        }
-    }
-    float* out = partial + static_cast<uint64_t>(blockIdx.x) * kNrcParams;
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        if (a >= ntask) break;
-        const WgTask k = wg_task(warp + 16 * a);
-        const int in = layer_in(k.l), outs = layer_out(k.l);
-#pragma unroll
-        for (int j = 0; j < 5; ++j) {
-            if (j >= k.nt) break;
-#pragma unroll
-            for (int c = 0; c < 4; ++c) {
-                const int m = k.m0 + g + 8 * (c >> 1);
-                const int nn = k.n0 + 8 * j + 2 * t + (c & 1);
-                if (m < outs) out[master_off(k.l) + m * in + nn] = acc[a][j][c];
-            }
-        }
+    // release TMEM only when no MMA of this CTA can still be in flight: after a
+    // timeout, wait (bounded) for the last commit first
+    if (*flag && tid == 0) (void)tc_wait(bar, phase ^ 1, kTcWaitLimit);
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(kTrCols));
     }
 }
 
 // ---------------------------------------------------------------------------
 // Adam and weight publication
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void publish_param(bf16* fwd, bf16* bwd, bf16* infer, int q, float w, float wi)
+__device__ __forceinline__ void publish_param(bf16* fwd, bf16* infer, int q, float w, float wi)
 {
     int l, o, i;
     param_coords(q, l, o, i);
-    const bf16 b = __float2bfloat16_rn(w);
-    fwd[fwd_off(l) + o * fwd_stride(l) + i] = b;
-    if (l >= 1) bwd[bwd_off(l) + i * bwd_stride(l) + o] = b;
+    fwd[fwd_off(l) + o * fwd_stride(l) + i] = __float2bfloat16_rn(w);
     infer[fwd_off(l) + o * fwd_stride(l) + i] = __float2bfloat16_rn(wi);
 }
 
 // Bias corrections 1 - beta^t of the moments and of the zero-started weight
-// average, t = the device step counter (already counting this step).
+// average, t = the device step counter + 1 (the step being taken).  Every
+// block reads the counter before it signals `done`; the last block to finish
+// advances the counter, so the next step's kernels see it incremented.
 // A block owns 32 consecutive parameters (lane = parameter, so every load of
 // a partial row is one coalesced 128-byte line); warp w sums partials w,
 // w + kAdamWarps, ... and warp 0 adds the warps' sums in order, so the
@@ -823,23 +748,30 @@ constexpr int kAdamWarps = 8;
 __global__ void __launch_bounds__(kAdamWarps * 32) k_nrc_adam(float* __restrict__ master, float* __restrict__ m,
                                                               float* __restrict__ v, const float* __restrict__ partial,
                                                               uint32_t splits, float lr, float b1, float b2, float eps,
-                                                              bf16* fwd, bf16* bwd, float* grad_out, bf16* infer,
+                                                              bf16* fwd, float* grad_out, bf16* infer,
                                                               float* __restrict__ ema, float decay,
-                                                              const uint32_t* __restrict__ step)
+                                                              uint32_t* __restrict__ step, uint32_t* __restrict__ done)
 {
     __shared__ float red[kAdamWarps][32];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int q = blockIdx.x * 32 + lane;
+    const float t = static_cast<float>(*step + 1u);
     float part = 0.0f;
     if (q < kNrcParams)
         for (uint32_t s = warp; s < splits; s += kAdamWarps) part += partial[static_cast<uint64_t>(s) * kNrcParams + q];
     red[warp][lane] = part;
     __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(done, 1u) == gridDim.x - 1) {
+            *done = 0u;
+            atomicAdd(step, 1u);
+        }
+    }
     if (warp != 0 || q >= kNrcParams) return;
     float gsum = 0.0f;
 #pragma unroll
     for (int w = 0; w < kAdamWarps; ++w) gsum += red[w][lane];
-    const float t = static_cast<float>(*step);
     const float bc1 = 1.0f - powf(b1, t), bc2 = 1.0f - powf(b2, t), ema_bc = 1.0f - powf(decay, t);
     if (grad_out) grad_out[q] = gsum;
     const float mm = b1 * m[q] + (1.0f - b1) * gsum;
@@ -854,16 +786,15 @@ __global__ void __launch_bounds__(kAdamWarps * 32) k_nrc_adam(float* __restrict_
         ema[q] = e;
         wi = e / ema_bc;
     }
-    publish_param(fwd, bwd, infer, q, w, wi);
+    publish_param(fwd, infer, q, w, wi);
 }
 
-__global__ void k_nrc_publish(const float* __restrict__ master, bf16* fwd, bf16* bwd, bf16* infer,
-                              float* __restrict__ ema)
+__global__ void k_nrc_publish(const float* __restrict__ master, bf16* fwd, bf16* infer, float* __restrict__ ema)
 {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= kNrcParams) return;
     ema[q] = 0.0f;
-    publish_param(fwd, bwd, infer, q, master[q], master[q]);
+    publish_param(fwd, infer, q, master[q], master[q]);
 }
 
 __global__ void k_nrc_blend(float* __restrict__ accum, const float* __restrict__ frame, uint64_t n, float w)
@@ -913,10 +844,6 @@ __global__ void k_nrc_targets(PathState P, NrcShade N, uint32_t n, uint32_t boun
 }
 
 int sms() { return device_sm_count(); }
-
-constexpr size_t kTrainSmem =
-    (kNrcFwdElems + kNrcBwdElems + kTrainWarps * 16 * 88) * sizeof(bf16) + kTrainWarps * 16 * sizeof(uint32_t);
-constexpr size_t kWgSmem = kWgElems * sizeof(bf16);
 
 // The shared-memory limit of a kernel is an attribute per device: raised once
 // per device (the flags are indexed by the current device).
@@ -997,38 +924,26 @@ cudaError_t launch_nrc_train_step(NrcOptimizer& O, const NrcTrainArgs& a, float*
 {
     if (a.rows == 0 || a.rows > O.max_rows) return cudaErrorInvalidValue;
     // shared-memory limits were raised by nrc_prepare (no attribute call here:
-    // this function is also recorded into a CUDA graph)
-    cudaError_t e = cudaSuccess;
-    // rows padded to whole chunks; split so that every block has whole chunks
-    const uint32_t chunks = (a.rows + kChunk - 1) / kChunk;
-    const uint32_t per = (chunks + O.max_splits - 1) / O.max_splits;
-    const uint32_t splits = (chunks + per - 1) / per;
-    const uint32_t rows_pad = splits * per * kChunk;
-    if (rows_pad > O.max_rows) return cudaErrorInvalidValue;
-    const uint64_t tiles = rows_pad / 16;
-    uint64_t blocks = (tiles + kTrainWarps - 1) / kTrainWarps;
-    const uint64_t cap = static_cast<uint64_t>(sms()) * 2;
-    if (blocks > cap) blocks = cap;
-    k_nrc_fwdbwd<<<static_cast<unsigned>(blocks), kTrainWarps * 32, kTrainSmem, st>>>(
-        static_cast<const bf16*>(O.fwd), static_cast<const bf16*>(O.bwd), a, rows_pad, O.acts, loss, O.d_step);
-    e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
-    k_nrc_wgrad<<<splits, kWgWarps * 32, kWgSmem, st>>>(O.acts, per * kChunk, O.partial, O.d_step);
-    e = cudaGetLastError();
+    // this function is also recorded into a CUDA graph).  One CTA per 128-row
+    // tile up to max_splits CTAs (each then loops over tiles); one gradient
+    // partial per CTA.
+    const uint32_t tiles = (a.rows + kTrRows - 1) / kTrRows;
+    const uint32_t splits = std::min<uint32_t>(tiles, O.max_splits);
+    k_nrc_train_tc<<<splits, kTrRows, kTrSmem, st>>>(static_cast<const bf16*>(O.fwd), a, tiles, O.partial, loss,
+                                                      O.d_step, O.err, infer_wait_limit());
+    cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     O.step += 1;
-    k_nrc_adam<<<(kNrcParams + 31) / 32, kAdamWarps * 32, 0, st>>>(O.master, O.m, O.v, O.partial, splits, O.lr, O.beta1,
-                                                        O.beta2, O.eps, static_cast<bf16*>(O.fwd),
-                                                        static_cast<bf16*>(O.bwd), grad_out,
-                                                        static_cast<bf16*>(O.infer), O.ema, O.ema_decay, O.d_step);
+    k_nrc_adam<<<(kNrcParams + 31) / 32, kAdamWarps * 32, 0, st>>>(
+        O.master, O.m, O.v, O.partial, splits, O.lr, O.beta1, O.beta2, O.eps, static_cast<bf16*>(O.fwd), grad_out,
+        static_cast<bf16*>(O.infer), O.ema, O.ema_decay, O.d_step, O.d_done);
     return cudaGetLastError();
 }
 
 cudaError_t nrc_prepare()
 {
-    static bool ok_t[kMaxDevices] = {}, ok_w[kMaxDevices] = {}, ok_i0[kMaxDevices] = {}, ok_i1[kMaxDevices] = {};
-    cudaError_t e = allow_smem(k_nrc_fwdbwd, kTrainSmem, ok_t);
-    if (e == cudaSuccess) e = allow_smem(k_nrc_wgrad, kWgSmem, ok_w);
+    static bool ok_t[kMaxDevices] = {}, ok_i0[kMaxDevices] = {}, ok_i1[kMaxDevices] = {};
+    cudaError_t e = allow_smem(k_nrc_train_tc, kTrSmem, ok_t);
     if (e == cudaSuccess) e = allow_smem(k_nrc_infer_tc<false>, kTcSmem, ok_i0);
     if (e == cudaSuccess) e = allow_smem(k_nrc_infer_tc<true>, kTcSmem, ok_i1);
     return e;
@@ -1037,8 +952,7 @@ cudaError_t nrc_prepare()
 cudaError_t launch_nrc_publish(const NrcOptimizer& O, cudaStream_t st)
 {
     k_nrc_publish<<<(kNrcParams + 255) / 256, 256, 0, st>>>(O.master, static_cast<bf16*>(O.fwd),
-                                                           static_cast<bf16*>(O.bwd), static_cast<bf16*>(O.infer),
-                                                           O.ema);
+                                                           static_cast<bf16*>(O.infer), O.ema);
     return cudaGetLastError();
 }
 

@@ -10,17 +10,15 @@
 
 namespace mt {
 
-// Network dimensions.  The output layer is padded to 8 rows for the m16n8k16
-// tensor-core tiles; rows 3..7 of its weights stay zero.
+// Network dimensions.  The output layer is padded to 8 rows in the weight
+// blob (16 in the kernels' shared-memory operands); rows 3.. stay zero.
 constexpr int kNrcIn = 80;
 constexpr int kNrcW = 64;
 constexpr int kNrcOutPad = 8;
 constexpr int kNrcParams = 80 * 64 + 3 * 64 * 64 + 64 * 3;
-// BF16 weight blobs in the padded layouts the kernels copy into shared memory:
-// forward: W_l as [out][in + 8]; backward: W_l^T as [in][out + 8] (l >= 1, the
-// output layer's transpose padded to 16 + 8 columns).
+// BF16 weight blob in the padded layout the kernels copy into shared memory:
+// W_l as [out][in + 8].  The backward pass reads the same bytes transposed.
 constexpr int kNrcFwdElems = 64 * 88 + 3 * 64 * 72 + 8 * 72;  // 20,032
-constexpr int kNrcBwdElems = 3 * 64 * 72 + 64 * 24;           // 15,360
 
 // Render-stage hooks of one wavefront batch.
 #define MT_NRC_OFF 0
@@ -53,14 +51,6 @@ struct NrcShade {
     float target_cap = 0.0f;
 };
 
-// Transposable activations of one training batch, row-major BF16 per row.
-struct NrcActs {
-    void* x;      // [rows][80]
-    void* h[4];   // [rows][64] hidden outputs after ReLU
-    void* d[4];   // [rows][64] loss gradient w.r.t. the hidden pre-activations
-    void* dy;     // [rows][8]  loss gradient w.r.t. the outputs (cols 3..7 zero)
-};
-
 // Cache queries of a batch: adds throughput * max(cache, 0) to P.indirect.
 cudaError_t launch_nrc_query(const void* net, const PathState& P, const float4* rec, const uint32_t* count,
                              uint32_t capacity, uint32_t* total, int* err, cudaStream_t st);
@@ -91,18 +81,18 @@ struct NrcOptimizer {
     float* master;      // kNrcParams fp32 weights
     float* m;           // Adam first moments
     float* v;           // Adam second moments
-    float* partial;     // splits x kNrcParams weight-gradient partial sums
-    void* fwd;          // bf16 forward blob of the trained weights
-    void* bwd;          // bf16 backward blob
-    void* infer;        // bf16 forward blob the renderer queries (moving average)
+    float* partial;     // splits x kNrcParams weight-gradient partial sums (one per training CTA)
+    void* fwd;          // bf16 blob of the trained weights
+    void* infer;        // bf16 blob the renderer queries (moving average)
     float* ema;         // fp32 moving average (zero-started, bias-corrected on use)
     float ema_decay;    // 0: infer = trained weights
-    NrcActs acts;       // sized for max_rows
-    uint32_t max_rows;  // multiple of 64
-    uint32_t max_splits;
+    uint32_t max_rows;  // rows of a step at most
+    uint32_t max_splits;  // training CTAs (gradient partials) at most
     float lr, beta1, beta2, eps;
     uint64_t step;      // Adam steps taken (host copy)
     uint32_t* d_step;   // Adam steps taken (device; the kernels' bias corrections and sample draws)
+    uint32_t* d_done;   // Adam blocks finished with the current step (the last one advances d_step)
+    int* err;           // device error word (MT_ERRBIT_TIMEOUT)
 };
 cudaError_t launch_nrc_train_step(NrcOptimizer& O, const NrcTrainArgs& a, float* loss, float* grad_out,
                                   cudaStream_t st);
