@@ -29,7 +29,9 @@ Extra keys (rank 0, one GPU): the minimal-spp search over seeds, the radiance
 cache's time to the same relMSE over seeds (`nrc`), the 256-spp throughput in
 Mrays/s with its own roofline and stage split (`throughput`), the 16 M
 incoherent-ray microbench on the 6.1 M-triangle scene (`incoherent`), the
-cache's tensor-core kernels (`nrc_kernels`) and the adjoint (`adjoint`).
+cache's tensor-core kernels (`nrc_kernels`), the adjoint (`adjoint`) and the
+radiance cache's 4-spp x 256-frame regimen with its relMSE curve
+(`nrc_regimen`).
 
 --impl reference runs the CPU arm alone: each step renders the same image on
 the host cores with the oracle (the reference itself cannot be built here);
@@ -91,6 +93,8 @@ def parse():
     p.add_argument("--nrc-end-at", type=int, default=1)
     p.add_argument("--nrc-steps", type=int, default=None)
     p.add_argument("--nrc-rows", type=int, default=1920 * 1080 * 4)
+    p.add_argument("--nrc-regimen-frames", type=int, default=256,
+                   help="frames of the 4-spp radiance-cache regimen (0: skip)")
     p.add_argument("--case", choices=["render", "adjoint", "nrc_train", "nrc_frame", "microbench"], default=None,
                    help="run one small workload of a kernel family and print its timings (profiling runs)")
     return p.parse_args()
@@ -740,6 +744,35 @@ def nrc_leg(a, ctx, ref):
             "seconds_to_target_mean": statistics.mean(ok) if ok else None}
 
 
+def nrc_regimen(a, ctx, ref, frames=256):
+    """Config 5's regimen with the library's defaults (4 spp per frame, paths
+    ending after their first diffuse-ish vertex, 65,536 training paths and 128
+    Adam steps per frame): `frames` frames folded into a running mean, each
+    timed with CUDA events; relMSE of the running mean against the reference
+    after frames 1, 2, 4, ..., frames (evaluated between frames, untimed)."""
+    import mitrace_gb300 as mt
+
+    torch = ctx.torch
+    scene, cfg = scene_and_config(a, 4, 450)
+    acc = torch.zeros_like(ref)
+    curve, total = [], 0.0
+    with mt.Tracer(scene, cfg) as tr:
+        c = tr.nrc_enable()
+        for f in range(frames):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(ctx.stream)
+            tr.nrc_frame(acc.data_ptr(), f, ctx.sptr)
+            e1.record(ctx.stream)
+            e1.synchronize()
+            total += e0.elapsed_time(e1) / 1e3
+            if (f + 1) & f == 0:  # powers of two
+                curve.append({"frames": f + 1, "seconds": total, "relmse": relmse_t(acc, ref)})
+    return {"config": {"spp_per_frame": c.spp, "end_at": c.end_at, "train_paths": c.train_paths,
+                       "train_batch": c.train_batch, "train_steps": c.train_steps, "frames": frames},
+            "ms_per_frame": total / frames * 1e3, "curve": curve,
+            "first_frames_at_target": next((x["frames"] for x in curve if x["relmse"] <= a.relmse_target), None)}
+
+
 # --------------------------------------------------------------------------- GPU arm
 def run_ours(a):
     ctx = GpuCtx(a)
@@ -811,6 +844,8 @@ def run_ours(a):
         line["nrc"] = nrc_leg(a, ctx, ref)
         if line["nrc"]["seconds_to_target"]:
             line["nrc"]["vs_plain_time"] = line["nrc"]["seconds_to_target"] / head["seconds"]
+        if a.nrc_regimen_frames:
+            line["nrc_regimen"] = nrc_regimen(a, ctx, ref, a.nrc_regimen_frames)
         del ref
         torch.cuda.empty_cache()
         line["throughput"] = throughput_leg(a, ctx, hbm_peak)
