@@ -247,6 +247,13 @@ typedef struct mt_stats {
 mt_status mt_create(const mt_scene_desc* scene, const mt_config* cfg, mt_handle** out);
 void mt_destroy(mt_handle* h);
 
+/* Device memory a destroyed handle used stays cached by the library for the
+ * next handle on the same device (at most MT_DEVICE_CACHE_BYTES per device,
+ * default an eighth of its memory; 0 turns the cache off), so that a new
+ * handle does not pay for allocating its render state again.  This call gives
+ * every cached block back to the driver.  No counterpart in the reference. */
+void mt_release_cached_memory(void);
+
 /* Starts an asynchronous render on the handle's own stream and returns.
  * Calling it while a render is running returns MT_ERR_STATE. */
 mt_status mt_start(mt_handle* h);

@@ -22,6 +22,7 @@ PROTOTYPES = [
     ("mt_config_defaults", None, [C.POINTER(mt_config)]),
     ("mt_create", C.c_int, [C.POINTER(mt_scene_desc), C.POINTER(mt_config), C.POINTER(_VP)]),
     ("mt_destroy", None, [_VP]),
+    ("mt_release_cached_memory", None, []),
     ("mt_start", C.c_int, [_VP]),
     ("mt_wait", C.c_int, [_VP, _VP]),
     ("mt_kill", C.c_int, [_VP]),

@@ -12,10 +12,12 @@
 #include <cstdlib>
 #include <cstring>
 #include <limits>
+#include <map>
 #include <mutex>
 #include <new>
 #include <string>
 #include <thread>
+#include <unordered_map>
 #include <vector>
 
 #include "../../include/mitrace_gpu.h"
@@ -99,6 +101,44 @@ void inverse4(const float* a, float* out)
     for (int i = 0; i < 16; ++i) out[i] = inv[i] * s;
 }
 
+// Device blocks released by a handle are kept for the next handle on the same
+// device instead of going back to the driver: a render's wavefront state is
+// gigabytes (3.4 GB for a 1080p 7-spp image), and cudaFree / cudaMalloc of it
+// cost milliseconds per mt_destroy / mt_create.  A request takes the smallest
+// cached block of at least its size and at most twice it.  The cache holds at
+// most MT_DEVICE_CACHE_BYTES per device (default: an eighth of the device's
+// memory; 0 disables it); mt_release_cached_memory gives every cached block
+// back.  A block enters the cache only once the device has finished with it
+// (mt_destroy synchronizes the device first, as cudaFree would).
+struct BlockCache {
+    std::mutex mu;
+    std::multimap<size_t, void*> free_blocks[64];
+    size_t cached[64] = {};
+    size_t cap[64] = {};
+    bool cap_known[64] = {};
+    std::unordered_map<void*, std::pair<int, size_t>> size_of;  // every live or cached block
+};
+// Set while mt_destroy deletes a handle after synchronizing the device: its
+// blocks can enter the cache without another synchronization.
+thread_local bool g_device_idle = false;
+BlockCache& block_cache()
+{
+    static BlockCache* c = new BlockCache();  // outlives static destruction at exit
+    return *c;
+}
+// (called with the cache's lock held)
+size_t cache_cap(BlockCache& c, int dev)
+{
+    const char* v = std::getenv("MT_DEVICE_CACHE_BYTES");
+    if (v && *v) return static_cast<size_t>(std::strtoull(v, nullptr, 10));
+    if (!c.cap_known[dev]) {
+        cudaDeviceProp prop{};
+        c.cap[dev] = cudaGetDeviceProperties(&prop, dev) == cudaSuccess ? prop.totalGlobalMem / 8 : 0;
+        c.cap_known[dev] = true;
+    }
+    return c.cap[dev];
+}
+
 // Every device allocation of a handle goes through here.  Fault injection for
 // tests: when MT_DEVICE_ALLOC_LIMIT holds a byte count, a single allocation
 // larger than that fails with cudaErrorMemoryAllocation, as if the device were
@@ -111,7 +151,109 @@ cudaError_t dev_malloc(void** p, size_t bytes)
         *p = nullptr;
         return cudaErrorMemoryAllocation;
     }
-    return cudaMalloc(p, bytes);
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= 64) return cudaMalloc(p, bytes);
+    BlockCache& c = block_cache();
+    {
+        std::lock_guard<std::mutex> lk(c.mu);
+        auto it = c.free_blocks[dev].lower_bound(bytes);
+        if (it != c.free_blocks[dev].end() && it->first <= 2 * bytes) {
+            *p = it->second;
+            c.cached[dev] -= it->first;
+            c.free_blocks[dev].erase(it);
+            return cudaSuccess;
+        }
+    }
+    e = cudaMalloc(p, bytes);
+    if (e == cudaErrorMemoryAllocation) {
+        // give the cached blocks back to the driver and try once more
+        mt_release_cached_memory();
+        (void)cudaGetLastError();
+        e = cudaMalloc(p, bytes);
+    }
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lk(c.mu);
+    c.size_of[*p] = {dev, bytes};
+    return cudaSuccess;
+}
+
+// Releases a block of dev_malloc: into the cache of its device while that has
+// room, else back to the driver.  Work still in flight may use the block, so
+// unless the device was just synchronized (mt_destroy) the device is
+// synchronized first, as cudaFree does.
+void dev_free(void* p)
+{
+    if (!p) return;
+    BlockCache& c = block_cache();
+    std::unique_lock<std::mutex> lk(c.mu);
+    auto it = c.size_of.find(p);
+    if (it == c.size_of.end()) {
+        lk.unlock();
+        cudaFree(p);
+        return;
+    }
+    const int dev = it->second.first;
+    const size_t bytes = it->second.second;
+    if (c.cached[dev] + bytes <= cache_cap(c, dev)) {
+        if (!g_device_idle) {
+            lk.unlock();
+            int cur = 0;
+            cudaGetDevice(&cur);
+            if (cur != dev) cudaSetDevice(dev);
+            const cudaError_t e = cudaDeviceSynchronize();
+            if (cur != dev) cudaSetDevice(cur);
+            lk.lock();
+            if (e != cudaSuccess) {  // a faulted context: hand the block back to the driver
+                c.size_of.erase(p);
+                lk.unlock();
+                cudaFree(p);
+                return;
+            }
+        }
+        c.free_blocks[dev].emplace(bytes, p);
+        c.cached[dev] += bytes;
+        return;
+    }
+    c.size_of.erase(it);
+    lk.unlock();
+    cudaFree(p);
+}
+
+// Pinned host words for the per-render counters, carved from pages allocated
+// once (cudaMallocHost / cudaFreeHost per handle cost far more than the
+// handle's whole scene upload).
+struct PinnedSlots {
+    std::mutex mu;
+    std::vector<unsigned long long*> free_slots;
+};
+PinnedSlots& pinned_slots()
+{
+    static PinnedSlots* s = new PinnedSlots();
+    return *s;
+}
+cudaError_t pinned_slot_alloc(unsigned long long** out)
+{
+    PinnedSlots& ps = pinned_slots();
+    std::lock_guard<std::mutex> lk(ps.mu);
+    if (ps.free_slots.empty()) {
+        constexpr size_t kSlots = 256, kWords = 4;
+        unsigned long long* page = nullptr;
+        const cudaError_t e = cudaMallocHost(reinterpret_cast<void**>(&page), kSlots * kWords * sizeof(*page));
+        if (e != cudaSuccess) return e;
+        for (size_t i = 0; i < kSlots; ++i) ps.free_slots.push_back(page + kWords * i);
+    }
+    *out = ps.free_slots.back();
+    ps.free_slots.pop_back();
+    return cudaSuccess;
+}
+void pinned_slot_free(unsigned long long* p)
+{
+    if (!p) return;
+    PinnedSlots& ps = pinned_slots();
+    std::lock_guard<std::mutex> lk(ps.mu);
+    ps.free_slots.push_back(p);
 }
 
 template <class T>
@@ -125,7 +267,7 @@ struct DevArray {
     ~DevArray() { reset(); }
     void reset()
     {
-        if (p) cudaFree(p);
+        if (p) dev_free(p);
         p = nullptr;
         n = 0;
     }
@@ -354,7 +496,7 @@ struct mt_handle {
     {
         if (worker.joinable()) worker.join();
         if (nrc.steps_graph) cudaGraphExecDestroy(nrc.steps_graph);
-        if (rays_host) cudaFreeHost(rays_host);
+        pinned_slot_free(rays_host);
         if (render_done) cudaEventDestroy(render_done);
         if (stream) cudaStreamDestroy(stream);
     }
@@ -678,7 +820,7 @@ mt_status alloc_wave(mt_handle* h, uint64_t batch)
         MT_CUDA(h->dcnt.alloc(batch));
     }
     if (!h->rays_host) {
-        MT_CUDA(cudaMallocHost(reinterpret_cast<void**>(&h->rays_host), 4 * sizeof(unsigned long long)));
+        MT_CUDA(pinned_slot_alloc(&h->rays_host));
         h->rays_host[0] = h->rays_host[1] = h->rays_host[2] = h->rays_host[3] = 0;
     }
     if (!h->render_done) MT_CUDA(cudaEventCreateWithFlags(&h->render_done, cudaEventDisableTiming));
@@ -1115,8 +1257,35 @@ void mt_destroy(mt_handle* h)
     if (!h) return;
     h->kill = 1;
     if (h->worker.joinable()) h->worker.join();
-    cudaStreamSynchronize(h->stream);
+    // work the caller enqueued on its own streams (mt_render_device, ray
+    // queries, the adjoint) may still read the handle's buffers: finish it
+    // before they are reused, as cudaFree would
+    int cur = 0;
+    cudaGetDevice(&cur);
+    const int dev = h->device;
+    if (cur != dev) cudaSetDevice(dev);
+    g_device_idle = cudaDeviceSynchronize() == cudaSuccess;
     delete h;
+    g_device_idle = false;
+    if (cur != dev) cudaSetDevice(cur);
+}
+
+void mt_release_cached_memory(void)
+{
+    BlockCache& c = block_cache();
+    std::vector<void*> blocks;
+    {
+        std::lock_guard<std::mutex> lk(c.mu);
+        for (int d = 0; d < 64; ++d) {
+            for (auto& kv : c.free_blocks[d]) {
+                blocks.push_back(kv.second);
+                c.size_of.erase(kv.second);
+            }
+            c.free_blocks[d].clear();
+            c.cached[d] = 0;
+        }
+    }
+    for (void* p : blocks) cudaFree(p);
 }
 
 mt_status mt_start(mt_handle* h)

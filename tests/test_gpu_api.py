@@ -151,3 +151,33 @@ def test_set_seed_equals_a_handle_created_with_that_seed():
         torch.cuda.synchronize()
     assert not torch.equal(a, b)
     np.testing.assert_array_equal(b.cpu().numpy(), c.cpu().numpy())
+
+
+def test_device_block_cache_reuses_memory_and_releases_it():
+    """A handle created after another was destroyed reuses its cached device
+    blocks and renders the same image; mt_release_cached_memory hands the
+    blocks back (free device memory rises); MT_DEVICE_CACHE_BYTES=0 turns the
+    cache off."""
+    torch = pytest.importorskip("torch")
+    scene, cfg = mt.box_room(width=128, height=128, samples=64, seed=9)
+    imgs = []
+    for _ in range(2):
+        with mt.Tracer(scene, cfg) as tr:
+            out = torch.zeros((128, 128, 3), device="cuda")
+            tr.render_device(out.data_ptr(), 0)
+            torch.cuda.synchronize()
+            imgs.append(out.cpu().numpy())
+    np.testing.assert_array_equal(imgs[0], imgs[1])
+    free_cached = torch.cuda.mem_get_info()[0]
+    A.lib.mt_release_cached_memory()
+    free_released = torch.cuda.mem_get_info()[0]
+    assert free_released > free_cached  # the 1 M-path wavefront went back to the driver
+    os.environ["MT_DEVICE_CACHE_BYTES"] = "0"
+    try:
+        with mt.Tracer(scene, cfg) as tr:
+            out = torch.zeros((128, 128, 3), device="cuda")
+            tr.render_device(out.data_ptr(), 0)
+            torch.cuda.synchronize()
+            np.testing.assert_array_equal(out.cpu().numpy(), imgs[0])
+    finally:
+        os.environ.pop("MT_DEVICE_CACHE_BYTES", None)
