@@ -453,7 +453,8 @@ mt_status mt_nrc_get_stats(mt_handle* h, mt_nrc_stats* out);
 mt_status mt_nrc_get_params(mt_handle* h, float* params);
 mt_status mt_nrc_set_params(mt_handle* h, const float* params);
 /* Cache outputs for n feature records (device buffers: n*20 floats in, n*3
- * out), from the weights the renderer queries (see ema_decay). */
+ * out; the records 16-byte aligned), from the weights the renderer queries
+ * (see ema_decay). */
 mt_status mt_nrc_infer(mt_handle* h, const float* d_features, uint32_t n, float* d_rgb, void* cuda_stream);
 /* One Adam step on n samples (device buffers: n*20 feature floats, n*3 target
  * floats).  d_loss (1 float, may be NULL) receives the batch's mean relative

@@ -1884,6 +1884,8 @@ mt_status mt_nrc_infer(mt_handle* h, const float* d_features, uint32_t n, float*
     mt_status rc = nrc_ready(h);
     if (rc != MT_OK) return rc;
     if (n && (!d_features || !d_rgb)) return set_err(MT_ERR_INVALID, "null argument");
+    if (reinterpret_cast<uintptr_t>(d_features) % 16)
+        return set_err(MT_ERR_INVALID, "d_features must be 16-byte aligned (records are copied as float4)");
     MT_CUDA(launch_nrc_infer(h->nrc.infer.p, d_features, n, d_rgb, h->error_flag.p + 1,
                              static_cast<cudaStream_t>(cuda_stream)));
     h->launches += n ? 1 : 0;
@@ -1896,6 +1898,8 @@ mt_status mt_nrc_train_step(mt_handle* h, const float* d_features, const float* 
     mt_status rc = nrc_ready(h);
     if (rc != MT_OK) return rc;
     if (!d_features || !d_targets) return set_err(MT_ERR_INVALID, "null argument");
+    if (reinterpret_cast<uintptr_t>(d_features) % 16)
+        return set_err(MT_ERR_INVALID, "d_features must be 16-byte aligned (records are read as float4)");
     if (n == 0 || static_cast<uint64_t>(n) > 4ull * h->nrc.cfg.train_batch)
         return set_err(MT_ERR_INVALID, "n must be in [1, 4 * train_batch]");
     cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);

@@ -160,10 +160,14 @@ constexpr int kTcW1 = kTcW0 + 64 * 80 * 2;        // 64 x 64 each
 constexpr int kTcW4 = kTcW1 + 3 * 64 * 64 * 2;    // 16 x 64 (rows 3..15 zero)
 constexpr int kTcA = kTcW4 + 16 * 64 * 2;         // per warpgroup: 128 x 80 operand tile
 constexpr int kTcABytes = kTcRows * 80 * 2;
-constexpr int kTcBar = kTcA + kTcGroups * kTcABytes;  // per warpgroup: mbarrier (8 B)
-constexpr int kTcTmem = kTcBar + 8 * kTcGroups;       // TMEM base address (4 B)
+constexpr int kTcRec = kTcA + kTcGroups * kTcABytes;  // per warpgroup: the tile's feature records
+constexpr int kTcRecBytes = kTcRows * 6 * 16;          // 128 records of up to 6 float4
+constexpr int kTcBar = kTcRec + kTcGroups * kTcRecBytes;  // per warpgroup: MMA mbarrier (8 B)
+constexpr int kTcRecBar = kTcBar + 8 * kTcGroups;     // per warpgroup: record-copy mbarrier (8 B)
+constexpr int kTcTmem = kTcRecBar + 8 * kTcGroups;    // TMEM base address (4 B)
 constexpr int kTcFlag = kTcTmem + 4;                  // per warpgroup: timeout flag (4 B)
 constexpr int kTcSmem = kTcFlag + 4 * kTcGroups;
+static_assert(kTcRec % 16 == 0 && kTcRecBytes % 16 == 0, "bulk-copy alignment");
 constexpr uint32_t kTcCols = 64 * kTcGroups;          // TMEM columns per CTA
 constexpr uint32_t kTcWaitLimit = 1u << 24;           // mbarrier polls before giving up
 
@@ -256,6 +260,34 @@ __device__ __forceinline__ void tc_layer(uint32_t tmem, uint32_t a_base, uint32_
     tc_commit(bar);
 }
 
+// Copies the forward weight blob into the canonical K-major operands at
+// kTcW0.. (W0 64 x 80, W1..W3 64 x 64, W4 16 x 64 with rows 3..15 zero).
+// Thread i writes the i-th 16-byte chunk of the operand region, so a warp's
+// shared-memory stores are contiguous (8 rows of one core matrix, then the
+// next core matrix); the blob reads are L2 hits.
+__device__ __forceinline__ void stage_weights(const bf16* __restrict__ blob, unsigned char* smem)
+{
+    constexpr uint32_t kChunks = (64 * 80 + 3 * 64 * 64 + 16 * 64) / 8;  // 16-byte chunks
+    for (uint32_t d = threadIdx.x; d < kChunks; d += blockDim.x) {
+        uint32_t l, off;
+        if (d < 640) {
+            l = 0; off = d;
+        } else if (d < 640 + 1536) {
+            l = 1 + (d - 640) / 512; off = (d - 640) % 512;
+        } else {
+            l = 4; off = d - 2176;
+        }
+        const uint32_t kc = l == 0 ? 10 : 8;
+        // canonical chunk index = ((r >> 3) * kc + c) * 8 + (r & 7)
+        const uint32_t r = (off / (8 * kc)) * 8 + (off & 7), c = (off / 8) % kc;
+        const uint32_t base = l == 0 ? kTcW0 : (l == 4 ? kTcW4 : kTcW1 + (l - 1) * 64 * 64 * 2);
+        uint4 v = make_uint4(0u, 0u, 0u, 0u);
+        if (l < 4 || r < 8)  // output rows 8..15 stay zero (the blob pads to 8)
+            v = *reinterpret_cast<const uint4*>(blob + fwd_off(l) + r * fwd_stride(l) + 8 * c);
+        *reinterpret_cast<uint4*>(smem + base + 16 * off) = v;
+    }
+}
+
 template <bool PATHS>
 __global__ void __launch_bounds__(kTcRows * kTcGroups) k_nrc_infer_tc(const bf16* __restrict__ blob,
                                                                       const float4* __restrict__ feat, uint32_t n_host,
@@ -269,29 +301,13 @@ __global__ void __launch_bounds__(kTcRows * kTcGroups) k_nrc_infer_tc(const bf16
     const uint32_t s0 = static_cast<uint32_t>(__cvta_generic_to_shared(smem));
     const uint32_t tid = threadIdx.x, warp = tid >> 5;
     const uint32_t group = tid >> 7, row = tid & 127;
-    // weights: padded rows of the forward blob -> canonical K-major operands
-    for (uint32_t i = tid; i < 64 * 10 + 3 * 64 * 8 + 16 * 8; i += blockDim.x) {
-        uint32_t l, r, c;
-        if (i < 640) {
-            l = 0; r = i / 10; c = i % 10;
-        } else if (i < 640 + 1536) {
-            const uint32_t j = i - 640;
-            l = 1 + j / 512; r = (j % 512) / 8; c = j % 8;
-        } else {
-            const uint32_t j = i - 2176;
-            l = 4; r = j / 8; c = j % 8;
-        }
-        const uint32_t kc = l == 0 ? 10 : 8;
-        const uint32_t base = l == 0 ? kTcW0 : (l == 4 ? kTcW4 : kTcW1 + (l - 1) * 64 * 64 * 2);
-        uint4 v = make_uint4(0u, 0u, 0u, 0u);
-        if (l < 4 || r < 8)  // output rows 8..15 stay zero (the blob pads to 8)
-            v = *reinterpret_cast<const uint4*>(blob + fwd_off(l) + r * fwd_stride(l) + 8 * c);
-        *reinterpret_cast<uint4*>(smem + base + canon_off(r, 8 * c, kc)) = v;
-    }
+    stage_weights(blob, smem);
     const uint32_t bar = s0 + kTcBar + 8 * group;
+    const uint32_t rbar = s0 + kTcRecBar + 8 * group;
     volatile int* flag = reinterpret_cast<volatile int*>(smem + kTcFlag) + group;
     if (row == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(rbar));
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
         *flag = 0;
     }
@@ -312,17 +328,50 @@ __global__ void __launch_bounds__(kTcRows * kTcGroups) k_nrc_infer_tc(const bf16
     const uint32_t n = PATHS ? *count : n_host;
     if (total && blockIdx.x == 0 && tid == 0) atomicAdd(total, n);
     const uint32_t tiles = (n + kTcRows - 1) / kTcRows;
-    uint32_t phase = 0;
-    for (uint32_t tile = blockIdx.x * kTcGroups + group; tile < tiles; tile += gridDim.x * kTcGroups) {
+    constexpr uint32_t kStride = PATHS ? 6 : 5;  // float4 per record
+    const float4* rec = reinterpret_cast<const float4*>(smem + kTcRec + group * kTcRecBytes);
+    const uint32_t rec_s = s0 + kTcRec + group * kTcRecBytes;
+    // the records of a tile arrive as one bulk copy (TMA) completing on rbar,
+    // issued by row 0 one tile ahead (while the current tile's MMAs run)
+    auto fetch_records = [&](uint32_t t) {
+        if (row != 0 || t >= tiles) return;
+        const uint32_t rows = min(static_cast<uint32_t>(kTcRows), n - t * kTcRows);
+        const uint32_t bytes = rows * kStride * 16u;
+        const float4* src = feat + static_cast<uint64_t>(t) * kTcRows * kStride;
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(rbar), "r"(bytes) : "memory");
+        asm volatile(
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(rec_s),
+            "l"(src), "r"(bytes), "r"(rbar)
+            : "memory");
+    };
+    uint32_t phase = 0, rphase = 0;
+    bool copy_pending = false;  // a record copy was issued and not yet waited for
+    const uint32_t first_tile = blockIdx.x * kTcGroups + group;
+    fetch_records(first_tile);
+    copy_pending = first_tile < tiles;
+    for (uint32_t tile = first_tile; tile < tiles; tile += gridDim.x * kTcGroups) {
         const uint32_t r = tile * kTcRows + row;
+        if (tc_wait(rbar, rphase, wait_limit)) {
+            rphase ^= 1;
+            copy_pending = false;
+        } else {
+            *flag = 1;  // the copy stays pending; the exit path waits for it (parity rphase)
+        }
+        group_sync(group);
+        if (*flag) {
+            if (row == 0) atomicOr(err, MT_ERRBIT_TIMEOUT);
+            break;
+        }
+        float4 thr = make_float4(0.0f, 0.0f, 0.0f, 0.0f);  // PATHS: throughput, path index
         // layer-0 operand: this thread's row, encoded
         {
             float e[80];
             if (r < n) {
-                const float4* f = feat + static_cast<uint64_t>(r) * (PATHS ? 6 : 5);
+                const float4* f = rec + row * kStride;
                 auto put = [&](int k, float v) { e[k] = v; };
                 encode_part0(f[0], f[3], f[4], put);
                 encode_part1(f[1], f[2], put);
+                if (PATHS) thr = f[5];
             } else {
 #pragma unroll
                 for (int k = 0; k < 80; ++k) e[k] = 0.0f;
@@ -345,6 +394,11 @@ __global__ void __launch_bounds__(kTcRows * kTcGroups) k_nrc_infer_tc(const bf16
             if (row == 0) {
                 const uint32_t w = l == 0 ? kTcW0 : (l == 4 ? kTcW4 : kTcW1 + (l - 1) * 64 * 64 * 2);
                 tc_layer(tmem, a_s, s0 + w, l == 0 ? 10 : 8, l == 4 ? 16 : 64, bar);
+            }
+            if (l == 0) {
+                // every row of the group has read its record: the buffer takes the next tile's
+                fetch_records(tile + gridDim.x * kTcGroups);
+                copy_pending = tile + gridDim.x * kTcGroups < tiles;
             }
             if (!tc_wait(bar, phase, wait_limit)) *flag = 1;
             phase ^= 1;
@@ -381,7 +435,7 @@ __global__ void __launch_bounds__(kTcRows * kTcGroups) k_nrc_infer_tc(const bf16
         }
         if (r < n) {
             if (PATHS) {
-                const float4 q = feat[6ull * r + 5];  // throughput, path index
+                const float4 q = thr;
                 const uint32_t p = __float_as_uint(q.w);
                 const float4 a = P.indirect[p];
                 P.indirect[p] = make_float4(a.x + q.x * fmaxf(y[0], 0.0f), a.y + q.y * fmaxf(y[1], 0.0f),
@@ -394,8 +448,10 @@ __global__ void __launch_bounds__(kTcRows * kTcGroups) k_nrc_infer_tc(const bf16
         }
     }
     // release TMEM only when no MMA of this CTA can still be in flight: after a
-    // timeout, wait (bounded) for the warpgroup's last commit first
+    // timeout, wait (bounded) for the warpgroup's last commit first; and do not
+    // leave while a record copy still writes this CTA's shared memory
     if (*flag && row == 0) (void)tc_wait(bar, phase ^ 1, kTcWaitLimit);
+    if (copy_pending && row == 0) (void)tc_wait(rbar, rphase, kTcWaitLimit);
     tc_fence_before();
     __syncthreads();
     if (warp == 0) {
@@ -497,24 +553,7 @@ __global__ void __launch_bounds__(kTrRows) k_nrc_train_tc(const bf16* __restrict
     unsigned char* smem = tc_smem;
     const uint32_t s0 = static_cast<uint32_t>(__cvta_generic_to_shared(smem));
     const uint32_t tid = threadIdx.x, warp = tid >> 5, row = tid;
-    // forward weights, canonical K-major (N = out rows, K = in)
-    for (uint32_t i = tid; i < 64 * 10 + 3 * 64 * 8 + 16 * 8; i += blockDim.x) {
-        uint32_t l, r, c;
-        if (i < 640) {
-            l = 0; r = i / 10; c = i % 10;
-        } else if (i < 640 + 1536) {
-            const uint32_t j = i - 640;
-            l = 1 + j / 512; r = (j % 512) / 8; c = j % 8;
-        } else {
-            const uint32_t j = i - 2176;
-            l = 4; r = j / 8; c = j % 8;
-        }
-        const uint32_t kc = l == 0 ? 10 : 8;
-        uint4 v = make_uint4(0u, 0u, 0u, 0u);
-        if (l < 4 || r < 8)
-            v = *reinterpret_cast<const uint4*>(fwd + fwd_off(l) + r * fwd_stride(l) + 8 * c);
-        *reinterpret_cast<uint4*>(smem + tr_w(l) + canon_off(r, 8 * c, kc)) = v;
-    }
+    stage_weights(fwd, smem);  // forward weights, canonical K-major (N = out rows, K = in)
     const uint32_t bar = s0 + kTrBar;
     volatile int* flag = reinterpret_cast<volatile int*>(smem + kTrFlag);
     if (tid == 0) {

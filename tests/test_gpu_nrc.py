@@ -280,3 +280,15 @@ def test_cache_spp_above_the_handle_samples_regrows_the_wavefront():
         torch.cuda.synchronize()
     np.testing.assert_array_equal(acc.cpu().numpy(), ref6.cpu().numpy())
     np.testing.assert_array_equal(after.cpu().numpy(), before.cpu().numpy())
+
+
+def test_misaligned_feature_records_are_rejected():
+    import ctypes as C
+
+    scene, cfg = small_room()
+    with mt.Tracer(scene, cfg) as tr:
+        tr.nrc_enable(train_paths=2048, train_batch=1024, spp=2)
+        f = torch.zeros(4 * 20 + 1, device="cuda")
+        out = torch.zeros(4 * 3, device="cuda")
+        rc = A.lib.mt_nrc_infer(tr.handle, C.c_void_p(f.data_ptr() + 4), 4, C.c_void_p(out.data_ptr()), None)
+        assert rc == A.MT_ERR_INVALID and "aligned" in A.lib.mt_last_error().decode()
