@@ -28,10 +28,13 @@ class Stats:
 
 
 class Tracer:
-    def __init__(self, scene: SceneData, config: A.mt_config):
+    def __init__(self, scene: SceneData, config: A.mt_config, packed: PackedScene = None):
+        """mt_create over the scene's host arrays.  `packed` (a PackedScene of
+        the same scene) saves re-building the C descriptor structs when one
+        scene is handed to many tracers; the data is uploaded either way."""
         self.scene = scene
         self.config = config
-        self._packed = PackedScene(scene)
+        self._packed = packed if packed is not None else PackedScene(scene)
         h = C.c_void_p()
         A.check(A.lib.mt_create(self._packed.ptr(), C.byref(config), C.byref(h)), "mt_create")
         self.handle = h
