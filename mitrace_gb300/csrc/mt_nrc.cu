@@ -13,8 +13,8 @@
 //                  TMEM, the backward and weight-gradient operands read as
 //                  transposed (MN-major) views of the forward ones; one
 //                  gradient partial per CTA.
-//   k_nrc_adam     sums the partials in block order, Adam, and rewrites the BF16
-//                  weight blobs.
+//   k_nrc_adam     sums the partials in a fixed order, Adam, and rewrites the
+//                  BF16 weight blobs (the kernels' shared-memory operand image).
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
@@ -34,12 +34,17 @@ using bf16 = __nv_bfloat16;
 // ---------------------------------------------------------------------------
 // Layouts
 // ---------------------------------------------------------------------------
-__host__ __device__ constexpr int fwd_off(int l) { return l == 0 ? 0 : 64 * 88 + (l - 1) * 64 * 72; }
-__host__ __device__ constexpr int fwd_stride(int l) { return l == 0 ? 88 : 72; }
-__host__ __device__ constexpr int master_off(int l) { return l == 0 ? 0 : 5120 + (l - 1) * 4096; }
+// element offset of W_l in the blob, and of its (o, i) entry: core matrix
+// (o / 8, i / 8) of the K-major operand, 8 x 8 elements each
+__host__ __device__ constexpr int blob_off(int l) { return l == 0 ? 0 : 64 * 80 + (l - 1) * 64 * 64; }
 __host__ __device__ constexpr int layer_in(int l) { return l == 0 ? 80 : 64; }
+__host__ __device__ constexpr int blob_index(int l, int o, int i)
+{
+    return blob_off(l) + ((o >> 3) * (layer_in(l) >> 3) + (i >> 3)) * 64 + (o & 7) * 8 + (i & 7);
+}
+__host__ __device__ constexpr int master_off(int l) { return l == 0 ? 0 : 5120 + (l - 1) * 4096; }
 __host__ __device__ constexpr int layer_out(int l) { return l == 4 ? 3 : 64; }
-static_assert(fwd_off(4) + 8 * 72 == kNrcFwdElems, "forward blob size");
+static_assert(blob_off(4) + 16 * 64 == kNrcFwdElems, "forward blob size");
 static_assert(master_off(4) + 3 * 64 == kNrcParams, "parameter count");
 
 __device__ __forceinline__ void param_coords(int q, int& l, int& o, int& i)
@@ -164,10 +169,13 @@ constexpr int kTcRec = kTcA + kTcGroups * kTcABytes;  // per warpgroup: the tile
 constexpr int kTcRecBytes = kTcRows * 6 * 16;          // 128 records of up to 6 float4
 constexpr int kTcBar = kTcRec + kTcGroups * kTcRecBytes;  // per warpgroup: MMA mbarrier (8 B)
 constexpr int kTcRecBar = kTcBar + 8 * kTcGroups;     // per warpgroup: record-copy mbarrier (8 B)
-constexpr int kTcTmem = kTcRecBar + 8 * kTcGroups;    // TMEM base address (4 B)
+constexpr int kTcWBar = kTcRecBar + 8 * kTcGroups;    // weight-copy mbarrier (8 B)
+constexpr int kTcTmem = kTcWBar + 8;                  // TMEM base address (4 B)
 constexpr int kTcFlag = kTcTmem + 4;                  // per warpgroup: timeout flag (4 B)
 constexpr int kTcSmem = kTcFlag + 4 * kTcGroups;
 static_assert(kTcRec % 16 == 0 && kTcRecBytes % 16 == 0, "bulk-copy alignment");
+constexpr uint32_t kTcWBytes = kNrcFwdElems * 2;       // the weight blob = the operands at kTcW0..
+static_assert(kTcA == kTcW0 + static_cast<int>(kTcWBytes) && kTcWBytes % 16 == 0, "weight image");
 constexpr uint32_t kTcCols = 64 * kTcGroups;          // TMEM columns per CTA
 constexpr uint32_t kTcWaitLimit = 1u << 24;           // mbarrier polls before giving up
 
@@ -260,32 +268,16 @@ __device__ __forceinline__ void tc_layer(uint32_t tmem, uint32_t a_base, uint32_
     tc_commit(bar);
 }
 
-// Copies the forward weight blob into the canonical K-major operands at
-// kTcW0.. (W0 64 x 80, W1..W3 64 x 64, W4 16 x 64 with rows 3..15 zero).
-// Thread i writes the i-th 16-byte chunk of the operand region, so a warp's
-// shared-memory stores are contiguous (8 rows of one core matrix, then the
-// next core matrix); the blob reads are L2 hits.
-__device__ __forceinline__ void stage_weights(const bf16* __restrict__ blob, unsigned char* smem)
+// The weight blob is the operand image at kTcW0: one bulk copy (TMA) into
+// shared memory completing on the mbarrier wbar (initialised, count 1, by the
+// calling thread, which alone issues it).
+__device__ __forceinline__ void fetch_weights(const bf16* __restrict__ blob, uint32_t smem_w, uint32_t wbar)
 {
-    constexpr uint32_t kChunks = (64 * 80 + 3 * 64 * 64 + 16 * 64) / 8;  // 16-byte chunks
-    for (uint32_t d = threadIdx.x; d < kChunks; d += blockDim.x) {
-        uint32_t l, off;
-        if (d < 640) {
-            l = 0; off = d;
-        } else if (d < 640 + 1536) {
-            l = 1 + (d - 640) / 512; off = (d - 640) % 512;
-        } else {
-            l = 4; off = d - 2176;
-        }
-        const uint32_t kc = l == 0 ? 10 : 8;
-        // canonical chunk index = ((r >> 3) * kc + c) * 8 + (r & 7)
-        const uint32_t r = (off / (8 * kc)) * 8 + (off & 7), c = (off / 8) % kc;
-        const uint32_t base = l == 0 ? kTcW0 : (l == 4 ? kTcW4 : kTcW1 + (l - 1) * 64 * 64 * 2);
-        uint4 v = make_uint4(0u, 0u, 0u, 0u);
-        if (l < 4 || r < 8)  // output rows 8..15 stay zero (the blob pads to 8)
-            v = *reinterpret_cast<const uint4*>(blob + fwd_off(l) + r * fwd_stride(l) + 8 * c);
-        *reinterpret_cast<uint4*>(smem + base + 16 * off) = v;
-    }
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(wbar), "r"(kTcWBytes) : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+                     smem_w),
+                 "l"(blob), "r"(kTcWBytes), "r"(wbar)
+                 : "memory");
 }
 
 template <bool PATHS>
@@ -301,15 +293,17 @@ __global__ void __launch_bounds__(kTcRows * kTcGroups) k_nrc_infer_tc(const bf16
     const uint32_t s0 = static_cast<uint32_t>(__cvta_generic_to_shared(smem));
     const uint32_t tid = threadIdx.x, warp = tid >> 5;
     const uint32_t group = tid >> 7, row = tid & 127;
-    stage_weights(blob, smem);
     const uint32_t bar = s0 + kTcBar + 8 * group;
     const uint32_t rbar = s0 + kTcRecBar + 8 * group;
+    const uint32_t wbar = s0 + kTcWBar;
     volatile int* flag = reinterpret_cast<volatile int*>(smem + kTcFlag) + group;
     if (row == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar));
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(rbar));
+        if (tid == 0) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(wbar));
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
         *flag = 0;
+        if (tid == 0) fetch_weights(blob, s0 + kTcW0, wbar);
     }
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(s0 + kTcTmem),
@@ -349,6 +343,12 @@ __global__ void __launch_bounds__(kTcRows * kTcGroups) k_nrc_infer_tc(const bf16
     const uint32_t first_tile = blockIdx.x * kTcGroups + group;
     fetch_records(first_tile);
     copy_pending = first_tile < tiles;
+    // the MMA issuer of each warpgroup waits for the weights once
+    bool w_ready = true;
+    if (row == 0 && !tc_wait(wbar, 0, wait_limit)) {
+        w_ready = false;
+        *flag = 1;  // seen after the first group_sync below
+    }
     for (uint32_t tile = first_tile; tile < tiles; tile += gridDim.x * kTcGroups) {
         const uint32_t r = tile * kTcRows + row;
         if (tc_wait(rbar, rphase, wait_limit)) {
@@ -452,6 +452,7 @@ __global__ void __launch_bounds__(kTcRows * kTcGroups) k_nrc_infer_tc(const bf16
     // leave while a record copy still writes this CTA's shared memory
     if (*flag && row == 0) (void)tc_wait(bar, phase ^ 1, kTcWaitLimit);
     if (copy_pending && row == 0) (void)tc_wait(rbar, rphase, kTcWaitLimit);
+    if (!w_ready) (void)tc_wait(wbar, 0, kTcWaitLimit);
     tc_fence_before();
     __syncthreads();
     if (warp == 0) {
@@ -516,7 +517,8 @@ constexpr int kTrDY = kTrH + 4 * kTrRows * 64 * 2;  // dY: 128 x 64 (128 x 16 at
 // operand read reaches past the allocation (checked below)
 constexpr int kTrPad = kTrDY + kTrRows * 64 * 2;
 constexpr int kTrBar = kTrPad + 8192;
-constexpr int kTrTmem = kTrBar + 8;
+constexpr int kTrWBar = kTrBar + 8;  // weight-copy mbarrier
+constexpr int kTrTmem = kTrWBar + 8;
 constexpr int kTrFlag = kTrTmem + 4;
 constexpr int kTrSmem = kTrFlag + 12;
 constexpr uint32_t kTrCols = 512;
@@ -553,13 +555,17 @@ __global__ void __launch_bounds__(kTrRows) k_nrc_train_tc(const bf16* __restrict
     unsigned char* smem = tc_smem;
     const uint32_t s0 = static_cast<uint32_t>(__cvta_generic_to_shared(smem));
     const uint32_t tid = threadIdx.x, warp = tid >> 5, row = tid;
-    stage_weights(fwd, smem);  // forward weights, canonical K-major (N = out rows, K = in)
-    const uint32_t bar = s0 + kTrBar;
+    const uint32_t bar = s0 + kTrBar, wbar = s0 + kTrWBar;
     volatile int* flag = reinterpret_cast<volatile int*>(smem + kTrFlag);
+    // forward weights (canonical K-major, N = out rows, K = in) by one bulk
+    // copy, in flight while the rows are gathered and encoded
+    bool w_wait = tid == 0;  // the MMA issuer still has to see the weights arrive
     if (tid == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(wbar));
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
         *flag = 0;
+        fetch_weights(fwd, s0 + kTcW0, wbar);
     }
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(s0 + kTrTmem),
@@ -619,7 +625,17 @@ __global__ void __launch_bounds__(kTrRows) k_nrc_train_tc(const bf16* __restrict
                     make_uint4(pack2(e[8 * c], e[8 * c + 1]), pack2(e[8 * c + 2], e[8 * c + 3]),
                                pack2(e[8 * c + 4], e[8 * c + 5]), pack2(e[8 * c + 6], e[8 * c + 7]));
         }
+        if (w_wait) {
+            if (tc_wait(wbar, 0, wait_limit))
+                w_wait = false;
+            else
+                *flag = 1;
+        }
         publish();
+        if (*flag) {
+            timed_out = true;
+            break;
+        }
         // forward
         uint32_t mask[4][2];
 #pragma unroll 1
@@ -755,6 +771,7 @@ __global__ void __launch_bounds__(kTrRows) k_nrc_train_tc(const bf16* __restrict
     // release TMEM only when no MMA of this CTA can still be in flight: after a
     // timeout, wait (bounded) for the last commit first
     if (*flag && tid == 0) (void)tc_wait(bar, phase ^ 1, kTcWaitLimit);
+    if (w_wait) (void)tc_wait(wbar, 0, kTcWaitLimit);  // the weight copy still writes shared memory
     tc_fence_before();
     __syncthreads();
     if (warp == 0) {
@@ -770,8 +787,8 @@ __device__ __forceinline__ void publish_param(bf16* fwd, bf16* infer, int q, flo
 {
     int l, o, i;
     param_coords(q, l, o, i);
-    fwd[fwd_off(l) + o * fwd_stride(l) + i] = __float2bfloat16_rn(w);
-    infer[fwd_off(l) + o * fwd_stride(l) + i] = __float2bfloat16_rn(wi);
+    fwd[blob_index(l, o, i)] = __float2bfloat16_rn(w);
+    infer[blob_index(l, o, i)] = __float2bfloat16_rn(wi);
 }
 
 // Bias corrections 1 - beta^t of the moments and of the zero-started weight
@@ -779,10 +796,11 @@ __device__ __forceinline__ void publish_param(bf16* fwd, bf16* infer, int q, flo
 // block reads the counter before it signals `done`; the last block to finish
 // advances the counter, so the next step's kernels see it incremented.
 // A block owns 32 consecutive parameters (lane = parameter, so every load of
-// a partial row is one coalesced 128-byte line); warp w sums partials w,
-// w + kAdamWarps, ... and warp 0 adds the warps' sums in order, so the
-// gradient is the same on every run.
-constexpr int kAdamWarps = 8;
+// a partial row is one coalesced 128-byte line); warp w loads partials w,
+// w + kAdamWarps, ..., w + 7 kAdamWarps at once and adds them pairwise, and
+// warp 0 adds the warps' sums in order, so the gradient is the same on every
+// run.
+constexpr int kAdamWarps = 16;
 
 __global__ void __launch_bounds__(kAdamWarps * 32) k_nrc_adam(float* __restrict__ master, float* __restrict__ m,
                                                               float* __restrict__ v, const float* __restrict__ partial,
@@ -796,8 +814,17 @@ __global__ void __launch_bounds__(kAdamWarps * 32) k_nrc_adam(float* __restrict_
     const int q = blockIdx.x * 32 + lane;
     const float t = static_cast<float>(*step + 1u);
     float part = 0.0f;
-    if (q < kNrcParams)
-        for (uint32_t s = warp; s < splits; s += kAdamWarps) part += partial[static_cast<uint64_t>(s) * kNrcParams + q];
+    if (q < kNrcParams) {
+        float acc[8];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const uint32_t s = warp + k * kAdamWarps;
+            acc[k] = s < splits ? partial[static_cast<uint64_t>(s) * kNrcParams + q] : 0.0f;
+        }
+        part = ((acc[0] + acc[1]) + (acc[2] + acc[3])) + ((acc[4] + acc[5]) + (acc[6] + acc[7]));
+        for (uint32_t s = warp + 8 * kAdamWarps; s < splits; s += kAdamWarps)
+            part += partial[static_cast<uint64_t>(s) * kNrcParams + q];
+    }
     red[warp][lane] = part;
     __syncthreads();
     if (threadIdx.x == 0) {

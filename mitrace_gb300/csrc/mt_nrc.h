@@ -16,9 +16,12 @@ constexpr int kNrcIn = 80;
 constexpr int kNrcW = 64;
 constexpr int kNrcOutPad = 8;
 constexpr int kNrcParams = 80 * 64 + 3 * 64 * 64 + 64 * 3;
-// BF16 weight blob in the padded layout the kernels copy into shared memory:
-// W_l as [out][in + 8].  The backward pass reads the same bytes transposed.
-constexpr int kNrcFwdElems = 64 * 88 + 3 * 64 * 72 + 8 * 72;  // 20,032
+// BF16 weight blob: byte for byte the shared-memory operands of the tensor-core
+// kernels (W_l as N = out rows x K = in, canonical K-major core matrices of 8
+// rows x 16 bytes; the output layer padded to 16 rows, rows 3.. zero), so a
+// kernel takes it with one bulk copy.  The backward pass reads the same bytes
+// transposed.
+constexpr int kNrcFwdElems = 64 * 80 + 3 * 64 * 64 + 16 * 64;  // 18,432 (36,864 bytes)
 
 // Render-stage hooks of one wavefront batch.
 #define MT_NRC_OFF 0
