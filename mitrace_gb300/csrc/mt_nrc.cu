@@ -246,6 +246,32 @@ __device__ __forceinline__ void tc_ld16(uint32_t taddr, float (&v)[16])
 }
 
 __device__ __forceinline__ void tc_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory"); }
+// Ties the registers of a TMEM load to the point after tcgen05.wait::ld: the
+// empty statement is ordered after the wait (both volatile) and every later use
+// reads its outputs, so no use can be scheduled before the data has arrived.
+__device__ __forceinline__ void tc_touch16(float (&v)[16])
+{
+    asm volatile(""
+                 : "+f"(v[0]), "+f"(v[1]), "+f"(v[2]), "+f"(v[3]), "+f"(v[4]), "+f"(v[5]), "+f"(v[6]), "+f"(v[7]),
+                   "+f"(v[8]), "+f"(v[9]), "+f"(v[10]), "+f"(v[11]), "+f"(v[12]), "+f"(v[13]), "+f"(v[14]),
+                   "+f"(v[15]));
+}
+// 16 columns, waited for
+__device__ __forceinline__ void tc_load16(uint32_t taddr, float (&v)[16])
+{
+    tc_ld16(taddr, v);
+    tc_wait_ld();
+    tc_touch16(v);
+}
+// 64 consecutive columns: four loads in flight, one wait
+__device__ __forceinline__ void tc_load64(uint32_t taddr, float (&v)[4][16])
+{
+#pragma unroll
+    for (int q = 0; q < 4; ++q) tc_ld16(taddr + 16 * q, v[q]);
+    tc_wait_ld();
+#pragma unroll
+    for (int q = 0; q < 4; ++q) tc_touch16(v[q]);
+}
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory"); }
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
@@ -409,11 +435,11 @@ __global__ void __launch_bounds__(kTcRows * kTcGroups) k_nrc_infer_tc(const bf16
             }
             tc_fence_after();
             if (l < 4) {
+                float vq[4][16];
+                tc_load64(lane_addr, vq);
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {
-                    float v[16];
-                    tc_ld16(lane_addr + 16 * q, v);
-                    tc_wait_ld();
+                    const float* v = vq[q];
 #pragma unroll
                     for (int c = 0; c < 2; ++c) {
                         const float* x = v + 8 * c;
@@ -425,8 +451,7 @@ __global__ void __launch_bounds__(kTcRows * kTcGroups) k_nrc_infer_tc(const bf16
                     }
                 }
             } else {
-                tc_ld16(lane_addr, y);
-                tc_wait_ld();
+                tc_load16(lane_addr, y);
             }
         }
         if (timed_out) {
@@ -608,6 +633,11 @@ __global__ void __launch_bounds__(kTrRows) k_nrc_train_tc(const bf16* __restrict
         const uint32_t r = tile * kTrRows + row;
         const bool valid = r < n;
         const uint32_t sample = a.count ? (n ? mix32(base + r) % cnt : 0u) : r;
+        float target[3] = {0.0f, 0.0f, 0.0f};  // loaded with the record, used after the forward pass
+        if (valid) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) target[c] = a.targets[static_cast<uint64_t>(sample) * a.tstride + c];
+        }
         {  // encoded input row
             float e[80];
             if (valid) {
@@ -653,11 +683,11 @@ __global__ void __launch_bounds__(kTrRows) k_nrc_train_tc(const bf16* __restrict
             if (l < 4) {
                 uint32_t m0 = 0, m1 = 0;
                 unsigned char* H = smem + tr_act(l + 1);
+                float vq[4][16];
+                tc_load64(lane_addr, vq);
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {
-                    float v[16];
-                    tc_ld16(lane_addr + 16 * q, v);
-                    tc_wait_ld();
+                    float* v = vq[q];
                     uint32_t bits = 0;
 #pragma unroll
                     for (int j = 0; j < 16; ++j) {
@@ -676,15 +706,13 @@ __global__ void __launch_bounds__(kTrRows) k_nrc_train_tc(const bf16* __restrict
                 mask[l][1] = m1;
             } else {
                 float y[16];
-                tc_ld16(lane_addr, y);
-                tc_wait_ld();
+                tc_load16(lane_addr, y);
                 // relative L2 loss |y - t|^2 / (y^2 + 0.01), y constant in the denominator
                 float dy[3] = {0.0f, 0.0f, 0.0f};
                 if (valid) {
 #pragma unroll
                     for (int c = 0; c < 3; ++c) {
-                        const float target = a.targets[static_cast<uint64_t>(sample) * a.tstride + c];
-                        const float diff = y[c] - target;
+                        const float diff = y[c] - target[c];
                         const float den = y[c] * y[c] + 0.01f;
                         lsum += diff * diff / den;
                         dy[c] = 2.0f * diff / den * scale;
@@ -718,11 +746,11 @@ __global__ void __launch_bounds__(kTrRows) k_nrc_train_tc(const bf16* __restrict
             }
             if (l == 0) break;
             // dY_{l-1} = dH masked by the ReLU of H_{l-1}
+            float vq[4][16];
+            tc_load64(lane_addr + 64, vq);
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
-                float v[16];
-                tc_ld16(lane_addr + 64 + 16 * q, v);
-                tc_wait_ld();
+                float* v = vq[q];
                 const uint32_t bits = (q < 2 ? mask[l - 1][0] >> (16 * q) : mask[l - 1][1] >> (16 * (q - 2)));
 #pragma unroll
                 for (int j = 0; j < 16; ++j)
@@ -747,8 +775,7 @@ __global__ void __launch_bounds__(kTrRows) k_nrc_train_tc(const bf16* __restrict
             const int nq = l == 4 ? 1 : 4;
             for (int q = 0; q < nq; ++q) {
                 float v[16];
-                tc_ld16(lane_addr + 128 + 64 * l + 16 * q, v);
-                tc_wait_ld();
+                tc_load16(lane_addr + 128 + 64 * l + 16 * q, v);
                 if (static_cast<int>(row) < in) {
 #pragma unroll
                     for (int j = 0; j < 16; ++j) {
