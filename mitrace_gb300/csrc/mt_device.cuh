@@ -273,6 +273,43 @@ __device__ __forceinline__ bool tri_test(f3 o, f3 d, f3 v0, f3 e1, f3 e2, float&
     return true;
 }
 
+// tri_test in three stages, so that a warp can vote between them: begin()
+// applies the determinant and u rejections, second() the v rejection,
+// finish() forms t and applies 0 < t < dist (each called on every lane, with
+// the lane's result so far where it matters).  The same operations, values and
+// decisions as tri_test followed by that range check.
+struct TriStage {
+    f3 e1, e2, sv, q;
+    float det, sg, adet, us, u, v, t;
+    __device__ __forceinline__ bool begin(f3 o, f3 d, float4 v0, float4 e1w, float4 e2w)
+    {
+        e1 = xyz(e1w);
+        e2 = xyz(e2w);
+        const f3 p = cross(d, e2);
+        det = dot(e1, p);
+        sg = det > 0.0f ? 1.0f : -1.0f;
+        adet = fabsf(det);
+        sv = o - xyz(v0);
+        u = dot(sv, p);
+        us = u * sg;
+        return adet > FLT_EPSILON && !(us < 0.0f || us > adet);
+    }
+    __device__ __forceinline__ bool second(f3 d)
+    {
+        q = cross(sv, e1);
+        v = dot(d, q);
+        const float vs = v * sg;
+        return !(vs < 0.0f || __fadd_rn(us, vs) > adet);
+    }
+    // t is formed (one division) only on a lane that is still a candidate
+    __device__ __forceinline__ bool finish(bool ok, float dist)
+    {
+        t = FLT_MAX;
+        if (ok) t = __fmul_rn(dot(e2, q), __fdiv_rn(1.0f, det));
+        return ok && t > 0.0f && t < dist;
+    }
+};
+
 struct LocalHit {
     float t, u, v;
     uint32_t slot;     // winning slot (triangle id is in its v0.w)
@@ -783,13 +820,19 @@ __device__ __forceinline__ void trace_persistent(const DevScene& S, Work& W, uin
                     const float4* sl = S.slots + 3ull * (baseb + i);
                     B0 = __ldg(sl); B1 = __ldg(sl + 1); B2 = __ldg(sl + 2);
                 }
-                float ta = FLT_MAX, ua = 0.0f, va = 0.0f, da = 1.0f, tb = FLT_MAX, ub = 0.0f, vb = 0.0f, db = 1.0f;
-                const bool oka = ina && tri_test(roa, rda, xyz(A0), xyz(A1), xyz(A2), ta, ua, va, da) && ta > 0.0f &&
-                                 ta < dista;
-                const bool okb = inb && tri_test(rob, rdb, xyz(B0), xyz(B1), xyz(B2), tb, ub, vb, db) && tb > 0.0f &&
-                                 tb < distb;
-                chunk_min(oka, ta, ua, va, da, c, bta, bua, bva, bia);
-                chunk_min(okb, tb, ub, vb, db, c, btb, bub, bvb, bib);
+                TriStage sa, sb;
+                bool oka = sa.begin(roa, rda, A0, A1, A2) && ina;  // every lane runs each stage
+                bool okb = sb.begin(rob, rdb, B0, B1, B2) && inb;
+                if (__any_sync(MT_FULL, oka || okb)) {
+                    oka = sa.second(rda) && oka;
+                    okb = sb.second(rdb) && okb;
+                    if (__any_sync(MT_FULL, oka || okb)) {
+                        oka = sa.finish(oka, dista);
+                        okb = sb.finish(okb, distb);
+                        chunk_min(oka, sa.t, sa.u, sa.v, sa.det, c, bta, bua, bva, bia);
+                        chunk_min(okb, sb.t, sb.u, sb.v, sb.det, c, btb, bub, bvb, bib);
+                    }
+                }
             }
             if (lane == La) leaf_done(ca, bia, bta, bua, bva);
             if (lane == Lb) leaf_done(cb, bib, btb, bub, bvb);
@@ -808,14 +851,40 @@ __device__ __forceinline__ void trace_persistent(const DevScene& S, Work& W, uin
             uint32_t bidx = 0xffffffffu;
             for (uint32_t c = 0; c < count; c += 32) {
                 const uint32_t i = c + lane;
-                float t = FLT_MAX, u = 0.0f, v = 0.0f, det = 1.0f;
-                bool ok = false;
+                // the staged test with a warp vote after each stage: the rest
+                // runs only while some lane still has a candidate (per leaf visit,
+                // ~28% of the material grid's chunks lose every lane at the u
+                // bound and ~70% at the v bound)
+                float4 A = make_float4(0.f, 0.f, 0.f, 0.f), B = A, C = A;
                 if (i < count) {
                     const float4* sl = S.slots + 3ull * (base + i);
-                    const float4 A = __ldg(sl), B = __ldg(sl + 1), C = __ldg(sl + 2);
-                    ok = tri_test(ro, rd, xyz(A), xyz(B), xyz(C), t, u, v, det) && t > 0.0f && t < dist;
+                    A = __ldg(sl);
+                    B = __ldg(sl + 1);
+                    C = __ldg(sl + 2);
                 }
-                chunk_min(ok, t, u, v, det, c, bt, bu, bv, bidx);
+                // TriStage's operations written out (the form that measured
+                // fastest here); every lane runs each stage
+                const f3 e1 = xyz(B), e2 = xyz(C);
+                const f3 pv = cross(rd, e2);
+                const float det = dot(e1, pv);
+                const float sg = det > 0.0f ? 1.0f : -1.0f;
+                const float adet = fabsf(det);
+                const f3 sv = ro - xyz(A);
+                const float u = dot(sv, pv);
+                const float us = u * sg;
+                bool ok = i < count && adet > FLT_EPSILON && !(us < 0.0f || us > adet);
+                if (__any_sync(MT_FULL, ok)) {
+                    const f3 q = cross(sv, e1);
+                    const float v = dot(rd, q);
+                    const float vs = v * sg;
+                    ok = ok && !(vs < 0.0f || __fadd_rn(us, vs) > adet);
+                    if (__any_sync(MT_FULL, ok)) {
+                        float t = FLT_MAX;
+                        if (ok) t = __fmul_rn(dot(e2, q), __fdiv_rn(1.0f, det));
+                        ok = ok && t > 0.0f && t < dist;
+                        chunk_min(ok, t, u, v, det, c, bt, bu, bv, bidx);
+                    }
+                }
             }
             if (lane == L) leaf_done(count, bidx, bt, bu, bv);
         }
