@@ -281,6 +281,12 @@ __device__ __forceinline__ void group_sync(uint32_t group)
     asm volatile("bar.sync %0, 128;\n" ::"r"(1u + group) : "memory");
 }
 
+// Programmatic dependent launch: the next kernel of the stream (launched with
+// programmatic serialization) may start its CTAs now; and this thread waits
+// until the kernel before it has completed and its writes are visible.
+__device__ __forceinline__ void pdl_allow_next() { asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory"); }
+__device__ __forceinline__ void pdl_wait_prev() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
+
 // Issues one layer: D[128 x n] = A[128 x 8*kc] * W^T, W given as n x 8*kc.
 __device__ __forceinline__ void tc_layer(uint32_t tmem, uint32_t a_base, uint32_t w_base, uint32_t kc, uint32_t n,
                                          uint32_t bar)
@@ -582,15 +588,17 @@ __global__ void __launch_bounds__(kTrRows) k_nrc_train_tc(const bf16* __restrict
     const uint32_t tid = threadIdx.x, warp = tid >> 5, row = tid;
     const uint32_t bar = s0 + kTrBar, wbar = s0 + kTrWBar;
     volatile int* flag = reinterpret_cast<volatile int*>(smem + kTrFlag);
-    // forward weights (canonical K-major, N = out rows, K = in) by one bulk
-    // copy, in flight while the rows are gathered and encoded
+    // launched with programmatic serialization after the previous step's Adam:
+    // the set-up below overlaps that kernel's tail; everything it writes (the
+    // weights, the step counter, the partial rows it reads) is touched only
+    // after pdl_wait_prev
+    pdl_allow_next();
     bool w_wait = tid == 0;  // the MMA issuer still has to see the weights arrive
     if (tid == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar));
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(wbar));
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
         *flag = 0;
-        fetch_weights(fwd, s0 + kTcW0, wbar);
     }
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(s0 + kTrTmem),
@@ -603,6 +611,10 @@ __global__ void __launch_bounds__(kTrRows) k_nrc_train_tc(const bf16* __restrict
     tc_fence_after();
     const uint32_t tmem = *reinterpret_cast<const uint32_t*>(smem + kTrTmem);
     const uint32_t lane_addr = tmem + ((warp * 32u) << 16);
+    pdl_wait_prev();
+    // forward weights (canonical K-major, N = out rows, K = in) by one bulk
+    // copy, in flight while the rows are gathered and encoded
+    if (tid == 0) fetch_weights(fwd, s0 + kTcW0, wbar);
 
     const uint32_t cnt = a.count ? min(*a.count, a.count_cap) : a.rows;
     const uint32_t base = *step * a.rows;
@@ -839,6 +851,8 @@ __global__ void __launch_bounds__(kAdamWarps * 32) k_nrc_adam(float* __restrict_
     __shared__ float red[kAdamWarps][32];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int q = blockIdx.x * 32 + lane;
+    pdl_wait_prev();   // the partial rows of this step are complete
+    pdl_allow_next();  // the next step's training CTAs may set up meanwhile
     const float t = static_cast<float>(*step + 1u);
     float part = 0.0f;
     if (q < kNrcParams) {
@@ -1022,15 +1036,29 @@ cudaError_t launch_nrc_train_step(NrcOptimizer& O, const NrcTrainArgs& a, float*
     // partial per CTA.
     const uint32_t tiles = (a.rows + kTrRows - 1) / kTrRows;
     const uint32_t splits = std::min<uint32_t>(tiles, O.max_splits);
-    k_nrc_train_tc<<<splits, kTrRows, kTrSmem, st>>>(static_cast<const bf16*>(O.fwd), a, tiles, O.partial, loss,
-                                                      O.d_step, O.err, infer_wait_limit());
-    cudaError_t e = cudaGetLastError();
+    // both kernels with programmatic serialization: each may start while the
+    // one before it drains, and waits (griddepcontrol.wait) before it reads
+    // that kernel's output
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t lc = {};
+    lc.gridDim = dim3(splits);
+    lc.blockDim = dim3(kTrRows);
+    lc.dynamicSmemBytes = kTrSmem;
+    lc.stream = st;
+    lc.attrs = attr;
+    lc.numAttrs = 1;
+    cudaError_t e = cudaLaunchKernelEx(&lc, k_nrc_train_tc, static_cast<const bf16*>(O.fwd), a, tiles, O.partial,
+                                       loss, static_cast<const uint32_t*>(O.d_step), O.err, infer_wait_limit());
     if (e != cudaSuccess) return e;
     O.step += 1;
-    k_nrc_adam<<<(kNrcParams + 31) / 32, kAdamWarps * 32, 0, st>>>(
-        O.master, O.m, O.v, O.partial, splits, O.lr, O.beta1, O.beta2, O.eps, static_cast<bf16*>(O.fwd), grad_out,
-        static_cast<bf16*>(O.infer), O.ema, O.ema_decay, O.d_step, O.d_done);
-    return cudaGetLastError();
+    lc.gridDim = dim3((kNrcParams + 31) / 32);
+    lc.blockDim = dim3(kAdamWarps * 32);
+    lc.dynamicSmemBytes = 0;
+    return cudaLaunchKernelEx(&lc, k_nrc_adam, O.master, O.m, O.v, static_cast<const float*>(O.partial), splits,
+                              O.lr, O.beta1, O.beta2, O.eps, static_cast<bf16*>(O.fwd), grad_out,
+                              static_cast<bf16*>(O.infer), O.ema, O.ema_decay, O.d_step, O.d_done);
 }
 
 cudaError_t nrc_prepare()
