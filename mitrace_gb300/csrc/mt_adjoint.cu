@@ -305,25 +305,72 @@ __global__ void k_grad_pixel(const float* __restrict__ sr, const float* __restri
     if ((threadIdx.x & 31) == 0 && loss) atomicAdd(loss, local);
 }
 
-// One thread per path of a recorded batch.
-__global__ void __launch_bounds__(128) k_adjoint(DevScene S, GradParams G, RecordBuffers R,
-                                                 const float* __restrict__ sr, const float* __restrict__ sg,
-                                                 const float* __restrict__ sb, uint64_t g0, uint32_t n,
+// The bin of path p of a batch: its vertex count, or the last bin when its
+// sample is rejected by the firefly clamp (no gradient flows through it).
+__device__ __forceinline__ uint32_t adjoint_bin(const DevScene& S, const GradParams& G, const RecordBuffers& R,
+                                                const float* __restrict__ sr, const float* __restrict__ sg,
+                                                const float* __restrict__ sb, uint64_t g0, uint32_t p,
+                                                uint32_t band_pix)
+{
+    const uint64_t g = g0 + p;
+    const uint32_t s = static_cast<uint32_t>(g / band_pix);
+    const uint32_t j = static_cast<uint32_t>(g - static_cast<uint64_t>(s) * band_pix);
+    if (S.firefly_enable) {
+        const float4 px = G.pix[2 * j];
+        const float in = __fdiv_rn(__fadd_rn(__fadd_rn(sr[g], sg[g]), sb[g]), 3.0f);
+        if (fabsf(__fsub_rn(in, px.x)) > px.y) return kAdjointBins - 1;
+    }
+    const int nv = static_cast<int>(R.path[2 * p].w);
+    return nv >= 0 && nv <= MT_GRAD_MAX_BOUNCES ? static_cast<uint32_t>(nv) : kAdjointBins - 1;
+}
+
+// Counting pass (first) and placement pass of the grouping by vertex count:
+// lanes with the same bin reserve their slots with one atomic per warp.
+template <bool PLACE>
+__global__ void k_adjoint_order(DevScene S, GradParams G, RecordBuffers R, const float* __restrict__ sr,
+                                const float* __restrict__ sg, const float* __restrict__ sb, uint64_t g0, uint32_t n,
+                                uint32_t band_pix)
+{
+    const uint32_t lane = threadIdx.x & 31;
+    uint32_t first[kAdjointBins];
+    if (PLACE) {  // longest paths first: the short ones fill the launch's tail
+        uint32_t acc = 0;
+        for (int b = kAdjointBins - 2; b >= 0; --b) {
+            first[b] = acc;
+            acc += G.bins[b];
+        }
+        first[kAdjointBins - 1] = acc;
+    }
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        const uint32_t p = base + threadIdx.x;
+        const bool in = p < n;
+        const uint32_t b = in ? adjoint_bin(S, G, R, sr, sg, sb, g0, p, band_pix) : 0xffffffffu;
+        const uint32_t same = __match_any_sync(0xffffffffu, b);
+        const uint32_t leader = __ffs(same) - 1;
+        uint32_t slot = 0;
+        if (in && lane == leader) slot = atomicAdd(&G.bins[(PLACE ? kAdjointBins : 0) + b], __popc(same));
+        slot = __shfl_sync(0xffffffffu, slot, leader) + __popc(same & ((1u << lane) - 1u));
+        if (PLACE && in && b < kAdjointBins - 1) G.order[first[b] + slot] = p;
+    }
+}
+
+// One thread per path of a recorded batch, in the order k_adjoint_order
+// gave (the rejected samples left out).
+__global__ void __launch_bounds__(128) k_adjoint(DevScene S, GradParams G, RecordBuffers R, uint64_t g0,
                                                  uint32_t band_pix)
 {
     extern __shared__ float sh[];  // per block: materials x 5, then lights
     const uint32_t nm = G.smem_materials, nlg = G.smem_lights;
     for (uint32_t i = threadIdx.x; i < nm * 5 + nlg; i += blockDim.x) sh[i] = 0.0f;
+    uint32_t kept = 0;
+    for (uint32_t b = 0; b + 1 < kAdjointBins; ++b) kept += G.bins[b];
     __syncthreads();
-    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < kept; i += gridDim.x * blockDim.x) {
+        const uint32_t p = G.order[i];
         const uint64_t g = g0 + p;
         const uint32_t s = static_cast<uint32_t>(g / band_pix);
         const uint32_t j = static_cast<uint32_t>(g - static_cast<uint64_t>(s) * band_pix);
         const float4 px = G.pix[2 * j];
-        if (S.firefly_enable) {
-            const float in = __fdiv_rn(__fadd_rn(__fadd_rn(sr[g], sg[g]), sb[g]), 3.0f);
-            if (fabsf(__fsub_rn(in, px.x)) > px.y) continue;  // rejected sample: no gradient
-        }
         const float4 res = G.pix[2 * j + 1];
         const float4 pr0 = R.path[2 * p], pr1 = R.path[2 * p + 1];
         const float e = S.exposure;
@@ -332,7 +379,6 @@ __global__ void __launch_bounds__(128) k_adjoint(DevScene S, GradParams G, Recor
                        res.z * px.z * aces_d(pr0.z * e) * e};
         const int nv = static_cast<int>(pr0.w);
         const int miss = static_cast<int>(pr1.w);
-        if (nv > MT_GRAD_MAX_BOUNCES) continue;
         // forward: throughput before each vertex
         f3 cur[MT_GRAD_MAX_BOUNCES + 1];
         cur[0] = splat(1.0f);
@@ -452,9 +498,14 @@ cudaError_t launch_grad_pixel(const DevScene& S, const WaveBuffers& W, uint32_t 
 cudaError_t launch_adjoint(const DevScene& S, const GradParams& G, const RecordBuffers& R, const WaveBuffers& W,
                            uint64_t g0, uint32_t n, uint32_t band_pix, cudaStream_t st)
 {
+    cudaError_t e = cudaMemsetAsync(G.bins, 0, 2 * kAdjointBins * sizeof(uint32_t), st);
+    if (e != cudaSuccess) return e;
+    const unsigned og = static_cast<unsigned>((n + 255) / 256 < 4096 ? (n + 255) / 256 : 4096);
+    k_adjoint_order<false><<<og ? og : 1, 256, 0, st>>>(S, G, R, W.sr, W.sg, W.sb, g0, n, band_pix);
+    k_adjoint_order<true><<<og ? og : 1, 256, 0, st>>>(S, G, R, W.sr, W.sg, W.sb, g0, n, band_pix);
     const size_t smem = (static_cast<size_t>(G.smem_materials) * 5 + G.smem_lights) * sizeof(float);
     const unsigned grid = static_cast<unsigned>((n + 127) / 128 < 8192 ? (n + 127) / 128 : 8192);
-    k_adjoint<<<grid ? grid : 1, 128, smem, st>>>(S, G, R, W.sr, W.sg, W.sb, g0, n, band_pix);
+    k_adjoint<<<grid ? grid : 1, 128, smem, st>>>(S, G, R, g0, band_pix);
     return cudaGetLastError();
 }
 

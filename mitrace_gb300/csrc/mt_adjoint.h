@@ -24,7 +24,13 @@ struct GradParams {
     float4* pix;               // per band pixel: (mean, threshold, 2 / kept, -), (residual rgb, -)
     uint32_t smem_materials;   // materials reduced in shared memory (0: global atomics)
     uint32_t smem_lights;
+    uint32_t* order;           // per replayed path of a batch: path indices grouped by vertex count
+    uint32_t* bins;            // kAdjointBins counts, then kAdjointBins cursors
 };
+// paths of a batch are processed grouped by vertex count (0..MT_GRAD_MAX_BOUNCES)
+// so that a warp's threads walk equally long paths; the last bin holds the
+// paths without a gradient (firefly-rejected samples)
+constexpr uint32_t kAdjointBins = MT_GRAD_MAX_BOUNCES + 2;
 
 cudaError_t launch_grad_pixel(const DevScene& S, const WaveBuffers& W, uint32_t band_pix, uint32_t pix_base,
                               const float* image, const GradParams& G, cudaStream_t st);

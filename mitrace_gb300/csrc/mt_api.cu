@@ -452,6 +452,7 @@ struct mt_handle {
     // adjoint
     uint32_t grad_batch = 0;
     DevArray<float4> rec_vert, rec_path, grad_pix;
+    DevArray<uint32_t> grad_order, grad_bins;
     DevArray<long long> texel_off;
     uint64_t grad_texels = 0;
     // neural radiance cache (mt_nrc_enable)
@@ -896,6 +897,8 @@ void rc_settle_and_release_wave(mt_handle* h)
     h->rec_vert.reset();
     h->rec_path.reset();
     h->grad_pix.reset();
+    h->grad_order.reset();
+    h->grad_bins.reset();
 }
 
 struct WaveViews {
@@ -1463,12 +1466,13 @@ mt_status mt_render_grad(mt_handle* h, const mt_grad_buffers* g, void* cuda_stre
     const uint64_t rows_per_band = h->band_capacity / (static_cast<uint64_t>(c.width) * c.samples);
     if (!h->grad_batch) {
         // Paths replayed per batch: their vertex records (5 float4 per bounce
-        // plus 2 per path) are the adjoint's only storage, O(batch).  Sixteen
+        // plus 2 per path, and the path's place in the grouping by length) are
+        // the adjoint's only storage, O(batch).  Sixteen
         // samples per pixel of a band (at least 2^20 paths) keep the memory
         // proportional to the pixels, not to the samples, while batches stay
         // large enough that the replay's traversal launches are not dominated
         // by their tails; capped at an eighth of the free device memory.
-        const uint64_t rec_bytes = (static_cast<uint64_t>(std::max<uint32_t>(1, c.bounces)) * 5 + 2) * 16;
+        const uint64_t rec_bytes = (static_cast<uint64_t>(std::max<uint32_t>(1, c.bounces)) * 5 + 2) * 16 + 4;
         uint64_t want = std::max<uint64_t>(1ull << 20, 16ull * rows_per_band * c.width);
         size_t free_b = 0, total_b = 0;
         if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess && free_b > 0)
@@ -1477,6 +1481,8 @@ mt_status mt_render_grad(mt_handle* h, const mt_grad_buffers* g, void* cuda_stre
         MT_CUDA(h->rec_vert.alloc(gb * std::max<uint32_t>(1, c.bounces) * 5));
         MT_CUDA(h->rec_path.alloc(gb * 2));
         MT_CUDA(h->grad_pix.alloc(2 * rows_per_band * c.width));
+        MT_CUDA(h->grad_order.alloc(gb));
+        MT_CUDA(h->grad_bins.alloc(2 * kAdjointBins));
         h->grad_batch = static_cast<uint32_t>(gb);  // set once every record buffer exists
     }
     cudaStream_t st = static_cast<cudaStream_t>(cuda_stream);
@@ -1492,6 +1498,8 @@ mt_status mt_render_grad(mt_handle* h, const mt_grad_buffers* g, void* cuda_stre
     G.d_texels = h->grad_texels ? g->d_texels : nullptr;
     G.texel_off = h->texel_off.p;
     G.pix = h->grad_pix.p;
+    G.order = h->grad_order.p;
+    G.bins = h->grad_bins.p;
     const uint32_t nmat = static_cast<uint32_t>(h->materials.n);
     G.smem_materials = nmat <= 1024 ? nmat : 0;
     G.smem_lights = h->S.num_lights <= 256 ? h->S.num_lights : 0;
@@ -1517,7 +1525,7 @@ mt_status mt_render_grad(mt_handle* h, const mt_grad_buffers* g, void* cuda_stre
             const uint32_t n = static_cast<uint32_t>(std::min<uint64_t>(h->grad_batch, paths - g0));
             MT_CUDA(launch_batch(h->S, v.P, v.SQ, v.W, g0, n, band_pix, pix_base, st, &launches, nullptr, &R));
             MT_CUDA(launch_adjoint(h->S, G, R, v.W, g0, n, band_pix, st));
-            ++launches;
+            launches += 3;
         }
     }
     h->launches += launches;
