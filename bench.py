@@ -96,7 +96,10 @@ def parse():
     p.add_argument("--nrc-rows", type=int, default=1920 * 1080 * 4)
     p.add_argument("--nrc-regimen-frames", type=int, default=256,
                    help="frames of the 4-spp radiance-cache regimen (0: skip)")
-    p.add_argument("--case", choices=["render", "adjoint", "nrc_train", "nrc_frame", "microbench"], default=None,
+    p.add_argument("--inverse-iters", type=int, default=40,
+                   help="Adam iterations of the inverse-materials optimisation leg (0: skip)")
+    p.add_argument("--case", choices=["render", "adjoint", "inverse", "nrc_train", "nrc_frame", "microbench"],
+                   default=None,
                    help="run one small workload of a kernel family and print its timings (profiling runs)")
     return p.parse_args()
 
@@ -702,6 +705,86 @@ def adjoint_bench(ctx):
             "forward_ms": f, "gradient_vs_forward": t / f}
 
 
+def inverse_leg(ctx, iters):
+    """Config 4's optimisation at its stated size: hidden per-sphere base colour,
+    roughness and metallic (seeded) render a 1024-spp target of the 512x512
+    inverse-materials scene; Adam on the 49 x 5 sphere parameters from a uniform
+    start, one 64-spp gradient per iteration (forward render, path replay and
+    adjoint, the 786,432 texel and 2 light gradients included), the materials
+    updated on the same handle between gradients.  Reports the image loss and
+    the mean absolute parameter errors before and after, the gradient time
+    (CUDA events) and the time per iteration (wall clock: gradient, host Adam
+    step and material upload)."""
+    import numpy as np
+
+    import mitrace_gb300 as mt
+
+    torch = ctx.torch
+    rng = np.random.default_rng(2024)
+    hidden = np.concatenate([rng.uniform(0.2, 0.9, (49, 3)), rng.uniform(0.05, 1.0, (49, 1)),
+                             rng.uniform(0.0, 1.0, (49, 1))], 1).astype(np.float32)
+
+    def set_spheres(scene, x):
+        for k in range(49):
+            m = scene.materials[k]
+            m.base_color = (float(x[k, 0]), float(x[k, 1]), float(x[k, 2]), 1.0)
+            m.roughness = float(x[k, 3])
+            m.metallic = float(x[k, 4])
+
+    tscene, tcfg = mt.scenes.adjoint_scene(samples=1024)
+    set_spheres(tscene, hidden)
+    target = torch.empty((tcfg.height, tcfg.width, 3), device=ctx.dev)
+    with mt.Tracer(tscene, tcfg) as tr:
+        tr.render_device(target.data_ptr(), ctx.sptr)
+    torch.cuda.synchronize()
+    del tscene
+    scene, cfg = mt.scenes.adjoint_scene()
+    nm, nl = len(scene.materials), len(scene.lights)
+    nt = mt.scenes.num_grad_texels(scene)
+    x = np.full((49, 5), 0.5, np.float32)
+    lo = np.array([0.0, 0.0, 0.0, 0.05, 0.0], np.float32)
+    set_spheres(scene, x)
+    names = ("image", "loss", "d_base", "d_roughness", "d_metallic", "d_light", "d_texels")
+    sizes = (cfg.height * cfg.width * 3, 1, nm * 3, nm, nm, max(nl, 1), max(nt, 1))
+    bufs = {k: torch.zeros(n, device=ctx.dev) for k, n in zip(names, sizes)}
+
+    def errors(v):
+        d = np.abs(v - hidden)
+        return {"base": float(d[:, :3].mean()), "roughness": float(d[:, 3].mean()), "metallic": float(d[:, 4].mean())}
+
+    err0 = errors(x)
+    m1 = np.zeros_like(x)
+    m2 = np.zeros_like(x)
+    losses, grad_ms, iter_s = [], [], []
+    with mt.Tracer(scene, cfg) as tr:
+        for it in range(1, iters + 1):
+            t0 = time.perf_counter()
+            for b in bufs.values():
+                b.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(ctx.stream)
+            tr.render_grad_device(target.data_ptr(), *[bufs[k].data_ptr() for k in names], ctx.sptr)
+            e1.record(ctx.stream)
+            torch.cuda.synchronize()
+            grad_ms.append(e0.elapsed_time(e1))
+            losses.append(float(bufs["loss"].item()))
+            g = np.concatenate([bufs["d_base"].cpu().numpy().reshape(nm, 3)[:49],
+                                bufs["d_roughness"].cpu().numpy()[:49, None],
+                                bufs["d_metallic"].cpu().numpy()[:49, None]], 1)
+            m1 = 0.9 * m1 + 0.1 * g
+            m2 = 0.999 * m2 + 0.001 * g * g
+            x = np.clip(x - 0.02 * (m1 / (1 - 0.9 ** it)) / (np.sqrt(m2 / (1 - 0.999 ** it)) + 1e-8), lo, 1.0)
+            set_spheres(scene, x)
+            tr.update_materials(scene.materials)
+            iter_s.append(time.perf_counter() - t0)
+    return {"workload": f"inverse_materials_{cfg.width}x{cfg.height}_{cfg.samples}spp_target_{tcfg.samples}spp",
+            "parameters_optimised": 49 * 5, "gradient_parameters": nm * 5 + nl + nt, "iterations": iters,
+            "loss_first": losses[0], "loss_last": losses[-1],
+            "loss_curve": [losses[i] for i in range(0, iters, max(1, iters // 8))] + [losses[-1]],
+            "abs_error_start": err0, "abs_error_end": errors(x),
+            "gradient_ms": statistics.median(grad_ms), "seconds_per_iteration": statistics.median(iter_s)}
+
+
 def nrc_leg(a, ctx, ref):
     """The radiance-cache renderer on the same scene, per seed: cached frames of
     --nrc-spp samples (65,536 training paths and the library's Adam steps per
@@ -859,6 +942,9 @@ def run_ours(a):
         line["nrc_kernels"] = nrc_microbench(ctx, bf16_peak, a.nrc_rows)
         torch.cuda.empty_cache()
         line["adjoint"] = adjoint_bench(ctx)
+        torch.cuda.empty_cache()
+        if a.inverse_iters:
+            line["inverse"] = inverse_leg(ctx, a.inverse_iters)
     line["wall_s"] = time.perf_counter() - t_start
     print(json.dumps(line), flush=True)
     if ctx.world > 1:
@@ -868,7 +954,8 @@ def run_ours(a):
 def run_case(a):
     """One workload per kernel family, for profiler runs: `render` renders
     --warmup + --steps images of the headline configuration (--width, --height,
-    --spp); `adjoint` is the adjoint leg; `nrc_train` the cache's kernels;
+    --spp); `adjoint` is the adjoint leg; `inverse` the inverse-materials
+    optimisation; `nrc_train` the cache's kernels;
     `nrc_frame` two cached frames; `microbench` --microbench-rays incoherent rays
     on the large scene."""
     import mitrace_gb300 as mt
@@ -893,6 +980,8 @@ def run_case(a):
             out.update(ms=ms, rays=tr.GetStats().rays, launches=tr.kernel_launches())
     elif a.case == "adjoint":
         out["adjoint"] = adjoint_bench(ctx)
+    elif a.case == "inverse":
+        out["inverse"] = inverse_leg(ctx, a.inverse_iters)
     elif a.case == "nrc_train":
         out["nrc_kernels"] = nrc_microbench(ctx, bf16_peak, a.nrc_rows)
     elif a.case == "nrc_frame":
