@@ -357,253 +357,288 @@ __global__ void __launch_bounds__(128, MT_SHADE_MIN_BLOCKS) k_shade(DevScene S, 
                                                int cur, RecordBuffers R, NrcShade NC)
 {
     const uint32_t n = counts[cur];
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const uint32_t p = q[i];
+    // one path that hit: the shading body (Tracer.cpp:150-233, 255-336)
+    auto shade_hit = [&](const uint32_t p) {
         const uint4 hb = P.hitB[p];
         const f3 rd = ld4(P.rd, p);
         const f3 cur_e = ld4(P.cur, p);
-        if (hb.x == MT_NO_HIT) {
-            // Tracer.cpp:244-252: previous vertex's base colour times energy times sky.
-            const f3 color = bounce > 0 ? ld4(P.prev, p) : splat(1.0f);
-            const f3 sky = sample_sky(S, rd, bounce == 0);
-            st4(P.sky, p, ld4(P.sky, p) + (color * cur_e) * sky);
-            if (R.path) R.path[2 * p + 1] = make_float4(sky.x, sky.y, sky.z, static_cast<float>(bounce));
-            continue;
-        }
-        uint32_t pixel, sample;
-        path_coords(S, B, p, pixel, sample);
-        const float4 ha = P.hitA[p];
-        const f3 hit_pos = xyz(ha);
-        const float hit_dist = ha.w;
-        const float bu = __uint_as_float(hb.z), bv = __uint_as_float(hb.w);
-        const DevInstance& I = S.instances[hb.x];
-        const DevMesh m = S.meshes[__ldg(&I.mesh)];
-        // RayHitGeometryInfo (Ray.cpp:7-48)
-        const uint32_t tri = m.attr_off + hb.y;
-        const float w = __fsub_rn(__fsub_rn(1.0f, bu), bv);
-        const float* nr = S.normals + 9ull * tri;
-        f3 ni = {__fadd_rn(__fadd_rn(__fmul_rn(w, __ldg(nr + 0)), __fmul_rn(bu, __ldg(nr + 3))), __fmul_rn(bv, __ldg(nr + 6))),
-                 __fadd_rn(__fadd_rn(__fmul_rn(w, __ldg(nr + 1)), __fmul_rn(bu, __ldg(nr + 4))), __fmul_rn(bv, __ldg(nr + 7))),
-                 __fadd_rn(__fadd_rn(__fmul_rn(w, __ldg(nr + 2)), __fmul_rn(bu, __ldg(nr + 5))), __fmul_rn(bv, __ldg(nr + 8)))};
-        ni = normalize(ni);
-        float model[16];
-#pragma unroll
-        for (int k = 0; k < 16; ++k) model[k] = __ldg(&I.model[k]);
-        // normalize(model * vec4(n, 0)) with the vec4 pairwise dot
-        const float nx = mrow(model, 0, ni.x, ni.y, ni.z, 0.0f);
-        const float ny = mrow(model, 1, ni.x, ni.y, ni.z, 0.0f);
-        const float nz = mrow(model, 2, ni.x, ni.y, ni.z, 0.0f);
-        const float nw = mrow(model, 3, ni.x, ni.y, ni.z, 0.0f);
-        const float ns = __fdiv_rn(1.0f, __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(nx, nx), __fmul_rn(ny, ny)),
-                                                              __fadd_rn(__fmul_rn(nz, nz), __fmul_rn(nw, nw)))));
-        const f3 geom_n = {__fmul_rn(nx, ns), __fmul_rn(ny, ns), __fmul_rn(nz, ns)};
-        float tu = 0.0f, tv = 0.0f;
-        if (m.has_uv) {
-            const float* uv = S.uvs + 6ull * tri;
-            tu = __fadd_rn(__fadd_rn(__fmul_rn(w, __ldg(uv + 0)), __fmul_rn(bu, __ldg(uv + 2))), __fmul_rn(bv, __ldg(uv + 4)));
-            tv = __fadd_rn(__fadd_rn(__fmul_rn(w, __ldg(uv + 1)), __fmul_rn(bu, __ldg(uv + 3))), __fmul_rn(bv, __ldg(uv + 5)));
-        }
-        const MatPoint mp = sample_material(S, __ldg(&I.material), tu, tv);
-        const f3 base = {__fadd_rn(__fmul_rn(mp.base.x, 0.96f), 0.04f),
-                         __fadd_rn(__fmul_rn(mp.base.y, 0.96f), 0.04f),
-                         __fadd_rn(__fmul_rn(mp.base.z, 0.96f), 0.04f)};
-        const f3 N = compute_normal(geom_n, mp.normal);
-        const f3 view = -rd;
+            uint32_t pixel, sample;
+            path_coords(S, B, p, pixel, sample);
+            const float4 ha = P.hitA[p];
+            const f3 hit_pos = xyz(ha);
+            const float hit_dist = ha.w;
+            const float bu = __uint_as_float(hb.z), bv = __uint_as_float(hb.w);
+            const DevInstance& I = S.instances[hb.x];
+            const DevMesh m = S.meshes[__ldg(&I.mesh)];
+            // RayHitGeometryInfo (Ray.cpp:7-48)
+            const uint32_t tri = m.attr_off + hb.y;
+            const float w = __fsub_rn(__fsub_rn(1.0f, bu), bv);
+            const float* nr = S.normals + 9ull * tri;
+            f3 ni = {__fadd_rn(__fadd_rn(__fmul_rn(w, __ldg(nr + 0)), __fmul_rn(bu, __ldg(nr + 3))), __fmul_rn(bv, __ldg(nr + 6))),
+                     __fadd_rn(__fadd_rn(__fmul_rn(w, __ldg(nr + 1)), __fmul_rn(bu, __ldg(nr + 4))), __fmul_rn(bv, __ldg(nr + 7))),
+                     __fadd_rn(__fadd_rn(__fmul_rn(w, __ldg(nr + 2)), __fmul_rn(bu, __ldg(nr + 5))), __fmul_rn(bv, __ldg(nr + 8)))};
+            ni = normalize(ni);
+            float model[16];
+    #pragma unroll
+            for (int k = 0; k < 16; ++k) model[k] = __ldg(&I.model[k]);
+            // normalize(model * vec4(n, 0)) with the vec4 pairwise dot
+            const float nx = mrow(model, 0, ni.x, ni.y, ni.z, 0.0f);
+            const float ny = mrow(model, 1, ni.x, ni.y, ni.z, 0.0f);
+            const float nz = mrow(model, 2, ni.x, ni.y, ni.z, 0.0f);
+            const float nw = mrow(model, 3, ni.x, ni.y, ni.z, 0.0f);
+            const float ns = __fdiv_rn(1.0f, __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(nx, nx), __fmul_rn(ny, ny)),
+                                                                  __fadd_rn(__fmul_rn(nz, nz), __fmul_rn(nw, nw)))));
+            const f3 geom_n = {__fmul_rn(nx, ns), __fmul_rn(ny, ns), __fmul_rn(nz, ns)};
+            float tu = 0.0f, tv = 0.0f;
+            if (m.has_uv) {
+                const float* uv = S.uvs + 6ull * tri;
+                tu = __fadd_rn(__fadd_rn(__fmul_rn(w, __ldg(uv + 0)), __fmul_rn(bu, __ldg(uv + 2))), __fmul_rn(bv, __ldg(uv + 4)));
+                tv = __fadd_rn(__fadd_rn(__fmul_rn(w, __ldg(uv + 1)), __fmul_rn(bu, __ldg(uv + 3))), __fmul_rn(bv, __ldg(uv + 5)));
+            }
+            const MatPoint mp = sample_material(S, __ldg(&I.material), tu, tv);
+            const f3 base = {__fadd_rn(__fmul_rn(mp.base.x, 0.96f), 0.04f),
+                             __fadd_rn(__fmul_rn(mp.base.y, 0.96f), 0.04f),
+                             __fadd_rn(__fmul_rn(mp.base.z, 0.96f), 0.04f)};
+            const f3 N = compute_normal(geom_n, mp.normal);
+            const f3 view = -rd;
 
-        // Emission (Tracer.cpp:255)
-        const f3 emit_now = ld4(P.emit, p) + (cur_e * S.emission_base) * mp.emission;
-        st4(P.emit, p, emit_now);
-        float seen_diffuse = 0.0f;
-        bool end_here = false;  // AT_DIFFUSE query: the path ends after this vertex's NEE
-        if (HOOKS && NC.mode != MT_NRC_OFF) {
-            // Radiance-cache feature record of this vertex (mt_nrc.h)
-            seen_diffuse = P.prev[p].w;
-            const bool query =
-                NC.mode == MT_NRC_QUERY && (NC.end_at == MT_NRC_END_AT_DIFFUSE
-                                                ? mp.roughness >= NC.rough_min
-                                                : bounce >= 1 && seen_diffuse != 0.0f);
-            float4* fr = nullptr;
-            if (query)
-                fr = NC.rec + 6ull * warp_append(NC.count);
-            else if (NC.mode == MT_NRC_TRAIN)
-                fr = NC.rec + (static_cast<uint64_t>(p) * S.bounces + bounce) * 8;
-            if (fr) {
-                const f3 pn = {(hit_pos.x - NC.lo[0]) * NC.inv_ext[0], (hit_pos.y - NC.lo[1]) * NC.inv_ext[1],
-                               (hit_pos.z - NC.lo[2]) * NC.inv_ext[2]};
-                const float m = mp.metallic;
-                // what the rest of the path may still collect: the bounce budget
-                // left and the headroom above the energy cut-off
-                const float remaining = S.bounces > 1 ? static_cast<float>(S.bounces - 1 - bounce) /
-                                                            static_cast<float>(S.bounces - 1)
-                                                      : 0.0f;
-                float headroom = 1.0f;
-                if (S.terminate_energy > 0.0f) {
-                    const float te = length(ld4(P.tot, p));
-                    headroom = fminf(fmaxf(log2f(fmaxf(te, 1e-30f) / S.terminate_energy) * 0.0625f, 0.0f), 1.0f);
+            // Emission (Tracer.cpp:255)
+            const f3 emit_now = ld4(P.emit, p) + (cur_e * S.emission_base) * mp.emission;
+            st4(P.emit, p, emit_now);
+            float seen_diffuse = 0.0f;
+            bool end_here = false;  // AT_DIFFUSE query: the path ends after this vertex's NEE
+            if (HOOKS && NC.mode != MT_NRC_OFF) {
+                // Radiance-cache feature record of this vertex (mt_nrc.h)
+                seen_diffuse = P.prev[p].w;
+                const bool query =
+                    NC.mode == MT_NRC_QUERY && (NC.end_at == MT_NRC_END_AT_DIFFUSE
+                                                    ? mp.roughness >= NC.rough_min
+                                                    : bounce >= 1 && seen_diffuse != 0.0f);
+                float4* fr = nullptr;
+                if (query)
+                    fr = NC.rec + 6ull * warp_append(NC.count);
+                else if (NC.mode == MT_NRC_TRAIN)
+                    fr = NC.rec + (static_cast<uint64_t>(p) * S.bounces + bounce) * 8;
+                if (fr) {
+                    const f3 pn = {(hit_pos.x - NC.lo[0]) * NC.inv_ext[0], (hit_pos.y - NC.lo[1]) * NC.inv_ext[1],
+                                   (hit_pos.z - NC.lo[2]) * NC.inv_ext[2]};
+                    const float m = mp.metallic;
+                    // what the rest of the path may still collect: the bounce budget
+                    // left and the headroom above the energy cut-off
+                    const float remaining = S.bounces > 1 ? static_cast<float>(S.bounces - 1 - bounce) /
+                                                                static_cast<float>(S.bounces - 1)
+                                                          : 0.0f;
+                    float headroom = 1.0f;
+                    if (S.terminate_energy > 0.0f) {
+                        const float te = length(ld4(P.tot, p));
+                        headroom = fminf(fmaxf(log2f(fmaxf(te, 1e-30f) / S.terminate_energy) * 0.0625f, 0.0f), 1.0f);
+                    }
+                    fr[0] = make_float4(pn.x, pn.y, pn.z, mp.roughness);
+                    fr[1] = make_float4(view.x, view.y, view.z, remaining);
+                    fr[2] = make_float4(N.x, N.y, N.z, headroom);
+                    fr[3] = make_float4(base.x * (1.0f - m), base.y * (1.0f - m), base.z * (1.0f - m), 0.0f);
+                    fr[4] = make_float4(0.04f * (1.0f - m) + base.x * m, 0.04f * (1.0f - m) + base.y * m,
+                                        0.04f * (1.0f - m) + base.z * m, 0.0f);
+                    fr[5] = make_float4(cur_e.x, cur_e.y, cur_e.z, __uint_as_float(p));
+                    if (!query) {
+                        const f3 pre = ((emit_now + ld4(P.direct, p)) + ld4(P.indirect, p)) + ld4(P.sky, p);
+                        fr[6] = make_float4(pre.x, pre.y, pre.z, 1.0f);
+                        fr[7] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);  // NEE, set by the shadow stage
+                    }
                 }
-                fr[0] = make_float4(pn.x, pn.y, pn.z, mp.roughness);
-                fr[1] = make_float4(view.x, view.y, view.z, remaining);
-                fr[2] = make_float4(N.x, N.y, N.z, headroom);
-                fr[3] = make_float4(base.x * (1.0f - m), base.y * (1.0f - m), base.z * (1.0f - m), 0.0f);
-                fr[4] = make_float4(0.04f * (1.0f - m) + base.x * m, 0.04f * (1.0f - m) + base.y * m,
-                                    0.04f * (1.0f - m) + base.z * m, 0.0f);
-                fr[5] = make_float4(cur_e.x, cur_e.y, cur_e.z, __uint_as_float(p));
-                if (!query) {
-                    const f3 pre = ((emit_now + ld4(P.direct, p)) + ld4(P.indirect, p)) + ld4(P.sky, p);
-                    fr[6] = make_float4(pre.x, pre.y, pre.z, 1.0f);
-                    fr[7] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);  // NEE, set by the shadow stage
+                if (query) {
+                    if (NC.end_at != MT_NRC_END_AT_DIFFUSE) return;  // the cache stands in for the rest
+                    end_here = true;
                 }
+                if (mp.roughness >= NC.rough_min) seen_diffuse = 1.0f;
             }
-            if (query) {
-                if (NC.end_at != MT_NRC_END_AT_DIFFUSE) continue;  // the cache stands in for the rest
-                end_here = true;
-            }
-            if (mp.roughness >= NC.rough_min) seen_diffuse = 1.0f;
-        }
-        float4* vr = R.vert ? R.vert + (static_cast<uint64_t>(p) * S.bounces + bounce) * 5 : nullptr;
-        if (vr) {
-            vr[0] = make_float4(N.x, N.y, N.z, __uint_as_float(__ldg(&I.material)));
-            vr[1] = make_float4(view.x, view.y, view.z, __uint_as_float(MT_VREC_HIT));
-            vr[2] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            vr[3] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            vr[4] = make_float4(tu, tv, __uint_as_float(0u), 0.0f);
-            R.path[2 * p].w = static_cast<float>(bounce + 1);
-        }
-
-        // Weighted reservoir light pick (Tracer.cpp:257-279)
-        int chosen = -1;
-        float pick = 0.0f, total = 0.0f;
-        uint4 rp = make_uint4(0, 0, 0, 0);
-        for (uint32_t li = 0; li < S.num_lights; ++li) {
-            if ((li & 3) == 0) rp = draw(S, pixel, sample, bounce, SLOT_LIGHT_PICK + (li >> 2));
-            const DevLight& L = S.lights[li];
-            const f3 lp = f3{__ldg(&L.pos[0]), __ldg(&L.pos[1]), __ldg(&L.pos[2])} - hit_pos;
-            const float score = __fdiv_rn(__ldg(&L.simple), __fadd_rn(dot(lp, lp), 1.0f));
-            total = __fadd_rn(total, score);
-            const uint32_t word = (li & 3) == 0 ? rp.x : ((li & 3) == 1 ? rp.y : ((li & 3) == 2 ? rp.z : rp.w));
-            if (__fmul_rn(urange(word, 0.0f, 1.0f), total) < score) {
-                chosen = static_cast<int>(li);
-                pick = score;
-            }
-        }
-        pick = __fdiv_rn(pick, total);
-        if (chosen >= 0) {
-            const DevLight& L = S.lights[chosen];
-            const int type = __ldg(&L.type);
-            const f3 lpos0 = {__ldg(&L.pos[0]), __ldg(&L.pos[1]), __ldg(&L.pos[2])};
-            f3 lpos = lpos0;
-            if (type == MT_LIGHT_POINT || type == MT_LIGHT_SPOT) {
-                const uint4 rj = draw(S, pixel, sample, bounce, SLOT_LIGHT_JITTER);
-                const float a = urange(rj.x, 0.0f, __fmul_rn(2.0f, kPi));
-                const float b = urange(rj.y, -kPi / 2.0f, kPi / 2.0f);
-                const f3 dir = normalize(f3{__fmul_rn(cosf(a), cosf(b)), sinf(b), __fmul_rn(sinf(a), cosf(b))});
-                lpos = lpos0 + dir * __ldg(&L.point_size);
-            }
-            const f3 lvec = lpos - hit_pos;
-            const f3 ldir = normalize(lvec);
-            f3 lcol = {__ldg(&L.color[0]), __ldg(&L.color[1]), __ldg(&L.color[2])};
-            float spot = 1.0f;
-            if (type == MT_LIGHT_SPOT) {
-                const f3 sd = {__ldg(&L.dir[0]), __ldg(&L.dir[1]), __ldg(&L.dir[2])};
-                const float dd = dot(-ldir, sd);
-                const float inten = __fdiv_rn(__fsub_rn(dd, __ldg(&L.outer_cos)),
-                                              __fsub_rn(__ldg(&L.inner_cos), __ldg(&L.outer_cos)));
-                spot = gclamp(inten, 0.0f, 1.0f);
-                lcol = lcol * spot;
-            }
-            const float llen = length(lvec);
-            const f3 brdf = eval_brdf(ldir, view, N, base, mp.roughness, mp.metallic);
-            const float nl = gmax(dot(N, ldir), 0.0f);
-            const float fall = __fdiv_rn(1.0f, __fadd_rn(__fmul_rn(llen, llen), 1.0f));
-            const f3 le = brdf * nl * fall;
-            const f3 contrib = ((cur_e * le) * lcol) / pick;
-            const uint32_t slot = warp_append(&counts[2]);
-            const f3 so = hit_pos + lvec * 0.0001f;
-            SQ.o[slot] = make_float4(so.x, so.y, so.z, llen);
-            SQ.d[slot] = make_float4(ldir.x, ldir.y, ldir.z, __uint_as_float(p));
-            SQ.c[slot] = make_float4(contrib.x, contrib.y, contrib.z, static_cast<float>(bounce));
+            float4* vr = R.vert ? R.vert + (static_cast<uint64_t>(p) * S.bounces + bounce) * 5 : nullptr;
             if (vr) {
-                vr[1].w = __uint_as_float(MT_VREC_HIT | MT_VREC_CHOSEN);
-                vr[3] = make_float4(ldir.x, ldir.y, ldir.z, nl * fall / pick);
-                vr[4].z = __uint_as_float(static_cast<uint32_t>(chosen));
-                vr[4].w = spot;
+                vr[0] = make_float4(N.x, N.y, N.z, __uint_as_float(__ldg(&I.material)));
+                vr[1] = make_float4(view.x, view.y, view.z, __uint_as_float(MT_VREC_HIT));
+                vr[2] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                vr[3] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                vr[4] = make_float4(tu, tv, __uint_as_float(0u), 0.0f);
+                R.path[2 * p].w = static_cast<float>(bounce + 1);
             }
-        }
 
-        // First-hit debug values (ProcessDebugRay, Tracer.cpp:411-482)
-        const bool dbg0 = HOOKS && P.dval && bounce == 0;
-        if (dbg0) {
-            f3 dv = splat(0.0f);
-            bool set = true;
-            switch (S.debug_mode) {
-                case MT_DEBUG_ALBEDO: dv = base; break;
-                case MT_DEBUG_METALLIC_ROUGHNESS: dv = f3{0.0f, mp.metallic, mp.roughness}; break;
-                case MT_DEBUG_GEOMETRIC_NORMAL: dv = geom_n * 0.5f + splat(0.5f); break;
-                case MT_DEBUG_SHADING_NORMAL: dv = N * 0.5f + splat(0.5f); break;
-                case MT_DEBUG_COLOR_PER_MESH: dv = random_color_u16(hb.x); break;
-                case MT_DEBUG_COLOR_PER_TRIANGLE: dv = random_color_u16(hb.y); break;
-                case MT_DEBUG_DEPTH: dv = splat(length(hit_pos - ld4(P.ro, p))); break;
-                case MT_DEBUG_FIRST_HIT_FRESNEL:
-                    dv = fresnel_schlick(gmax(dot(N, -rd), 0.0f), base_reflectivity(base, mp.metallic));
-                    break;
-                default: set = false; break;
+            // Weighted reservoir light pick (Tracer.cpp:257-279)
+            int chosen = -1;
+            float pick = 0.0f, total = 0.0f;
+            uint4 rp = make_uint4(0, 0, 0, 0);
+            for (uint32_t li = 0; li < S.num_lights; ++li) {
+                if ((li & 3) == 0) rp = draw(S, pixel, sample, bounce, SLOT_LIGHT_PICK + (li >> 2));
+                const DevLight& L = S.lights[li];
+                const f3 lp = f3{__ldg(&L.pos[0]), __ldg(&L.pos[1]), __ldg(&L.pos[2])} - hit_pos;
+                const float score = __fdiv_rn(__ldg(&L.simple), __fadd_rn(dot(lp, lp), 1.0f));
+                total = __fadd_rn(total, score);
+                const uint32_t word = (li & 3) == 0 ? rp.x : ((li & 3) == 1 ? rp.y : ((li & 3) == 2 ? rp.z : rp.w));
+                if (__fmul_rn(urange(word, 0.0f, 1.0f), total) < score) {
+                    chosen = static_cast<int>(li);
+                    pick = score;
+                }
             }
-            if (set) {
+            pick = __fdiv_rn(pick, total);
+            if (chosen >= 0) {
+                const DevLight& L = S.lights[chosen];
+                const int type = __ldg(&L.type);
+                const f3 lpos0 = {__ldg(&L.pos[0]), __ldg(&L.pos[1]), __ldg(&L.pos[2])};
+                f3 lpos = lpos0;
+                if (type == MT_LIGHT_POINT || type == MT_LIGHT_SPOT) {
+                    const uint4 rj = draw(S, pixel, sample, bounce, SLOT_LIGHT_JITTER);
+                    const float a = urange(rj.x, 0.0f, __fmul_rn(2.0f, kPi));
+                    const float b = urange(rj.y, -kPi / 2.0f, kPi / 2.0f);
+                    const f3 dir = normalize(f3{__fmul_rn(cosf(a), cosf(b)), sinf(b), __fmul_rn(sinf(a), cosf(b))});
+                    lpos = lpos0 + dir * __ldg(&L.point_size);
+                }
+                const f3 lvec = lpos - hit_pos;
+                const f3 ldir = normalize(lvec);
+                f3 lcol = {__ldg(&L.color[0]), __ldg(&L.color[1]), __ldg(&L.color[2])};
+                float spot = 1.0f;
+                if (type == MT_LIGHT_SPOT) {
+                    const f3 sd = {__ldg(&L.dir[0]), __ldg(&L.dir[1]), __ldg(&L.dir[2])};
+                    const float dd = dot(-ldir, sd);
+                    const float inten = __fdiv_rn(__fsub_rn(dd, __ldg(&L.outer_cos)),
+                                                  __fsub_rn(__ldg(&L.inner_cos), __ldg(&L.outer_cos)));
+                    spot = gclamp(inten, 0.0f, 1.0f);
+                    lcol = lcol * spot;
+                }
+                const float llen = length(lvec);
+                const f3 brdf = eval_brdf(ldir, view, N, base, mp.roughness, mp.metallic);
+                const float nl = gmax(dot(N, ldir), 0.0f);
+                const float fall = __fdiv_rn(1.0f, __fadd_rn(__fmul_rn(llen, llen), 1.0f));
+                const f3 le = brdf * nl * fall;
+                const f3 contrib = ((cur_e * le) * lcol) / pick;
+                const uint32_t slot = warp_append(&counts[2]);
+                const f3 so = hit_pos + lvec * 0.0001f;
+                SQ.o[slot] = make_float4(so.x, so.y, so.z, llen);
+                SQ.d[slot] = make_float4(ldir.x, ldir.y, ldir.z, __uint_as_float(p));
+                SQ.c[slot] = make_float4(contrib.x, contrib.y, contrib.z, static_cast<float>(bounce));
+                if (vr) {
+                    vr[1].w = __uint_as_float(MT_VREC_HIT | MT_VREC_CHOSEN);
+                    vr[3] = make_float4(ldir.x, ldir.y, ldir.z, nl * fall / pick);
+                    vr[4].z = __uint_as_float(static_cast<uint32_t>(chosen));
+                    vr[4].w = spot;
+                }
+            }
+
+            // First-hit debug values (ProcessDebugRay, Tracer.cpp:411-482)
+            const bool dbg0 = HOOKS && P.dval && bounce == 0;
+            if (dbg0) {
+                f3 dv = splat(0.0f);
+                bool set = true;
+                switch (S.debug_mode) {
+                    case MT_DEBUG_ALBEDO: dv = base; break;
+                    case MT_DEBUG_METALLIC_ROUGHNESS: dv = f3{0.0f, mp.metallic, mp.roughness}; break;
+                    case MT_DEBUG_GEOMETRIC_NORMAL: dv = geom_n * 0.5f + splat(0.5f); break;
+                    case MT_DEBUG_SHADING_NORMAL: dv = N * 0.5f + splat(0.5f); break;
+                    case MT_DEBUG_COLOR_PER_MESH: dv = random_color_u16(hb.x); break;
+                    case MT_DEBUG_COLOR_PER_TRIANGLE: dv = random_color_u16(hb.y); break;
+                    case MT_DEBUG_DEPTH: dv = splat(length(hit_pos - ld4(P.ro, p))); break;
+                    case MT_DEBUG_FIRST_HIT_FRESNEL:
+                        dv = fresnel_schlick(gmax(dot(N, -rd), 0.0f), base_reflectivity(base, mp.metallic));
+                        break;
+                    default: set = false; break;
+                }
+                if (set) {
+                    const float4 o = P.dval[p];
+                    P.dval[p] = make_float4(dv.x, dv.y, dv.z, o.w);
+                }
+            }
+
+            if (HOOKS && end_here) return;  // the cache stands in for the reflected rest
+
+            // Bounce sampling (Tracer.cpp:177-208); the last vertex never extends
+            // (the debug modes that show the first vertex's sample draw it anyway).
+            const bool last = bounce + 1 >= S.bounces;
+            if (last && !(dbg0 && (S.debug_mode == MT_DEBUG_FIRST_HIT_BRDF || S.debug_mode == MT_DEBUG_FIRST_HIT_PDF)))
+                return;
+            const float ps = specular_probability(view, N, base, mp.metallic);
+            const uint4 rl = draw(S, pixel, sample, bounce, SLOT_LOBE);
+            f3 nd;
+            if (urange(rl.x, 0.0f, 1.0f) < ps) {
+                if (!ggx_reflection(rd, N, mp.roughness, urange(rl.y, 0.0f, 1.0f), urange(rl.z, 0.0f, 1.0f), nd)) {
+                    const uint4 rf = draw(S, pixel, sample, bounce, SLOT_FALLBACK);
+                    nd = cosine_hemisphere(urange(rf.x, 0.0f, 1.0f), urange(rf.y, 0.0f, 1.0f), N);
+                }
+            } else {
+                nd = cosine_hemisphere(urange(rl.y, 0.0f, 1.0f), urange(rl.z, 0.0f, 1.0f), N);
+            }
+            const float dp = diffuse_pdf(nd, N);
+            const float sp = specular_pdf(nd, view, N, mp.roughness);
+            const float pdf = __fadd_rn(__fmul_rn(__fsub_rn(1.0f, ps), dp), __fmul_rn(ps, sp));
+            const f3 brdf = eval_brdf(nd, view, N, base, mp.roughness, mp.metallic);
+            const float nl = gmax(dot(N, nd), 0.0f);
+            const f3 energy = pdf > 0.0f ? brdf * __fdiv_rn(nl, pdf) : splat(0.0f);
+            if (dbg0 && (S.debug_mode == MT_DEBUG_FIRST_HIT_BRDF || S.debug_mode == MT_DEBUG_FIRST_HIT_PDF)) {
                 const float4 o = P.dval[p];
+                const float dv = S.debug_mode == MT_DEBUG_FIRST_HIT_PDF ? pdf : __fadd_rn(__fadd_rn(brdf.x, brdf.y), brdf.z);
+                P.dval[p] = make_float4(dv, dv, dv, o.w);
+            }
+            if (last) return;
+            if (chosen >= 0) st4(P.cur, p, cur_e * energy);  // Tracer.cpp:339
+            if (vr) {
+                vr[1].w = __uint_as_float(__float_as_uint(vr[1].w) | MT_VREC_NEXT);
+                vr[2] = make_float4(nd.x, nd.y, nd.z, pdf > 0.0f ? nl / pdf : 0.0f);
+            }
+            const f3 tot = ld4(P.tot, p) * energy;
+            st4(P.tot, p, tot);
+            if (length(tot) < S.terminate_energy) return;  // Tracer.cpp:207-208
+            if (dbg0 && S.debug_mode == MT_DEBUG_REFLECTED_DIRECTION) {
+                // path[1].ray.direction * 0.5 + 0.5: the path has a second step
+                const float4 o = P.dval[p];
+                const f3 dv = nd * 0.5f + splat(0.5f);
                 P.dval[p] = make_float4(dv.x, dv.y, dv.z, o.w);
             }
-        }
-
-        if (HOOKS && end_here) continue;  // the cache stands in for the reflected rest
-
-        // Bounce sampling (Tracer.cpp:177-208); the last vertex never extends
-        // (the debug modes that show the first vertex's sample draw it anyway).
-        const bool last = bounce + 1 >= S.bounces;
-        if (last && !(dbg0 && (S.debug_mode == MT_DEBUG_FIRST_HIT_BRDF || S.debug_mode == MT_DEBUG_FIRST_HIT_PDF)))
-            continue;
-        const float ps = specular_probability(view, N, base, mp.metallic);
-        const uint4 rl = draw(S, pixel, sample, bounce, SLOT_LOBE);
-        f3 nd;
-        if (urange(rl.x, 0.0f, 1.0f) < ps) {
-            if (!ggx_reflection(rd, N, mp.roughness, urange(rl.y, 0.0f, 1.0f), urange(rl.z, 0.0f, 1.0f), nd)) {
-                const uint4 rf = draw(S, pixel, sample, bounce, SLOT_FALLBACK);
-                nd = cosine_hemisphere(urange(rf.x, 0.0f, 1.0f), urange(rf.y, 0.0f, 1.0f), N);
+            const f3 ro = xyz(P.ro[p]);
+            const f3 no = (ro + rd * hit_dist) + N * 0.0001f;
+            st4(P.ro, p, no);
+            st4(P.rd, p, nd);
+            st4(P.prev, p, base, seen_diffuse);
+            nq[warp_append(&counts[cur ^ 1])] = p;
+    };
+    // A miss costs a sky lookup, a hit the whole body above: misses are
+    // handled as a warp reads the queue, hits are collected per warp in shared
+    // memory and shaded 32 at a time, so a warp's lanes run the long body
+    // together instead of beside lanes that have finished
+    __shared__ uint32_t s_hits[4][64];
+    const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+    uint32_t next = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32u;
+    uint32_t held = 0;
+    while (true) {
+        if (held < 32 && next < n) {
+            const uint32_t i = next + lane;
+            next += nwarps * 32u;
+            bool hit = false;
+            uint32_t p = 0;
+            if (i < n) {
+                p = q[i];
+                if (P.hitB[p].x == MT_NO_HIT) {
+                    // Tracer.cpp:244-252: previous vertex's base colour times energy times sky.
+                    const f3 rd = ld4(P.rd, p);
+                    const f3 cur_e = ld4(P.cur, p);
+                    const f3 color = bounce > 0 ? ld4(P.prev, p) : splat(1.0f);
+                    const f3 sky = sample_sky(S, rd, bounce == 0);
+                    st4(P.sky, p, ld4(P.sky, p) + (color * cur_e) * sky);
+                    if (R.path) R.path[2 * p + 1] = make_float4(sky.x, sky.y, sky.z, static_cast<float>(bounce));
+                } else {
+                    hit = true;
+                }
             }
-        } else {
-            nd = cosine_hemisphere(urange(rl.y, 0.0f, 1.0f), urange(rl.z, 0.0f, 1.0f), N);
+            const uint32_t m = __ballot_sync(MT_FULL, hit);
+            if (hit) s_hits[wib][held + __popc(m & ((1u << lane) - 1u))] = p;
+            held += __popc(m);
+            __syncwarp();
+            continue;
         }
-        const float dp = diffuse_pdf(nd, N);
-        const float sp = specular_pdf(nd, view, N, mp.roughness);
-        const float pdf = __fadd_rn(__fmul_rn(__fsub_rn(1.0f, ps), dp), __fmul_rn(ps, sp));
-        const f3 brdf = eval_brdf(nd, view, N, base, mp.roughness, mp.metallic);
-        const float nl = gmax(dot(N, nd), 0.0f);
-        const f3 energy = pdf > 0.0f ? brdf * __fdiv_rn(nl, pdf) : splat(0.0f);
-        if (dbg0 && (S.debug_mode == MT_DEBUG_FIRST_HIT_BRDF || S.debug_mode == MT_DEBUG_FIRST_HIT_PDF)) {
-            const float4 o = P.dval[p];
-            const float dv = S.debug_mode == MT_DEBUG_FIRST_HIT_PDF ? pdf : __fadd_rn(__fadd_rn(brdf.x, brdf.y), brdf.z);
-            P.dval[p] = make_float4(dv, dv, dv, o.w);
-        }
-        if (last) continue;
-        if (chosen >= 0) st4(P.cur, p, cur_e * energy);  // Tracer.cpp:339
-        if (vr) {
-            vr[1].w = __uint_as_float(__float_as_uint(vr[1].w) | MT_VREC_NEXT);
-            vr[2] = make_float4(nd.x, nd.y, nd.z, pdf > 0.0f ? nl / pdf : 0.0f);
-        }
-        const f3 tot = ld4(P.tot, p) * energy;
-        st4(P.tot, p, tot);
-        if (length(tot) < S.terminate_energy) continue;  // Tracer.cpp:207-208
-        if (dbg0 && S.debug_mode == MT_DEBUG_REFLECTED_DIRECTION) {
-            // path[1].ray.direction * 0.5 + 0.5: the path has a second step
-            const float4 o = P.dval[p];
-            const f3 dv = nd * 0.5f + splat(0.5f);
-            P.dval[p] = make_float4(dv.x, dv.y, dv.z, o.w);
-        }
-        const f3 ro = xyz(P.ro[p]);
-        const f3 no = (ro + rd * hit_dist) + N * 0.0001f;
-        st4(P.ro, p, no);
-        st4(P.rd, p, nd);
-        st4(P.prev, p, base, seen_diffuse);
-        nq[warp_append(&counts[cur ^ 1])] = p;
+        if (held == 0) break;
+        const uint32_t take = held < 32 ? held : 32;
+        held -= take;
+        const bool active = lane < take;
+        const uint32_t p = active ? s_hits[wib][held + lane] : 0u;
+        __syncwarp();
+        if (active) shade_hit(p);
     }
 }
 
