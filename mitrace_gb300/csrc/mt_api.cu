@@ -401,6 +401,10 @@ mt_status validate_scene(const mt_scene_desc* d, const mt_config& cfg, std::stri
 struct mt_handle {
     int device = 0;
     cudaStream_t stream = nullptr;
+    // a second stream and two events for the shadow stages that run beside the
+    // next bounce's extension (launch_batch)
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_shaded = nullptr, ev_shadowed = nullptr;
     mt_config cfg{};
     DevScene S{};
     // scene storage
@@ -499,6 +503,9 @@ struct mt_handle {
         if (nrc.steps_graph) cudaGraphExecDestroy(nrc.steps_graph);
         pinned_slot_free(rays_host);
         if (render_done) cudaEventDestroy(render_done);
+        if (ev_shaded) cudaEventDestroy(ev_shaded);
+        if (ev_shadowed) cudaEventDestroy(ev_shadowed);
+        if (side) cudaStreamDestroy(side);
         if (stream) cudaStreamDestroy(stream);
     }
 };
@@ -935,6 +942,9 @@ WaveViews views(mt_handle* h)
     v.W.sr = h->samples.p;
     v.W.sg = h->samples.p + h->band_capacity;
     v.W.sb = h->samples.p + 2 * h->band_capacity;
+    v.W.side = h->side;
+    v.W.ev_shaded = h->ev_shaded;
+    v.W.ev_shadowed = h->ev_shadowed;
     return v;
 }
 
@@ -1242,6 +1252,9 @@ mt_status mt_create(const mt_scene_desc* scene, const mt_config* cfg, mt_handle*
     h->cfg = *cfg;
     cudaError_t e = cudaGetDevice(&h->device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_shaded, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_shadowed, cudaEventDisableTiming);
     if (e != cudaSuccess) {
         delete h;
         return set_err(MT_ERR_CUDA, std::string("CUDA unavailable: ") + cudaGetErrorString(e));

@@ -313,15 +313,17 @@ struct ExtendWork {
 template <bool COUNT, bool DBG, int CHUNK = 32>
 __global__ void __launch_bounds__(128, MT_TRAVERSE_MIN_BLOCKS) k_extend(DevScene S, PathState P,
                                                 const uint32_t* __restrict__ q,
-                                                uint32_t* counts, int cur,
+                                                uint32_t* counts, int cur, int sqi,
                                                 unsigned long long* rays,
                                                 unsigned long long* cnt)
 {
     const uint32_t n = counts[cur];
     if (blockIdx.x == 0 && threadIdx.x == 0) {
+        // the next queue and this bounce's shadow queue start empty; the
+        // previous bounce's shadow stage, which may still run beside this
+        // kernel, counts in the other shadow-queue slot
         counts[cur ^ 1] = 0;
-        counts[2] = 0;
-        counts[4] = 0;  // ray fetch counter of this bounce's shadow stage
+        counts[sqi] = 0;
         atomicAdd(rays, static_cast<unsigned long long>(n));
     }
     ExtendWork<COUNT, DBG> W{P, q, n, 0, 0, 0, 0, S.debug_mode};
@@ -354,9 +356,16 @@ __global__ void __launch_bounds__(128, MT_SHADE_MIN_BLOCKS) k_shade(DevScene S, 
                                                BatchInfo B, uint32_t bounce,
                                                const uint32_t* __restrict__ q,
                                                uint32_t* __restrict__ nq, uint32_t* counts,
-                                               int cur, RecordBuffers R, NrcShade NC)
+                                               int cur, int sqi, RecordBuffers R, NrcShade NC)
 {
     const uint32_t n = counts[cur];
+    // this bounce's extension is done and the previous bounce's shadow stage
+    // has finished: the ray fetch counters of the next extension and of this
+    // bounce's shadow stage start at zero
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        counts[3] = 0;
+        counts[4] = 0;
+    }
     // one path that hit: the shading body (Tracer.cpp:150-233, 255-336)
     auto shade_hit = [&](const uint32_t p) {
         const uint4 hb = P.hitB[p];
@@ -509,7 +518,7 @@ __global__ void __launch_bounds__(128, MT_SHADE_MIN_BLOCKS) k_shade(DevScene S, 
                 const float fall = __fdiv_rn(1.0f, __fadd_rn(__fmul_rn(llen, llen), 1.0f));
                 const f3 le = brdf * nl * fall;
                 const f3 contrib = ((cur_e * le) * lcol) / pick;
-                const uint32_t slot = warp_append(&counts[2]);
+                const uint32_t slot = warp_append(&counts[sqi]);
                 const f3 so = hit_pos + lvec * 0.0001f;
                 SQ.o[slot] = make_float4(so.x, so.y, so.z, llen);
                 SQ.d[slot] = make_float4(ldir.x, ldir.y, ldir.z, __uint_as_float(p));
@@ -688,16 +697,13 @@ struct ShadowWork {
 
 template <bool COUNT, int CHUNK = 32>
 __global__ void __launch_bounds__(128, MT_TRAVERSE_MIN_BLOCKS) k_shadow(DevScene S, PathState P, ShadowQueue SQ,
-                                                uint32_t* counts,
+                                                uint32_t* counts, int sqi,
                                                 unsigned long long* rays,
                                                 unsigned long long* cnt,
                                                 RecordBuffers R)
 {
-    const uint32_t n = counts[2];
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        counts[3] = 0;  // ray fetch counter of the next bounce's extend
-        atomicAdd(rays, static_cast<unsigned long long>(n));
-    }
+    const uint32_t n = counts[sqi];
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(rays, static_cast<unsigned long long>(n));
     ShadowWork<COUNT> W{P, SQ, R, S.bounces, n, 0, 0, 0, 0};
     trace_persistent<COUNT, true, true, CHUNK, false, true>(S, W, &counts[4]);
     if (COUNT) flush_counts(cnt, W.pops, W.inner, W.tris);
@@ -1023,34 +1029,52 @@ cudaError_t launch_batch(const DevScene& S, const PathState& P, const ShadowQueu
     end(MT_STAGE_RAYGEN);
     uint64_t l = 1;
     int cur = 0;
+    // A bounce's shadow rays and the next bounce's extension rays are
+    // independent (both come from the bounce's shading), so with a side stream
+    // the shadow stage runs there, beside the next extension, and fills that
+    // kernel's tail; the next shading waits for both.  Profiled renders keep
+    // one stream, so that each stage's events time that stage alone.
+    const bool overlap = W.side && !prof;
+    cudaError_t e = cudaSuccess;
     for (uint32_t b = 0; b < S.bounces; ++b) {
+        const int sqi = sq_slot(b);
         begin(MT_STAGE_EXTEND);
         if (P.dval)  // debug modes: counting traversal plus the per-path debug planes
-            k_extend<true, true><<<g_ext[2], 128, 0, st>>>(S, P, W.q[cur], W.counts, cur, W.rays, cnt);
+            k_extend<true, true><<<g_ext[2], 128, 0, st>>>(S, P, W.q[cur], W.counts, cur, sqi, W.rays, cnt);
         else if (count)
-            k_extend<true, false><<<g_ext[1], 128, 0, st>>>(S, P, W.q[cur], W.counts, cur, W.rays, cnt);
+            k_extend<true, false><<<g_ext[1], 128, 0, st>>>(S, P, W.q[cur], W.counts, cur, sqi, W.rays, cnt);
         else if (wide)
-            k_extend<false, false, 64><<<g_ext[3], 128, 0, st>>>(S, P, W.q[cur], W.counts, cur, W.rays, cnt);
+            k_extend<false, false, 64><<<g_ext[3], 128, 0, st>>>(S, P, W.q[cur], W.counts, cur, sqi, W.rays, cnt);
         else
-            k_extend<false, false><<<g_ext[0], 128, 0, st>>>(S, P, W.q[cur], W.counts, cur, W.rays, cnt);
+            k_extend<false, false><<<g_ext[0], 128, 0, st>>>(S, P, W.q[cur], W.counts, cur, sqi, W.rays, cnt);
         end(MT_STAGE_EXTEND);
+        if (overlap && b > 0 && e == cudaSuccess) e = cudaStreamWaitEvent(st, W.ev_shadowed, 0);
         begin(MT_STAGE_SHADE);
         if (NC.mode != MT_NRC_OFF || P.dval)
-            k_shade<true><<<gw, 128, 0, st>>>(S, P, SQ, B, b, W.q[cur], W.q[cur ^ 1], W.counts, cur, R, NC);
+            k_shade<true><<<gw, 128, 0, st>>>(S, P, SQ, B, b, W.q[cur], W.q[cur ^ 1], W.counts, cur, sqi, R, NC);
         else
-            k_shade<false><<<gw, 128, 0, st>>>(S, P, SQ, B, b, W.q[cur], W.q[cur ^ 1], W.counts, cur, R, NC);
+            k_shade<false><<<gw, 128, 0, st>>>(S, P, SQ, B, b, W.q[cur], W.q[cur ^ 1], W.counts, cur, sqi, R, NC);
         end(MT_STAGE_SHADE);
+        cudaStream_t ss = st;
+        if (overlap && e == cudaSuccess) {
+            e = cudaEventRecord(W.ev_shaded, st);
+            if (e == cudaSuccess) e = cudaStreamWaitEvent(W.side, W.ev_shaded, 0);
+            ss = W.side;
+        }
         begin(MT_STAGE_SHADOW);
         if (prof && prof->counting)
-            k_shadow<true><<<g_sh[1], 128, 0, st>>>(S, P, SQ, W.counts, W.rays + 1, cnt ? cnt + 3 : nullptr, R);
+            k_shadow<true><<<g_sh[1], 128, 0, ss>>>(S, P, SQ, W.counts, sqi, W.rays + 1, cnt ? cnt + 3 : nullptr, R);
         else if (wide)
-            k_shadow<false, 64><<<g_sh[2], 128, 0, st>>>(S, P, SQ, W.counts, W.rays + 1, nullptr, R);
+            k_shadow<false, 64><<<g_sh[2], 128, 0, ss>>>(S, P, SQ, W.counts, sqi, W.rays + 1, nullptr, R);
         else
-            k_shadow<false><<<g_sh[0], 128, 0, st>>>(S, P, SQ, W.counts, W.rays + 1, nullptr, R);
+            k_shadow<false><<<g_sh[0], 128, 0, ss>>>(S, P, SQ, W.counts, sqi, W.rays + 1, nullptr, R);
         end(MT_STAGE_SHADOW);
+        if (overlap && e == cudaSuccess) e = cudaEventRecord(W.ev_shadowed, W.side);
         l += 3;
         cur ^= 1;
     }
+    if (overlap && S.bounces > 0 && e == cudaSuccess) e = cudaStreamWaitEvent(st, W.ev_shadowed, 0);
+    if (e != cudaSuccess) return e;
     if (NC.mode == MT_NRC_TRAIN) {
         // training paths feed the cache only; no image samples
         const cudaError_t e = launch_nrc_targets(P, NC, n, S.bounces, st);

@@ -44,14 +44,20 @@ struct ShadowQueue {
 
 struct WaveBuffers {
     uint32_t* q[2];                // ping-pong queues of live path indices
-    uint32_t* counts;              // [0],[1] queue sizes, [2] shadow-queue size,
-                                   // [3] extend / [4] shadow ray fetch counters,
-                                   // [7] debug heatmap maximum (scratch)
+    uint32_t* counts;              // [0],[1] queue sizes, [2] / [5] shadow-queue size
+                                   // of even / odd bounces, [3] extend / [4] shadow
+                                   // ray fetch counters, [7] debug heatmap maximum
     unsigned long long* rays;      // [0] extension rays, [1] shadow rays traced
     float* sr;                     // per-sample tonemapped R, sample-major in a band
     float* sg;
     float* sb;
+    // optional: a second stream and two events of the owner, with which a
+    // bounce's shadow rays are traced beside the next bounce's extension rays
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_shaded = nullptr, ev_shadowed = nullptr;
 };
+// counts[] slot of the shadow-queue size of bounce b
+__host__ __device__ inline int sq_slot(uint32_t b) { return (b & 1u) ? 5 : 2; }
 
 // Per-vertex records written by a recording (path-replay) pass of the render
 // stages; null pointers in ordinary renders.  Vertex record of path p, bounce b:
