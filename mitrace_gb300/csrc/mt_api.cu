@@ -478,6 +478,15 @@ struct mt_handle {
         uint64_t plane_capacity = 0;  // samples the cached render's band planes hold
         uint32_t train_chunk = 0;     // training paths per wavefront batch
         uint32_t sample_cap = 0;
+        // the training paths' own wavefront state and stream: a frame traces
+        // them and trains beside the cached render, whose cache queries wait
+        // for the training (ev_trained)
+        DevArray<float4> tstate, tsq;
+        DevArray<uint4> thit;
+        DevArray<uint32_t> tqueues, tcounts;
+        DevArray<unsigned long long> trays;
+        cudaStream_t tstream = nullptr;
+        cudaEvent_t ev_fork = nullptr, ev_trained = nullptr;
     } nrc;
     // query scratch
     DevArray<mt_ray> qrays;
@@ -503,6 +512,9 @@ struct mt_handle {
         if (nrc.steps_graph) cudaGraphExecDestroy(nrc.steps_graph);
         pinned_slot_free(rays_host);
         if (render_done) cudaEventDestroy(render_done);
+        if (nrc.ev_fork) cudaEventDestroy(nrc.ev_fork);
+        if (nrc.ev_trained) cudaEventDestroy(nrc.ev_trained);
+        if (nrc.tstream) cudaStreamDestroy(nrc.tstream);
         if (ev_shaded) cudaEventDestroy(ev_shaded);
         if (ev_shadowed) cudaEventDestroy(ev_shadowed);
         if (side) cudaStreamDestroy(side);
@@ -1115,6 +1127,43 @@ uint64_t gcd64(uint64_t a, uint64_t b)
     return a;
 }
 
+// The frame's training steps recorded once as a CUDA graph (the launches are
+// fixed; step numbers live on the device), when the cache is enabled and again
+// whenever the step count changes.
+mt_status nrc_steps_graph(mt_handle* h)
+{
+    auto& N = h->nrc;
+    const mt_nrc_config& nc = N.cfg;
+    if (N.steps_graph && N.graph_steps == nc.train_steps) return MT_OK;
+    if (N.steps_graph) cudaGraphExecDestroy(N.steps_graph);
+    N.steps_graph = nullptr;
+    cudaStream_t cs = nullptr;
+    MT_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+    const uint64_t host_step = N.opt.step;
+    for (uint32_t s = 0; s < nc.train_steps && e == cudaSuccess; ++s) {
+        NrcTrainArgs a{};
+        a.feat = N.samples.p;
+        a.fstride = 6;
+        a.targets = reinterpret_cast<const float*>(N.samples.p + 5);
+        a.tstride = 24;
+        a.count = N.counters.p + 1;
+        a.count_cap = N.sample_cap;
+        a.rows = nc.train_batch;
+        e = launch_nrc_train_step(N.opt, a, reinterpret_cast<float*>(N.counters.p + 3), nullptr, cs);
+    }
+    N.opt.step = host_step;  // captured, not run
+    const cudaError_t e2 = cudaStreamEndCapture(cs, &graph);
+    if (e == cudaSuccess) e = e2;
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&N.steps_graph, graph, 0);
+    if (graph) cudaGraphDestroy(graph);
+    cudaStreamDestroy(cs);
+    MT_CUDA(e);
+    N.graph_steps = nc.train_steps;
+    return MT_OK;
+}
+
 mt_status nrc_alloc(mt_handle* h, const mt_nrc_config& c)
 {
     auto& N = h->nrc;
@@ -1163,6 +1212,23 @@ mt_status nrc_alloc(mt_handle* h, const mt_nrc_config& c)
     N.train_chunk = std::min<uint32_t>(c.train_paths, h->batch);
     MT_CUDA(N.trec.alloc(static_cast<size_t>(N.train_chunk) * bounces * 8));
     MT_CUDA(cudaMemsetAsync(N.trec.p, 0, N.trec.n * sizeof(float4), st));
+    MT_CUDA(N.tstate.alloc(10ull * N.train_chunk));
+    MT_CUDA(N.thit.alloc(N.train_chunk));
+    MT_CUDA(N.tsq.alloc(3ull * N.train_chunk));
+    MT_CUDA(N.tqueues.alloc(2ull * N.train_chunk));
+    MT_CUDA(N.tcounts.alloc(8));
+    MT_CUDA(cudaMemsetAsync(N.tcounts.p, 0, 8 * sizeof(uint32_t), st));
+    MT_CUDA(N.trays.alloc(2));
+    MT_CUDA(cudaMemsetAsync(N.trays.p, 0, 2 * sizeof(unsigned long long), st));
+    if (!N.tstream) {
+        // the training is on the frame's critical path (the cache queries wait
+        // for it): its kernels take free SMs before the render's
+        int lo = 0, hi = 0;
+        MT_CUDA(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+        MT_CUDA(cudaStreamCreateWithPriority(&N.tstream, cudaStreamNonBlocking, hi));
+    }
+    if (!N.ev_fork) MT_CUDA(cudaEventCreateWithFlags(&N.ev_fork, cudaEventDisableTiming));
+    if (!N.ev_trained) MT_CUDA(cudaEventCreateWithFlags(&N.ev_trained, cudaEventDisableTiming));
     N.sample_cap = c.train_paths * bounces;
     MT_CUDA(N.samples.alloc(static_cast<size_t>(N.sample_cap) * 6));
     MT_CUDA(N.qrec.alloc(static_cast<size_t>(h->batch) * 6));
@@ -1185,6 +1251,10 @@ mt_status nrc_alloc(mt_handle* h, const mt_nrc_config& c)
     MT_CUDA(launch_nrc_publish(O, st));
     MT_CUDA(cudaStreamSynchronize(st));
     N.frames = 0;
+    if (c.train_steps) {
+        const mt_status rg = nrc_steps_graph(h);
+        if (rg != MT_OK) return rg;
+    }
     N.on = true;
     return MT_OK;
 }
@@ -1760,7 +1830,39 @@ mt_status mt_nrc_frame(mt_handle* h, float* d_accum, uint32_t accum_index, void*
     if (mul == 0) mul = 1;
     while (gcd64(mul, npix) != 1) mul = (mul + 1) % npix ? (mul + 1) % npix : 1;
     const uint64_t add0 = (N.frames * 0x632BE5ABull) % npix;
-    MT_CUDA(cudaMemsetAsync(N.counters.p + 1, 0, 3 * sizeof(uint32_t), st));
+    // the training (paths, targets, Adam steps) runs on the cache's own stream
+    // with its own wavefront state, beside the cached render below
+    const cudaStream_t ts = N.tstream;
+    MT_CUDA(cudaEventRecord(N.ev_fork, st));
+    MT_CUDA(cudaStreamWaitEvent(ts, N.ev_fork, 0));
+    MT_CUDA(cudaMemsetAsync(N.counters.p + 1, 0, sizeof(uint32_t), ts));  // training samples
+    MT_CUDA(cudaMemsetAsync(N.counters.p + 3, 0, sizeof(uint32_t), ts));  // summed step losses
+    MT_CUDA(cudaMemsetAsync(N.counters.p + 2, 0, sizeof(uint32_t), st));  // the frame's queries
+    PathState Pt;
+    {
+        const uint64_t B = N.train_chunk;
+        float4* f = N.tstate.p;
+        Pt.ro = f;
+        Pt.rd = f + B;
+        Pt.cur = f + 2 * B;
+        Pt.tot = f + 3 * B;
+        Pt.prev = f + 4 * B;
+        Pt.emit = f + 5 * B;
+        Pt.direct = f + 6 * B;
+        Pt.indirect = f + 7 * B;
+        Pt.sky = f + 8 * B;
+        Pt.hitA = f + 9 * B;
+        Pt.hitB = N.thit.p;
+    }
+    ShadowQueue SQt;
+    SQt.o = N.tsq.p;
+    SQt.d = N.tsq.p + N.train_chunk;
+    SQt.c = N.tsq.p + 2ull * N.train_chunk;
+    WaveBuffers Wt{};  // no sample planes: training paths add no image samples
+    Wt.q[0] = N.tqueues.p;
+    Wt.q[1] = N.tqueues.p + N.train_chunk;
+    Wt.counts = N.tcounts.p;
+    Wt.rays = N.trays.p;
     for (uint32_t c0 = 0; c0 < nc.train_paths; c0 += N.train_chunk) {
         const uint32_t n = std::min<uint32_t>(N.train_chunk, nc.train_paths - c0);
         BatchExtra X;
@@ -1768,44 +1870,19 @@ mt_status mt_nrc_frame(mt_handle* h, float* d_accum, uint32_t accum_index, void*
         X.sample_base = 0;
         X.scatter_mul = static_cast<uint32_t>(mul);
         X.scatter_add = static_cast<uint32_t>((add0 + (static_cast<uint64_t>(c0) % npix) * mul) % npix);
-        MT_CUDA(launch_batch(St, v.P, v.SQ, v.W, 0, n, static_cast<uint32_t>(npix), 0, st, &launches, nullptr,
+        MT_CUDA(launch_batch(St, Pt, SQt, Wt, 0, n, static_cast<uint32_t>(npix), 0, ts, &launches, nullptr,
                              nullptr, &X));
     }
     // 2. Adam steps on random vertices of those paths, replayed as one CUDA
     //    graph (the launches are fixed; step numbers live on the device)
     if (nc.train_steps) {
-        if (!N.steps_graph || N.graph_steps != nc.train_steps) {
-            if (N.steps_graph) cudaGraphExecDestroy(N.steps_graph);
-            N.steps_graph = nullptr;
-            cudaStream_t cs = nullptr;
-            MT_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
-            cudaGraph_t graph = nullptr;
-            cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
-            const uint64_t host_step = N.opt.step;
-            for (uint32_t s = 0; s < nc.train_steps && e == cudaSuccess; ++s) {
-                NrcTrainArgs a{};
-                a.feat = N.samples.p;
-                a.fstride = 6;
-                a.targets = reinterpret_cast<const float*>(N.samples.p + 5);
-                a.tstride = 24;
-                a.count = N.counters.p + 1;
-                a.count_cap = N.sample_cap;
-                a.rows = nc.train_batch;
-                e = launch_nrc_train_step(N.opt, a, reinterpret_cast<float*>(N.counters.p + 3), nullptr, cs);
-            }
-            N.opt.step = host_step;  // captured, not run
-            const cudaError_t e2 = cudaStreamEndCapture(cs, &graph);
-            if (e == cudaSuccess) e = e2;
-            if (e == cudaSuccess) e = cudaGraphInstantiate(&N.steps_graph, graph, 0);
-            if (graph) cudaGraphDestroy(graph);
-            cudaStreamDestroy(cs);
-            MT_CUDA(e);
-            N.graph_steps = nc.train_steps;
-        }
-        MT_CUDA(cudaGraphLaunch(N.steps_graph, st));
+        rc = nrc_steps_graph(h);
+        if (rc != MT_OK) return rc;
+        MT_CUDA(cudaGraphLaunch(N.steps_graph, ts));
         N.opt.step += nc.train_steps;
         launches += 3ull * nc.train_steps;
     }
+    MT_CUDA(cudaEventRecord(N.ev_trained, ts));
     // 3. the cached render
     if (d_accum) {
         DevScene Sr = h->S;
@@ -1833,6 +1910,7 @@ mt_status mt_nrc_frame(mt_handle* h, float* d_accum, uint32_t accum_index, void*
                 BatchExtra X;
                 X.nrc = &Q;
                 X.sample_base = static_cast<uint32_t>(N.frames * nc.spp);
+                X.query_after = N.ev_trained;
                 MT_CUDA(launch_batch(Sr, v.P, v.SQ, Wr, g0, n, band_pix, pix_base, st, &launches, nullptr, nullptr,
                                      &X));
             }
@@ -1842,6 +1920,7 @@ mt_status mt_nrc_frame(mt_handle* h, float* d_accum, uint32_t accum_index, void*
         MT_CUDA(launch_nrc_blend(d_accum, N.frame.p, npix * 3, accum_index, st));
         ++launches;
     }
+    MT_CUDA(cudaStreamWaitEvent(st, N.ev_trained, 0));  // the frame's work ends on the caller's stream
     N.frames += 1;
     h->launches += launches;
     return MT_OK;

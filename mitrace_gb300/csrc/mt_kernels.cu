@@ -1083,6 +1083,10 @@ cudaError_t launch_batch(const DevScene& S, const PathState& P, const ShadowQueu
         return cudaSuccess;
     }
     if (NC.mode == MT_NRC_QUERY) {
+        if (X.query_after) {
+            const cudaError_t ew = cudaStreamWaitEvent(st, X.query_after, 0);
+            if (ew != cudaSuccess) return ew;
+        }
         const cudaError_t e = launch_nrc_query(NC.net, P, NC.rec, NC.count, n, NC.total, NC.err, st);
         if (e != cudaSuccess) return e;
         ++l;

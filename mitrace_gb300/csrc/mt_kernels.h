@@ -107,6 +107,7 @@ struct BatchExtra {
     uint32_t sample_base = 0;       // added to every path's sample index
     uint32_t scatter_mul = 0;       // nonzero: path p renders pixel (p * mul + add) mod W*H
     uint32_t scatter_add = 0;
+    cudaEvent_t query_after = nullptr;  // cache queries wait for this event (the frame's training)
 };
 
 cudaError_t launch_batch(const DevScene& S, const PathState& P, const ShadowQueue& SQ,
