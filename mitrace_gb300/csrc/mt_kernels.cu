@@ -909,6 +909,18 @@ static const DeviceGrids& device_grids()
     return g;
 }
 
+cudaError_t preload_render_kernels()
+{
+    cudaFuncAttributes fa;
+    cudaError_t e = cudaFuncGetAttributes(&fa, k_raygen);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_shade<true>);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_shade<false>);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_finalize);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_resolve);
+    if (e == cudaSuccess) (void)device_grids();  // the traversal kernels (occupancy queries)
+    return e;
+}
+
 int device_sm_count() { return device_grids().sms; }
 
 static unsigned grid_for(uint64_t n, unsigned block, unsigned per_sm)

@@ -110,6 +110,10 @@ struct BatchExtra {
     cudaEvent_t query_after = nullptr;  // cache queries wait for this event (the frame's training)
 };
 
+// Loads the render stages' kernels now (lazy module loading would load each at
+// its first launch).
+cudaError_t preload_render_kernels();
+
 cudaError_t launch_batch(const DevScene& S, const PathState& P, const ShadowQueue& SQ,
                          const WaveBuffers& W, uint64_t g0, uint32_t n, uint32_t band_pix,
                          uint32_t pix_base, cudaStream_t st, uint64_t* launches, Profiler* prof,

@@ -1067,6 +1067,15 @@ cudaError_t nrc_prepare()
     cudaError_t e = allow_smem(k_nrc_train_tc, kTrSmem, ok_t);
     if (e == cudaSuccess) e = allow_smem(k_nrc_infer_tc<false>, kTcSmem, ok_i0);
     if (e == cudaSuccess) e = allow_smem(k_nrc_infer_tc<true>, kTcSmem, ok_i1);
+    // with lazy module loading a kernel is loaded at its first launch, which
+    // can hold up the other stream of a frame; the cache's kernels and the
+    // render's hook variant are loaded here instead
+    cudaFuncAttributes fa;
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_nrc_adam);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_nrc_targets);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_nrc_blend);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_nrc_publish);
+    if (e == cudaSuccess) e = preload_render_kernels();
     return e;
 }
 
