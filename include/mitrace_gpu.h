@@ -278,7 +278,10 @@ mt_status mt_set_seed(mt_handle* h, uint64_t seed);
 
 /* Render into a caller-owned DEVICE buffer (W*H*3 floats) enqueued on the
  * given CUDA stream (0 = the legacy default stream).  Returns when the work is
- * enqueued; mt_get_stats reports its rays once the stream has finished it. */
+ * enqueued; mt_get_stats reports its rays once the stream has finished it.
+ * Part of the work (each bounce's shadow rays) runs on a second stream of the
+ * handle, forked from and joined back into the given stream by events, so the
+ * render completes on that stream as one unit (also under stream capture). */
 mt_status mt_render_device(mt_handle* h, float* d_rgb_out, void* cuda_stream);
 
 /* Render of image rows [row0, row1) into a caller-owned DEVICE buffer holding
@@ -445,7 +448,9 @@ mt_status mt_nrc_enable(mt_handle* h, const mt_nrc_config* c);
  *     like mt_render_device (per-sample ACES, firefly clamp over the frame's
  *     spp) and fold the frame into d_accum (W*H*3) as a running mean:
  *     accum += (frame - accum) / (accum_index + 1).
- * Frames draw distinct random numbers (sample indices continue across frames). */
+ * Frames draw distinct random numbers (sample indices continue across frames).
+ * Steps 1 and 2 run on a stream of the cache beside step 3, whose cache
+ * queries wait for them; the frame completes on cuda_stream. */
 mt_status mt_nrc_frame(mt_handle* h, float* d_accum, uint32_t accum_index, void* cuda_stream);
 mt_status mt_nrc_get_stats(mt_handle* h, mt_nrc_stats* out);
 /* Copies the FP32 master parameters out / in (MT_NRC_PARAMS floats, host).
