@@ -102,6 +102,28 @@ def test_small_batches_and_bands_give_same_image(monkeypatch):
     np.testing.assert_array_equal(img, img2)
 
 
+def test_shadow_stage_beside_extension_gives_the_sequential_image():
+    """A render traces each bounce's shadow rays on a second stream beside the
+    next bounce's extension; with the stage timing on every stage runs in order
+    on one stream.  Both give the same image bit for bit, the counter RNG and the
+    reference's RNG alike (the shadow stage is the only writer of the direct and
+    indirect light, in bounce order either way), and count the same rays."""
+    torch = pytest.importorskip("torch")
+    for name in ("material_grid", "many_instances"):
+        scene, cfg = CASES[name]()
+        imgs, rays = [], []
+        with mt.Tracer(scene, cfg) as tr:
+            out = torch.zeros((cfg.height, cfg.width, 3), dtype=torch.float32, device="cuda")
+            for profiled in (0, 1):
+                A.check(A.lib.mt_profile_enable(tr.handle, profiled, 0), "profile")
+                tr.render_device(out.data_ptr(), torch.cuda.current_stream().cuda_stream)
+                torch.cuda.synchronize()
+                imgs.append(out.cpu().numpy().copy())
+                rays.append(tr.GetStats().rays)
+        np.testing.assert_array_equal(imgs[0], imgs[1])
+        assert rays[0] == rays[1]
+
+
 def test_kill_render_and_state_errors():
     # long enough (about 1 s, 16 batches of 2^26 paths) that the kill lands mid-render
     scene, cfg = mt.material_grid(width=1920, height=1080, samples=512)
