@@ -105,9 +105,9 @@ def test_small_batches_and_bands_give_same_image(monkeypatch):
 def test_shadow_stage_beside_extension_gives_the_sequential_image():
     """A render traces each bounce's shadow rays on a second stream beside the
     next bounce's extension; with the stage timing on every stage runs in order
-    on one stream.  Both give the same image bit for bit, the counter RNG and the
-    reference's RNG alike (the shadow stage is the only writer of the direct and
-    indirect light, in bounce order either way), and count the same rays."""
+    on one stream.  Both give the same image bit for bit (the shadow stage is
+    the only writer of the direct and indirect light, in bounce order either
+    way) and count the same rays."""
     torch = pytest.importorskip("torch")
     for name in ("material_grid", "many_instances"):
         scene, cfg = CASES[name]()
