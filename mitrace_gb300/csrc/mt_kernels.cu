@@ -609,7 +609,8 @@ __global__ void __launch_bounds__(128, MT_SHADE_MIN_BLOCKS) k_shade(DevScene S, 
     // A miss costs a sky lookup, a hit the whole body above: misses are
     // handled as a warp reads the queue, hits are collected per warp in shared
     // memory and shaded 32 at a time, so a warp's lanes run the long body
-    // together instead of beside lanes that have finished
+    // together instead of beside lanes that have finished (blocks of 128
+    // threads: four warps, each holding fewer than 64 hits at a time)
     __shared__ uint32_t s_hits[4][64];
     const uint32_t lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -1089,17 +1090,14 @@ cudaError_t launch_batch(const DevScene& S, const PathState& P, const ShadowQueu
     if (e != cudaSuccess) return e;
     if (NC.mode == MT_NRC_TRAIN) {
         // training paths feed the cache only; no image samples
-        const cudaError_t e = launch_nrc_targets(P, NC, n, S.bounces, st);
+        e = launch_nrc_targets(P, NC, n, S.bounces, st);
         if (e != cudaSuccess) return e;
         if (launches) *launches += l + 1;
         return cudaSuccess;
     }
     if (NC.mode == MT_NRC_QUERY) {
-        if (X.query_after) {
-            const cudaError_t ew = cudaStreamWaitEvent(st, X.query_after, 0);
-            if (ew != cudaSuccess) return ew;
-        }
-        const cudaError_t e = launch_nrc_query(NC.net, P, NC.rec, NC.count, n, NC.total, NC.err, st);
+        if (X.query_after) e = cudaStreamWaitEvent(st, X.query_after, 0);
+        if (e == cudaSuccess) e = launch_nrc_query(NC.net, P, NC.rec, NC.count, n, NC.total, NC.err, st);
         if (e != cudaSuccess) return e;
         ++l;
     }
