@@ -15,7 +15,7 @@
   hit (instance, triangle, bvIndex, barycentrics, world distance), the
   reference's per-hit counters and the any-hit verdict are compared with the
   oracle's IntersectScene (src/Tracer/Intersect.cpp:201-219) bit for bit.
-  the benchmark spec allows near-ties (hits within 1e-6 relative t of each other) to
+  Near-ties (hits within 1e-6 relative t of each other) could be allowed to
   differ; none is exempted here: every ray must match exactly.  t and the
   barycentrics are also checked against an FP64 recomputation, to 1e-5
   relative where single precision allows it and everywhere within the error
