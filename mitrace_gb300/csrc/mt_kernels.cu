@@ -1090,9 +1090,9 @@ cudaError_t launch_batch(const DevScene& S, const PathState& P, const ShadowQueu
     if (e != cudaSuccess) return e;
     if (NC.mode == MT_NRC_TRAIN) {
         // training paths feed the cache only; no image samples
-        e = launch_nrc_targets(P, NC, n, S.bounces, st);
+        e = launch_nrc_targets(P, NC, n, S.bounces, W.q[0], st);  // the queues are free after the bounces
         if (e != cudaSuccess) return e;
-        if (launches) *launches += l + 1;
+        if (launches) *launches += l + 3;
         return cudaSuccess;
     }
     if (NC.mode == MT_NRC_QUERY) {

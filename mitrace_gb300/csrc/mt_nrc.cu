@@ -914,39 +914,117 @@ __global__ void k_nrc_blend(float* __restrict__ accum, const float* __restrict__
 // ---------------------------------------------------------------------------
 // Training targets from recorded training paths
 // ---------------------------------------------------------------------------
-__global__ void k_nrc_targets(PathState P, NrcShade N, uint32_t n, uint32_t bounces)
+// Training samples of path p, in bounce order: calls keep(k, record, target)
+// for every recorded vertex whose target is usable and mark(record) for every
+// recorded vertex.
+template <class Keep, class Mark>
+__device__ __forceinline__ void path_targets(const PathState& P, const NrcShade& N, uint32_t p, uint32_t bounces,
+                                             Keep keep, Mark mark)
+{
+    const float4 e = P.emit[p], d = P.direct[p], ind = P.indirect[p], s = P.sky[p];
+    const float tot[3] = {((e.x + d.x) + ind.x) + s.x, ((e.y + d.y) + ind.y) + s.y, ((e.z + d.z) + ind.z) + s.z};
+    for (uint32_t k = 0; k < bounces; ++k) {
+        float4* r = N.rec + (static_cast<uint64_t>(p) * bounces + k) * 8;
+        const float4 pre = r[6];
+        if (pre.w != 1.0f) break;  // vertices are recorded in bounce order
+        mark(r);
+        const float cur[3] = {r[5].x, r[5].y, r[5].z};
+        // AT_DIFFUSE: the cache stands for what the vertex reflects from the
+        // rest of its path, so its own NEE is part of the prefix
+        const float4 nee = N.end_at == MT_NRC_END_AT_DIFFUSE ? r[7] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        const float prv[3] = {pre.x + nee.x, pre.y + nee.y, pre.z + nee.z};
+        float tg[3];
+        bool ok = true;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            ok = ok && cur[c] > 1e-6f;
+            float sfx = fmaxf(tot[c] - prv[c], 0.0f);
+            if (N.target_cap > 0.0f) sfx = fminf(sfx, N.target_cap);
+            tg[c] = sfx / cur[c];
+            ok = ok && isfinite(tg[c]);
+        }
+        if (ok) keep(r, tg);
+    }
+}
+
+// Pass 1: usable samples per path.
+__global__ void k_nrc_target_count(PathState P, NrcShade N, uint32_t n, uint32_t bounces, uint32_t* counts)
 {
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
-        const float4 e = P.emit[p], d = P.direct[p], ind = P.indirect[p], s = P.sky[p];
-        const float tot[3] = {((e.x + d.x) + ind.x) + s.x, ((e.y + d.y) + ind.y) + s.y, ((e.z + d.z) + ind.z) + s.z};
-        for (uint32_t k = 0; k < bounces; ++k) {
-            float4* r = N.rec + (static_cast<uint64_t>(p) * bounces + k) * 8;
-            const float4 pre = r[6];
-            if (pre.w != 1.0f) break;  // vertices are recorded in bounce order
-            r[6].w = 0.0f;
-            const float cur[3] = {r[5].x, r[5].y, r[5].z};
-            // AT_DIFFUSE: the cache stands for what the vertex reflects from the
-            // rest of its path, so its own NEE is part of the prefix
-            const float4 nee = N.end_at == MT_NRC_END_AT_DIFFUSE ? r[7] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            const float prv[3] = {pre.x + nee.x, pre.y + nee.y, pre.z + nee.z};
-            float tg[3];
-            bool ok = true;
+        uint32_t c = 0;
+        path_targets(P, N, p, bounces, [&](const float4*, const float*) { ++c; }, [](float4*) {});
+        counts[p] = c;
+    }
+}
+
+// Exclusive prefix of the per-path counts, continuing after the samples
+// already in the buffer (*N.sample_count), which then counts these as well:
+// one block of 1024 threads, 16 consecutive paths per thread per tile.
+__global__ void __launch_bounds__(1024) k_nrc_target_scan(NrcShade N, uint32_t n, uint32_t* counts)
+{
+    __shared__ uint32_t warp_sum[32];
+    __shared__ uint32_t carry;
+    const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    if (tid == 0) carry = *N.sample_count;
+    __syncthreads();
+    constexpr uint32_t kPer = 16, kTile = 1024 * kPer;
+    for (uint32_t t0 = 0; t0 < n; t0 += kTile) {
+        const uint32_t first = t0 + tid * kPer;
+        uint32_t v[kPer], sum = 0;
 #pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                ok = ok && cur[c] > 1e-6f;
-                float sfx = fmaxf(tot[c] - prv[c], 0.0f);
-                if (N.target_cap > 0.0f) sfx = fminf(sfx, N.target_cap);
-                tg[c] = sfx / cur[c];
-                ok = ok && isfinite(tg[c]);
-            }
-            if (!ok) continue;
-            const uint32_t slot = atomicAdd(N.sample_count, 1u);
-            if (slot >= N.sample_cap) continue;
-            float4* o = N.samples + static_cast<uint64_t>(slot) * 6;
-#pragma unroll
-            for (int i = 0; i < 5; ++i) o[i] = r[i];
-            o[5] = make_float4(tg[0], tg[1], tg[2], 0.0f);
+        for (uint32_t i = 0; i < kPer; ++i) {
+            v[i] = first + i < n ? counts[first + i] : 0u;
+            sum += v[i];
         }
+        uint32_t incl = sum;  // inclusive scan of the threads' sums
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t x = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= static_cast<uint32_t>(o)) incl += x;
+        }
+        if (lane == 31) warp_sum[warp] = incl;
+        __syncthreads();
+        if (warp == 0) {
+            uint32_t w = warp_sum[lane], wi = w;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t x = __shfl_up_sync(0xffffffffu, wi, o);
+                if (lane >= static_cast<uint32_t>(o)) wi += x;
+            }
+            warp_sum[lane] = wi - w;  // exclusive over warps
+        }
+        __syncthreads();
+        uint32_t run = carry + warp_sum[warp] + (incl - sum);
+#pragma unroll
+        for (uint32_t i = 0; i < kPer; ++i) {
+            if (first + i < n) counts[first + i] = run;
+            run += v[i];
+        }
+        __syncthreads();
+        if (tid == 1023) carry = run;
+        __syncthreads();
+    }
+    if (tid == 0) *N.sample_count = carry;
+}
+
+// Pass 2: the samples at their places (training vertices in path order, so
+// a frame's sample buffer is the same on every run).
+__global__ void k_nrc_targets(PathState P, NrcShade N, uint32_t n, uint32_t bounces, const uint32_t* offsets)
+{
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+        uint32_t slot = offsets[p];
+        path_targets(
+            P, N, p, bounces,
+            [&](const float4* r, const float* tg) {
+                if (slot < N.sample_cap) {
+                    float4* o = N.samples + static_cast<uint64_t>(slot) * 6;
+#pragma unroll
+                    for (int i = 0; i < 5; ++i) o[i] = r[i];
+                    o[5] = make_float4(tg[0], tg[1], tg[2], 0.0f);
+                }
+                ++slot;
+            },
+            [](float4* r) { r[6].w = 0.0f; });
     }
 }
 
@@ -1019,10 +1097,12 @@ cudaError_t launch_nrc_encode(const float* features, uint32_t n, float* out, cud
 }
 
 cudaError_t launch_nrc_targets(const PathState& P, const NrcShade& N, uint32_t n, uint32_t bounces,
-                               cudaStream_t st)
+                               uint32_t* scratch, cudaStream_t st)
 {
     const unsigned blocks = static_cast<unsigned>(std::min<uint64_t>((n + 255) / 256, 4096));
-    k_nrc_targets<<<blocks ? blocks : 1, 256, 0, st>>>(P, N, n, bounces);
+    k_nrc_target_count<<<blocks ? blocks : 1, 256, 0, st>>>(P, N, n, bounces, scratch);
+    k_nrc_target_scan<<<1, 1024, 0, st>>>(N, n, scratch);
+    k_nrc_targets<<<blocks ? blocks : 1, 256, 0, st>>>(P, N, n, bounces, scratch);
     return cudaGetLastError();
 }
 
@@ -1073,6 +1153,8 @@ cudaError_t nrc_prepare()
     cudaFuncAttributes fa;
     if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_nrc_adam);
     if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_nrc_targets);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_nrc_target_count);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_nrc_target_scan);
     if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_nrc_blend);
     if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_nrc_publish);
     if (e == cudaSuccess) e = preload_render_kernels();

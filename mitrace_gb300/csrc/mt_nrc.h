@@ -57,9 +57,10 @@ struct NrcShade {
 // Cache queries of a batch: adds throughput * max(cache, 0) to P.indirect.
 cudaError_t launch_nrc_query(const void* net, const PathState& P, const float4* rec, const uint32_t* count,
                              uint32_t capacity, uint32_t* total, int* err, cudaStream_t st);
-// Training targets of a batch of training paths -> samples.
+// Training targets of a batch of training paths -> samples, placed in path
+// order (scratch: n uint32 for the per-path counts and offsets).
 cudaError_t launch_nrc_targets(const PathState& P, const NrcShade& N, uint32_t n, uint32_t bounces,
-                               cudaStream_t st);
+                               uint32_t* scratch, cudaStream_t st);
 // Plain inference into out (n x 3).
 cudaError_t launch_nrc_infer(const void* net, const float* features, uint32_t n, float* out, int* err,
                              cudaStream_t st);

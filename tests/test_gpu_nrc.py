@@ -138,6 +138,26 @@ def test_cache_hooks_leave_plain_paths_unchanged(end_at):
     np.testing.assert_array_equal(acc.cpu().numpy(), img.cpu().numpy())
 
 
+def test_cached_frames_are_reproducible():
+    """A frame trains on the cache's own stream beside its render, whose cache
+    queries wait for the training; the training vertices are placed in path
+    order and the gradient sums have a fixed order.  Two handles with the same
+    scene and cache configuration render the same two frames bit for bit."""
+    scene, cfg = small_room()
+    st = torch.cuda.current_stream().cuda_stream
+    accs = []
+    for _ in range(2):
+        acc = torch.zeros((cfg.height, cfg.width, 3), device="cuda")
+        with mt.Tracer(scene, cfg) as tr:
+            tr.nrc_enable(train_paths=4096, train_batch=1024, train_steps=16, spp=cfg.samples)
+            for f in range(2):
+                tr.nrc_frame(acc.data_ptr(), f, st)
+            torch.cuda.synchronize()
+        accs.append(acc.cpu().numpy())
+    assert np.abs(accs[0]).max() > 0
+    np.testing.assert_array_equal(accs[0], accs[1])
+
+
 @pytest.mark.parametrize("end_at", [A.MT_NRC_END_AFTER_DIFFUSE, A.MT_NRC_END_AT_DIFFUSE])
 def test_cached_frames_converge_near_plain_render(end_at):
     """Box room at +15 EV, where the per-sample ACES curve is linear (so the
