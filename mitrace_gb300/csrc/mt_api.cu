@@ -295,6 +295,10 @@ bool bvh_depth(const std::vector<mt_bvh_node>& nodes, const std::vector<uint32_t
         why = "empty BVH";
         return false;
     }
+    if (nodes.size() >= MT_BVH_LEAF_BIT) {  // traversal stack entries flag leaves with that bit
+        why = "BVH with 2^31 nodes or more";
+        return false;
+    }
     std::vector<std::pair<uint32_t, uint32_t>> st{{0u, 0u}};
     size_t visited = 0;
     while (!st.empty()) {

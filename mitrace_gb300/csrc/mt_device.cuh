@@ -280,7 +280,7 @@ __device__ __forceinline__ bool tri_test(f3 o, f3 d, f3 v0, f3 e1, f3 e2, float&
 // decisions as tri_test followed by that range check.
 struct TriStage {
     f3 e1, e2, sv, q;
-    float det, sg, adet, us, u, v, t;
+    float det, sg, adet, us, u, v, t, inv;
     __device__ __forceinline__ bool begin(f3 o, f3 d, float4 v0, float4 e1w, float4 e2w)
     {
         e1 = xyz(e1w);
@@ -301,11 +301,16 @@ struct TriStage {
         const float vs = v * sg;
         return !(vs < 0.0f || __fadd_rn(us, vs) > adet);
     }
-    // t is formed (one division) only on a lane that is still a candidate
+    // t is formed (one division, 1/det, which also scales u and v of the
+    // winner) only on a lane that is still a candidate
     __device__ __forceinline__ bool finish(bool ok, float dist)
     {
         t = FLT_MAX;
-        if (ok) t = __fmul_rn(dot(e2, q), __fdiv_rn(1.0f, det));
+        inv = 0.0f;
+        if (ok) {
+            inv = __fdiv_rn(1.0f, det);
+            t = __fmul_rn(dot(e2, q), inv);
+        }
         return ok && t > 0.0f && t < dist;
     }
 };
@@ -460,6 +465,11 @@ __device__ __forceinline__ void trace_persistent(const DevScene& S, Work& W, uin
     float top_dist = 0.0f;
     bool pending = false;
     uint32_t pfirst = 0, pcount = 0, pnode = 0;
+    // Stack entries (and top_node): an inner node as its a word, the index of
+    // its first child (siblings sit at (a, a + 1), 64 contiguous bytes), a leaf
+    // as its own index | MT_BVH_LEAF_BIT.  A child's a word comes with its box,
+    // so popping an inner node loads its children's boxes without first
+    // loading the node itself.
     uint32_t stk_node[MT_STACK_SIZE];
     float stk_dist[MT_STACK_SIZE];
 
@@ -630,13 +640,14 @@ __device__ __forceinline__ void trace_persistent(const DevScene& S, Work& W, uin
                     in_inst = true;
                     if (m.has_bvh) {
                         const float4 a = __ldg(nodes + 0), b = __ldg(nodes + 1);
+                        const uint32_t root = (f2u(a.w) & MT_BVH_LEAF_BIT) ? MT_BVH_LEAF_BIT : f2u(a.w);
                         if (STACK_TOP) {
-                            top_node = 0;
+                            top_node = root;
                             top_dist = slab(lo, linv, xyz(a), xyz(b));
                             top = true;
                             sp = 0;
                         } else {
-                            stk_node[0] = 0;
+                            stk_node[0] = root;
                             stk_dist[0] = slab(lo, linv, xyz(a), xyz(b));
                             sp = 1;
                         }
@@ -673,21 +684,24 @@ __device__ __forceinline__ void trace_persistent(const DevScene& S, Work& W, uin
                 }
                 if (COUNT) ++h.bvh_tests;
                 if (!(nd < 0.0f) && !(nd > __fadd_rn(h.t, 0.1f))) {
-                    const uint32_t na = f2u(__ldg(&nodes[2 * ni].w));
-                    const uint32_t nb = f2u(__ldg(&nodes[2 * ni + 1].w));
-                    if (na & MT_BVH_LEAF_BIT) {
+                    if (ni & MT_BVH_LEAF_BIT) {
+                        const uint32_t leaf = ni & ~MT_BVH_LEAF_BIT;
                         pending = true;
-                        pfirst = na & ~MT_BVH_LEAF_BIT;
-                        pcount = nb & ~MT_BVH_LEAF_BIT;
-                        pnode = ni;
+                        pfirst = f2u(__ldg(&nodes[2 * leaf].w)) & ~MT_BVH_LEAF_BIT;
+                        pcount = f2u(__ldg(&nodes[2 * leaf + 1].w)) & ~MT_BVH_LEAF_BIT;
+                        pnode = leaf;
                         if (S.trav_prefetch && pcount)
                             prefetch_l2(S.slots + 3ull * (slot_base + pfirst), 48u * (pcount < 32u ? pcount : 32u));
                     } else {
                         if (COUNT) ++h.inner;
+                        // the children (na, na + 1) are the 64 bytes at node na
+                        const uint32_t na = ni, nb = ni + 1;
                         const float4 a0 = __ldg(nodes + 2 * na), a1 = __ldg(nodes + 2 * na + 1);
                         const float4 b0 = __ldg(nodes + 2 * nb), b1 = __ldg(nodes + 2 * nb + 1);
                         const float da = slab(lo, linv, xyz(a0), xyz(a1));
                         const float db = slab(lo, linv, xyz(b0), xyz(b1));
+                        const uint32_t ea = (f2u(a0.w) & MT_BVH_LEAF_BIT) ? (na | MT_BVH_LEAF_BIT) : f2u(a0.w);
+                        const uint32_t eb = (f2u(b0.w) & MT_BVH_LEAF_BIT) ? (nb | MT_BVH_LEAF_BIT) : f2u(b0.w);
                         const float lim = __fadd_rn(h.t, 0.1f);
                         const bool pa = da >= 0.0f && da <= lim;
                         const bool pb = db >= 0.0f && db <= lim;
@@ -699,29 +713,29 @@ __device__ __forceinline__ void trace_persistent(const DevScene& S, Work& W, uin
                             // far child to memory, near child (popped next) to the top
                             if (pa && pb) {
                                 const bool a_near = da < db;
-                                stk_node[sp] = a_near ? nb : na;
+                                stk_node[sp] = a_near ? eb : ea;
                                 stk_dist[sp] = a_near ? db : da;
                                 ++sp;
-                                top_node = a_near ? na : nb;
+                                top_node = a_near ? ea : eb;
                                 top_dist = a_near ? da : db;
                                 top = true;
                             } else if (pa || pb) {
-                                top_node = pa ? na : nb;
+                                top_node = pa ? ea : eb;
                                 top_dist = pa ? da : db;
                                 top = true;
                             }
                         } else if (pa && pb) {
                             if (da < db) {
-                                stk_node[sp] = nb; stk_dist[sp] = db; ++sp;
-                                stk_node[sp] = na; stk_dist[sp] = da; ++sp;
+                                stk_node[sp] = eb; stk_dist[sp] = db; ++sp;
+                                stk_node[sp] = ea; stk_dist[sp] = da; ++sp;
                             } else {
-                                stk_node[sp] = na; stk_dist[sp] = da; ++sp;
-                                stk_node[sp] = nb; stk_dist[sp] = db; ++sp;
+                                stk_node[sp] = ea; stk_dist[sp] = da; ++sp;
+                                stk_node[sp] = eb; stk_dist[sp] = db; ++sp;
                             }
                         } else if (pa) {
-                            stk_node[sp] = na; stk_dist[sp] = da; ++sp;
+                            stk_node[sp] = ea; stk_dist[sp] = da; ++sp;
                         } else if (pb) {
-                            stk_node[sp] = nb; stk_dist[sp] = db; ++sp;
+                            stk_node[sp] = eb; stk_dist[sp] = db; ++sp;
                         }
                     }
                 }
@@ -767,7 +781,7 @@ __device__ __forceinline__ void trace_persistent(const DevScene& S, Work& W, uin
         // whose IEEE bit patterns order like the values, so one unsigned min
         // finds the smallest t and the lowest lane holding it is the first such
         // triangle of the chunk
-        auto chunk_min = [&](bool ok, float t, float u, float v, float det, uint32_t c, float& bt, float& bu,
+        auto chunk_min = [&](bool ok, float t, float u, float v, float inv, uint32_t c, float& bt, float& bu,
                              float& bv, uint32_t& bidx) {
             const uint32_t key = ok ? __float_as_uint(t) : 0xffffffffu;
             const uint32_t kmin = __reduce_min_sync(MT_FULL, key);
@@ -775,9 +789,8 @@ __device__ __forceinline__ void trace_persistent(const DevScene& S, Work& W, uin
                 const uint32_t w = __ffs(__ballot_sync(MT_FULL, key == kmin)) - 1;
                 float uu = 0.0f, vv = 0.0f;
                 if (lane == w) {
-                    const float id = __fdiv_rn(1.0f, det);
-                    uu = __fmul_rn(u, id);
-                    vv = __fmul_rn(v, id);
+                    uu = __fmul_rn(u, inv);
+                    vv = __fmul_rn(v, inv);
                 }
                 bt = __uint_as_float(kmin);
                 bidx = c + w;
@@ -829,8 +842,8 @@ __device__ __forceinline__ void trace_persistent(const DevScene& S, Work& W, uin
                     if (__any_sync(MT_FULL, oka || okb)) {
                         oka = sa.finish(oka, dista);
                         okb = sb.finish(okb, distb);
-                        chunk_min(oka, sa.t, sa.u, sa.v, sa.det, c, bta, bua, bva, bia);
-                        chunk_min(okb, sb.t, sb.u, sb.v, sb.det, c, btb, bub, bvb, bib);
+                        chunk_min(oka, sa.t, sa.u, sa.v, sa.inv, c, bta, bua, bva, bia);
+                        chunk_min(okb, sb.t, sb.u, sb.v, sb.inv, c, btb, bub, bvb, bib);
                     }
                 }
             }
@@ -879,10 +892,13 @@ __device__ __forceinline__ void trace_persistent(const DevScene& S, Work& W, uin
                     const float vs = v * sg;
                     ok = ok && !(vs < 0.0f || __fadd_rn(us, vs) > adet);
                     if (__any_sync(MT_FULL, ok)) {
-                        float t = FLT_MAX;
-                        if (ok) t = __fmul_rn(dot(e2, q), __fdiv_rn(1.0f, det));
+                        float t = FLT_MAX, inv = 0.0f;
+                        if (ok) {
+                            inv = __fdiv_rn(1.0f, det);
+                            t = __fmul_rn(dot(e2, q), inv);
+                        }
                         ok = ok && t > 0.0f && t < dist;
-                        chunk_min(ok, t, u, v, det, c, bt, bu, bv, bidx);
+                        chunk_min(ok, t, u, v, inv, c, bt, bu, bv, bidx);
                     }
                 }
             }

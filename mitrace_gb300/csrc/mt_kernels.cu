@@ -174,7 +174,43 @@ struct BatchInfo {
     uint32_t sample_base;  // added to the sample index of every path
     uint32_t scatter_mul;  // nonzero: path p is pixel (p * mul + add) mod W*H, sample sample_base
     uint32_t scatter_add;
+    uint32_t tiled;     // nonzero: a sample's paths visit the band in pixel tiles (tile_pixel)
 };
+
+// Pixel tiles of MT_PIXEL_TILE_W x (32 / MT_PIXEL_TILE_W): with `tiled`, the 32
+// consecutive paths of a warp cover one tile instead of 32 pixels of a row, so
+// their camera rays (and the origins of the next bounces) lie close together
+// and the warp's lanes walk the same nodes and leaves.  The order only decides
+// which path computes which (pixel, sample); every path's result, which the
+// counter-based draws key by pixel and sample, is unchanged.
+#ifndef MT_PIXEL_TILE_W
+#define MT_PIXEL_TILE_W 4
+#endif
+static_assert(MT_PIXEL_TILE_W >= 1 && MT_PIXEL_TILE_W <= 32 && 32 % MT_PIXEL_TILE_W == 0, "tile width");
+
+// Row-major offset inside a band of width W and band_pix pixels of the k-th
+// pixel in tile order: whole tiles first (row of tiles by row of tiles), then
+// the columns right of the last whole tile in those rows, then the rows below
+// the last whole row of tiles, both row-major.  A bijection of [0, band_pix).
+__device__ __forceinline__ uint32_t tile_pixel(uint32_t k, uint32_t W, uint32_t band_pix)
+{
+    constexpr uint32_t TW = MT_PIXEL_TILE_W, TH = 32 / MT_PIXEL_TILE_W;
+    const uint32_t rows = band_pix / W;
+    const uint32_t rfull = rows - rows % TH;
+    const uint32_t wfull = W - W % TW;
+    if (k < rfull * wfull) {
+        const uint32_t t = k >> 5, w = k & 31u;
+        const uint32_t per_row = wfull / TW;
+        const uint32_t tr = t / per_row, tc = t - tr * per_row;
+        return (tr * TH + w / TW) * W + tc * TW + w % TW;
+    }
+    if (k < rfull * W) {
+        const uint32_t m = k - rfull * wfull, mw = W - wfull;
+        const uint32_t y = m / mw;
+        return y * W + wfull + (m - y * mw);
+    }
+    return k;
+}
 
 __device__ __forceinline__ void path_coords(const DevScene& S, const BatchInfo& B, uint32_t p,
                                             uint32_t& pixel, uint32_t& sample)
@@ -186,8 +222,16 @@ __device__ __forceinline__ void path_coords(const DevScene& S, const BatchInfo& 
         return;
     }
     const uint64_t g = B.g0 + p;
-    sample = static_cast<uint32_t>(g / B.band_pix);
-    pixel = B.pix_base + static_cast<uint32_t>(g - static_cast<uint64_t>(sample) * B.band_pix);
+    uint32_t k;
+    if (g >> 32) {
+        sample = static_cast<uint32_t>(g / B.band_pix);
+        k = static_cast<uint32_t>(g - static_cast<uint64_t>(sample) * B.band_pix);
+    } else {  // 32-bit division for the common case
+        const uint32_t g32 = static_cast<uint32_t>(g);
+        sample = g32 / B.band_pix;
+        k = g32 - sample * B.band_pix;
+    }
+    pixel = B.pix_base + (B.tiled ? tile_pixel(k, S.width, B.band_pix) : k);
     sample += B.sample_base;
 }
 
@@ -756,7 +800,13 @@ __global__ void __launch_bounds__(256) k_finalize(DevScene S, PathState P, Batch
         }
         f3 c = aces(total, S.exposure);
         if (P.dval) c = debug_sample(S, P, p, c);
-        const uint64_t g = B.g0 + p;
+        // plane slot of the path's (pixel, sample): sample-major, row-major pixels
+        uint64_t g = B.g0 + p;
+        if (B.tiled) {
+            uint32_t pixel, sample;
+            path_coords(S, B, p, pixel, sample);
+            g = static_cast<uint64_t>(sample - B.sample_base) * B.band_pix + (pixel - B.pix_base);
+        }
         sr[g] = c.x;
         sg[g] = c.y;
         sb[g] = c.z;
@@ -1027,7 +1077,10 @@ cudaError_t launch_batch(const DevScene& S, const PathState& P, const ShadowQueu
     const BatchExtra X = extra ? *extra : BatchExtra{};
     const NrcShade NC = X.nrc ? *X.nrc : NrcShade{};
     if (NC.mode == MT_NRC_TRAIN) R.nrc = NC.rec;
-    BatchInfo B{g0, n, band_pix, pix_base, X.sample_base, X.scatter_mul, X.scatter_add};
+    // tile order for image batches; the adjoint's record batches keep the
+    // row-major order that its replay indexes paths by
+    const uint32_t tiled = !rec && !X.scatter_mul && S.width && band_pix % S.width == 0;
+    BatchInfo B{g0, n, band_pix, pix_base, X.sample_base, X.scatter_mul, X.scatter_add, tiled};
     const unsigned gw = grid_for(n, 128, 16);
     const DeviceGrids& G = device_grids();
     const unsigned* g_ext = G.ext;

@@ -2,7 +2,8 @@
 an empty scene (sky only, and black without a sky), a scene without lights,
 spot / directional / area lights (the reference shades every non-spot light
 as a point at its node position, Tracer.cpp:295-297), a 1x1 image at 1 spp
-and 1 bounce, ragged batches and bands, and a zero-spp config rejected."""
+and 1 bounce, ragged batches and bands, the tiled path order at ragged
+image edges, and a zero-spp config rejected."""
 import ctypes as C
 
 import numpy as np
@@ -78,6 +79,21 @@ def test_ragged_batches_and_bands(monkeypatch):
     monkeypatch.setenv("MT_SAMPLE_BUDGET_MB", "0")  # one image row per band
     img, ref, *_ = both(scene, cfg)
     close(img, ref)
+
+
+def test_tiled_path_order_with_ragged_edges(monkeypatch):
+    """One 37x23 band: four rows of whole 8x4 pixel tiles, the 5 columns right
+    of them and the 3 rows below, in batches of 1021 paths that cut tiles and
+    samples.  The image equals the oracle's, and bit for bit the one rendered
+    in bands of one row (whose paths keep the row-major order)."""
+    scene, cfg = small_grid(width=37, height=23, samples=5, seed=9)
+    monkeypatch.setenv("MT_BATCH_PATHS", "1021")
+    img, ref, st, rays, samples = both(scene, cfg)
+    close(img, ref)
+    assert st.samples == samples and st.rays == rays
+    monkeypatch.setenv("MT_SAMPLE_BUDGET_MB", "0")  # one image row per band
+    row_major, *_ = both(scene, cfg)
+    np.testing.assert_array_equal(img, row_major)
 
 
 def test_zero_samples_rejected():
