@@ -609,14 +609,19 @@ __global__ void __launch_bounds__(128, MT_SHADE_MIN_BLOCKS) k_shade(DevScene S, 
             const float ps = specular_probability(view, N, base, mp.metallic);
             const uint4 rl = draw(S, pixel, sample, bounce, SLOT_LOBE);
             f3 nd;
+            // the diffuse lobe and the GGX fallback share one cosine sample
+            // (one copy of its code), with the uniforms of their draw
+            uint32_t cu1 = rl.y, cu2 = rl.z;
+            bool cosine = true;
             if (urange(rl.x, 0.0f, 1.0f) < ps) {
-                if (!ggx_reflection(rd, N, mp.roughness, urange(rl.y, 0.0f, 1.0f), urange(rl.z, 0.0f, 1.0f), nd)) {
+                cosine = !ggx_reflection(rd, N, mp.roughness, urange(rl.y, 0.0f, 1.0f), urange(rl.z, 0.0f, 1.0f), nd);
+                if (cosine) {
                     const uint4 rf = draw(S, pixel, sample, bounce, SLOT_FALLBACK);
-                    nd = cosine_hemisphere(urange(rf.x, 0.0f, 1.0f), urange(rf.y, 0.0f, 1.0f), N);
+                    cu1 = rf.x;
+                    cu2 = rf.y;
                 }
-            } else {
-                nd = cosine_hemisphere(urange(rl.y, 0.0f, 1.0f), urange(rl.z, 0.0f, 1.0f), N);
             }
+            if (cosine) nd = cosine_hemisphere(urange(cu1, 0.0f, 1.0f), urange(cu2, 0.0f, 1.0f), N);
             const float dp = diffuse_pdf(nd, N);
             const float sp = specular_pdf(nd, view, N, mp.roughness);
             const float pdf = __fadd_rn(__fmul_rn(__fsub_rn(1.0f, ps), dp), __fmul_rn(ps, sp));
