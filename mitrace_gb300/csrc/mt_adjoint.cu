@@ -123,7 +123,7 @@ __device__ void brdf_vjp(f3 L, f3 V, f3 N, f3 base, float rough, float metal, f3
     const D5 r = dmax(dvar(rough, 3), 0.05f);
     const D5 m = dvar(metal, 4);
     const D5 mc = dclamp01(m);
-    const float p5 = powf(1.0f - hv, 5.0f);
+    const float p5 = pow5(1.0f - hv);
     // D (GGX) and G (Smith-Schlick), functions of roughness only
     const D5 a = r * r;
     const D5 a2 = a * a;

@@ -977,10 +977,29 @@ __device__ __forceinline__ void camera_ray(const DevScene& S, float u, float v, 
 // ---------------------------------------------------------------------------
 // BRDF (src/Tracer/BRDF.hpp:9-97)
 // ---------------------------------------------------------------------------
+// x^5 for x in [0, 1] (the Schlick factor's pow(1 - cos, 5)) by compensated
+// products: Dekker's TwoProduct, with an FMA giving each product's rounding
+// error exactly (Ogita, Rump and Oishi, "Accurate sum and dot product", 2005).
+// x^2 = p2 + e2 and p2^2 = p4 + e4 exactly, so x^4 = p4 + (e4 + 2 p2 e2)
+// up to e2^2 (2^-48 relative); p4 x = p5 + e5 exactly, so
+// x^5 = p5 + (e5 + (e4 + 2 p2 e2) x), and the one rounding of that sum leaves
+// the result within 2^-45 relative of x^5 before it: the correctly rounded
+// value except when x^5 lies that close to a rounding tie.  The reference's
+// powf is within 1 ulp; a general power function is much more code.
+__device__ __forceinline__ float pow5(float x)
+{
+    const float p2 = __fmul_rn(x, x);
+    const float e2 = __fmaf_rn(x, x, -p2);
+    const float p4 = __fmul_rn(p2, p2);
+    const float t4 = __fmaf_rn(__fmul_rn(2.0f, p2), e2, __fmaf_rn(p2, p2, -p4));
+    const float p5 = __fmul_rn(p4, x);
+    const float e5 = __fmaf_rn(p4, x, -p5);
+    return __fadd_rn(p5, __fmaf_rn(t4, x, e5));
+}
 __device__ __forceinline__ f3 fresnel_schlick(float c, f3 f0)
 {
     c = gclamp(c, 0.0f, 1.0f);
-    const float p = powf(__fsub_rn(1.0f, c), 5.0f);
+    const float p = pow5(__fsub_rn(1.0f, c));
     return f0 + (splat(1.0f) - f0) * splat(p);
 }
 __device__ __forceinline__ f3 base_reflectivity(f3 base, float metallic)
@@ -1002,7 +1021,7 @@ __device__ __forceinline__ float geometry_schlick_ggx(float nv, float r)
 {
     nv = gclamp(nv, 0.0f, 1.0f);
     const float rr = __fadd_rn(r, 1.0f);
-    const float k = __fdiv_rn(__fmul_rn(rr, rr), 8.0f);
+    const float k = __fmul_rn(__fmul_rn(rr, rr), 0.125f);  // the same rounded value as x / 8
     const float den = __fadd_rn(__fmul_rn(nv, __fsub_rn(1.0f, k)), k);
     return __fdiv_rn(nv, den);
 }
@@ -1053,7 +1072,9 @@ __device__ __forceinline__ f3 cosine_hemisphere(float u1, float u2, f3 n)
     const float phi = __fmul_rn(__fmul_rn(2.0f, kPi), u2);
     f3 t, b;
     build_tbn(n, t, b);
-    const float lx = __fmul_rn(r, cosf(phi)), ly = __fmul_rn(r, sinf(phi));
+    float sp, cp;
+    sincosf(phi, &sp, &cp);  // one argument reduction for both
+    const float lx = __fmul_rn(r, cp), ly = __fmul_rn(r, sp);
     const float lz = __fsqrt_rn(gmax(0.0f, __fsub_rn(1.0f, u1)));
     return normalize(t * lx + b * ly + n * lz);
 }
@@ -1079,7 +1100,9 @@ __device__ __forceinline__ bool ggx_reflection(f3 rd, f3 N, float roughness, flo
     const float sinT = __fsqrt_rn(gmax(0.0f, __fsub_rn(1.0f, __fmul_rn(cosT, cosT))));
     f3 t, b;
     build_tbn(N, t, b);
-    f3 h = normalize(t * __fmul_rn(sinT, cosf(phi)) + b * __fmul_rn(sinT, sinf(phi)) + N * cosT);
+    float sp, cp;
+    sincosf(phi, &sp, &cp);  // one argument reduction for both
+    f3 h = normalize(t * __fmul_rn(sinT, cp) + b * __fmul_rn(sinT, sp) + N * cosT);
     if (dot(h, -rd) < 0.0f) h = -h;
     const f3 r = reflect(rd, h);
     if (!(dot(r, N) > 0.0f)) return false;

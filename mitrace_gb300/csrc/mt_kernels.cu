@@ -541,7 +541,10 @@ __global__ void __launch_bounds__(128, MT_SHADE_MIN_BLOCKS) k_shade(DevScene S, 
                     const uint4 rj = draw(S, pixel, sample, bounce, SLOT_LIGHT_JITTER);
                     const float a = urange(rj.x, 0.0f, __fmul_rn(2.0f, kPi));
                     const float b = urange(rj.y, -kPi / 2.0f, kPi / 2.0f);
-                    const f3 dir = normalize(f3{__fmul_rn(cosf(a), cosf(b)), sinf(b), __fmul_rn(sinf(a), cosf(b))});
+                    float sa, ca, sb, cb;
+                    sincosf(a, &sa, &ca);  // one argument reduction for both
+                    sincosf(b, &sb, &cb);
+                    const f3 dir = normalize(f3{__fmul_rn(ca, cb), sb, __fmul_rn(sa, cb)});
                     lpos = lpos0 + dir * __ldg(&L.point_size);
                 }
                 const f3 lvec = lpos - hit_pos;

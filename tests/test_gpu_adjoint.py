@@ -230,7 +230,10 @@ def test_autograd_function_backpropagates():
     loss = RenderLoss.apply(base, scene, cfg, target)
     loss.backward()
     g = gpu_grad(scene, cfg, target)
-    np.testing.assert_allclose(base.grad.numpy(), g["d_base"], rtol=1e-6)
+    # a second run of the adjoint: its float atomic sums add in a scheduling-
+    # dependent order, so the two agree to rounding (measured up to ~1.1e-6
+    # relative), not bit for bit
+    np.testing.assert_allclose(base.grad.numpy(), g["d_base"], rtol=1e-5)
     assert np.abs(base.grad.numpy()).max() > 0
 
 
