@@ -395,12 +395,16 @@ __device__ __forceinline__ void st4(float4* p, uint32_t i, f3 v, float w = 0.0f)
 #ifndef MT_SHADE_MIN_BLOCKS
 #define MT_SHADE_MIN_BLOCKS 8
 #endif
+#ifndef MT_SKIP_ZERO_NEE
+#define MT_SKIP_ZERO_NEE 1
+#endif
 template <bool HOOKS>
 __global__ void __launch_bounds__(128, MT_SHADE_MIN_BLOCKS) k_shade(DevScene S, PathState P, ShadowQueue SQ,
                                                BatchInfo B, uint32_t bounce,
                                                const uint32_t* __restrict__ q,
                                                uint32_t* __restrict__ nq, uint32_t* counts,
-                                               int cur, int sqi, RecordBuffers R, NrcShade NC)
+                                               int cur, int sqi, RecordBuffers R, NrcShade NC,
+                                               unsigned long long* shadow_rays)
 {
     const uint32_t n = counts[cur];
     // this bounce's extension is done and the previous bounce's shadow stage
@@ -410,6 +414,7 @@ __global__ void __launch_bounds__(128, MT_SHADE_MIN_BLOCKS) k_shade(DevScene S, 
         counts[3] = 0;
         counts[4] = 0;
     }
+    uint32_t untraced = 0;  // zero-contribution shadow rays counted, not queued
     // one path that hit: the shading body (Tracer.cpp:150-233, 255-336)
     auto shade_hit = [&](const uint32_t p) {
         const uint4 hb = P.hitB[p];
@@ -565,11 +570,22 @@ __global__ void __launch_bounds__(128, MT_SHADE_MIN_BLOCKS) k_shade(DevScene S, 
                 const float fall = __fdiv_rn(1.0f, __fadd_rn(__fmul_rn(llen, llen), 1.0f));
                 const f3 le = brdf * nl * fall;
                 const f3 contrib = ((cur_e * le) * lcol) / pick;
-                const uint32_t slot = warp_append(&counts[sqi]);
-                const f3 so = hit_pos + lvec * 0.0001f;
-                SQ.o[slot] = make_float4(so.x, so.y, so.z, llen);
-                SQ.d[slot] = make_float4(ldir.x, ldir.y, ldir.z, __uint_as_float(p));
-                SQ.c[slot] = make_float4(contrib.x, contrib.y, contrib.z, static_cast<float>(bounce));
+                // A shadow ray whose contribution is exactly zero (the light
+                // below the surface: nl = 0) cannot change the image whatever
+                // it meets; without records or debug counts to fill it is
+                // counted, as the reference counts it (Tracer.cpp:319), but
+                // not traced.
+                const bool trace = HOOKS || vr || !MT_SKIP_ZERO_NEE ||
+                                   !(contrib.x == 0.0f && contrib.y == 0.0f && contrib.z == 0.0f);
+                if (trace) {
+                    const uint32_t slot = warp_append(&counts[sqi]);
+                    const f3 so = hit_pos + lvec * 0.0001f;
+                    SQ.o[slot] = make_float4(so.x, so.y, so.z, llen);
+                    SQ.d[slot] = make_float4(ldir.x, ldir.y, ldir.z, __uint_as_float(p));
+                    SQ.c[slot] = make_float4(contrib.x, contrib.y, contrib.z, static_cast<float>(bounce));
+                } else {
+                    ++untraced;
+                }
                 if (vr) {
                     vr[1].w = __uint_as_float(MT_VREC_HIT | MT_VREC_CHOSEN);
                     vr[3] = make_float4(ldir.x, ldir.y, ldir.z, nl * fall / pick);
@@ -701,6 +717,12 @@ __global__ void __launch_bounds__(128, MT_SHADE_MIN_BLOCKS) k_shade(DevScene S, 
         const uint32_t p = active ? s_hits[wib][held + lane] : 0u;
         __syncwarp();
         if (active) shade_hit(p);
+    }
+    if (!HOOKS && MT_SKIP_ZERO_NEE) {
+        uint32_t u = untraced;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) u += __shfl_down_sync(MT_FULL, u, o);
+        if (lane == 0 && u) atomicAdd(shadow_rays, static_cast<unsigned long long>(u));
     }
 }
 
@@ -1125,9 +1147,11 @@ cudaError_t launch_batch(const DevScene& S, const PathState& P, const ShadowQueu
         if (overlap && b > 0 && e == cudaSuccess) e = cudaStreamWaitEvent(st, W.ev_shadowed, 0);
         begin(MT_STAGE_SHADE);
         if (NC.mode != MT_NRC_OFF || P.dval)
-            k_shade<true><<<gw, 128, 0, st>>>(S, P, SQ, B, b, W.q[cur], W.q[cur ^ 1], W.counts, cur, sqi, R, NC);
+            k_shade<true><<<gw, 128, 0, st>>>(S, P, SQ, B, b, W.q[cur], W.q[cur ^ 1], W.counts, cur, sqi, R, NC,
+                                              W.rays + 1);
         else
-            k_shade<false><<<gw, 128, 0, st>>>(S, P, SQ, B, b, W.q[cur], W.q[cur ^ 1], W.counts, cur, sqi, R, NC);
+            k_shade<false><<<gw, 128, 0, st>>>(S, P, SQ, B, b, W.q[cur], W.q[cur ^ 1], W.counts, cur, sqi, R, NC,
+                                               W.rays + 1);
         end(MT_STAGE_SHADE);
         cudaStream_t ss = st;
         if (overlap && e == cudaSuccess) {
