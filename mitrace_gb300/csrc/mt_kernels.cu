@@ -572,10 +572,11 @@ __global__ void __launch_bounds__(128, MT_SHADE_MIN_BLOCKS) k_shade(DevScene S, 
                 const f3 contrib = ((cur_e * le) * lcol) / pick;
                 // A shadow ray whose contribution is exactly zero (the light
                 // below the surface: nl = 0) cannot change the image whatever
-                // it meets; without records or debug counts to fill it is
-                // counted, as the reference counts it (Tracer.cpp:319), but
-                // not traced.
-                const bool trace = HOOKS || vr || !MT_SKIP_ZERO_NEE ||
+                // it meets (nor a cache training record, whose NEE term stays
+                // zero); unless adjoint records or debug counts need its
+                // visit it is counted, as the reference counts it
+                // (Tracer.cpp:319), but not traced.
+                const bool trace = vr || P.dval || !MT_SKIP_ZERO_NEE ||
                                    !(contrib.x == 0.0f && contrib.y == 0.0f && contrib.z == 0.0f);
                 if (trace) {
                     const uint32_t slot = warp_append(&counts[sqi]);
@@ -718,7 +719,7 @@ __global__ void __launch_bounds__(128, MT_SHADE_MIN_BLOCKS) k_shade(DevScene S, 
         __syncwarp();
         if (active) shade_hit(p);
     }
-    if (!HOOKS && MT_SKIP_ZERO_NEE) {
+    if (MT_SKIP_ZERO_NEE) {
         uint32_t u = untraced;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) u += __shfl_down_sync(MT_FULL, u, o);
