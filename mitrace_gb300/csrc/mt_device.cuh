@@ -273,14 +273,15 @@ __device__ __forceinline__ bool tri_test(f3 o, f3 d, f3 v0, f3 e1, f3 e2, float&
     return true;
 }
 
-// tri_test in three stages, so that a warp can vote between them: begin()
-// applies the determinant and u rejections, second() the v rejection,
-// finish() forms t and applies 0 < t < dist (each called on every lane, with
-// the lane's result so far where it matters).  The same operations, values and
+// tri_test in stages, so that a warp can vote between them: begin() applies
+// the determinant and u rejections, second() the v rejection, ahead() the
+// sign of t (known from dot(e2, q) and det before the division), finish()
+// forms t and applies 0 < t < dist (each called on every lane, with the
+// lane's result so far where it matters).  The same operations, values and
 // decisions as tri_test followed by that range check.
 struct TriStage {
     f3 e1, e2, sv, q;
-    float det, sg, adet, us, u, v, t, inv;
+    float det, sg, adet, us, u, v, tn, t, inv;
     __device__ __forceinline__ bool begin(f3 o, f3 d, float4 v0, float4 e1w, float4 e2w)
     {
         e1 = xyz(e1w);
@@ -301,6 +302,13 @@ struct TriStage {
         const float vs = v * sg;
         return !(vs < 0.0f || __fadd_rn(us, vs) > adet);
     }
+    // the sign of t = tn * (1/det) before the division: a candidate whose t
+    // cannot be positive drops out
+    __device__ __forceinline__ bool ahead(bool ok)
+    {
+        tn = dot(e2, q);
+        return ok && (det > 0.0f ? tn > 0.0f : tn < 0.0f);
+    }
     // t is formed (one division, 1/det, which also scales u and v of the
     // winner) only on a lane that is still a candidate
     __device__ __forceinline__ bool finish(bool ok, float dist)
@@ -309,7 +317,7 @@ struct TriStage {
         inv = 0.0f;
         if (ok) {
             inv = __fdiv_rn(1.0f, det);
-            t = __fmul_rn(dot(e2, q), inv);
+            t = __fmul_rn(tn, inv);
         }
         return ok && t > 0.0f && t < dist;
     }
@@ -839,6 +847,8 @@ __device__ __forceinline__ void trace_persistent(const DevScene& S, Work& W, uin
                 if (__any_sync(MT_FULL, oka || okb)) {
                     oka = sa.second(rda) && oka;
                     okb = sb.second(rdb) && okb;
+                    oka = sa.ahead(oka);
+                    okb = sb.ahead(okb);
                     if (__any_sync(MT_FULL, oka || okb)) {
                         oka = sa.finish(oka, dista);
                         okb = sb.finish(okb, distb);
@@ -892,13 +902,22 @@ __device__ __forceinline__ void trace_persistent(const DevScene& S, Work& W, uin
                     const float vs = v * sg;
                     ok = ok && !(vs < 0.0f || __fadd_rn(us, vs) > adet);
                     if (__any_sync(MT_FULL, ok)) {
-                        float t = FLT_MAX, inv = 0.0f;
-                        if (ok) {
-                            inv = __fdiv_rn(1.0f, det);
-                            t = __fmul_rn(dot(e2, q), inv);
+                        // t = tn * (1/det) is positive only when tn and det
+                        // have the same sign: a candidate behind the origin
+                        // (the triangle a secondary ray leaves, most often)
+                        // drops out before the division, and a chunk left
+                        // with none skips it
+                        const float tn = dot(e2, q);
+                        ok = ok && (det > 0.0f ? tn > 0.0f : tn < 0.0f);
+                        if (__any_sync(MT_FULL, ok)) {
+                            float t = FLT_MAX, inv = 0.0f;
+                            if (ok) {
+                                inv = __fdiv_rn(1.0f, det);
+                                t = __fmul_rn(tn, inv);
+                            }
+                            ok = ok && t > 0.0f && t < dist;
+                            chunk_min(ok, t, u, v, inv, c, bt, bu, bv, bidx);
                         }
-                        ok = ok && t > 0.0f && t < dist;
-                        chunk_min(ok, t, u, v, inv, c, bt, bu, bv, bidx);
                     }
                 }
             }
