@@ -72,7 +72,11 @@ typedef struct mt_mesh_desc {
     const float* uv0;       /* 6 * num_triangles floats, or NULL            */
     /* Optional prebuilt BVH in the reference layout.  When NULL the library
      * builds one on the host with mt_bvh_build semantics, if the mesh has more
-     * than bvh_max_triangles triangles and BVHs are enabled (Mesh.cpp:37-40). */
+     * than bvh_max_triangles triangles and BVHs are enabled (Mesh.cpp:37-40).
+     * mt_create rejects (MT_ERR_INVALID) a prebuilt BVH whose inner nodes'
+     * children are not adjacent (b == a + 1, as the reference's builder lays
+     * them out), that has 2^31 nodes or more, a node or leaf range out of
+     * bounds, or a depth beyond the traversal stack. */
     const mt_bvh_node* bvh_nodes;
     uint32_t num_bvh_nodes;
     const uint32_t* bvh_indices;
