@@ -385,8 +385,9 @@ __device__ __forceinline__ void st4(float4* p, uint32_t i, f3 v, float w = 0.0f)
     p[i] = make_float4(v.x, v.y, v.z, w);
 }
 
-// HOOKS: the radiance-cache and debug-mode code paths; the plain render runs
-// the variant without them.
+// HOOKS: the radiance-cache and debug-mode code paths; REC: the adjoint's
+// vertex and path records.  The plain render runs the variant without either
+// (a smaller body: the shading stage waits on instruction fetch).
 // Occupancy hint of the shade kernel (blocks of 128 threads per SM): 8 caps it
 // at 64 registers with a few bytes of spills; the kernel waits on scattered
 // path-state and material loads, so more resident warps pay (measured on the
@@ -398,7 +399,7 @@ __device__ __forceinline__ void st4(float4* p, uint32_t i, f3 v, float w = 0.0f)
 #ifndef MT_SKIP_ZERO_NEE
 #define MT_SKIP_ZERO_NEE 1
 #endif
-template <bool HOOKS>
+template <bool HOOKS, bool REC>
 __global__ void __launch_bounds__(128, MT_SHADE_MIN_BLOCKS) k_shade(DevScene S, PathState P, ShadowQueue SQ,
                                                BatchInfo B, uint32_t bounce,
                                                const uint32_t* __restrict__ q,
@@ -510,7 +511,7 @@ __global__ void __launch_bounds__(128, MT_SHADE_MIN_BLOCKS) k_shade(DevScene S, 
                 }
                 if (mp.roughness >= NC.rough_min) seen_diffuse = 1.0f;
             }
-            float4* vr = R.vert ? R.vert + (static_cast<uint64_t>(p) * S.bounces + bounce) * 5 : nullptr;
+            float4* vr = REC && R.vert ? R.vert + (static_cast<uint64_t>(p) * S.bounces + bounce) * 5 : nullptr;
             if (vr) {
                 vr[0] = make_float4(N.x, N.y, N.z, __uint_as_float(__ldg(&I.material)));
                 vr[1] = make_float4(view.x, view.y, view.z, __uint_as_float(MT_VREC_HIT));
@@ -553,7 +554,8 @@ __global__ void __launch_bounds__(128, MT_SHADE_MIN_BLOCKS) k_shade(DevScene S, 
                     lpos = lpos0 + dir * __ldg(&L.point_size);
                 }
                 const f3 lvec = lpos - hit_pos;
-                const f3 ldir = normalize(lvec);
+                const float llen = length(lvec);
+                const f3 ldir = lvec * __fdiv_rn(1.0f, llen);  // normalize(lvec), its length formed once
                 f3 lcol = {__ldg(&L.color[0]), __ldg(&L.color[1]), __ldg(&L.color[2])};
                 float spot = 1.0f;
                 if (type == MT_LIGHT_SPOT) {
@@ -564,7 +566,6 @@ __global__ void __launch_bounds__(128, MT_SHADE_MIN_BLOCKS) k_shade(DevScene S, 
                     spot = gclamp(inten, 0.0f, 1.0f);
                     lcol = lcol * spot;
                 }
-                const float llen = length(lvec);
                 const f3 brdf = eval_brdf(ldir, view, N, base, mp.roughness, mp.metallic);
                 const float nl = gmax(dot(N, ldir), 0.0f);
                 const float fall = __fdiv_rn(1.0f, __fadd_rn(__fmul_rn(llen, llen), 1.0f));
@@ -700,7 +701,7 @@ __global__ void __launch_bounds__(128, MT_SHADE_MIN_BLOCKS) k_shade(DevScene S, 
                     const f3 color = bounce > 0 ? ld4(P.prev, p) : splat(1.0f);
                     const f3 sky = sample_sky(S, rd, bounce == 0);
                     st4(P.sky, p, ld4(P.sky, p) + (color * cur_e) * sky);
-                    if (R.path) R.path[2 * p + 1] = make_float4(sky.x, sky.y, sky.z, static_cast<float>(bounce));
+                    if (REC && R.path) R.path[2 * p + 1] = make_float4(sky.x, sky.y, sky.z, static_cast<float>(bounce));
                 } else {
                     hit = true;
                 }
@@ -995,8 +996,9 @@ cudaError_t preload_render_kernels()
 {
     cudaFuncAttributes fa;
     cudaError_t e = cudaFuncGetAttributes(&fa, k_raygen);
-    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_shade<true>);
-    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_shade<false>);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_shade<true, true>);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_shade<false, true>);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_shade<false, false>);
     if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_finalize);
     if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_resolve);
     if (e == cudaSuccess) (void)device_grids();  // the traversal kernels (occupancy queries)
@@ -1148,11 +1150,14 @@ cudaError_t launch_batch(const DevScene& S, const PathState& P, const ShadowQueu
         if (overlap && b > 0 && e == cudaSuccess) e = cudaStreamWaitEvent(st, W.ev_shadowed, 0);
         begin(MT_STAGE_SHADE);
         if (NC.mode != MT_NRC_OFF || P.dval)
-            k_shade<true><<<gw, 128, 0, st>>>(S, P, SQ, B, b, W.q[cur], W.q[cur ^ 1], W.counts, cur, sqi, R, NC,
-                                              W.rays + 1);
+            k_shade<true, true><<<gw, 128, 0, st>>>(S, P, SQ, B, b, W.q[cur], W.q[cur ^ 1], W.counts, cur, sqi, R,
+                                                    NC, W.rays + 1);
+        else if (R.vert || R.path)
+            k_shade<false, true><<<gw, 128, 0, st>>>(S, P, SQ, B, b, W.q[cur], W.q[cur ^ 1], W.counts, cur, sqi, R,
+                                                     NC, W.rays + 1);
         else
-            k_shade<false><<<gw, 128, 0, st>>>(S, P, SQ, B, b, W.q[cur], W.q[cur ^ 1], W.counts, cur, sqi, R, NC,
-                                               W.rays + 1);
+            k_shade<false, false><<<gw, 128, 0, st>>>(S, P, SQ, B, b, W.q[cur], W.q[cur ^ 1], W.counts, cur, sqi,
+                                                      R, NC, W.rays + 1);
         end(MT_STAGE_SHADE);
         cudaStream_t ss = st;
         if (overlap && e == cudaSuccess) {
