@@ -242,7 +242,11 @@ typedef struct mt_stats {
     float time_elapsed;             /* seconds since mt_start            */
     float estimated_time_remaining; /* seconds                           */
     float reserved;
-    uint64_t rays;                  /* path + shadow rays (Tracer.cpp:146,319) */
+    uint64_t rays;                  /* path + shadow rays (Tracer.cpp:146,319), counted
+                                       as the reference counts them: a shadow ray
+                                       whose contribution is exactly zero counts,
+                                       although it is not traced (its visibility
+                                       cannot change the image) */
     uint64_t samples;               /* camera samples (Tracer.cpp:342)   */
 } mt_stats;
 
