@@ -1,6 +1,7 @@
 """BRDF eval / pdf parity of the CUDA functions with the oracle's restatement of
-src/Tracer/BRDF.hpp:9-97 on seeded inputs (relative 1e-5; the only inexact step
-on either side is powf)."""
+src/Tracer/BRDF.hpp:9-97 on seeded inputs (relative 1e-5; the only step not
+correctly rounded on either side is Schlick's (1 - cos)^5: powf in the oracle,
+compensated products on the GPU)."""
 import numpy as np
 import pytest
 
@@ -68,8 +69,9 @@ def test_brdf_sampling_matches_oracle():
     mixture pdf to 1e-5 relative of the reference functions evaluated at the
     sampled direction.
 
-    The direction goes through sinf/cosf/sqrtf, whose last-ulp rounding differs
-    between the GPU and the host C library, and a near-mirror GGX lobe (alpha
+    The direction goes through sinf/cosf (one sincosf per angle on the GPU),
+    whose last-ulp rounding differs between the GPU and the host C library, and
+    a near-mirror GGX lobe (alpha
     down to 0.0025) turns a 1e-7 change of direction into percents of pdf, in
     exact arithmetic as in float.  So the pdf is checked where it is defined:
     the oracle's DiffusePdf / SpecularPdf (BRDF.hpp:80-97) and mixture
