@@ -1,7 +1,8 @@
 """BRDF eval / pdf parity of the CUDA functions with the oracle's restatement of
-src/Tracer/BRDF.hpp:9-97 on seeded inputs (relative 1e-5; the only step not
-correctly rounded on either side is Schlick's (1 - cos)^5: powf in the oracle,
-compensated products on the GPU)."""
+src/Tracer/BRDF.hpp:9-97 on seeded inputs (relative 1e-5; the only step the
+two sides compute differently is Schlick's (1 - cos)^5: the C library's powf
+in the oracle, compensated products on the GPU, correctly rounded except near
+a rounding tie)."""
 import numpy as np
 import pytest
 
