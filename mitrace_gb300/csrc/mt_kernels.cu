@@ -396,9 +396,6 @@ __device__ __forceinline__ void st4(float4* p, uint32_t i, f3 v, float w = 0.0f)
 #ifndef MT_SHADE_MIN_BLOCKS
 #define MT_SHADE_MIN_BLOCKS 8
 #endif
-#ifndef MT_SKIP_ZERO_NEE
-#define MT_SKIP_ZERO_NEE 1
-#endif
 template <bool HOOKS, bool REC>
 __global__ void __launch_bounds__(128, MT_SHADE_MIN_BLOCKS) k_shade(DevScene S, PathState P, ShadowQueue SQ,
                                                BatchInfo B, uint32_t bounce,
@@ -577,8 +574,7 @@ __global__ void __launch_bounds__(128, MT_SHADE_MIN_BLOCKS) k_shade(DevScene S, 
                 // zero); unless adjoint records or debug counts need its
                 // visit it is counted, as the reference counts it
                 // (Tracer.cpp:319), but not traced.
-                const bool trace = vr || P.dval || !MT_SKIP_ZERO_NEE ||
-                                   !(contrib.x == 0.0f && contrib.y == 0.0f && contrib.z == 0.0f);
+                const bool trace = vr || P.dval || !(contrib.x == 0.0f && contrib.y == 0.0f && contrib.z == 0.0f);
                 if (trace) {
                     const uint32_t slot = warp_append(&counts[sqi]);
                     const f3 so = hit_pos + lvec * 0.0001f;
@@ -720,12 +716,10 @@ __global__ void __launch_bounds__(128, MT_SHADE_MIN_BLOCKS) k_shade(DevScene S, 
         __syncwarp();
         if (active) shade_hit(p);
     }
-    if (MT_SKIP_ZERO_NEE) {
-        uint32_t u = untraced;
+    uint32_t u = untraced;
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) u += __shfl_down_sync(MT_FULL, u, o);
-        if (lane == 0 && u) atomicAdd(shadow_rays, static_cast<unsigned long long>(u));
-    }
+    for (int o = 16; o > 0; o >>= 1) u += __shfl_down_sync(MT_FULL, u, o);
+    if (lane == 0 && u) atomicAdd(shadow_rays, static_cast<unsigned long long>(u));
 }
 
 // Shadow rays queued by k_shade: an unoccluded ray adds its contribution to
